@@ -1,0 +1,247 @@
+// ORACLE — test infrastructure only (see igr_common.hpp for the parity status).
+// extern "C" entry points over the CPU restatement, loaded with ctypes by the
+// tests and by the CPU-baseline leg of bench.py. Arrays use the reference's
+// Julia column-major layout. Every function returns 0 on success, 1 on a bad
+// argument (unknown solver/objective), 2 on any other exception.
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "igr1d.hpp"
+#include "igr2d_adjoint.hpp"
+
+using namespace igr;
+
+namespace {
+thread_local std::string g_err;
+Grid2D make_grid(int p, const double* xi, const double* w, const double* Dcol, int Nex, int Ney, double Lx, double Ly) {
+  Basis b = (xi && w && Dcol) ? basis_from_arrays(p, xi, w, Dcol) : make_basis(p);
+  return Grid2D(b, make_mesh2d(Nex, Ney, Lx, Ly));
+}
+template <class F> int guard(F&& f) {
+  try { f(); return 0; }
+  catch (const std::invalid_argument& e) { g_err = e.what(); return 1; }
+  catch (const std::exception& e) { g_err = e.what(); return 2; }
+}
+}  // namespace
+
+#define GRID2D_ARGS int p, const double *xi, const double *w, const double *Dcol, int Nex, int Ney, double Lx, double Ly
+#define GRID2D make_grid(p, xi, w, Dcol, Nex, Ney, Lx, Ly)
+
+extern "C" {
+
+const char* orc_last_error() { return g_err.c_str(); }
+
+int orc_basis(int p, double* xi, double* w, double* Dcol) {
+  return guard([&] {
+    Basis b = make_basis(p);
+    for (int i = 0; i < b.np; ++i) { xi[i] = b.xi[i]; w[i] = b.w[i]; }
+    for (int i = 0; i < b.np; ++i) for (int k = 0; k < b.np; ++k) Dcol[i + (size_t)k * b.np] = b.Dik(i, k);
+  });
+}
+
+int orc2d_hyperbolic_rhs(GRID2D_ARGS, double gamma, const double* mx, const double* my, const double* rho, const double* E,
+                         const double* Sig, double* dmx, double* dmy, double* drho, double* dE) {
+  return guard([&] {
+    Grid2D G = GRID2D; const double* q[4] = {mx, my, rho, E}; double* dq[4] = {dmx, dmy, drho, dE};
+    std::vector<double> F[8]; hyperbolic_rhs(G, gamma, q, Sig, dq, F);
+  });
+}
+
+int orc2d_apply_sip(GRID2D_ARGS, double alpha, const double* x, const double* rho, double* y) {
+  return guard([&] { Grid2D G = GRID2D; apply_sip(G, y, x, rho, alpha); });
+}
+
+int orc2d_igr_rhs(GRID2D_ARGS, double alpha, const double* mx, const double* my, const double* rho, double* b) {
+  return guard([&] { Grid2D G = GRID2D; igr_rhs(G, b, mx, my, rho, alpha); });
+}
+
+int orc2d_sip_diagonal(GRID2D_ARGS, double alpha, const double* rho, double* M) {
+  return guard([&] { Grid2D G = GRID2D; sip_diagonal(G, M, rho, alpha); });
+}
+
+int orc2d_solve_elliptic(GRID2D_ARGS, double alpha, int n_iter, int solver, const double* mx, const double* my,
+                         const double* rho, const double* E, double* Sig) {
+  return guard([&] {
+    Grid2D G = GRID2D; const double* q[4] = {mx, my, rho, E};
+    Work2D<double> W; W.alloc(G.N); solve_elliptic(G, Sig, q, alpha, n_iter, solver, W);
+  });
+}
+
+// cg_solve! (tol exit) or cg_fixed! (fixed=1) on A x = b with A = SIP(rho, alpha).
+int orc2d_cg(GRID2D_ARGS, double alpha, const double* rho, const double* b, double* x, double tol, int maxiter, int fixed, int* iters) {
+  return guard([&] {
+    Grid2D G = GRID2D; Work2D<double> W; W.alloc(G.N);
+    *iters = cg_solve(G, x, b, rho, alpha, tol, maxiter, fixed != 0, W);
+  });
+}
+
+int orc2d_igr_euler_rhs(GRID2D_ARGS, double gamma, double alpha, int n_iter, int solver, const double* mx, const double* my,
+                        const double* rho, const double* E, double* Sig, double* dmx, double* dmy, double* drho, double* dE) {
+  return guard([&] {
+    Grid2D G = GRID2D; const double* q[4] = {mx, my, rho, E};
+    Work2D<double> W; W.alloc(G.N); igr_euler_rhs(G, q, Sig, gamma, alpha, n_iter, solver, W);
+    double* out[4] = {dmx, dmy, drho, dE};
+    for (int v = 0; v < 4; ++v) std::memcpy(out[v], W.dq[v].data(), G.N * sizeof(double));
+  });
+}
+
+int orc2d_run_forward(GRID2D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver,
+                      double* mx, double* my, double* rho, double* E, double* Sig) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid2D G = GRID2D; double* q[4] = {mx, my, rho, E}; run_forward(G, q, Sig, dt, T_end, gamma, alpha, n_iter, solver);
+  });
+}
+
+// Fixed-step forward (no dt re-rounding, Sigma from zero): the objective loop
+// of enzyme_adjoint.jl. State in-out; Sig out (Sigma after the last stage); J out.
+int orc2d_objective_run(GRID2D_ARGS, double gamma, double alpha, int n_steps, double dt, int n_iter, int solver, int obj,
+                        const double* prm, double* mx, double* my, double* rho, double* E, double* J) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    if (obj < 0 || obj > 5) throw std::invalid_argument("Unknown objective");
+    Grid2D G = GRID2D; double* q[4] = {mx, my, rho, E};
+    *J = objective_run(G, obj, q, n_steps, dt, gamma, alpha, n_iter, solver, prm);
+  });
+}
+
+int orc2d_adjoint(GRID2D_ARGS, double gamma, double alpha, int n_steps, double dt, int n_iter, int solver, int obj,
+                  const double* prm, const double* mx, const double* my, const double* rho, const double* E, double* J,
+                  double* dmx, double* dmy, double* drho, double* dE, double* dgamma, double* dalpha) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    if (obj < 0 || obj > 5) throw std::invalid_argument("Unknown objective");
+    Grid2D G = GRID2D; const double* q0[4] = {mx, my, rho, E}; double* dq[4] = {dmx, dmy, drho, dE};
+    *J = adjoint_ic(G, obj, prm, q0, n_steps, dt, gamma, alpha, n_iter, solver, dq, dgamma, dalpha);
+  });
+}
+
+// Batched adjoint on the host: B instances sharing one mesh, each with its own
+// state, gamma and alpha; OpenMP over instances (instance-major arrays).
+int orc2d_adjoint_batch(GRID2D_ARGS, int B, const double* gammas, const double* alphas, int n_steps, double dt, int n_iter,
+                        int solver, int obj, const double* prm, const double* q0, double* J, double* dq0, double* dgamma,
+                        double* dalpha, int n_threads) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid2D G = GRID2D; const size_t N = G.N;
+    std::string err;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads > 0 ? n_threads : 1)
+    for (int b = 0; b < B; ++b) {
+      try {
+        const double* qi[4]; double* di[4];
+        for (int v = 0; v < 4; ++v) { qi[v] = q0 + ((size_t)b * 4 + v) * N; di[v] = dq0 + ((size_t)b * 4 + v) * N; }
+        J[b] = adjoint_ic(G, obj, prm, qi, n_steps, dt, gammas[b], alphas[b], n_iter, solver, di, dgamma + b, dalpha + b);
+      } catch (const std::exception& e) {
+#pragma omp critical
+        err = e.what();
+      }
+    }
+    if (!err.empty()) throw std::runtime_error(err);
+  });
+}
+
+// Forward-mode directional derivative of the objective loop: seeds v (4 fields),
+// vg (gamma) and va (alpha); returns J and dJ = <grad, (v, vg, va)>.
+int orc2d_objective_dual(GRID2D_ARGS, double gamma, double alpha, int n_steps, double dt, int n_iter, int solver, int obj,
+                         const double* prm, const double* mx, const double* my, const double* rho, const double* E,
+                         const double* vmx, const double* vmy, const double* vrho, const double* vE, double vg, double va,
+                         double* J, double* dJ) {
+  return guard([&] {
+    typedef Dual<1> D1;
+    Grid2D G = GRID2D; const size_t N = G.N;
+    std::vector<D1> q[4];
+    const double* src[4] = {mx, my, rho, E}; const double* dir[4] = {vmx, vmy, vrho, vE};
+    for (int v = 0; v < 4; ++v) { q[v].resize(N); for (size_t k = 0; k < N; ++k) { q[v][k].v = src[v][k]; q[v][k].d[0] = dir[v][k]; } }
+    D1 g(gamma); g.d[0] = vg; D1 a(alpha); a.d[0] = va;
+    D1* qp[4] = {q[0].data(), q[1].data(), q[2].data(), q[3].data()};
+    D1 r = objective_run(G, obj, qp, n_steps, dt, g, a, n_iter, solver, prm);
+    *J = r.v; *dJ = r.d[0];
+  });
+}
+
+int orc2d_run_sensitivity(GRID2D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver, double s_gamma,
+                          double* mx, double* my, double* rho, double* E, double* Sig, double* zx, double* zy, double* sr,
+                          double* et, double* vs) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid2D G = GRID2D; double* q[4] = {mx, my, rho, E}; double* s[4] = {zx, zy, sr, et};
+    run_sensitivity(G, q, s, Sig, vs, dt, T_end, gamma, alpha, n_iter, solver, s_gamma);
+  });
+}
+
+// ----------------------------------- 1D -----------------------------------
+#define GRID1D_ARGS int p, const double *xi, const double *w, const double *Dcol, int Ne, double L
+static Grid1D make_grid1(int p, const double* xi, const double* w, const double* Dcol, int Ne, double L) {
+  Basis b = (xi && w && Dcol) ? basis_from_arrays(p, xi, w, Dcol) : make_basis(p);
+  return Grid1D(b, make_mesh1d(Ne, L));
+}
+#define GRID1D make_grid1(p, xi, w, Dcol, Ne, L)
+
+int orc1d_hyperbolic_rhs(GRID1D_ARGS, double gamma, const double* mu, const double* rho, const double* E, const double* Sig,
+                         double* dmu, double* drho, double* dE) {
+  return guard([&] {
+    Grid1D G = GRID1D; const double* q[3] = {mu, rho, E}; double* dq[3] = {dmu, drho, dE};
+    hyperbolic_rhs1d(G, gamma, q, Sig, dq);
+  });
+}
+
+int orc1d_apply_sip(GRID1D_ARGS, double alpha, const double* x, const double* rho, double* y) {
+  return guard([&] { Grid1D G = GRID1D; apply_sip1d(G, y, x, rho, alpha); });
+}
+
+int orc1d_run_forward(GRID1D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver,
+                      double* mu, double* rho, double* E, double* Sig) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid1D G = GRID1D; double* q[3] = {mu, rho, E}; run_forward1d(G, q, Sig, dt, T_end, gamma, alpha, n_iter, solver);
+  });
+}
+
+int orc1d_objective_run(GRID1D_ARGS, double gamma, double alpha, int n_steps, double dt, int n_iter, int solver, int obj,
+                        const double* prm, double* mu, double* rho, double* E, double* J) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid1D G = GRID1D; double* q[3] = {mu, rho, E};
+    *J = objective_run1d(G, obj, q, n_steps, dt, gamma, alpha, n_iter, solver, prm);
+  });
+}
+
+int orc1d_objective_dual(GRID1D_ARGS, double gamma, double alpha, int n_steps, double dt, int n_iter, int solver, int obj,
+                         const double* prm, const double* mu, const double* rho, const double* E, const double* vmu,
+                         const double* vrho, const double* vE, double vg, double va, double* J, double* dJ) {
+  return guard([&] {
+    typedef Dual<1> D1;
+    Grid1D G = GRID1D; const size_t N = G.N;
+    std::vector<D1> q[3];
+    const double* src[3] = {mu, rho, E}; const double* dir[3] = {vmu, vrho, vE};
+    for (int v = 0; v < 3; ++v) { q[v].resize(N); for (size_t k = 0; k < N; ++k) { q[v][k].v = src[v][k]; q[v][k].d[0] = dir[v][k]; } }
+    D1 g(gamma); g.d[0] = vg; D1 a(alpha); a.d[0] = va;
+    D1* qp[3] = {q[0].data(), q[1].data(), q[2].data()};
+    D1 r = objective_run1d(G, obj, qp, n_steps, dt, g, a, n_iter, solver, prm);
+    *J = r.v; *dJ = r.d[0];
+  });
+}
+
+int orc1d_adjoint(GRID1D_ARGS, double gamma, double alpha, int n_steps, double dt, int n_iter, int solver, int obj,
+                  const double* prm, const double* mu, const double* rho, const double* E, double* J, double* dmu,
+                  double* drho, double* dE, double* dgamma, double* dalpha) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid1D G = GRID1D; const double* q0[3] = {mu, rho, E}; double* dq[3] = {dmu, drho, dE};
+    *J = adjoint_ic1d(G, obj, prm, q0, n_steps, dt, gamma, alpha, n_iter, solver, dq, dgamma, dalpha);
+  });
+}
+
+int orc1d_run_sensitivity(GRID1D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver, int form,
+                          double s_gamma, double* mu, double* rho, double* E, double* Sig, double* smu, double* srho,
+                          double* sE, double* sSig) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    if (form != 1 && form != 2) throw std::invalid_argument("Unknown elliptic_rhs (use :form1 or :form2)");
+    Grid1D G = GRID1D; double* q[3] = {mu, rho, E}; double* s[3] = {smu, srho, sE};
+    run_sensitivity1d(G, q, s, Sig, sSig, dt, T_end, gamma, alpha, n_iter, solver, form, s_gamma);
+  });
+}
+
+}  // extern "C"
