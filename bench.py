@@ -1,0 +1,315 @@
+"""Benchmark: 2D P3 128^2 discrete-adjoint gradients/s, batched vs plain.
+
+Workload (one "step" = one batched gradient call): B = 32 instances of the
+2D IGR-Euler discrete adjoint on a 128 x 128 P3 mesh (262,144 nodes x 4
+vars each), Chebyshev-Jacobi 5 iterations per stage, 200 SSP-RK3 steps,
+objective J = sum over nodes in a seeded square window of w_i w_j Jx Jy rho^2,
+gradient w.r.t. the initial state, gamma and alpha. Initial states: seeded
+Gaussian pressure pulses (3 pulses, amplitude U[1,10], width 0.03, centres
+U[0.2,0.8]; synthetic stand-ins of the reference's pulse family), gamma = 1.4,
+alpha = 3 (1/128)^2, dt from CFL 0.1.
+
+`value` times the batched call with inputs and outputs resident in HBM; `e2e`
+times the same call through the C ABI with host buffers (H2D of q0, D2H of
+dq0 inside the timed region). "plain" runs the same kernels one instance at a
+time. The working set (tape) is far larger than L2, so no flush is needed.
+
+Under torchrun (N > 1) every rank runs its own batch (instances shard with no
+exchange: weak scaling); rank 0 prints the max-over-ranks timing.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+P, NE, N_STEPS, N_ITER, SOLVER, OBJ = 3, 128, 200, 5, "chebyshev", "window_rho2"
+GAMMA = 1.4
+METRIC = "2D P3 128² adjoint gradients/s: batched vs plain, same GPU, rel err ≤1e-9"
+
+# FP64 operations per node executed by each kernel family (FMA = 2), P3,
+# counted from the kernels' instruction mix (ncu FP64 instruction counts of
+# one launch divided by nodes; see profiles/). Used for the live roofline.
+FLOPS_PER_NODE = {0: 110.0, 1: 56.0, 2: 230.0, 3: 330.0, 4: 110.0, 5: 150.0}
+# FP64 bytes moved per node per launch by each family (reads + writes of
+# whole fields, halo re-reads excluded), for the HBM fraction.
+BYTES_PER_NODE = {0: 8 * 13, 1: 8 * 15, 2: 8 * 19, 3: 8 * 27, 4: 8 * 22, 5: 8 * 17}
+FAMILY = {0: "k2_setup", 1: "k2_apply", 2: "k2_hyp_rk", 3: "k2_hyp_rev", 4: "k2_apply_rev", 5: "k2_setup_rev"}
+
+
+def make_batch(igr, W, B, first=0):
+    basis = igr.DGBasis(P)
+    mesh = igr.CartesianMesh2D(NE, NE, 1.0, 1.0, basis)
+    q0 = np.empty((B, 4, mesh.x.size))
+    dts = np.empty(B)
+    for b in range(B):
+        q = W.seeded_pulses_2d(mesh, GAMMA, W.seed_for(3, first + b), n_pulses=3, width=0.03)
+        for v in range(4):
+            q0[b, v] = np.asarray(q[v]).reshape(-1, order="F")
+        dts[b] = W.cfl_dt_2d(mesh, P, q, GAMMA, 0.1)
+    alpha = 3.0 * (1.0 / NE) ** 2
+    return basis, mesh, q0, np.full(B, GAMMA), np.full(B, alpha), dts, W.seeded_window(W.seed_for(3, first))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
+            else "/tmp/igr_clocks_bench.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax.append(float(parts[2].split()[0]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(B_cpu, n_steps_sample, threads):
+    """The CPU oracle (C++ restatement of the reference) on a bounded sample:
+    B_cpu instances for n_steps_sample steps, OpenMP over instances."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    from igr_sensitivities_gb300 import workloads as W
+    import igr_sensitivities_gb300 as igr
+    basis, mesh, q0, gam, alp, dts, prm = make_batch(igr, W, B_cpu)
+    G = O.Grid2D(P, NE, NE)
+    t0 = time.perf_counter()
+    O.adjoint_batch_2d(G, gam, alp, n_steps_sample, float(dts[0]), N_ITER, SOLVER, OBJ, q0, prm, n_threads=threads)
+    t = time.perf_counter() - t0
+    # per-step cost is uniform: a full 200-step gradient costs 200/n_steps_sample times the sample
+    return B_cpu / (t * N_STEPS / n_steps_sample), t
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    B_cpu = threads
+    n_sample = 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(B_cpu, n_sample, threads)
+    for _ in range(args.steps):
+        v, t = cpu_baseline(B_cpu, n_sample, threads)
+        vals.append((v, t))
+    value = statistics.median(v for v, _ in vals)
+    ms = statistics.median(t for _, t in vals) * 1e3
+    sample = "%d instances x %d of %d steps (OpenMP over instances), scaled to full gradients" % (B_cpu, n_sample, N_STEPS)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "gradients/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args.batch),
+            "cpu_baseline": {"value": value, "unit": "gradients/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is Julia, absent on this machine; this arm times the C++ CPU oracle (a restatement "
+                    "of the reference's algorithm)"}
+    print(json.dumps(line))
+
+
+def config_dict(B):
+    return {"workload": "2D IGR-Euler discrete adjoint, P3 128x128 (262,144 nodes x 4 vars per instance), "
+                        "Chebyshev-Jacobi 5 iters/stage, 200 SSP-RK3 steps, J = window rho^2",
+            "batch": B, "mesh": "128x128", "p": P, "n_steps": N_STEPS, "solver": "chebyshev", "n_iter": N_ITER,
+            "objective": OBJ, "gradient_wrt": "q0 (4 fields), gamma, alpha",
+            "l2": "inputs and tape far larger than L2 (no flush needed)", "parallelism": "instances per GPU (no exchange)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import igr_sensitivities_gb300 as igr
+    from igr_sensitivities_gb300 import _lib, workloads as W
+    import ctypes as C
+
+    ctx = igr.Context(local)
+    if args.profile_case:
+        basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, 2)
+        q0d = torch.from_numpy(q0h).to(torch.device("cuda", local))
+        for _ in range(2):
+            igr.adjoint_batch(q0d, gam, alp, dts, 4, basis, mesh, n_iter=N_ITER, solver=SOLVER, objective=OBJ,
+                              obj_params=prm, ctx=ctx, device_arrays=True)
+        torch.cuda.synchronize()
+        print("profile case done")
+        return
+    n_steps = args.n_steps
+    B = args.batch
+    basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, B, first=rank * B)
+    dev = torch.device("cuda", local)
+    q0d = torch.from_numpy(q0h).to(dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    def run_dev():
+        return igr.adjoint_batch(q0d, gam, alp, dts, n_steps, basis, mesh, n_iter=N_ITER, solver=SOLVER, objective=OBJ,
+                                 obj_params=prm, ctx=ctx, device_arrays=True)
+
+    for _ in range(args.warmup):
+        run_dev()
+    lib = _lib.lib()
+    lib.igr_profile_reset(ctx.handle)
+    lib.igr_profile_enable(ctx.handle, 1)
+    clk = ClockSampler(local)
+    clk.start()
+    barrier()
+    t0 = time.perf_counter()
+    launches = 0
+    for _ in range(args.steps):
+        run_dev()
+        launches += ctx.last_launch_count()
+    barrier()
+    t = time.perf_counter() - t0
+    clocks = clk.stop()
+    lib.igr_profile_enable(ctx.handle, 0)
+    fam = {}
+    for k in range(9):
+        ms, cnt, nn = C.c_double(0), C.c_longlong(0), C.c_double(0)
+        lib.igr_profile_read(ctx.handle, k, C.byref(ms), C.byref(cnt))
+        lib.igr_profile_nodes(ctx.handle, k, C.byref(nn))
+        fam[k] = (ms.value, cnt.value, nn.value)
+    tmax = t
+    if dist is not None:
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tmax = float(tt.item())
+    value = B * world * args.steps / tmax
+
+    # end to end: host buffers through the C ABI
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        igr.adjoint_batch(q0h, gam, alp, dts, n_steps, basis, mesh, n_iter=N_ITER, solver=SOLVER, objective=OBJ,
+                          obj_params=prm, ctx=ctx)
+    barrier()
+    te = (time.perf_counter() - t0) / max(1, args.steps // 2)
+    e2e = B * world / te
+
+    # plain: the same kernels, one instance per call
+    plain = None
+    if not args.no_plain:
+        nplain = 2
+        run1 = lambda b: igr.adjoint_batch(q0d[b:b + 1].contiguous(), gam[b:b + 1], alp[b:b + 1], dts[b:b + 1], n_steps, basis,
+                                           mesh, n_iter=N_ITER, solver=SOLVER, objective=OBJ, obj_params=prm, ctx=ctx,
+                                           device_arrays=True)
+        run1(0)
+        barrier()
+        t0 = time.perf_counter()
+        for b in range(nplain):
+            run1(b)
+        barrier()
+        tp = (time.perf_counter() - t0) / nplain
+        plain = {"value": 1.0 / tp, "unit": "gradients/s", "ms_per_gradient": tp * 1e3}
+
+    if rank != 0:
+        return
+    peak = C.c_double(0)
+    lib.igr_probe_fp64_peak(ctx.handle, C.byref(peak))
+    share = {FAMILY[k]: fam[k][0] for k in FAMILY}
+    tot = sum(v[0] for v in fam.values()) or 1.0
+    dom = max(FAMILY, key=lambda k: fam[k][0])
+    ms_launch = fam[dom][0] / max(fam[dom][1], 1)
+    nodes = fam[dom][2] / max(fam[dom][1], 1)       # nodes per launch (one instance group)
+    flops = FLOPS_PER_NODE[dom] * nodes
+    achieved = flops / (ms_launch * 1e-3) / 1e12
+    hbm = BYTES_PER_NODE[dom] * nodes / (ms_launch * 1e-3) / 1e9
+    all_flops = sum(FLOPS_PER_NODE[k] * fam[k][2] for k in FAMILY)
+    all_ms = sum(fam[k][0] for k in FAMILY)
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        hbm_peak, hbm_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        hbm_peak, hbm_src = 6800.0, "fallback"
+    roofline = {"bound": "fp64", "kernel": FAMILY[dom], "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                "peak_source": "measured live (DFMA-chain probe in libigr_gb300.so)",
+                "ms_per_launch": ms_launch, "flops_per_launch": flops, "nodes_per_launch": nodes,
+                "all_kernels_fp64_tflops": all_flops / (all_ms * 1e-3) / 1e12 if all_ms else None,
+                "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak, "peak_source": hbm_src},
+                "time_share": {k: v / tot for k, v in share.items()}}
+    cfg = config_dict(B)
+    cfg["n_steps"] = n_steps
+    line = {"metric": METRIC, "value": value, "unit": "gradients/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tmax / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian pressure pulses)",
+            "config": cfg, "plain": plain,
+            "batched_over_plain": (value / world / plain["value"]) if plain else None,
+            "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": int(q0h.nbytes),
+                    "d2h_bytes_per_step": int(q0h.nbytes + 3 * 8 * B)},
+            "gpu_launches": launches, "roofline": roofline, "clocks": clocks}
+    if not args.no_cpu and world == 1:
+        threads = os.cpu_count() or 1
+        v, tcpu = cpu_baseline(threads, 1, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "gradients/s", "cores": threads, "kind": "port",
+                                "sample": "%d instances x 1 of %d steps (OpenMP over instances, %.1f s), scaled to full "
+                                          "gradients" % (threads, N_STEPS, tcpu)}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,302 @@
+"""GB300 engine for the IGR-regularised Euler forward map and its derivatives.
+
+Host-side mirror of the reference's Julia module API (IGRAdjoints2D /
+IGRAdjoints1D of f-t-s/IGR_sensitivities) over the C ABI in
+include/igr_gb300.h. Function names, argument order and meaning follow the
+reference; Julia's mutating `f!` functions are spelled `f_` here.
+
+Arrays are numpy float64 arrays in the reference's layout: 2D fields have
+shape (n_p, n_p, N_ex, N_ey) and 1D fields (n_p, N_e), indexed [i, j, ex, ey]
+with the memory order of Julia (column-major, `order="F"`). All arithmetic
+runs in the CUDA library; there is no CPU fallback, and importing a function
+raises if the library is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._lib import Context, check, default_context, lib
+
+__all__ = [
+    "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
+    "run_forward", "run_forward_", "enzyme_adjoint_ic", "adjoint_batch", "objective_value",
+    "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
+]
+
+SOLVERS = {"pcg": 0, "jacobi": 1, "chebyshev": 2}
+OBJECTIVES = {"l2_density": 0, "l2_pressure": 1, "kinetic_energy": 2, "windowed_kinetic_energy": 3,
+              "weighted_momentum": 4, "window_rho2": 5, "interval_rho": 6}
+
+_D = C.POINTER(C.c_double)
+
+
+def _lgl(p):
+    """LGL nodes and weights: closed forms for p <= 4 (the values
+    FastGaussQuadrature.gausslobatto returns up to rounding), Newton on
+    (1 - x^2) P_p'(x) above."""
+    if p == 1:
+        return np.array([-1.0, 1.0]), np.array([1.0, 1.0])
+    if p == 2:
+        return np.array([-1.0, 0.0, 1.0]), np.array([1 / 3, 4 / 3, 1 / 3])
+    if p == 3:
+        a = np.sqrt(1.0 / 5.0)
+        return np.array([-1.0, -a, a, 1.0]), np.array([1 / 6, 5 / 6, 5 / 6, 1 / 6])
+    if p == 4:
+        a = np.sqrt(3.0 / 7.0)
+        return np.array([-1.0, -a, 0.0, a, 1.0]), np.array([1 / 10, 49 / 90, 32 / 45, 49 / 90, 1 / 10])
+    n = p + 1
+    x = -np.cos(np.pi * np.arange(n) / p)
+    for _ in range(100):
+        P0, P1 = np.ones_like(x), x.copy()
+        for k in range(2, p + 1):
+            P0, P1 = P1, ((2 * k - 1) * x * P1 - (k - 1) * P0) / k
+        dx = (x * P1 - P0) / (n * P1)
+        x = x - dx
+        if np.max(np.abs(dx)) < 1e-16:
+            break
+    P0, P1 = np.ones_like(x), x.copy()
+    for k in range(2, p + 1):
+        P0, P1 = P1, ((2 * k - 1) * x * P1 - (k - 1) * P0) / k
+    return x, 2.0 / (p * n * P1 * P1)
+
+
+class DGBasis:
+    """DG basis of degree p: LGL nodes `xi`, weights `w`, differentiation
+    matrix `D` (IGR_adjoints_2d/basis.jl:7-68)."""
+
+    def __init__(self, p, xi=None, w=None, D=None):
+        self.p = int(p)
+        if xi is None:
+            xi, w = _lgl(self.p)
+        self.xi = np.ascontiguousarray(xi, dtype=np.float64)
+        self.w = np.ascontiguousarray(w, dtype=np.float64)
+        if D is None:
+            n = self.p + 1
+            lam = np.ones(n)  # barycentric weights, basis.jl:19-30
+            for j in range(n):
+                for i in range(n):
+                    if i != j:
+                        lam[j] *= self.xi[j] - self.xi[i]
+                lam[j] = 1.0 / lam[j]
+            D = np.zeros((n, n))  # basis.jl:38-49
+            for j in range(n):
+                for i in range(n):
+                    if i == j:
+                        continue
+                    D[i, j] = (lam[j] / lam[i]) / (self.xi[i] - self.xi[j])
+                    D[i, i] -= D[i, j]
+        self.D = np.asarray(D, dtype=np.float64)
+        self._Dcol = np.ascontiguousarray(self.D.reshape(-1, order="F"))
+
+    @property
+    def n_p(self):
+        return self.p + 1
+
+
+class CartesianMesh2D:
+    """Uniform doubly-periodic mesh (IGR_adjoints_2d/mesh.jl:89-125)."""
+
+    def __init__(self, N_ex, N_ey, Lx, Ly, basis):
+        self.N_ex, self.N_ey, self.Lx, self.Ly = int(N_ex), int(N_ey), float(Lx), float(Ly)
+        self.dx, self.dy = self.Lx / self.N_ex, self.Ly / self.N_ey
+        self.Jx, self.Jy = self.dx / 2.0, self.dy / 2.0
+        n = basis.n_p
+        ex = np.arange(self.N_ex)[None, None, :, None]
+        ey = np.arange(self.N_ey)[None, None, None, :]
+        self.x = np.asfortranarray(np.broadcast_to((ex * self.dx) + self.Jx * (1.0 + basis.xi[:, None, None, None]),
+                                                   (n, n, self.N_ex, self.N_ey)))
+        self.y = np.asfortranarray(np.broadcast_to((ey * self.dy) + self.Jy * (1.0 + basis.xi[None, :, None, None]),
+                                                   (n, n, self.N_ex, self.N_ey)))
+
+    def shape(self, basis):
+        return (basis.n_p, basis.n_p, self.N_ex, self.N_ey)
+
+
+class PeriodicMesh1D:
+    """Uniform periodic 1D mesh (IGR_adjoints_1d/mesh.jl:7-33)."""
+
+    def __init__(self, N_e, L, basis):
+        self.N_e, self.L = int(N_e), float(L)
+        self.dx = self.L / self.N_e
+        self.J = self.dx / 2.0
+        e = np.arange(self.N_e)[None, :]
+        self.x = np.asfortranarray((e * self.dx) + self.J * (1.0 + basis.xi[:, None]))
+
+
+class _Disc2D(C.Structure):
+    _fields_ = [("p", C.c_int), ("n_ex", C.c_int), ("n_ey", C.c_int), ("lx", C.c_double), ("ly", C.c_double),
+                ("xi", _D), ("w", _D), ("D", _D)]
+
+
+def _disc2d(basis, mesh):
+    d = _Disc2D(basis.p, mesh.N_ex, mesh.N_ey, mesh.Lx, mesh.Ly, basis.xi.ctypes.data_as(_D),
+                basis.w.ctypes.data_as(_D), basis._Dcol.ctypes.data_as(_D))
+    d._keep = (basis,)
+    return d
+
+
+def _flat(a, n):
+    f = np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, order="F"))
+    if f.size != n:
+        raise ValueError("array has %d entries, expected %d" % (f.size, n))
+    return f
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_D)
+
+
+def _solver(solver):
+    if isinstance(solver, str):
+        solver = solver.lstrip(":")
+        if solver not in SOLVERS:
+            raise ValueError("Unknown solver: %s (use :pcg, :jacobi, or :chebyshev)" % solver)
+        return SOLVERS[solver]
+    return int(solver)
+
+
+def _objective(obj):
+    if isinstance(obj, str):
+        obj = obj.lstrip(":")
+        if obj not in OBJECTIVES:
+            raise ValueError("Unknown objective: %s" % obj)
+        return OBJECTIVES[obj]
+    return int(obj)
+
+
+def _prm(obj_params):
+    return np.ascontiguousarray(np.zeros(4) if obj_params is None else np.asarray(obj_params, dtype=np.float64))
+
+
+def run_forward_(mux, muy, rho, E, Sigma, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
+    """run_forward! (IGR_adjoints_2d/forward.jl:41-75): state arrays updated in place to time T."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n) for a in (mux, muy, rho, E)]
+    S = np.zeros(n)
+    check(ctx, lib().igr2d_run_forward(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma), C.c_double(alpha),
+                                       C.c_double(dt), C.c_double(T), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                       *[_ptr(a) for a in q], _ptr(S)))
+    for dst, src in zip((mux, muy, rho, E, Sigma), q + [S]):
+        dst[...] = src.reshape(shape, order="F")
+
+
+def run_forward(mux0, muy0, rho0, E0, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
+    """run_forward (IGR_adjoints_2d/forward.jl:84-99): returns (mux, muy, rho, E, Sigma) at time T."""
+    shape = mesh.shape(basis)
+    out = [np.array(np.asarray(a, dtype=np.float64).reshape(shape, order="F"), order="F") for a in (mux0, muy0, rho0, E0)]
+    S = np.zeros(shape, order="F")
+    run_forward_(*out, S, dt, T, basis, mesh, gamma, alpha, n_iter, solver, ctx)
+    return (*out, S)
+
+
+def enzyme_adjoint_ic(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",
+                      objective="l2_density", obj_params=None, with_params=False, ctx=None):
+    """enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:428-454).
+
+    Returns (J, dmux0, dmuy0, drho0, dE0), the objective and its gradient with
+    respect to the initial conservative state after `n_steps` SSP-RK3 steps of
+    size `dt`, computed by the hand-written discrete adjoint on the GPU. With
+    with_params=True, (dJ/dgamma, dJ/dalpha) are appended.
+    """
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n) for a in (mux0, muy0, rho0, E0)]
+    dq = [np.zeros(n) for _ in range(4)]
+    J, dg, da = C.c_double(0), C.c_double(0), C.c_double(0)
+    prm = _prm(obj_params)
+    check(ctx, lib().igr2d_adjoint_ic(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma), C.c_double(alpha),
+                                      C.c_int(n_steps), C.c_double(dt), C.c_int(max(n_iter, 1)), C.c_int(_solver(solver)),
+                                      C.c_int(_objective(objective)), _ptr(prm), *[_ptr(a) for a in q], C.byref(J),
+                                      *[_ptr(a) for a in dq], C.byref(dg), C.byref(da)))
+    out = (J.value,) + tuple(a.reshape(shape, order="F") for a in dq)
+    return out + (dg.value, da.value) if with_params else out
+
+
+def adjoint_batch(q0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solver="pcg", objective="l2_density",
+                  obj_params=None, ctx=None, device_arrays=False):
+    """Batched enzyme_adjoint_ic over instances sharing one mesh.
+
+    q0: (n_inst, 4, N) float64, variables (mux, muy, rho, E) in the Julia node
+    order. Returns (J[n_inst], dq0 (n_inst, 4, N), dgamma[n_inst], dalpha[n_inst]).
+    With device_arrays=True, q0 is a torch CUDA tensor and dq0 is returned as one.
+    """
+    ctx = ctx or default_context()
+    gammas = np.ascontiguousarray(gammas, dtype=np.float64)
+    alphas = np.ascontiguousarray(alphas, dtype=np.float64)
+    dts = np.ascontiguousarray(dts, dtype=np.float64)
+    B = gammas.size
+    J, dg, da = np.zeros(B), np.zeros(B), np.zeros(B)
+    prm = _prm(obj_params)
+    d = _disc2d(basis, mesh)
+    if device_arrays:
+        import torch
+        dq = torch.empty_like(q0)
+        check(ctx, lib().igr2d_adjoint_batch_dev(ctx.handle, C.byref(d), C.c_int(B), _ptr(gammas), _ptr(alphas), _ptr(dts),
+                                                 C.c_int(n_steps), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                                 C.c_int(_objective(objective)), _ptr(prm),
+                                                 C.cast(C.c_void_p(q0.data_ptr()), _D), _ptr(J),
+                                                 C.cast(C.c_void_p(dq.data_ptr()), _D), _ptr(dg), _ptr(da)))
+        return J, dq, dg, da
+    q0 = np.ascontiguousarray(q0, dtype=np.float64)
+    dq = np.zeros_like(q0)
+    check(ctx, lib().igr2d_adjoint_batch(ctx.handle, C.byref(d), C.c_int(B), _ptr(gammas), _ptr(alphas), _ptr(dts),
+                                         C.c_int(n_steps), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                         C.c_int(_objective(objective)), _ptr(prm), _ptr(q0), _ptr(J), _ptr(dq), _ptr(dg),
+                                         _ptr(da)))
+    return J, dq, dg, da
+
+
+def objective_value(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",
+                    objective="l2_density", obj_params=None, ctx=None):
+    """The primal objective of enzyme_adjoint_ic (the inlined RK3 loop of
+    IGR_adjoints_2d/enzyme_adjoint.jl:206-235 and its objective tail)."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n).copy() for a in (mux0, muy0, rho0, E0)]
+    J = C.c_double(0)
+    check(ctx, lib().igr2d_objective(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma), C.c_double(alpha),
+                                     C.c_int(n_steps), C.c_double(dt), C.c_int(max(n_iter, 1)), C.c_int(_solver(solver)),
+                                     C.c_int(_objective(objective)), _ptr(_prm(obj_params)), *[_ptr(a) for a in q],
+                                     C.byref(J)))
+    return J.value
+
+
+def apply_sip_(y, x, rho, basis, mesh, alpha, ctx=None):
+    """apply_sip! (IGR_adjoints_2d/elliptic.jl:30-145): y = A x."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    out = np.zeros(n)
+    check(ctx, lib().igr2d_apply_sip(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(alpha), _ptr(_flat(x, n)),
+                                     _ptr(_flat(rho, n)), _ptr(out)))
+    y[...] = out.reshape(shape, order="F")
+
+
+def compute_hyperbolic_rhs_(dmux, dmuy, drho, dE, mux, muy, rho, E, Sigma, basis, mesh, gamma, ctx=None):
+    """compute_hyperbolic_rhs! (IGR_adjoints_2d/hyperbolic.jl:27-119)."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n) for a in (mux, muy, rho, E, Sigma)]
+    out = [np.zeros(n) for _ in range(4)]
+    check(ctx, lib().igr2d_hyperbolic_rhs(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma),
+                                          *[_ptr(a) for a in q], *[_ptr(a) for a in out]))
+    for dst, src in zip((dmux, dmuy, drho, dE), out):
+        dst[...] = src.reshape(shape, order="F")
+
+
+def solve_elliptic_(Sigma, mux, muy, rho, E, basis, mesh, alpha, n_iter=10, solver="pcg", ctx=None):
+    """solve_elliptic! (IGR_adjoints_2d/elliptic.jl:413-427); Sigma is the warm start and the result."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n) for a in (mux, muy, rho, E)]
+    S = _flat(Sigma, n).copy()
+    check(ctx, lib().igr2d_solve_elliptic(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(alpha), C.c_int(n_iter),
+                                          C.c_int(_solver(solver)), *[_ptr(a) for a in q], _ptr(S)))
+    Sigma[...] = S.reshape(shape, order="F")

@@ -1,0 +1,84 @@
+"""Loads libigr_gb300.so (built in-tree by build.py) and manages contexts.
+
+There is no fallback: if the library cannot be loaded, every call raises.
+"""
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libigr_gb300.so")
+
+STATUS = {0: "IGR_OK", 1: "IGR_EINVAL", 2: "IGR_EUNSUPPORTED", 3: "IGR_ENONFINITE", 4: "IGR_ECUDA", 5: "IGR_ENOMEM",
+          6: "IGR_ETIMEOUT"}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class IGRError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError("libigr_gb300.so is not built; run igr_sensitivities_gb300/build.py "
+                                   "(or __graft_entry__.build()) first")
+            _lib = C.CDLL(LIB_PATH)
+            _lib.igr_last_error.restype = C.c_char_p
+            _lib.igr_last_error.argtypes = [C.c_void_p]
+            _lib.igr_ctx_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+            _lib.igr_ctx_destroy.argtypes = [C.c_void_p]
+            _lib.igr_set_tape_budget.argtypes = [C.c_void_p, C.c_size_t]
+            _lib.igr_last_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        return _lib
+
+
+class Context:
+    """One CUDA stream plus device workspace (igr_ctx). Not thread-safe."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        rc = lib().igr_ctx_create(int(device), C.byref(h))
+        if rc != 0:
+            raise IGRError(rc, "igr_ctx_create failed (no usable CUDA device %d?)" % device)
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().igr_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tape_budget(self, nbytes):
+        check(self, lib().igr_set_tape_budget(self.handle, C.c_size_t(int(nbytes))))
+
+    def last_launch_count(self):
+        n = C.c_longlong(0)
+        check(self, lib().igr_last_launch_count(self.handle, C.byref(n)))
+        return n.value
+
+
+_default = None
+
+
+def default_context():
+    global _default
+    if _default is None:
+        _default = Context(int(os.environ.get("IGR_DEVICE", "0")))
+    return _default
+
+
+def check(ctx, rc):
+    if rc != 0:
+        raise IGRError(rc, lib().igr_last_error(ctx.handle).decode())

@@ -1,0 +1,349 @@
+// extern "C" boundary (include/igr_gb300.h): argument checks, host<->device
+// transfers and status codes around the engine.
+#include <cmath>
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/igr_gb300.h"
+#include "igr_engine.h"
+
+using namespace igrgpu;
+
+struct igr_ctx {
+  Ctx c;
+};
+
+namespace {
+
+template <class F>
+int guarded(igr_ctx* ctx, F&& f) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.err.clear();
+  ctx->c.launches = 0;
+  try {
+    cuda_check(cudaSetDevice(ctx->c.device), "cudaSetDevice");
+    f();
+    return IGR_OK;
+  } catch (const Error& e) {
+    ctx->c.err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    ctx->c.err = "host allocation failed";
+    return IGR_ENOMEM;
+  } catch (const std::exception& e) {
+    ctx->c.err = e.what();
+    return IGR_ECUDA;
+  }
+}
+
+void check_disc(const igr_disc2d* d) {
+  if (!d || !d->xi || !d->w || !d->D) throw Error(IGR_EINVAL, "null discretisation");
+  if (d->p < 1 || d->p > 4) throw Error(IGR_EINVAL, "polynomial degree p must be in 1..4");
+  if (d->n_ex < 1 || d->n_ey < 1 || !(d->lx > 0) || !(d->ly > 0)) throw Error(IGR_EINVAL, "bad mesh");
+}
+
+void check_solver(int solver, int n_iter) {
+  if (solver < 0 || solver > 2) throw Error(IGR_EINVAL, "Unknown solver (use :pcg, :jacobi, or :chebyshev)");
+  if (n_iter < 1) throw Error(IGR_EINVAL, "n_iter must be >= 1");
+}
+
+long long nodes2d(const igr_disc2d* d) { return (long long)(d->p + 1) * (d->p + 1) * d->n_ex * d->n_ey; }
+
+void h2d(Ctx& c, double* dst, const double* src, long long n) {
+  if (!src) throw Error(IGR_EINVAL, "null array");
+  cuda_check(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, c.stream), "H2D");
+}
+void d2h(Ctx& c, double* dst, const double* src, long long n) {
+  if (!dst) throw Error(IGR_EINVAL, "null array");
+  cuda_check(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream), "D2H");
+}
+void sync(Ctx& c) { cuda_check(cudaStreamSynchronize(c.stream), "stream sync"); }
+
+Plan2D plan_single(Ctx& c, const igr_disc2d* d, double gamma, double alpha, double dt, const char* tag) {
+  check_disc(d);
+  BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+  Inst2DDesc I{d->n_ex, d->n_ey, d->lx, d->ly, gamma, alpha, dt};
+  return make_plan2d(c, B, {I}, tag);
+}
+
+}  // namespace
+
+extern "C" {
+
+int igr_ctx_create(int device, igr_ctx** out) {
+  if (!out) return IGR_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return IGR_ECUDA;
+  std::unique_ptr<igr_ctx> ctx(new igr_ctx());
+  ctx->c.device = device;
+  if (cudaSetDevice(device) != cudaSuccess) return IGR_ECUDA;
+  if (cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking) != cudaSuccess) return IGR_ECUDA;
+  if (cudaMalloc(&ctx->c.d_status, sizeof(int)) != cudaSuccess) return IGR_ECUDA;
+  if (cudaMemset(ctx->c.d_status, 0, sizeof(int)) != cudaSuccess) return IGR_ECUDA;
+  *out = ctx.release();
+  return IGR_OK;
+}
+
+int igr_ctx_destroy(igr_ctx* ctx) {
+  if (!ctx) return IGR_OK;
+  cudaSetDevice(ctx->c.device);
+  if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+  ctx->c.ws.release_all();
+  if (ctx->c.d_status) cudaFree(ctx->c.d_status);
+  if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+  return IGR_OK;
+}
+
+const char* igr_last_error(const igr_ctx* ctx) { return ctx ? ctx->c.err.c_str() : "null context"; }
+
+int igr_set_tape_budget(igr_ctx* ctx, size_t bytes) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.tape_budget = bytes;
+  return IGR_OK;
+}
+
+int igr_last_launch_count(const igr_ctx* ctx, long long* out) {
+  if (!ctx || !out) return IGR_EINVAL;
+  *out = ctx->c.launches;
+  return IGR_OK;
+}
+
+int igr_profile_enable(igr_ctx* ctx, int on) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.prof.harvest();
+  ctx->c.prof.on = on != 0;
+  return IGR_OK;
+}
+
+int igr_profile_reset(igr_ctx* ctx) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.prof.reset();
+  return IGR_OK;
+}
+
+int igr_profile_read(igr_ctx* ctx, int kernel_family, double* total_ms, long long* launches) {
+  if (!ctx || !total_ms || !launches || kernel_family < 0 || kernel_family >= KID_COUNT) return IGR_EINVAL;
+  ctx->c.prof.harvest();
+  *total_ms = ctx->c.prof.ms[kernel_family];
+  *launches = ctx->c.prof.count[kernel_family];
+  return IGR_OK;
+}
+
+int igr_profile_nodes(igr_ctx* ctx, int kernel_family, double* nodes) {
+  if (!ctx || !nodes || kernel_family < 0 || kernel_family >= KID_COUNT) return IGR_EINVAL;
+  ctx->c.prof.harvest();
+  *nodes = ctx->c.prof.nodes[kernel_family];
+  return IGR_OK;
+}
+
+int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops) {
+  return guarded(ctx, [&] {
+    if (!tflops) throw Error(IGR_EINVAL, "null output");
+    *tflops = probe_fp64_tflops(ctx->c);
+  });
+}
+
+int igr2d_run_forward(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
+                      int n_iter, int solver, double* mux, double* muy, double* rho, double* E, double* sigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+    // forward.jl:48-49
+    const int n_steps = (int)std::ceil(t_end / dt);
+    const double dtr = t_end / n_steps;
+    Plan2D P = plan_single(c, d, gamma, alpha, dtr, "fwd");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:q", 5 * N);
+    double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* S = buf + 4 * N;
+    const double* in[4] = {mux, muy, rho, E};
+    for (int v = 0; v < 4; ++v) h2d(c, q[v], in[v], N);
+    cuda_check(cudaMemsetAsync(S, 0, N * sizeof(double), c.stream), "zero Sigma");  // forward.jl:42
+    Solve2DOpts o{n_iter, solver};
+    forward2d(c, P, q, S, n_steps, o);
+    if (alpha > 0) {  // forward.jl:71-73
+      const double* qc[4] = {q[0], q[1], q[2], q[3]};
+      solve_elliptic2d(c, P, qc, S, o);
+    }
+    double* out[4] = {mux, muy, rho, E};
+    for (int v = 0; v < 4; ++v) d2h(c, out[v], q[v], N);
+    d2h(c, sigma, S, N);
+    sync(c);
+  });
+}
+
+int igr2d_objective(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_steps, double dt,
+                    int n_iter, int solver, int objective, const double* obj_params, double* mux, double* muy,
+                    double* rho, double* E, double* J) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    Plan2D P = plan_single(c, d, gamma, alpha, dt, "obj");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:q", 5 * N);
+    double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* io[4] = {mux, muy, rho, E};
+    for (int v = 0; v < 4; ++v) h2d(c, q[v], io[v], N);
+    Solve2DOpts o{n_iter, solver};
+    objective2d(c, P, q, n_steps, o, objective, obj_params, J);
+    for (int v = 0; v < 4; ++v) d2h(c, io[v], q[v], N);
+    sync(c);
+  });
+}
+
+static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                               const double* dts, int n_steps, int n_iter, int solver, int objective,
+                               const double* obj_params, const double* q0, bool q0_dev, double* J, double* dq0,
+                               bool dq0_dev, double* dgamma, double* dalpha) {
+  check_disc(d);
+  check_solver(solver, n_iter);
+  if (n_inst < 1 || !gammas || !alphas || !dts || !J) throw Error(IGR_EINVAL, "bad batch arguments");
+  BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+  const long long N = nodes2d(d);
+  // Instances per group: as many as fit with a full tape (no recompute);
+  // a single instance that does not fit runs with segment checkpointing.
+  int G = n_inst;
+  if (c.tape_budget == 0) {
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    const size_t avail = fr + c.ws.bytes();
+    const size_t reserve = (size_t)2 << 30;
+    const bool apos = alphas[0] > 0;
+    const size_t F = 14 + (apos ? 2 * (size_t)n_iter : 0);
+    const size_t per_inst = ((size_t)3 * F * std::max(n_steps, 1) + 120) * N * sizeof(double);
+    const size_t fit = avail > reserve ? (avail - reserve) / per_inst : 0;
+    G = (int)std::max<size_t>(1, std::min<size_t>((size_t)n_inst, fit));
+  }
+  for (int g0 = 0; g0 < n_inst; g0 += G) {
+    const int gn = std::min(G, n_inst - g0);
+    std::vector<Inst2DDesc> insts;
+    for (int b = g0; b < g0 + gn; ++b) insts.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], alphas[b], dts[b]});
+    Plan2D P = make_plan2d(c, B, insts, "adj");
+    const long long NG = P.NG;
+    double* buf = c.ws.dbl("capi:bq", 8 * (size_t)N * G);
+    double* q[4];
+    double* dq[4];
+    for (int v = 0; v < 4; ++v) { q[v] = buf + v * NG; dq[v] = buf + (4 + v) * NG; }
+    // [inst][var][N] -> field-major [var][inst*N]
+    const cudaMemcpyKind kin = q0_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const double* qg = q0 + (size_t)g0 * 4 * N;
+    for (int v = 0; v < 4; ++v)
+      cuda_check(cudaMemcpy2DAsync(q[v], N * sizeof(double), qg + v * N, 4 * N * sizeof(double), N * sizeof(double), gn, kin,
+                                   c.stream), "gather q0");
+    Solve2DOpts o{n_iter, solver};
+    const double* qc[4] = {q[0], q[1], q[2], q[3]};
+    adjoint2d(c, P, qc, n_steps, o, objective, obj_params, J + g0, dq, dgamma ? dgamma + g0 : nullptr,
+              dalpha ? dalpha + g0 : nullptr);
+    const cudaMemcpyKind kout = dq0_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    double* dg = dq0 + (size_t)g0 * 4 * N;
+    for (int v = 0; v < 4; ++v)
+      cuda_check(cudaMemcpy2DAsync(dg + v * N, 4 * N * sizeof(double), dq[v], N * sizeof(double), N * sizeof(double), gn, kout,
+                                   c.stream), "scatter dq0");
+  }
+  sync(c);
+}
+
+int igr2d_adjoint_ic(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_steps, double dt,
+                     int n_iter, int solver, int objective, const double* obj_params, const double* mux0,
+                     const double* muy0, const double* rho0, const double* E0, double* J, double* dmux0,
+                     double* dmuy0, double* drho0, double* dE0, double* dgamma, double* dalpha) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc(d);
+    const long long N = nodes2d(d);
+    std::vector<double> q0(4 * N), dq0(4 * N);
+    const double* in[4] = {mux0, muy0, rho0, E0};
+    for (int v = 0; v < 4; ++v) {
+      if (!in[v]) throw Error(IGR_EINVAL, "null array");
+      std::memcpy(q0.data() + v * N, in[v], N * sizeof(double));
+    }
+    adjoint_batch_impl(c, d, 1, &gamma, &alpha, &dt, n_steps, n_iter, solver, objective, obj_params, q0.data(), false, J,
+                       dq0.data(), false, dgamma, dalpha);
+    double* out[4] = {dmux0, dmuy0, drho0, dE0};
+    for (int v = 0; v < 4; ++v) {
+      if (!out[v]) throw Error(IGR_EINVAL, "null array");
+      std::memcpy(out[v], dq0.data() + v * N, N * sizeof(double));
+    }
+  });
+}
+
+int igr2d_adjoint_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                        const double* dts, int n_steps, int n_iter, int solver, int objective,
+                        const double* obj_params, const double* q0, double* J, double* dq0, double* dgamma,
+                        double* dalpha) {
+  return guarded(ctx, [&] {
+    if (!q0 || !dq0) throw Error(IGR_EINVAL, "null array");
+    adjoint_batch_impl(ctx->c, d, n_inst, gammas, alphas, dts, n_steps, n_iter, solver, objective, obj_params, q0, false, J, dq0,
+                       false, dgamma, dalpha);
+  });
+}
+
+int igr2d_adjoint_batch_dev(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas,
+                            const double* alphas, const double* dts, int n_steps, int n_iter, int solver,
+                            int objective, const double* obj_params, const double* q0_dev, double* J,
+                            double* dq0_dev, double* dgamma, double* dalpha) {
+  return guarded(ctx, [&] {
+    if (!q0_dev || !dq0_dev) throw Error(IGR_EINVAL, "null array");
+    adjoint_batch_impl(ctx->c, d, n_inst, gammas, alphas, dts, n_steps, n_iter, solver, objective, obj_params, q0_dev, true, J,
+                       dq0_dev, true, dgamma, dalpha);
+  });
+}
+
+int igr2d_apply_sip(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* x, const double* rho, double* y) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    Plan2D P = plan_single(c, d, 1.4, alpha, 0.0, "sip");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:sip", 3 * N);
+    h2d(c, buf, x, N);
+    h2d(c, buf + N, rho, N);
+    apply_sip2d(c, P, buf, buf + N, buf + 2 * N);
+    d2h(c, y, buf + 2 * N, N);
+    sync(c);
+  });
+}
+
+int igr2d_hyperbolic_rhs(igr_ctx* ctx, const igr_disc2d* d, double gamma, const double* mux, const double* muy,
+                         const double* rho, const double* E, const double* sigma, double* dmux, double* dmuy,
+                         double* drho, double* dE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    Plan2D P = plan_single(c, d, gamma, 0.0, 0.0, "rhs");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:rhs", 9 * N);
+    const double* in[5] = {mux, muy, rho, E, sigma};
+    for (int v = 0; v < 5; ++v) h2d(c, buf + v * N, in[v], N);
+    const double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* k[4] = {buf + 5 * N, buf + 6 * N, buf + 7 * N, buf + 8 * N};
+    hyperbolic_rhs2d(c, P, q, buf + 4 * N, k);
+    double* out[4] = {dmux, dmuy, drho, dE};
+    for (int v = 0; v < 4; ++v) d2h(c, out[v], k[v], N);
+    sync(c);
+  });
+}
+
+int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_iter, int solver,
+                         const double* mux, const double* muy, const double* rho, const double* E, double* sigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    Plan2D P = plan_single(c, d, 1.4, alpha, 0.0, "sol");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:sol", 5 * N);
+    const double* in[4] = {mux, muy, rho, E};
+    for (int v = 0; v < 4; ++v) h2d(c, buf + v * N, in[v], N);
+    h2d(c, buf + 4 * N, sigma, N);
+    const double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    Solve2DOpts o{n_iter, solver};
+    solve_elliptic2d(c, P, q, buf + 4 * N, o);
+    d2h(c, sigma, buf + 4 * N, N);
+    sync(c);
+  });
+}
+
+}  // extern "C"

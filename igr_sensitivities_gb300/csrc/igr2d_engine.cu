@@ -1,0 +1,805 @@
+// 2D host engine: plans, forward / adjoint drivers and the small pointwise and
+// reduction kernels that do not depend on the polynomial degree.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "igr2d_kernels.cuh"
+#include "igr2d_launch.h"
+#include "igr2d_rev_kernels.cuh"
+#include "igr_engine.h"
+
+namespace igrgpu {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw Error(4, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+Workspace::~Workspace() { release_all(); }
+void* Workspace::get(const std::string& name, size_t bytes) {
+  if (bytes == 0) bytes = 8;
+  Buf& b = bufs_[name];
+  if (b.n < bytes) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+    cuda_check(cudaMalloc(&b.p, bytes), ("cudaMalloc " + name).c_str());
+    b.n = bytes;
+  }
+  return b.p;
+}
+void Workspace::release_all() {
+  for (auto& kv : bufs_) if (kv.second.p) cudaFree(kv.second.p);
+  bufs_.clear();
+}
+size_t Workspace::bytes() const {
+  size_t s = 0;
+  for (auto& kv : bufs_) s += kv.second.n;
+  return s;
+}
+
+cudaEvent_t Profiler::get() {
+  if (next < pool.size()) return pool[next++];
+  cudaEvent_t e;
+  cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+  pool.push_back(e);
+  ++next;
+  return e;
+}
+void Profiler::begin(cudaStream_t s, int kid, long long n) {
+  Rec r{kid, n, get(), get()};
+  cudaEventRecord(r.a, s);
+  recs.push_back(r);
+}
+void Profiler::end(cudaStream_t s) { cudaEventRecord(recs.back().b, s); }
+void Profiler::harvest() {
+  for (auto& r : recs) {
+    cudaEventSynchronize(r.b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    ms[r.kid] += t;
+    count[r.kid] += 1;
+    nodes[r.kid] += (double)r.nodes;
+  }
+  recs.clear();
+  next = 0;
+}
+void Profiler::reset() {
+  harvest();
+  for (int k = 0; k < KID_COUNT; ++k) { ms[k] = 0; count[k] = 0; nodes[k] = 0; }
+}
+Profiler::~Profiler() {
+  for (auto e : pool) cudaEventDestroy(e);
+}
+
+BasisDev make_basis_dev(int p, const double* xi, const double* w, const double* D) {
+  if (p < 1 || p > MAXNP - 1) throw Error(1, "polynomial degree p must be in 1..4");
+  BasisDev B;
+  std::memset(&B, 0, sizeof(B));
+  B.np = p + 1;
+  for (int i = 0; i < B.np; ++i) { B.w[i] = w[i]; B.xi[i] = xi[i]; }
+  for (int i = 0; i < B.np; ++i)
+    for (int k = 0; k < B.np; ++k) B.D[i][k] = D[i + (size_t)k * B.np];
+  for (int i = 0; i < B.np; ++i)
+    for (int k = 0; k < B.np; ++k) B.W2[i][k] = B.w[i] * (B.D[i][k] * B.D[i][k]);
+  // chebyshev_fixed!, elliptic.jl:373-378
+  const double table[4] = {1.5, 2.0, 2.1, 2.2};
+  const double lmax = table[std::min(p, 4) - 1], lmin = 1.0;
+  B.cheb_theta = (lmax + lmin) / 2;
+  B.cheb_delta = (lmax - lmin) / 2;
+  B.cheb_sigma = B.cheb_theta / std::max(B.cheb_delta, 1e-10);
+  B.hw = -0.5 / B.w[0];
+  B.iw0 = 1.0 / B.w[0];
+  B.iwL = 1.0 / B.w[B.np - 1];
+  return B;
+}
+
+// Chebyshev recurrence coefficients of iteration it = 1..n:
+// d_it = a_it d_{it-1} + c_it M^-1 r_{it-1} (elliptic.jl:383-391).
+static void cheb_coeffs(const BasisDev& B, int n, std::vector<double>& a, std::vector<double>& cc) {
+  a.assign(n + 1, 0.0);
+  cc.assign(n + 1, 0.0);
+  double rc = 1 / B.cheb_sigma;
+  for (int it = 1; it <= n; ++it) {
+    if (it == 1) { a[it] = 0.0; cc[it] = 1.0 / B.cheb_theta; }
+    else { const double rn = 1 / (2 * B.cheb_sigma - rc); a[it] = rn * rc; cc[it] = 2 * rn / B.cheb_delta; rc = rn; }
+  }
+}
+
+static void tile_shape(int np, int* tx, int* ty) {
+  switch (np) {
+    case 2: tile_shape2d<2>(tx, ty); break;
+    case 3: tile_shape2d<3>(tx, ty); break;
+    case 4: tile_shape2d<4>(tx, ty); break;
+    case 5: tile_shape2d<5>(tx, ty); break;
+    default: throw Error(1, "unsupported polynomial degree");
+  }
+}
+
+Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& insts, const std::string& tag) {
+  Plan2D P;
+  P.B = B;
+  P.np = B.np;
+  int tx, ty;
+  tile_shape(P.np, &tx, &ty);
+  long long off = 0;
+  for (size_t i = 0; i < insts.size(); ++i) {
+    const Inst2DDesc& d = insts[i];
+    if (d.nex < 1 || d.ney < 1) throw Error(1, "mesh must have at least one element per direction");
+    Inst2D I;
+    I.off = off;
+    I.nex = d.nex; I.ney = d.ney;
+    I.lx = d.lx; I.ly = d.ly;
+    I.dx = d.lx / d.nex; I.dy = d.ly / d.ney;
+    I.jx = I.dx / 2.0; I.jy = I.dy / 2.0;
+    I.gamma = d.gamma; I.alpha = d.alpha; I.dt = d.dt;
+    I.ijx = 1.0 / I.jx; I.ijy = 1.0 / I.jy; I.idx = 1.0 / I.dx; I.idy = 1.0 / I.dy;
+    I.ialpha = d.alpha > 0 ? 1.0 / d.alpha : 0.0;
+    P.inst.push_back(I);
+    const long long n = (long long)P.np * P.np * d.nex * d.ney;
+    P.inst_nodes.push_back(n);
+    off += n;
+    for (int ey0 = 0; ey0 < d.ney; ey0 += ty)
+      for (int ex0 = 0; ex0 < d.nex; ex0 += tx) P.tiles.push_back(Tile2D{(int)i, ex0, ey0, 0});
+  }
+  P.NG = off;
+  c.cur_nodes = off;
+  P.d_inst = static_cast<Inst2D*>(c.ws.get(tag + ":inst", sizeof(Inst2D) * P.inst.size()));
+  P.d_tiles = static_cast<Tile2D*>(c.ws.get(tag + ":tiles", sizeof(Tile2D) * P.tiles.size()));
+  cuda_check(cudaMemcpyAsync(P.d_inst, P.inst.data(), sizeof(Inst2D) * P.inst.size(), cudaMemcpyHostToDevice, c.stream), "upload inst");
+  cuda_check(cudaMemcpyAsync(P.d_tiles, P.tiles.data(), sizeof(Tile2D) * P.tiles.size(), cudaMemcpyHostToDevice, c.stream), "upload tiles");
+  return P;
+}
+
+// ------------------------------------------------------------------------------------------
+// Pointwise and reduction kernels (degree independent)
+// ------------------------------------------------------------------------------------------
+__global__ void k_recip(const double* __restrict__ x, double* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) y[i] = 1.0 / x[i];
+}
+
+// Per-node objective integrands (enzyme_adjoint.jl:230-385 and the nodal
+// window extension). j1 = integrand, j2 = mass integrand (kinetic energy only).
+struct ObjArgs2D {
+  const Inst2D* inst; int ninst; BasisDev B;
+  const double *q[4];
+  int obj; double prm[4];
+  double *j1, *j2;
+  const double *s1, *s2;       // per-instance sums (gradient kernel)
+  double *qb[4], *gb;          // gradient outputs: d/dq and per-node d/dgamma
+  long long NG;
+};
+
+__device__ __forceinline__ int find_inst(const Inst2D* inst, int ninst, long long n) {
+  int lo = 0, hi = ninst - 1;
+  while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (inst[mid].off <= n) lo = mid; else hi = mid - 1; }
+  return lo;
+}
+
+__device__ __forceinline__ void node_coords2d(const BasisDev& B, const Inst2D& I, long long local, double* c, double* x, double* y) {
+  const int nn = B.np * B.np;
+  const long long el = local / nn;
+  const int nd = (int)(local % nn);
+  const int i = nd % B.np, j = nd / B.np;
+  const int ex = (int)(el % I.nex), ey = (int)(el / I.nex);
+  *c = B.w[i] * B.w[j] * I.jx * I.jy;
+  *x = ex * I.dx + I.jx * (1.0 + B.xi[i]);
+  *y = ey * I.dy + I.jy * (1.0 + B.xi[j]);
+}
+
+__global__ void k2_obj_nodes(ObjArgs2D a) {
+  const double pi = 3.14159265358979323846;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.NG; n += (long long)gridDim.x * blockDim.x) {
+    const Inst2D I = a.inst[find_inst(a.inst, a.ninst, n)];
+    double c, x, y;
+    node_coords2d(a.B, I, n - I.off, &c, &x, &y);
+    const double mx = a.q[0][n], my = a.q[1][n], r = a.q[2][n], E = a.q[3][n];
+    double v1 = 0.0, v2 = 0.0;
+    switch (a.obj) {
+      case OBJ_L2_DENSITY: v1 = c * (r * r); break;
+      case OBJ_L2_PRESSURE: { const double P = (I.gamma - 1.0) * (E - (mx * mx + my * my) / (2.0 * r)); v1 = c * (P * P); break; }
+      case OBJ_KINETIC_ENERGY: v1 = c * (mx * mx + my * my) / (2.0 * r); v2 = c * r; break;
+      case OBJ_WINDOWED_KE: {
+        const double wx = exp(-((x - 0.55) * (x - 0.55) + (y - 0.50) * (y - 0.50)) / (0.15 * 0.15));
+        v1 = c * wx * (mx * mx + my * my) / (2.0 * r); break;
+      }
+      case OBJ_WEIGHTED_MOMENTUM: {
+        const double Lx = I.lx, Ly = I.ly;
+        v1 = c * mx * (sin(2 * pi * x / Lx) * sin(2 * pi * y / Ly)); break;
+      }
+      case OBJ_WINDOW_RHO2: {
+        const bool in = x >= a.prm[0] && x <= a.prm[0] + a.prm[2] && y >= a.prm[1] && y <= a.prm[1] + a.prm[2];
+        v1 = in ? c * (r * r) : 0.0; break;
+      }
+      default: break;
+    }
+    a.j1[n] = v1;
+    if (a.j2) a.j2[n] = v2;
+  }
+}
+
+__global__ void k2_obj_grad(ObjArgs2D a) {
+  const double pi = 3.14159265358979323846;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.NG; n += (long long)gridDim.x * blockDim.x) {
+    const int ii = find_inst(a.inst, a.ninst, n);
+    const Inst2D I = a.inst[ii];
+    double c, x, y;
+    node_coords2d(a.B, I, n - I.off, &c, &x, &y);
+    const double mx = a.q[0][n], my = a.q[1][n], r = a.q[2][n], E = a.q[3][n];
+    double g0 = 0, g1 = 0, g2 = 0, g3 = 0, gg = 0;
+    switch (a.obj) {
+      case OBJ_L2_DENSITY: g2 = 2.0 * c * r; break;
+      case OBJ_L2_PRESSURE: {
+        const double K = (mx * mx + my * my) / (2.0 * r), P = (I.gamma - 1.0) * (E - K);
+        const double Pb = 2.0 * c * P, Kb = -Pb * (I.gamma - 1.0);
+        gg = Pb * (E - K); g3 = Pb * (I.gamma - 1.0); g0 = Kb * mx / r; g1 = Kb * my / r; g2 = -Kb * K / r; break;
+      }
+      case OBJ_KINETIC_ENERGY: {
+        const double KE = a.s1[ii], Ms = a.s2[ii];
+        const double KEb = 1.0 / Ms, Mb = -KE / (Ms * Ms);
+        g0 = KEb * c * mx / r; g1 = KEb * c * my / r; g2 = -KEb * c * (mx * mx + my * my) / (2.0 * r * r) + Mb * c; break;
+      }
+      case OBJ_WINDOWED_KE: {
+        const double wx = exp(-((x - 0.55) * (x - 0.55) + (y - 0.50) * (y - 0.50)) / (0.15 * 0.15));
+        g0 = c * wx * mx / r; g1 = c * wx * my / r; g2 = -c * wx * (mx * mx + my * my) / (2.0 * r * r); break;
+      }
+      case OBJ_WEIGHTED_MOMENTUM: {
+        const double Lx = I.lx, Ly = I.ly;
+        g0 = c * (sin(2 * pi * x / Lx) * sin(2 * pi * y / Ly)); break;
+      }
+      case OBJ_WINDOW_RHO2: {
+        const bool in = x >= a.prm[0] && x <= a.prm[0] + a.prm[2] && y >= a.prm[1] && y <= a.prm[1] + a.prm[2];
+        g2 = in ? 2.0 * c * r : 0.0; break;
+      }
+      default: break;
+    }
+    a.qb[0][n] = g0; a.qb[1][n] = g1; a.qb[2][n] = g2; a.qb[3][n] = g3;
+    if (a.gb) a.gb[n] = gg;   // per-node d/dgamma of the objective (l2_pressure)
+  }
+}
+
+// Deterministic per-instance sum: one block per instance, fixed order.
+__global__ void k_inst_sum(const double* __restrict__ f, const long long* __restrict__ off, const long long* __restrict__ cnt,
+                           double* __restrict__ out) {
+  __shared__ double s[256];
+  const long long o = off[blockIdx.x], n = cnt[blockIdx.x];
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += f[o + i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = s[0];
+}
+
+__global__ void k_fill(double* p, double v, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// ------------------------------------------------------------------------------------------
+// Launch helpers
+// ------------------------------------------------------------------------------------------
+static int grid_for(long long n) { return (int)std::min<long long>((n + 255) / 256, 152LL * 16); }
+
+#define NP_DISPATCH(np, CALL)                         \
+  switch (np) {                                       \
+    case 2: { constexpr int NPV = 2; CALL; } break;   \
+    case 3: { constexpr int NPV = 3; CALL; } break;   \
+    case 4: { constexpr int NPV = 4; CALL; } break;   \
+    case 5: { constexpr int NPV = 5; CALL; } break;   \
+    default: throw Error(1, "unsupported polynomial degree"); \
+  }
+
+static void recip(Ctx& c, const double* x, double* y, long long n) {
+  LaunchScope ls(c, KID_OTHER);
+  k_recip<<<grid_for(n), 256, 0, c.stream>>>(x, y, n);
+}
+
+// Per-stage storage: tape slot or scratch.
+struct StageBuf {
+  double* q[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* invr = nullptr;
+  double* Sout = nullptr;
+  double *b = nullptr, *cm = nullptr, *ckx = nullptr, *cky = nullptr, *cinvM = nullptr, *cpx = nullptr, *cpy = nullptr, *cM = nullptr;
+  std::vector<double*> xk, rk;  // taped iterates (empty when untaped)
+};
+
+constexpr int STAGE_FIXED_FIELDS = 14;  // q(4) invr Sout b cm ckx cky cinvM cpx cpy cM
+
+static int stage_fields(const Solve2DOpts& o, bool alpha_pos) {
+  return STAGE_FIXED_FIELDS + (alpha_pos ? 2 * o.n_iter : 0);
+}
+
+static StageBuf stage_from(double* base, long long NG, const Solve2DOpts& o, bool alpha_pos, bool taped) {
+  StageBuf s;
+  int f = 0;
+  auto nxt = [&]() { return base + (long long)(f++) * NG; };
+  for (int v = 0; v < 4; ++v) s.q[v] = nxt();
+  s.invr = nxt(); s.Sout = nxt(); s.b = nxt(); s.cm = nxt(); s.ckx = nxt(); s.cky = nxt();
+  s.cinvM = nxt(); s.cpx = nxt(); s.cpy = nxt(); s.cM = nxt();
+  if (taped && alpha_pos) {
+    for (int k = 0; k < o.n_iter; ++k) s.xk.push_back(nxt());
+    for (int k = 0; k < o.n_iter; ++k) s.rk.push_back(nxt());
+  }
+  return s;
+}
+
+static bool any_alpha_pos(const Plan2D& P) {
+  for (auto& I : P.inst) if (I.alpha > 0) return true;
+  return false;
+}
+static bool all_alpha_pos(const Plan2D& P) {
+  for (auto& I : P.inst) if (!(I.alpha > 0)) return false;
+  return true;
+}
+
+// Setup + fixed-count solve of one stage. x0: warm start (read only);
+// result in st.Sout; xa/xb/dbuf: scratch.
+static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* x0, double* xa,
+                        double* xb, double* dbuf) {
+  const int nb = P.ntiles();
+  SetupArgs2D sa;
+  sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
+  sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
+  sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = st.cM;
+  { LaunchScope ls(c, KID_SETUP); NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, nb, c.stream)); }
+  if (o.solver == SOLVER_PCG) throw Error(1, "PCG is not available in this build of the 2D engine");
+  const int epi = o.solver == SOLVER_CHEBYSHEV ? EPI_CHEB : EPI_JACOBI;
+  std::vector<double> ca, cc;
+  cheb_coeffs(P.B, o.n_iter, ca, cc);
+  const double* x = x0;
+  for (int k = 0; k < o.n_iter; ++k) {
+    ApplyArgs2D a;
+    std::memset(&a, 0, sizeof(a));
+    a.tiles = P.d_tiles; a.inst = P.d_inst; a.B = P.B;
+    a.x = x;
+    a.cm = st.cm; a.ckx = st.ckx; a.cky = st.cky; a.cpx = st.cpx; a.cpy = st.cpy; a.b = st.b; a.cinvM = st.cinvM;
+    a.d_in = k == 0 ? nullptr : dbuf;
+    a.d_out = dbuf;
+    double* xo = (k == o.n_iter - 1) ? st.Sout : ((k % 2 == 0) ? xa : xb);
+    a.x_out = xo;
+    a.tape_x = st.xk.empty() ? nullptr : st.xk[k];
+    a.tape_r = st.rk.empty() ? nullptr : st.rk[k];
+    a.ca = ca[k + 1]; a.cc = cc[k + 1];
+    a.omega = 2.0 / 3.0;
+    { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(epi, a, nb, c.stream)); }
+    x = xo;
+  }
+}
+
+// One SSP-RK3 step: stage inputs st[0..2] (st[0].q holds q^n), warm start
+// Sin, output state into (qout, invrout) (may alias st[0].q: pointwise).
+static void step_forward(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf st[3], const double* Sin, double* const qout[4],
+                         double* invrout, double* xa, double* xb, double* dbuf) {
+  const int nb = P.ntiles();
+  const bool apos = any_alpha_pos(P);
+  const double c0s[3] = {0.0, 3.0 / 4, 1.0 / 3}, c1s[3] = {1.0, 1.0 / 4, 2.0 / 3}, c2s[3] = {1.0, 1.0 / 4, 2.0 / 3};
+  const double* sprev = Sin;
+  for (int s = 0; s < 3; ++s) {
+    if (apos) stage_solve(c, P, o, st[s], sprev, xa, xb, dbuf);
+    HypArgs2D h;
+    std::memset(&h, 0, sizeof(h));
+    h.tiles = P.d_tiles; h.inst = P.d_inst; h.B = P.B;
+    for (int v = 0; v < 4; ++v) { h.q[v] = st[s].q[v]; h.qn[v] = st[0].q[v]; }
+    h.invr = st[s].invr;
+    h.S = st[s].Sout;
+    h.c0 = c0s[s]; h.c1 = c1s[s]; h.c2 = c2s[s];
+    for (int v = 0; v < 4; ++v) h.qo[v] = s < 2 ? st[s + 1].q[v] : qout[v];
+    h.invro = s < 2 ? st[s + 1].invr : invrout;
+    h.status = c.d_status;
+    { LaunchScope ls(c, KID_HYP); NP_DISPATCH(P.np, launch_k2_hyp_rk<NPV>(h, nb, c.stream)); }
+    sprev = st[s].Sout;
+  }
+}
+
+static void check_status(Ctx& c) {
+  int st = 0;
+  cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
+  cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
+  if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
+}
+
+static void check_alpha_uniform(const Plan2D& P) {
+  if (any_alpha_pos(P) && !all_alpha_pos(P)) throw Error(1, "a batch must have alpha > 0 for all instances or for none");
+}
+
+void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_steps, const Solve2DOpts& o) {
+  check_alpha_uniform(P);
+  const long long NG = P.NG;
+  const bool apos = any_alpha_pos(P);
+  double* scratch = c.ws.dbl("fwd:stages", (size_t)NG * 3 * STAGE_FIXED_FIELDS);
+  StageBuf st[3];
+  for (int s = 0; s < 3; ++s) st[s] = stage_from(scratch + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false);
+  double* xa = c.ws.dbl("fwd:xa", NG);
+  double* xb = c.ws.dbl("fwd:xb", NG);
+  double* db = c.ws.dbl("fwd:d", NG);
+  for (int v = 0; v < 4; ++v) st[0].q[v] = q[v];
+  recip(c, q[2], st[0].invr, NG);
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  if (!apos) cuda_check(cudaMemsetAsync(Sig, 0, NG * sizeof(double), c.stream), "zero Sigma");
+  // Sigma ping-pong: the stage-3 output of step s is the warm start of step s+1.
+  double* sig_cur = Sig;
+  for (int s = 0; s < n_steps; ++s) {
+    for (int k = 0; k < 3; ++k) st[k].Sout = !apos ? Sig : ((k % 2 == 0) ? c.ws.dbl("fwd:sA", NG) : c.ws.dbl("fwd:sB", NG));
+    step_forward(c, P, o, st, sig_cur, q, st[0].invr, xa, xb, db);
+    if (apos) {
+      cuda_check(cudaMemcpyAsync(Sig, st[2].Sout, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Sigma copy");
+      sig_cur = Sig;
+    }
+  }
+  check_status(c);
+}
+
+void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o) {
+  const long long NG = P.NG;
+  if (!any_alpha_pos(P)) return;
+  check_alpha_uniform(P);
+  double* scratch = c.ws.dbl("sol:stage", (size_t)NG * STAGE_FIXED_FIELDS);
+  StageBuf st = stage_from(scratch, NG, o, true, false);
+  for (int v = 0; v < 4; ++v) st.q[v] = const_cast<double*>(q[v]);
+  recip(c, q[2], st.invr, NG);
+  double* x0 = c.ws.dbl("sol:x0", NG);
+  cuda_check(cudaMemcpyAsync(x0, Sig, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "x0 copy");
+  st.Sout = Sig;
+  stage_solve(c, P, o, st, x0, c.ws.dbl("sol:xa", NG), c.ws.dbl("sol:xb", NG), c.ws.dbl("sol:d", NG));
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void hyperbolic_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], const double* Sig, double* const k[4]) {
+  const long long NG = P.NG;
+  double* ir = c.ws.dbl("rhs:invr", NG);
+  recip(c, q[2], ir, NG);
+  HypArgs2D h;
+  std::memset(&h, 0, sizeof(h));
+  h.tiles = P.d_tiles; h.inst = P.d_inst; h.B = P.B;
+  for (int v = 0; v < 4; ++v) { h.q[v] = q[v]; h.qn[v] = q[v]; h.k_out[v] = k[v]; h.qo[v] = nullptr; }
+  h.invr = ir; h.S = Sig;
+  h.c0 = 0.0; h.c1 = 1.0; h.c2 = 0.0;
+  h.status = nullptr;
+  { LaunchScope ls(c, KID_HYP); NP_DISPATCH(P.np, launch_k2_hyp_rk<NPV>(h, P.ntiles(), c.stream)); }
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, double* y) {
+  const long long NG = P.NG;
+  double* scratch = c.ws.dbl("sip:stage", (size_t)NG * STAGE_FIXED_FIELDS);
+  Solve2DOpts o;
+  StageBuf st = stage_from(scratch, NG, o, true, false);
+  double* zeros = c.ws.dbl("sip:zero", NG);
+  cuda_check(cudaMemsetAsync(zeros, 0, NG * sizeof(double), c.stream), "zero");
+  st.q[0] = zeros; st.q[1] = zeros; st.q[2] = const_cast<double*>(rho); st.q[3] = zeros;
+  recip(c, rho, st.invr, NG);
+  SetupArgs2D sa;
+  sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
+  sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
+  sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = nullptr;
+  { LaunchScope ls(c, KID_SETUP); NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, P.ntiles(), c.stream)); }
+  ApplyArgs2D a;
+  std::memset(&a, 0, sizeof(a));
+  a.tiles = P.d_tiles; a.inst = P.d_inst; a.B = P.B;
+  a.x = x; a.cm = st.cm; a.ckx = st.ckx; a.cky = st.cky; a.cpx = st.cpx; a.cpy = st.cpy; a.b = st.b; a.cinvM = st.cinvM;
+  a.y_out = y;
+  { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_RESID, a, P.ntiles(), c.stream)); }
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+// ------------------------------------------------------------------------------------------
+// Objective and adjoint
+// ------------------------------------------------------------------------------------------
+static void inst_sums(Ctx& c, const Plan2D& P, const double* f, double* out_dev) {
+  const int ni = (int)P.inst.size();
+  std::vector<long long> off(ni), cnt(ni);
+  for (int i = 0; i < ni; ++i) { off[i] = P.inst[i].off; cnt[i] = P.inst_nodes[i]; }
+  long long* d = static_cast<long long*>(c.ws.get("sum:meta", sizeof(long long) * 2 * ni));
+  cuda_check(cudaMemcpyAsync(d, off.data(), sizeof(long long) * ni, cudaMemcpyHostToDevice, c.stream), "meta");
+  cuda_check(cudaMemcpyAsync(d + ni, cnt.data(), sizeof(long long) * ni, cudaMemcpyHostToDevice, c.stream), "meta");
+  LaunchScope ls(c, KID_OTHER);
+  k_inst_sum<<<ni, 256, 0, c.stream>>>(f, d, d + ni, out_dev);
+}
+
+static ObjArgs2D obj_args(const Plan2D& P, const double* const q[4], int objective, const double* prm) {
+  ObjArgs2D a;
+  std::memset(&a, 0, sizeof(a));
+  a.inst = P.d_inst; a.ninst = (int)P.inst.size(); a.B = P.B;
+  for (int v = 0; v < 4; ++v) a.q[v] = q[v];
+  a.obj = objective;
+  for (int k = 0; k < 4; ++k) a.prm[k] = prm ? prm[k] : 0.0;
+  a.NG = P.NG;
+  return a;
+}
+
+// J per instance (device array out, ninst) from the final state q.
+static void objective_value(Ctx& c, const Plan2D& P, const double* const q[4], int objective, const double* prm, double* J_host,
+                            double* s1_dev, double* s2_dev) {
+  const long long NG = P.NG;
+  const int ni = (int)P.inst.size();
+  ObjArgs2D a = obj_args(P, q, objective, prm);
+  a.j1 = c.ws.dbl("obj:j1", NG);
+  a.j2 = c.ws.dbl("obj:j2", NG);
+  { LaunchScope ls(c, KID_OTHER); k2_obj_nodes<<<grid_for(NG), 256, 0, c.stream>>>(a); }
+  inst_sums(c, P, a.j1, s1_dev);
+  inst_sums(c, P, a.j2, s2_dev);
+  std::vector<double> s1(ni), s2(ni);
+  cuda_check(cudaMemcpyAsync(s1.data(), s1_dev, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream), "J readback");
+  cuda_check(cudaMemcpyAsync(s2.data(), s2_dev, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream), "J readback");
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+  for (int i = 0; i < ni; ++i) J_host[i] = objective == OBJ_KINETIC_ENERGY ? s1[i] / s2[i] : s1[i];
+}
+
+static void check_objective(int objective) {
+  if (objective < 0 || objective > OBJ_WINDOW_RHO2) throw Error(1, "Unknown objective");
+}
+static void check_solver(const Solve2DOpts& o) {
+  if (o.solver < 0 || o.solver > 2) throw Error(1, "Unknown solver (use :pcg, :jacobi, or :chebyshev)");
+  if (o.n_iter < 1) throw Error(1, "n_iter must be >= 1");
+}
+
+void objective2d(Ctx& c, const Plan2D& P, double* const q[4], int n_steps, const Solve2DOpts& o, int objective,
+                 const double* prm, double* J) {
+  check_objective(objective);
+  check_solver(o);
+  double* Sig = c.ws.dbl("obj:Sig", P.NG);
+  cuda_check(cudaMemsetAsync(Sig, 0, P.NG * sizeof(double), c.stream), "zero Sigma");
+  forward2d(c, P, q, Sig, n_steps, o);
+  const double* qc[4] = {q[0], q[1], q[2], q[3]};
+  objective_value(c, P, qc, objective, prm, J, c.ws.dbl("obj:s1", P.inst.size()), c.ws.dbl("obj:s2", P.inst.size()));
+}
+
+void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, const Solve2DOpts& o, int objective,
+               const double* prm, double* J, double* const dq0[4], double* dgamma, double* dalpha) {
+  check_objective(objective);
+  check_solver(o);
+  check_alpha_uniform(P);
+  if (n_steps < 0) throw Error(1, "n_steps must be >= 0");
+  const long long NG = P.NG;
+  const int ni = (int)P.inst.size();
+  const bool apos = any_alpha_pos(P);
+  const int F = stage_fields(o, apos);
+  // scratch for untaped steps and final state
+  double* scr = c.ws.dbl("adj:scr", (size_t)NG * 3 * STAGE_FIXED_FIELDS);
+  StageBuf ust[3];
+  for (int s = 0; s < 3; ++s) ust[s] = stage_from(scr + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false);
+  double* xa = c.ws.dbl("adj:xa", NG);
+  double* xb = c.ws.dbl("adj:xb", NG);
+  double* dbuf = c.ws.dbl("adj:d", NG);
+  double* qend = c.ws.dbl("adj:qend", 5 * NG);
+  double* qendp[4] = {qend, qend + NG, qend + 2 * NG, qend + 3 * NG};
+  double* sigA = c.ws.dbl("adj:sigA", NG);
+  double* sigB = c.ws.dbl("adj:sigB", NG);
+  double* sig0 = c.ws.dbl("adj:sig0", NG);
+  double* rb = c.ws.dbl("adj:rev", (size_t)NG * 24);
+  double* gnode = c.ws.dbl("adj:gnode", NG);
+  double* anode = c.ws.dbl("adj:anode", NG);
+  c.ws.dbl("obj:j1", NG);
+  c.ws.dbl("obj:j2", NG);
+  // ---- memory plan: the longest segment (steps taped at once) that fits
+  // next to the checkpoints (q, 1/rho, Sigma at every segment start).
+  const size_t step_bytes = (size_t)3 * F * NG * sizeof(double);
+  const size_t ckpt_bytes = (size_t)6 * NG * sizeof(double);
+  size_t budget = c.tape_budget;
+  if (budget == 0) {
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    const size_t reserve = (size_t)1 << 30;
+    budget = fr > reserve ? (size_t)((fr - reserve) * 0.95) : 0;
+  }
+  const int nsteps_eff = std::max(n_steps, 1);
+  int seg = 0;
+  for (int sg = nsteps_eff; sg >= 1; --sg) {
+    const size_t nseg = (size_t)((nsteps_eff + sg - 1) / sg);
+    if ((size_t)sg * step_bytes + nseg * ckpt_bytes <= budget) { seg = sg; break; }
+  }
+  if (seg < 1) throw Error(5, "device memory too small for one taped step of this batch");
+  const int n_seg = (nsteps_eff + seg - 1) / seg;
+  double* ckpt = c.ws.dbl("adj:ckpt", (size_t)n_seg * 6 * NG);
+  double* tape = c.ws.dbl("adj:tape", (size_t)seg * 3 * F * NG);
+  auto slot = [&](int local_step, int stage) {
+    return stage_from(tape + ((long long)local_step * 3 + stage) * F * NG, NG, o, apos, true);
+  };
+
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  cuda_check(cudaMemsetAsync(sig0, 0, NG * sizeof(double), c.stream), "zero Sigma");
+  // untaped state: ust[0].q / invr hold q^s
+  for (int v = 0; v < 4; ++v)
+    cuda_check(cudaMemcpyAsync(ust[0].q[v], q0[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "q0 copy");
+  recip(c, ust[0].q[2], ust[0].invr, NG);
+  if (!apos) {
+    for (int s = 0; s < 3; ++s) cuda_check(cudaMemsetAsync(ust[s].Sout, 0, NG * sizeof(double), c.stream), "zero Sout");
+  }
+  const double* sig_cur = sig0;
+
+  // Runs steps [s0, s1) taped into slots 0.. (state enters in slot 0 of s0),
+  // the final step's output goes to qend (or the next step's slot).
+  auto taped_range = [&](int s0, int s1, const double* sig_in) {
+    const double* sg = sig_in;
+    for (int s = s0; s < s1; ++s) {
+      StageBuf st[3] = {slot(s - s0, 0), slot(s - s0, 1), slot(s - s0, 2)};
+      if (!apos) for (int k = 0; k < 3; ++k) cuda_check(cudaMemsetAsync(st[k].Sout, 0, NG * sizeof(double), c.stream), "zero Sout");
+      double* qo[4];
+      double* iro;
+      if (s + 1 < s1) { StageBuf nx = slot(s + 1 - s0, 0); for (int v = 0; v < 4; ++v) qo[v] = nx.q[v]; iro = nx.invr; }
+      else { for (int v = 0; v < 4; ++v) qo[v] = qendp[v]; iro = qend + 4 * NG; }
+      step_forward(c, P, o, st, sg, qo, iro, xa, xb, dbuf);
+      sg = st[2].Sout;
+    }
+    return sg;
+  };
+
+  // ---- forward: untaped segments with checkpoints, last segment taped
+  for (int k = 0; k < n_seg; ++k) {
+    const int s0 = k * seg, s1 = std::min(n_steps, (k + 1) * seg);
+    double* ck = ckpt + (long long)k * 6 * NG;
+    for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(ck + v * NG, ust[0].q[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "ckpt");
+    cuda_check(cudaMemcpyAsync(ck + 4 * NG, ust[0].invr, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "ckpt");
+    cuda_check(cudaMemcpyAsync(ck + 5 * NG, sig_cur, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "ckpt");
+    if (k == n_seg - 1) {
+      if (s1 > s0) {
+        StageBuf first = slot(0, 0);
+        for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(first.q[v], ust[0].q[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "seg in");
+        cuda_check(cudaMemcpyAsync(first.invr, ust[0].invr, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "seg in");
+        taped_range(s0, s1, sig_cur);
+      } else {
+        for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(qendp[v], ust[0].q[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "q end");
+      }
+    } else {
+      for (int s = s0; s < s1; ++s) {
+        if (apos) for (int kk = 0; kk < 3; ++kk) ust[kk].Sout = (kk % 2 == 0) ? sigA : sigB;
+        step_forward(c, P, o, ust, sig_cur, ust[0].q, ust[0].invr, xa, xb, dbuf);
+        if (apos) {  // carried Sigma lives in sig0 (its zero start is only read by step 0)
+          cuda_check(cudaMemcpyAsync(sig0, ust[2].Sout, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Sigma carry");
+          sig_cur = sig0;
+        }
+      }
+    }
+  }
+  // ---- objective and its gradient at the final state
+  const double* qf[4] = {qendp[0], qendp[1], qendp[2], qendp[3]};
+  double* s1d = c.ws.dbl("adj:s1", ni);
+  double* s2d = c.ws.dbl("adj:s2", ni);
+  objective_value(c, P, qf, objective, prm, J, s1d, s2d);
+  // reverse buffers
+  double* QB[4]; double* QN[4]; double* Q2b[4]; double* Q1b[4];
+  for (int v = 0; v < 4; ++v) { QB[v] = rb + v * NG; QN[v] = rb + (4 + v) * NG; Q2b[v] = rb + (8 + v) * NG; Q1b[v] = rb + (12 + v) * NG; }
+  double* Sb = rb + 16 * NG;
+  double* U[2] = {rb + 17 * NG, rb + 18 * NG};
+  double* db = rb + 19 * NG;
+  double* bb = rb + 20 * NG;
+  double* Mb = rb + 21 * NG;
+  double* Zm = rb + 22 * NG;
+  double* Zs = rb + 23 * NG;
+  {
+    ObjArgs2D a = obj_args(P, qf, objective, prm);
+    a.s1 = s1d; a.s2 = s2d;
+    for (int v = 0; v < 4; ++v) a.qb[v] = QB[v];
+    a.gb = gnode;   // initialises the per-node gamma accumulator
+    LaunchScope ls(c, KID_OTHER);
+    k2_obj_grad<<<grid_for(NG), 256, 0, c.stream>>>(a);
+  }
+  cuda_check(cudaMemsetAsync(Sb, 0, NG * sizeof(double), c.stream), "zero Sb");
+  cuda_check(cudaMemsetAsync(anode, 0, NG * sizeof(double), c.stream), "zero anode");
+  std::vector<double> ca, cc;
+  cheb_coeffs(P.B, o.n_iter, ca, cc);
+  const int srev = !apos ? SREV_NONE : (o.solver == SOLVER_CHEBYSHEV ? SREV_CHEB : SREV_JACOBI);
+  const int nb = P.ntiles();
+  const double c0s[3] = {0.0, 3.0 / 4, 1.0 / 3}, c1s[3] = {1.0, 1.0 / 4, 2.0 / 3}, c2s[3] = {1.0, 1.0 / 4, 2.0 / 3};
+
+  auto reverse_step = [&](int local) {
+    StageBuf st[3] = {slot(local, 0), slot(local, 1), slot(local, 2)};
+    for (int s = 2; s >= 0; --s) {
+      HypRevArgs2D h;
+      std::memset(&h, 0, sizeof(h));
+      h.tiles = P.d_tiles; h.inst = P.d_inst; h.B = P.B;
+      for (int v = 0; v < 4; ++v) {
+        h.q[v] = st[s].q[v];
+        h.A[v] = s == 2 ? QB[v] : (s == 1 ? Q2b[v] : Q1b[v]);
+        h.Qn[v] = QN[v];
+        h.Qs[v] = s == 2 ? Q2b[v] : (s == 1 ? Q1b[v] : QN[v]);
+      }
+      h.invr = st[s].invr; h.S = st[s].Sout;
+      h.c0 = c0s[s]; h.c1 = c1s[s]; h.c2 = c2s[s];
+      h.qn_mode = s == 2 ? 1 : (s == 1 ? 2 : 0);
+      h.qs_add = s == 0 ? 1 : 0;
+      h.Sb = Sb; h.Sb_add = 1;
+      h.gnode = gnode;
+      h.srev = srev;
+      h.cinvM = st[s].cinvM;
+      h.r_last = apos ? st[s].rk[o.n_iter - 1] : nullptr;
+      h.u_out = U[0]; h.db = db; h.Mb = Mb;
+      h.ca = ca[o.n_iter]; h.cc = cc[o.n_iter]; h.omega = 2.0 / 3.0;
+      { LaunchScope ls(c, KID_HYP_REV); NP_DISPATCH(P.np, launch_k2_hyp_rev<NPV>(h, nb, c.stream)); }
+      if (!apos) continue;
+      int cur = 0;
+      for (int m = o.n_iter - 1; m >= 0; --m) {
+        ApplyRevArgs2D r;
+        std::memset(&r, 0, sizeof(r));
+        r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
+        r.u = U[cur]; r.xk = st[s].xk[m];
+        r.cm = st[s].cm; r.ckx = st[s].ckx; r.cky = st[s].cky; r.cpx = st[s].cpx; r.cpy = st[s].cpy; r.cinvM = st[s].cinvM;
+        r.invr = st[s].invr;
+        r.xb = Sb; r.bb = bb; r.Zm = Zm; r.Zs = Zs;
+        r.first = (m == o.n_iter - 1) ? 1 : 0;
+        r.zscale = -1.0;
+        r.has_next = m > 0 ? 1 : 0;
+        r.r_prev = m > 0 ? st[s].rk[m - 1] : nullptr;
+        r.u_out = U[1 - cur]; r.db = db; r.Mb = Mb;
+        r.ca = ca[m > 0 ? m : 1]; r.cc = cc[m > 0 ? m : 1]; r.omega = 2.0 / 3.0;
+        { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(srev, r, nb, c.stream)); }
+        cur = 1 - cur;
+      }
+      SetupRevArgs2D sr;
+      std::memset(&sr, 0, sizeof(sr));
+      sr.tiles = P.d_tiles; sr.inst = P.d_inst; sr.B = P.B;
+      sr.mx = st[s].q[0]; sr.my = st[s].q[1]; sr.invr = st[s].invr;
+      sr.b = st[s].b; sr.cm = st[s].cm; sr.cM = st[s].cM;
+      sr.bb = bb; sr.Mb = Mb; sr.Zm = Zm; sr.Zs = Zs;
+      double* const* QsP = s == 2 ? Q2b : (s == 1 ? Q1b : QN);
+      sr.Qs[0] = QsP[0]; sr.Qs[1] = QsP[1]; sr.Qs[2] = QsP[2];
+      sr.anode = anode;
+      { LaunchScope ls(c, KID_SETUP_REV); NP_DISPATCH(P.np, launch_k2_setup_rev<NPV>(sr, nb, c.stream)); }
+    }
+    for (int v = 0; v < 4; ++v) std::swap(QB[v], QN[v]);
+  };
+
+  for (int k = n_seg - 1; k >= 0; --k) {
+    const int s0 = k * seg, s1 = std::min(n_steps, (k + 1) * seg);
+    if (s1 <= s0) continue;
+    if (k != n_seg - 1) {
+      // recompute the segment from its checkpoint, taped
+      const double* ck = ckpt + (long long)k * 6 * NG;
+      StageBuf first = slot(0, 0);
+      for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(first.q[v], ck + v * NG, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "restore");
+      cuda_check(cudaMemcpyAsync(first.invr, ck + 4 * NG, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "restore");
+      taped_range(s0, s1, ck + 5 * NG);
+    }
+    for (int s = s1 - 1; s >= s0; --s) reverse_step(s - s0);
+  }
+  for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(dq0[v], QB[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "dq0");
+  // per-instance parameter gradients
+  double* gsum = c.ws.dbl("adj:gsum", ni);
+  double* asum = c.ws.dbl("adj:asum", ni);
+  inst_sums(c, P, gnode, gsum);
+  inst_sums(c, P, anode, asum);
+  if (dgamma) cuda_check(cudaMemcpyAsync(dgamma, gsum, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream), "dgamma");
+  if (dalpha) cuda_check(cudaMemcpyAsync(dalpha, asum, sizeof(double) * ni, cudaMemcpyDeviceToHost, c.stream), "dalpha");
+  check_status(c);
+}
+
+// FP64 throughput probe: independent DFMA chains on every SM (roofline
+// denominator of this FP64-bound path). Returns TFLOP/s (2 flops per DFMA).
+__global__ void k_dfma_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == 1234.5) out[threadIdx.x] = s;  // never true; keeps the chains live
+}
+
+double probe_fp64_tflops(Ctx& c) {
+  int sms = 0;
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device), "attr");
+  double* d = c.ws.dbl("probe", 1024);
+  const int grid = sms * 4, tpb = 256, iters = 4096;
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "event");
+  cuda_check(cudaEventCreate(&e1), "event");
+  k_dfma_probe<<<grid, tpb, 0, c.stream>>>(d, 64, 1.0000001, 1e-9);
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0, c.stream);
+    k_dfma_probe<<<grid, tpb, 0, c.stream>>>(d, iters, 1.0000001, 1e-9);
+    cudaEventRecord(e1, c.stream);
+    cuda_check(cudaEventSynchronize(e1), "probe sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return 2.0 * 8.0 * iters * (double)grid * tpb / (best * 1e-3) / 1e12;
+}
+
+}  // namespace igrgpu

@@ -1,0 +1,45 @@
+// Definitions of the 2D launchers declared in igr2d_launch.h. Included once
+// per NP by igr2d_np<NP>.cu, which instantiates them explicitly.
+#pragma once
+#include "igr2d_launch.h"
+#include "igr2d_rev_kernels.cuh"
+
+namespace igrgpu {
+
+template <int NP> int threads2d() { return Tiling2D<NP>::NT; }
+template <int NP> void tile_shape2d(int* tx, int* ty) { *tx = Tiling2D<NP>::TX; *ty = Tiling2D<NP>::TY; }
+
+template <int NP> void launch_k2_setup(const SetupArgs2D& a, int nb, cudaStream_t s) {
+  k2_setup<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_apply(int epi, const ApplyArgs2D& a, int nb, cudaStream_t s) {
+  if (epi == EPI_CHEB) k2_apply<NP, EPI_CHEB><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else if (epi == EPI_JACOBI) k2_apply<NP, EPI_JACOBI><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else k2_apply<NP, EPI_RESID><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_hyp_rk(const HypArgs2D& a, int nb, cudaStream_t s) {
+  k2_hyp_rk<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_hyp_rev(const HypRevArgs2D& a, int nb, cudaStream_t s) {
+  k2_hyp_rev<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_apply_rev(int srev, const ApplyRevArgs2D& a, int nb, cudaStream_t s) {
+  if (srev == SREV_CHEB) k2_apply_rev<NP, SREV_CHEB><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else if (srev == SREV_JACOBI) k2_apply_rev<NP, SREV_JACOBI><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else k2_apply_rev<NP, SREV_NONE><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_setup_rev(const SetupRevArgs2D& a, int nb, cudaStream_t s) {
+  k2_setup_rev<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+
+#define IGR2D_INSTANTIATE(NP)                                                                        \
+  template int threads2d<NP>();                                                                      \
+  template void tile_shape2d<NP>(int*, int*);                                                        \
+  template void launch_k2_setup<NP>(const SetupArgs2D&, int, cudaStream_t);                          \
+  template void launch_k2_apply<NP>(int, const ApplyArgs2D&, int, cudaStream_t);                     \
+  template void launch_k2_hyp_rk<NP>(const HypArgs2D&, int, cudaStream_t);                           \
+  template void launch_k2_hyp_rev<NP>(const HypRevArgs2D&, int, cudaStream_t);                       \
+  template void launch_k2_apply_rev<NP>(int, const ApplyRevArgs2D&, int, cudaStream_t);              \
+  template void launch_k2_setup_rev<NP>(const SetupRevArgs2D&, int, cudaStream_t);
+
+}  // namespace igrgpu

@@ -1,0 +1,133 @@
+// Host engine shared by the C ABI: context, device workspace, 2D/1D problem
+// descriptions and drivers. Not part of the public interface (see
+// include/igr_gb300.h for that).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "igr_device.cuh"
+
+namespace igrgpu {
+
+// Error raised by the engine; converted to an int status at the C boundary.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+
+// Named, grow-only device buffers owned by a context. Reusing the same names
+// across calls keeps large tapes allocated between repeated gradient calls.
+class Workspace {
+ public:
+  ~Workspace();
+  void* get(const std::string& name, size_t bytes);
+  double* dbl(const std::string& name, size_t n) { return static_cast<double*>(get(name, n * sizeof(double))); }
+  void release_all();
+  size_t bytes() const;
+
+ private:
+  struct Buf { void* p = nullptr; size_t n = 0; };
+  std::map<std::string, Buf> bufs_;
+};
+
+// Kernel families timed by the optional per-launch CUDA-event profiler.
+enum KernelId { KID_SETUP = 0, KID_APPLY, KID_HYP, KID_HYP_REV, KID_APPLY_REV, KID_SETUP_REV, KID_TAN, KID_1D, KID_OTHER,
+                KID_COUNT };
+
+struct Profiler {
+  bool on = false;
+  struct Rec { int kid; long long nodes; cudaEvent_t a, b; };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Rec> recs;
+  size_t next = 0;
+  double ms[KID_COUNT] = {0};
+  long long count[KID_COUNT] = {0};
+  double nodes[KID_COUNT] = {0};
+  cudaEvent_t get();
+  void begin(cudaStream_t s, int kid, long long nodes);
+  void end(cudaStream_t s);
+  void harvest();   // synchronises, accumulates ms/count, recycles events
+  void reset();
+  ~Profiler();
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int* d_status = nullptr;      // device status word (DEV_* flags)
+  std::string err;
+  Workspace ws;
+  size_t tape_budget = 0;       // 0: derive from free device memory
+  long long launches = 0;       // kernels launched by the last call (host-side count)
+  long long cur_nodes = 0;      // nodes of the plan being executed (profiler bookkeeping)
+  Profiler prof;
+};
+
+// Launch bookkeeping: count (and, when profiling, time) one kernel launch.
+struct LaunchScope {
+  Ctx& c;
+  LaunchScope(Ctx& cc, int kid) : c(cc) { if (c.prof.on) c.prof.begin(c.stream, kid, c.cur_nodes); }
+  ~LaunchScope() { ++c.launches; if (c.prof.on) c.prof.end(c.stream); }
+};
+
+// Basis arrays as the reference stores them: xi, w (n) and D (n x n, Julia
+// column-major, D[i + k*n] = D[i,k]).
+BasisDev make_basis_dev(int p, const double* xi, const double* w, const double* D_colmajor);
+
+enum Solver { SOLVER_PCG = 0, SOLVER_JACOBI = 1, SOLVER_CHEBYSHEV = 2 };
+enum Objective2D { OBJ_L2_DENSITY = 0, OBJ_L2_PRESSURE = 1, OBJ_KINETIC_ENERGY = 2, OBJ_WINDOWED_KE = 3,
+                   OBJ_WEIGHTED_MOMENTUM = 4, OBJ_WINDOW_RHO2 = 5, OBJ_INTERVAL_RHO = 6 };
+
+// One 2D instance as described by the caller.
+struct Inst2DDesc {
+  int nex, ney;
+  double lx, ly, gamma, alpha, dt;
+};
+
+// Device-side plan of a batch group: instances, tiles, node counts.
+struct Plan2D {
+  BasisDev B;
+  int np = 4;
+  std::vector<Inst2D> inst;
+  std::vector<Tile2D> tiles;
+  std::vector<long long> inst_nodes;
+  long long NG = 0;
+  Inst2D* d_inst = nullptr;
+  Tile2D* d_tiles = nullptr;
+  int ntiles() const { return (int)tiles.size(); }
+};
+
+Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& insts, const std::string& tag);
+
+// Drivers. Field pointers are device pointers to NG doubles each, in the
+// instance-major Julia layout.
+struct Solve2DOpts { int n_iter = 10; int solver = SOLVER_PCG; };
+
+// In-place forward over n_steps fixed steps (dt per instance), Sigma in/out
+// (warm start carried across stages and steps as forward.jl:41-75 does).
+void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_steps, const Solve2DOpts& o);
+// One elliptic solve (solve_elliptic!, elliptic.jl:413-427) with Sigma as warm start.
+void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o);
+// One hyperbolic RHS evaluation (compute_hyperbolic_rhs!, hyperbolic.jl:27).
+void hyperbolic_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], const double* Sig, double* const k[4]);
+// y = A x (apply_sip!, elliptic.jl:30).
+void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, double* y);
+
+// Gradient of the objective after n_steps fixed steps (enzyme_adjoint_ic,
+// enzyme_adjoint.jl:270): J[inst], dq0 (4 fields), dgamma[inst], dalpha[inst].
+void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, const Solve2DOpts& o, int objective,
+               const double* obj_params, double* J, double* const dq0[4], double* dgamma, double* dalpha);
+
+double probe_fp64_tflops(Ctx& c);
+
+// Objective value only (the primal of the adjoint call), final state in q.
+void objective2d(Ctx& c, const Plan2D& P, double* const q[4], int n_steps, const Solve2DOpts& o, int objective,
+                 const double* obj_params, double* J);
+
+}  // namespace igrgpu

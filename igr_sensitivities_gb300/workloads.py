@@ -1,0 +1,79 @@
+"""Host-side problem set-up: initial conditions and time steps.
+
+Mirrors the builders of IGR_adjoints_2d/initial_conditions.jl and
+IGR_adjoints_1d/initial_conditions.jl that the tests use, plus the seeded
+Gaussian-pulse family the benchmark workloads are drawn from (ambient gas at
+rest, rho = 1, p = 0.1 + sum_k A_k exp(-|x - c_k|^2 / w^2), E = p/(gamma-1),
+the form of build_sedov_blast_ic!, initial_conditions.jl:136-150). Seeds feed
+a SplitMix64 generator so that the same seed gives the same instance on every
+machine.
+"""
+import numpy as np
+
+MASK64 = (1 << 64) - 1
+
+
+class SplitMix64:
+    def __init__(self, seed):
+        self.s = seed & MASK64
+
+    def next_u64(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & MASK64
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+        return z ^ (z >> 31)
+
+    def uniform(self, lo=0.0, hi=1.0):
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
+
+
+def seed_for(config_id, instance):
+    return 0x16150000 + config_id * (1 << 20) + instance
+
+
+def pulse_ic_2d(mesh, gamma, amps, centers, width, p_bg=0.1):
+    """rho = 1, u = 0, p = p_bg + sum A exp(-r^2/width^2) (periodic images ignored)."""
+    x, y = mesh.x, mesh.y
+    p = np.full(x.shape, p_bg)
+    for A, (xc, yc) in zip(amps, centers):
+        p = p + A * np.exp(-((x - xc) ** 2 + (y - yc) ** 2) / width ** 2)
+    rho = np.ones(x.shape)
+    z = np.zeros(x.shape)
+    return (np.asfortranarray(z), np.asfortranarray(z.copy()), np.asfortranarray(rho), np.asfortranarray(p / (gamma - 1)))
+
+
+def seeded_pulses_2d(mesh, gamma, seed, n_pulses=3, width=0.03, amp=(1.0, 10.0), lo=0.2, hi=0.8):
+    rng = SplitMix64(seed)
+    amps = [rng.uniform(*amp) for _ in range(n_pulses)]
+    centers = [(rng.uniform(lo, hi), rng.uniform(lo, hi)) for _ in range(n_pulses)]
+    return pulse_ic_2d(mesh, gamma, amps, centers, width)
+
+
+def seeded_window(seed):
+    """Square window (x0, y0, side) for the window_rho2 objective."""
+    rng = SplitMix64(seed ^ 0x5DEECE66D)
+    side = rng.uniform(0.2, 0.4)
+    return (rng.uniform(0.0, 0.6), rng.uniform(0.0, 0.6), side)
+
+
+def taylor_green_ic(mesh, gamma, A):
+    """build_taylor_green_ic!, IGR_adjoints_2d/initial_conditions.jl:105-121."""
+    cx = 2 * np.pi * mesh.x / mesh.Lx
+    cy = 2 * np.pi * mesh.y / mesh.Ly
+    ux = A * np.sin(cx) * np.cos(cy)
+    uy = -A * np.cos(cx) * np.sin(cy)
+    rho = np.ones(mesh.x.shape)
+    return (np.asfortranarray(rho * ux), np.asfortranarray(rho * uy), np.asfortranarray(rho),
+            np.asfortranarray(1.0 / (gamma - 1) + 0.5 * rho * (ux ** 2 + uy ** 2)))
+
+
+def max_wavespeed_2d(mux, muy, rho, E, gamma):
+    P = (gamma - 1) * (E - (mux ** 2 + muy ** 2) / (2 * rho))
+    c = np.sqrt(gamma * P / rho)
+    return float(max(np.max(np.abs(mux / rho) + c), np.max(np.abs(muy / rho) + c)))
+
+
+def cfl_dt_2d(mesh, p, q, gamma, cfl):
+    """dt = CFL min(dx, dy) / ((2p+1) max wavespeed) (IGR_adjoints_2d/tests/run_euler_test.jl:100-106)."""
+    return cfl * min(mesh.dx, mesh.dy) / ((2 * p + 1) * max_wavespeed_2d(*q, gamma))

@@ -1,0 +1,145 @@
+/*
+ * igr_gb300.h — C ABI of the GB300 engine for the IGR-regularised Euler
+ * forward map and its derivatives (f-t-s/IGR_sensitivities).
+ *
+ * Every entry point is a drop-in for one function of the reference's Julia
+ * module API (IGRAdjoints2D / IGRAdjoints1D); the file:line of the function
+ * it replaces is given beside it. A Julia `ccall` binding for each is shown in
+ * INTEGRATION.md.
+ *
+ * Conventions
+ *  - Arrays are caller-owned host arrays of double in the reference's Julia
+ *    column-major layout: 2D fields are (n_p, n_p, N_ex, N_ey) with the x-node
+ *    index fastest; 1D fields are (n_p, N_e). Entry points ending in `_dev`
+ *    take device pointers instead.
+ *  - The basis is passed as the reference stores it in DGBasis
+ *    (IGR_adjoints_2d/basis.jl:7-12): xi and w of length p+1 and D as a
+ *    (p+1) x (p+1) column-major matrix, so results use the caller's exact
+ *    node and weight values. p must be 1..4.
+ *  - Solvers: 0 = :pcg, 1 = :jacobi, 2 = :chebyshev (elliptic.jl:417-425).
+ *  - Every function returns an igr_status; on failure igr_last_error(ctx)
+ *    holds a message. Unknown solver/objective symbols give IGR_EINVAL with
+ *    the reference's error text.
+ *  - A context owns a CUDA stream and device buffers; it is not thread-safe.
+ *    Use one context per host thread.
+ */
+#ifndef IGR_GB300_H
+#define IGR_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  IGR_OK = 0,
+  IGR_EINVAL = 1,      /* bad argument: unknown solver/objective, bad sizes */
+  IGR_EUNSUPPORTED = 2,/* valid request this build does not implement */
+  IGR_ENONFINITE = 3,  /* NaN/Inf or rho <= 0 appeared in the state */
+  IGR_ECUDA = 4,       /* CUDA runtime error */
+  IGR_ENOMEM = 5,      /* device memory too small */
+  IGR_ETIMEOUT = 6     /* a bounded device-side wait gave up */
+} igr_status;
+
+typedef struct igr_ctx igr_ctx;
+
+/* Objectives of enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:398-412)
+ * plus nodal-window extensions. */
+typedef enum {
+  IGR_OBJ_L2_DENSITY = 0,          /* :l2_density, enzyme_adjoint.jl:206 */
+  IGR_OBJ_L2_PRESSURE = 1,         /* :l2_pressure, enzyme_adjoint.jl:242 */
+  IGR_OBJ_KINETIC_ENERGY = 2,      /* :kinetic_energy, enzyme_adjoint.jl:279 */
+  IGR_OBJ_WINDOWED_KE = 3,         /* :windowed_kinetic_energy, enzyme_adjoint.jl:318 */
+  IGR_OBJ_WEIGHTED_MOMENTUM = 4,   /* :weighted_momentum, enzyme_adjoint.jl:357 */
+  IGR_OBJ_WINDOW_RHO2 = 5,         /* sum w_i w_j Jx Jy rho^2 over nodes inside the square
+                                      [x0, x0+s] x [y0, y0+s]; obj_params = {x0, y0, s} */
+  IGR_OBJ_INTERVAL_RHO = 6         /* 1D: sum w_i J rho over nodes in [a, b]; obj_params = {a, b} */
+} igr_objective;
+
+/* Discretisation of one 2D instance: DGBasis + CartesianMesh2D
+ * (IGR_adjoints_2d/basis.jl:7-12, mesh.jl:89-125). */
+typedef struct {
+  int p;
+  int n_ex, n_ey;
+  double lx, ly;
+  const double* xi; /* p+1 */
+  const double* w;  /* p+1 */
+  const double* D;  /* (p+1)^2, column-major */
+} igr_disc2d;
+
+/* ---- context -------------------------------------------------------------- */
+int igr_ctx_create(int device, igr_ctx** out);
+int igr_ctx_destroy(igr_ctx* ctx);
+const char* igr_last_error(const igr_ctx* ctx);
+/* Device bytes the adjoint may use for its tape; 0 (default) = most of the
+ * free memory. A smaller budget turns on segment checkpointing. */
+int igr_set_tape_budget(igr_ctx* ctx, size_t bytes);
+/* Kernels launched by the last call on this context. */
+int igr_last_launch_count(const igr_ctx* ctx, long long* out);
+
+/* Per-launch CUDA-event timing of the engine's kernel families (no reference
+ * counterpart; used by the benchmark for live kernel durations). Families:
+ * 0 setup, 1 SIP apply (solver iteration), 2 hyperbolic+RK, 3 hyperbolic
+ * reverse, 4 SIP apply reverse, 5 setup reverse, 6 tangent, 7 1D, 8 other. */
+int igr_profile_enable(igr_ctx* ctx, int on);
+int igr_profile_reset(igr_ctx* ctx);
+int igr_profile_read(igr_ctx* ctx, int kernel_family, double* total_ms, long long* launches);
+/* Nodes processed by the timed launches of a family (sum over launches). */
+int igr_profile_nodes(igr_ctx* ctx, int kernel_family, double* nodes);
+/* Measured FP64 FMA throughput of the device in TFLOP/s (the roofline
+ * denominator of this FP64-bound path; no reference counterpart). */
+int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops);
+
+/* ---- 2D ------------------------------------------------------------------- */
+
+/* run_forward! (IGR_adjoints_2d/forward.jl:41-75): in place, Sigma zeroed at
+ * entry, n_steps = ceil(T/dt), dt = T/n_steps, final solve at T when alpha > 0. */
+int igr2d_run_forward(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
+                      int n_iter, int solver, double* mux, double* muy, double* rho, double* E, double* sigma);
+
+/* enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:428-454): J and
+ * dJ/dq0 of the objective after n_steps SSP-RK3 steps of size dt (no dt
+ * re-rounding, Sigma warm start from zero). dgamma/dalpha (may be NULL) are
+ * dJ/dgamma and dJ/dalpha, which the reference does not compute. */
+int igr2d_adjoint_ic(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_steps, double dt,
+                     int n_iter, int solver, int objective, const double* obj_params, const double* mux0,
+                     const double* muy0, const double* rho0, const double* E0, double* J, double* dmux0,
+                     double* dmuy0, double* drho0, double* dE0, double* dgamma, double* dalpha);
+
+/* Batched enzyme_adjoint_ic: n_inst instances on one mesh, each with its own
+ * gamma, alpha, dt and initial state. q0 and dq0 are [n_inst][4][N] with the
+ * variables ordered (mux, muy, rho, E); J, dgamma, dalpha are [n_inst]. */
+int igr2d_adjoint_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                        const double* dts, int n_steps, int n_iter, int solver, int objective,
+                        const double* obj_params, const double* q0, double* J, double* dq0, double* dgamma,
+                        double* dalpha);
+/* Same with q0 and dq0 in device memory (J, dgamma, dalpha stay host arrays). */
+int igr2d_adjoint_batch_dev(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas,
+                            const double* alphas, const double* dts, int n_steps, int n_iter, int solver,
+                            int objective, const double* obj_params, const double* q0_dev, double* J,
+                            double* dq0_dev, double* dgamma, double* dalpha);
+
+/* Primal of the objective only (the `result[2]` of enzyme_adjoint_ic). */
+int igr2d_objective(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_steps, double dt,
+                    int n_iter, int solver, int objective, const double* obj_params, double* mux, double* muy,
+                    double* rho, double* E, double* J);
+
+/* apply_sip! (IGR_adjoints_2d/elliptic.jl:30-145): y = A(rho, alpha) x. */
+int igr2d_apply_sip(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* x, const double* rho, double* y);
+
+/* compute_hyperbolic_rhs! (IGR_adjoints_2d/hyperbolic.jl:27-119). */
+int igr2d_hyperbolic_rhs(igr_ctx* ctx, const igr_disc2d* d, double gamma, const double* mux, const double* muy,
+                         const double* rho, const double* E, const double* sigma, double* dmux, double* dmuy,
+                         double* drho, double* dE);
+
+/* solve_elliptic! (IGR_adjoints_2d/elliptic.jl:413-427): sigma is the warm
+ * start on entry and the solution on exit. */
+int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_iter, int solver,
+                         const double* mux, const double* muy, const double* rho, const double* E, double* sigma);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IGR_GB300_H */
