@@ -292,6 +292,10 @@ static int grid_for(long long n) { return (int)std::min<long long>((n + 255) / 2
     default: throw Error(1, "unsupported polynomial degree"); \
   }
 
+void launch_recip(const double* x, double* y, long long n, cudaStream_t s) {
+  k_recip<<<(int)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, s>>>(x, y, n);
+}
+
 static void recip(Ctx& c, const double* x, double* y, long long n) {
   LaunchScope ls(c, KID_OTHER);
   k_recip<<<grid_for(n), 256, 0, c.stream>>>(x, y, n);
@@ -341,6 +345,7 @@ static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf&
                         double* xb, double* dbuf) {
   const int nb = P.ntiles();
   SetupArgs2D sa;
+  std::memset(&sa, 0, sizeof(sa));
   sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
   sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
   sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = st.cM;
@@ -472,9 +477,11 @@ void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, do
   st.q[0] = zeros; st.q[1] = zeros; st.q[2] = const_cast<double*>(rho); st.q[3] = zeros;
   recip(c, rho, st.invr, NG);
   SetupArgs2D sa;
+  std::memset(&sa, 0, sizeof(sa));
   sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
   sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
   sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = nullptr;
+  sa.always = 1;
   { LaunchScope ls(c, KID_SETUP); NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, P.ntiles(), c.stream)); }
   ApplyArgs2D a;
   std::memset(&a, 0, sizeof(a));

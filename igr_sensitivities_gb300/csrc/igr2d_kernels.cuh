@@ -109,6 +109,7 @@ struct SetupArgs2D {
   const double *mx, *my, *invr;
   double *b, *cm, *ckx, *cky, *cinvM, *cpx, *cpy;
   double *cM;  // diag(A) itself (optional; the reverse needs it for d/d alpha)
+  int always;  // compute the coefficients even when alpha <= 0 (operator application on its own)
 };
 
 template <int NP>
@@ -122,7 +123,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
   const BasisDev& B = a.B;
   const int t = v.t, e = v.e;
   const double invJx = I.ijx, invJy = I.ijy;
-  if (I.alpha <= 0.0) return;  // no elliptic solve for this instance (forward.jl:24-28)
+  if (I.alpha <= 0.0 && !a.always) return;  // no elliptic solve for this instance (forward.jl:24-28)
 
   // ---- row phase (row t): velocities, x-derivatives, x part of the stiffness diagonal
   double ux[NP], uy[NP], ir[NP];

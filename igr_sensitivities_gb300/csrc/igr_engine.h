@@ -125,6 +125,8 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
                const double* obj_params, double* J, double* const dq0[4], double* dgamma, double* dalpha);
 
 double probe_fp64_tflops(Ctx& c);
+// y = 1 / x elementwise on stream s (no bookkeeping).
+void launch_recip(const double* x, double* y, long long n, cudaStream_t s);
 
 // Objective value only (the primal of the adjoint call), final state in q.
 void objective2d(Ctx& c, const Plan2D& P, double* const q[4], int n_steps, const Solve2DOpts& o, int objective,
