@@ -138,6 +138,20 @@ int igr2d_hyperbolic_rhs(igr_ctx* ctx, const igr_disc2d* d, double gamma, const 
 int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_iter, int solver,
                          const double* mux, const double* muy, const double* rho, const double* E, double* sigma);
 
+/* y = A(rho, alpha) x like igr2d_apply_sip, for callers that cannot let this
+ * library allocate device memory: hosts whose GPU memory belongs to another
+ * allocator (a Julia CUDA.jl pool, a framework's caching allocator with a
+ * fixed budget) or that cannot afford a synchronising cudaMalloc in their
+ * loop. No counterpart in the reference. x_dev, rho_dev and y_dev are device
+ * pointers; stream may be NULL (default stream); the call returns after the
+ * result is complete. It allocates nothing: its scratch is a fixed device
+ * array of about 4.8 MB, so it accepts at most 65,536 nodes
+ * ((p+1)^2 n_ex n_ey) and returns IGR_EINVAL above that. All calls share that
+ * array, so calls that overlap on the GPU race. The first call on each device
+ * looks up the array's address; make it before any stream capture. */
+int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const double* x_dev, const double* rho_dev,
+                            double* y_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
