@@ -213,8 +213,6 @@ def main():
     for _ in range(args.warmup):
         run_dev()
     lib = _lib.lib()
-    lib.igr_profile_reset(ctx.handle)
-    lib.igr_profile_enable(ctx.handle, 1)
     clk = ClockSampler(local)
     clk.start()
     barrier()
@@ -226,7 +224,19 @@ def main():
     barrier()
     t = time.perf_counter() - t0
     clocks = clk.stop()
+    # one more step with per-launch CUDA events on the engine's stream: kernel durations and shares
+    lib.igr_profile_reset(ctx.handle)
+    lib.igr_profile_enable(ctx.handle, 1)
+    barrier()
+    tp0 = time.perf_counter()
+    run_dev()
+    barrier()
+    t_prof = time.perf_counter() - tp0
     lib.igr_profile_enable(ctx.handle, 0)
+    pg = [C.c_int(0) for _ in range(4)]
+    lib.igr_last_adjoint_plan(ctx.handle, *[C.byref(x) for x in pg])
+    tape_plan = {"groups": pg[0].value, "instances_per_group": pg[1].value, "steps_per_segment": pg[2].value,
+                 "segments": pg[3].value}
     fam = {}
     for k in range(9):
         ms, cnt, nn = C.c_double(0), C.c_longlong(0), C.c_double(0)
@@ -291,9 +301,11 @@ def main():
                 "ms_per_launch": ms_launch, "flops_per_launch": flops, "nodes_per_launch": nodes,
                 "all_kernels_fp64_tflops": all_flops / (all_ms * 1e-3) / 1e12 if all_ms else None,
                 "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak, "peak_source": hbm_src},
-                "time_share": {k: v / tot for k, v in share.items()}}
+                "time_share": {k: v / tot for k, v in share.items()},
+                "profiled_step_ms": t_prof * 1e3, "kernel_ms_in_profiled_step": sum(v[0] for v in fam.values())}
     cfg = config_dict(B)
     cfg["n_steps"] = n_steps
+    cfg["tape_plan"] = tape_plan
     line = {"metric": METRIC, "value": value, "unit": "gradients/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tmax / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian pressure pulses)",

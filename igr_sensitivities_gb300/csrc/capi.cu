@@ -140,6 +140,15 @@ int igr_profile_nodes(igr_ctx* ctx, int kernel_family, double* nodes) {
   return IGR_OK;
 }
 
+int igr_last_adjoint_plan(const igr_ctx* ctx, int* groups, int* group_size, int* segment_steps, int* segments) {
+  if (!ctx || !groups || !group_size || !segment_steps || !segments) return IGR_EINVAL;
+  *groups = ctx->c.plan_groups;
+  *group_size = ctx->c.plan_group_size;
+  *segment_steps = ctx->c.plan_seg;
+  *segments = ctx->c.plan_nseg;
+  return IGR_OK;
+}
+
 int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops) {
   return guarded(ctx, [&] {
     if (!tflops) throw Error(IGR_EINVAL, "null output");
@@ -211,14 +220,21 @@ static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const do
   if (c.tape_budget == 0) {
     size_t fr = 0, tot = 0;
     cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
-    const size_t avail = fr + c.ws.bytes();
-    const size_t reserve = (size_t)2 << 30;
+    const size_t avail = fr + c.ws.bytes();  // workspace buffers are reused or regrown
+    const size_t reserve = (size_t)4 << 30;
     const bool apos = alphas[0] > 0;
-    const size_t F = 14 + (apos ? 2 * (size_t)n_iter : 0);
-    const size_t per_inst = ((size_t)3 * F * std::max(n_steps, 1) + 120) * N * sizeof(double);
-    const size_t fit = avail > reserve ? (avail - reserve) / per_inst : 0;
+    const size_t F = 16 + (apos ? 2 * (size_t)n_iter : 0);
+    // full tape (3 stages x F fields per step) + checkpoints + ~110 working fields per instance
+    const size_t per_inst = ((size_t)3 * F * std::max(n_steps, 1) + 6 + 110) * N * sizeof(double);
+    const size_t fit = avail > reserve ? (size_t)((avail - reserve) * 0.92) / per_inst : 0;
     G = (int)std::max<size_t>(1, std::min<size_t>((size_t)n_inst, fit));
+    if (G < n_inst) {  // equal-sized groups keep the workspace shapes identical across groups
+      const int ngroups = (n_inst + G - 1) / G;
+      G = (n_inst + ngroups - 1) / ngroups;
+    }
   }
+  c.plan_groups = (n_inst + G - 1) / G;
+  c.plan_group_size = G;
   for (int g0 = 0; g0 < n_inst; g0 += G) {
     const int gn = std::min(G, n_inst - g0);
     std::vector<Inst2DDesc> insts;

@@ -32,6 +32,10 @@ void Workspace::release_all() {
   for (auto& kv : bufs_) if (kv.second.p) cudaFree(kv.second.p);
   bufs_.clear();
 }
+size_t Workspace::held(const std::string& name) const {
+  auto it = bufs_.find(name);
+  return it == bufs_.end() ? 0 : it->second.n;
+}
 size_t Workspace::bytes() const {
   size_t s = 0;
   for (auto& kv : bufs_) s += kv.second.n;
@@ -307,10 +311,11 @@ struct StageBuf {
   double* invr = nullptr;
   double* Sout = nullptr;
   double *b = nullptr, *cm = nullptr, *ckx = nullptr, *cky = nullptr, *cinvM = nullptr, *cpx = nullptr, *cpy = nullptr, *cM = nullptr;
+  double *wsx = nullptr, *wsy = nullptr;  // LLF wave speeds at face nodes
   std::vector<double*> xk, rk;  // taped iterates (empty when untaped)
 };
 
-constexpr int STAGE_FIXED_FIELDS = 14;  // q(4) invr Sout b cm ckx cky cinvM cpx cpy cM
+constexpr int STAGE_FIXED_FIELDS = 16;  // q(4) invr Sout b cm ckx cky cinvM cpx cpy cM wsx wsy
 
 static int stage_fields(const Solve2DOpts& o, bool alpha_pos) {
   return STAGE_FIXED_FIELDS + (alpha_pos ? 2 * o.n_iter : 0);
@@ -323,6 +328,7 @@ static StageBuf stage_from(double* base, long long NG, const Solve2DOpts& o, boo
   for (int v = 0; v < 4; ++v) s.q[v] = nxt();
   s.invr = nxt(); s.Sout = nxt(); s.b = nxt(); s.cm = nxt(); s.ckx = nxt(); s.cky = nxt();
   s.cinvM = nxt(); s.cpx = nxt(); s.cpy = nxt(); s.cM = nxt();
+  s.wsx = nxt(); s.wsy = nxt();
   if (taped && alpha_pos) {
     for (int k = 0; k < o.n_iter; ++k) s.xk.push_back(nxt());
     for (int k = 0; k < o.n_iter; ++k) s.rk.push_back(nxt());
@@ -393,6 +399,7 @@ static void step_forward(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf
     h.c0 = c0s[s]; h.c1 = c1s[s]; h.c2 = c2s[s];
     for (int v = 0; v < 4; ++v) h.qo[v] = s < 2 ? st[s + 1].q[v] : qout[v];
     h.invro = s < 2 ? st[s + 1].invr : invrout;
+    h.ws_x = st[s].wsx; h.ws_y = st[s].wsy;
     h.status = c.d_status;
     { LaunchScope ls(c, KID_HYP); NP_DISPATCH(P.np, launch_k2_hyp_rk<NPV>(h, nb, c.stream)); }
     sprev = st[s].Sout;
@@ -587,10 +594,12 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   const size_t ckpt_bytes = (size_t)6 * NG * sizeof(double);
   size_t budget = c.tape_budget;
   if (budget == 0) {
+    // free memory plus what the tape and checkpoint buffers already hold (they are reused)
     size_t fr = 0, tot = 0;
     cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    const size_t avail = fr + c.ws.held("adj:tape") + c.ws.held("adj:ckpt");
     const size_t reserve = (size_t)1 << 30;
-    budget = fr > reserve ? (size_t)((fr - reserve) * 0.95) : 0;
+    budget = avail > reserve ? avail - reserve : 0;
   }
   const int nsteps_eff = std::max(n_steps, 1);
   int seg = 0;
@@ -600,6 +609,8 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   }
   if (seg < 1) throw Error(5, "device memory too small for one taped step of this batch");
   const int n_seg = (nsteps_eff + seg - 1) / seg;
+  c.plan_seg = seg;
+  c.plan_nseg = n_seg;
   double* ckpt = c.ws.dbl("adj:ckpt", (size_t)n_seg * 6 * NG);
   double* tape = c.ws.dbl("adj:tape", (size_t)seg * 3 * F * NG);
   auto slot = [&](int local_step, int stage) {
@@ -705,6 +716,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
         h.Qs[v] = s == 2 ? Q2b[v] : (s == 1 ? Q1b[v] : QN[v]);
       }
       h.invr = st[s].invr; h.S = st[s].Sout;
+      h.ws_x = st[s].wsx; h.ws_y = st[s].wsy;
       h.c0 = c0s[s]; h.c1 = c1s[s]; h.c2 = c2s[s];
       h.qn_mode = s == 2 ? 1 : (s == 1 ? 2 : 0);
       h.qs_add = s == 0 ? 1 : 0;

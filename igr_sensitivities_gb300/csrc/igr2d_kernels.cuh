@@ -1,18 +1,19 @@
 // 2D IGR-Euler forward kernels (sm_103a, FP64 CUDA cores).
 //
 // Thread mapping: a CTA owns a TX x TY tile of elements of one instance and
-// runs one thread per element *line*: in the xi-phase thread t of element e
-// owns row j = t (nodes (0..NP-1, t)), in the eta-phase column i = t. The
-// 1D contractions with the LGL differentiation matrix then run in registers,
-// loop-unrolled per line, which lets the compiler skip the structurally zero
-// interior diagonal entries of D for every lane alike (no divergence), and
-// face work lands on the threads that own the face nodes.
+// runs one thread per element *line*. In the xi-phase a thread owns one row
+// (nodes (0..NP-1, t)) of an element and handles that row's x faces; in the
+// eta-phase it owns one column and the y faces. The 1D contractions with the
+// LGL differentiation matrix then run in registers, unrolled per line, so the
+// structurally zero interior diagonal of D is skipped for every lane alike.
 //
-// GB300 has ~1.2 TFLOP/s of FP64 against 6.6 TB/s of HBM (about 5.6 B per
-// FP64 flop), so these kernels trade memory for FP64 instructions: per-stage
-// operator coefficients are precomputed once and re-read in every solver
-// iteration, reciprocals replace divisions, and the SIP face terms are folded
-// into the stiffness transpose (see apply_sip below).
+// GB300 issues about 1.2 TFLOP/s of FP64 against 6.6 TB/s of HBM (about
+// 5.6 B per FP64 flop), so these kernels are FP64-issue bound and trade
+// memory for FP64 instructions: per-stage operator coefficients are computed
+// once and re-read by every solver iteration, reciprocals of mesh constants
+// come precomputed from the host, the SIP face terms are folded into the
+// stiffness transpose, and out-of-tile (halo) work is packed into one warp
+// per phase (see elem_view) so that it is paid once per tile, converged.
 #pragma once
 #include "igr_device.cuh"
 
@@ -28,20 +29,36 @@ struct Tiling2D {
   static constexpr int L = NP - 1;
 };
 
-// Per-thread view of its element and of the periodic neighbours.
+// A thread's element and line in one phase.
 struct ElemView {
   int e, t, ext, eyt, ex, ey;
   bool valid;
   long long base;  // first node of the element
 };
 
+// Thread -> (element of the tile, line) for phase 0 (xi-phase, x faces) or
+// phase 1 (eta-phase, y faces). For P3 (64 threads = 2 warps of 8 elements x
+// 4 lines) warp 0 takes the 8 elements on the two tile edges normal to the
+// phase's faces and warp 1 the 8 interior ones, so the out-of-tile partner
+// work of a phase runs in one warp, with every lane on the same path.
 template <int NP>
-__device__ __forceinline__ ElemView elem_view(const Tile2D& tl, const Inst2D& I) {
+__device__ __forceinline__ ElemView elem_view(const Tile2D& tl, const Inst2D& I, int phase) {
+  constexpr int TX = Tiling2D<NP>::TX, TY = Tiling2D<NP>::TY;
   ElemView v;
-  v.e = threadIdx.x / NP;
-  v.t = threadIdx.x % NP;
-  v.ext = v.e % Tiling2D<NP>::TX;
-  v.eyt = v.e / Tiling2D<NP>::TX;
+  if (NP == 4 && TX == 4 && TY == 4) {
+    const int w = threadIdx.x >> 5, k = (threadIdx.x >> 2) & 7;
+    v.t = threadIdx.x & 3;
+    const int across = (w == 0) ? ((k & 4) ? 3 : 0) : ((k & 4) ? 2 : 1);
+    const int along = k & 3;
+    v.ext = phase == 0 ? across : along;
+    v.eyt = phase == 0 ? along : across;
+  } else {
+    const int e = threadIdx.x / NP;
+    v.t = threadIdx.x % NP;
+    v.ext = e % TX;
+    v.eyt = e / TX;
+  }
+  v.e = v.ext + TX * v.eyt;
   v.ex = tl.ex0 + v.ext;
   v.ey = tl.ey0 + v.eyt;
   v.valid = (v.ex < I.nex) && (v.ey < I.ney);
@@ -83,6 +100,17 @@ __device__ __forceinline__ double dot_row(const BasisDev& B, int i, const double
   return s;
 }
 
+// Derivative at the first (last == false) or last end node of a line, with
+// the row chosen at run time by register selects (no divergence, no local
+// memory): the form the halo loads need.
+template <int NP>
+__device__ __forceinline__ double dot_end(const BasisDev& B, bool last, const double* v) {
+  double s = (last ? B.D[NP - 1][0] : B.D[0][0]) * v[0];
+#pragma unroll
+  for (int k = 1; k < NP; ++k) s = fma(last ? B.D[NP - 1][k] : B.D[0][k], v[k], s);
+  return s;
+}
+
 // acc + sum_i D[i][k] v[i] (transpose contraction, node k)
 template <int NP>
 __device__ __forceinline__ double dot_col(const BasisDev& B, int k, const double* v, double acc) {
@@ -93,6 +121,10 @@ __device__ __forceinline__ double dot_col(const BasisDev& B, int k, const double
   }
   return acc;
 }
+
+// Which face of a phase to process first: the out-of-tile one for edge
+// elements, so the halo loads of warp 0 run converged.
+__device__ __forceinline__ int first_side(int pos_across, int extent) { return pos_across == extent - 1 ? 1 : 0; }
 
 // ---------------------------------------------------------------------------
 // Stage setup: IGR source b (elliptic.jl:159-197), diag(A) (elliptic.jl:205-264)
@@ -117,20 +149,28 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
   using TL = Tiling2D<NP>;
   constexpr int TE = TL::TE, NN = TL::NN, L = TL::L;
   __shared__ double s_ux[TE][NN], s_uy[TE][NN], s_ir[TE][NN], s_uxx[TE][NN], s_uyx[TE][NN], s_mx[TE][NN];
+  __shared__ double s_c[3][NN];  // w_i w_j Jx Jy, alpha w_i w_j Jy/Jx, alpha w_i w_j Jx/Jy  [node j*NP+i]
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const ElemView v = elem_view<NP>(tl, I);
+  const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
-  const int t = v.t, e = v.e;
   const double invJx = I.ijx, invJy = I.ijy;
   if (I.alpha <= 0.0 && !a.always) return;  // no elliptic solve for this instance (forward.jl:24-28)
+  if (threadIdx.x < NN) {
+    const int i = threadIdx.x % NP, j = threadIdx.x / NP;
+    const double ww = B.w[i] * B.w[j];
+    s_c[0][threadIdx.x] = ww * I.jx * I.jy;
+    s_c[1][threadIdx.x] = I.alpha * ww * I.jy * invJx;
+    s_c[2][threadIdx.x] = I.alpha * ww * I.jx * invJy;
+  }
 
-  // ---- row phase (row t): velocities, x-derivatives, x part of the stiffness diagonal
-  double ux[NP], uy[NP], ir[NP];
-  if (v.valid) {
+  // ---- row phase (row t of element vr): velocities, x-derivatives, x part of the stiffness diagonal
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
+    double ux[NP], uy[NP], ir[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      const long long n = v.base + t * NP + i;
+      const long long n = vr.base + t * NP + i;
       ir[i] = a.invr[n];
       ux[i] = a.mx[n] * ir[i];
       uy[i] = a.my[n] * ir[i];
@@ -148,19 +188,20 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
     }
   }
   __syncthreads();
-  if (!v.valid) return;
+  if (!vc.valid) return;
 
-  // ---- column phase (column t): y-derivatives, source, diagonal, coefficients
+  // ---- column phase (column t of element vc): y-derivatives, source, diagonal, coefficients
+  const int t = vc.t, e = vc.e;
   double cux[NP], cuy[NP], cir[NP];
 #pragma unroll
   for (int l = 0; l < NP; ++l) { cux[l] = s_ux[e][l * NP + t]; cuy[l] = s_uy[e][l * NP + t]; cir[l] = s_ir[e][l * NP + t]; }
   const double cys = I.alpha * B.w[t] * I.jx * invJy;
   const double eta = (double)(NP * NP);
-  // partner 1/rho across the x-faces of column t (t == 0 or t == L) and the y-faces (l == 0, l == L)
-  double irx[NP];  // partner for the x-face at node (t, l)
+  // partner 1/rho across the x faces of column t (only t == 0 or t == L) and the y faces (l == 0, l == L)
+  double irx[NP];
   if (t == 0 || t == L) {
     int it;
-    const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, t == 0 ? -1 : 1, 0, &it);
+    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, t == 0 ? -1 : 1, 0, &it);
     const int pi = t == 0 ? L : 0;
 #pragma unroll
     for (int l = 0; l < NP; ++l) irx[l] = it >= 0 ? s_ir[it][l * NP + pi] : a.invr[pb + l * NP + pi];
@@ -168,46 +209,46 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
   double iry[2];
   {
     int it;
-    const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, 0, -1, &it);  // bottom partner: node (t, L)
+    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, -1, &it);  // bottom partner: node (t, L)
     iry[0] = it >= 0 ? s_ir[it][L * NP + t] : a.invr[pb + L * NP + t];
-    const long long pt = neighbour<NP>(tl, I, v.ex, v.ey, 0, 1, &it);   // top partner: node (t, 0)
+    const long long pt = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, 1, &it);   // top partner: node (t, 0)
     iry[1] = it >= 0 ? s_ir[it][t] : a.invr[pt + t];
   }
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
-    double uxy = dot_row<NP>(B, l, cux) * invJy;
-    double uyy = dot_row<NP>(B, l, cuy) * invJy;
+    const long long n = vc.base + l * NP + t;
+    const double uxy = dot_row<NP>(B, l, cux) * invJy;
+    const double uyy = dot_row<NP>(B, l, cuy) * invJy;
     const double uxx = s_uxx[e][l * NP + t], uyx = s_uyx[e][l * NP + t];
     const double s = uxx + uyy;
     double R = fma(s, s, uxx * uxx);
     R = fma(2.0 * uxy, uyx, R);
     R = fma(uyy, uyy, R);
-    const double ww = B.w[t] * B.w[l];
-    a.b[n] = ww * I.jx * I.jy * (I.alpha * R);
+    const int nd = l * NP + t;
+    a.b[n] = s_c[0][nd] * (I.alpha * R);
     double my_ = B.W2[0][l] * cir[0];
 #pragma unroll
     for (int k = 1; k < NP; ++k) my_ = fma(B.W2[k][l], cir[k], my_);
-    const double mass = ww * I.jx * I.jy * cir[l];
-    double M = mass + s_mx[e][l * NP + t] + cys * my_;
+    const double mass = s_c[0][nd] * cir[l];
+    double M = fma(cys, my_, mass + s_mx[e][nd]);
     double px = 0.0, py = 0.0;
     if (t == 0 || t == L) {
       const double wf = B.w[l] * I.jy;
       const double sig = eta * fmax(t == L ? cir[l] : irx[l], t == L ? irx[l] : cir[l]) * I.idx;
       px = I.alpha * sig * wf;
       // x-face self terms: right side of its left face (t == 0) / left side of its right face (t == L)
-      M += (t == L ? -I.alpha * invJx * B.D[L][L] : I.alpha * invJx * B.D[0][0]) * cir[l] * wf + px;
+      M += fma((t == L ? -I.alpha * invJx * B.D[L][L] : I.alpha * invJx * B.D[0][0]) * wf, cir[l], px);
     }
     if (l == 0 || l == L) {
       const double wf = B.w[t] * I.jx;
       const double ip = iry[l == 0 ? 0 : 1];
       const double sig = eta * fmax(l == L ? cir[l] : ip, l == L ? ip : cir[l]) * I.idy;
       py = I.alpha * sig * wf;
-      M += (l == L ? -I.alpha * invJy * B.D[L][L] : I.alpha * invJy * B.D[0][0]) * cir[l] * wf + py;
+      M += fma((l == L ? -I.alpha * invJy * B.D[L][L] : I.alpha * invJy * B.D[0][0]) * wf, cir[l], py);
     }
     a.cm[n] = mass;
-    a.ckx[n] = I.alpha * ww * I.jy * invJx * cir[l];
-    a.cky[n] = I.alpha * ww * I.jx * invJy * cir[l];
+    a.ckx[n] = s_c[1][nd] * cir[l];
+    a.cky[n] = s_c[2][nd] * cir[l];
     a.cpx[n] = px;
     a.cpy[n] = py;
     a.cinvM[n] = 1.0 / M;
@@ -238,71 +279,79 @@ struct ApplyArgs2D {
   double ca, cc, omega;                  // d_{k+1} = ca d_k + cc M^-1 r_k ; Jacobi omega
 };
 
+// Partner data across one face: its value and end-node derivative of x, and its stiffness coefficient.
+struct Partner1 { double x, d, k; };
+
 template <int NP, int EPI>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
   using TL = Tiling2D<NP>;
-  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L;
+  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
   __shared__ double s_x[TE][NN], s_yx[TE][NN], s_gxf[TE][NP][2], s_gyf[TE][NP][2];
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const ElemView v = elem_view<NP>(tl, I);
+  const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
-  const int t = v.t, e = v.e;
   const double hw = B.hw;
 
-  // ---- xi-phase part 1: row t, derivatives
+  // ---- xi-phase part 1: row derivatives
   double xr[NP], gx[NP];
-  double xc[NP], gy[NP];
-  if (v.valid) {
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) { xr[i] = a.x[v.base + t * NP + i]; s_x[e][t * NP + i] = xr[i]; }
+    for (int i = 0; i < NP; ++i) { xr[i] = a.x[vr.base + t * NP + i]; s_x[e][t * NP + i] = xr[i]; }
 #pragma unroll
     for (int i = 0; i < NP; ++i) gx[i] = dot_row<NP>(B, i, xr);
     s_gxf[e][t][0] = gx[0]; s_gxf[e][t][1] = gx[L];
     if (a.tape_x) {
 #pragma unroll
-      for (int i = 0; i < NP; ++i) a.tape_x[v.base + t * NP + i] = xr[i];
+      for (int i = 0; i < NP; ++i) a.tape_x[vr.base + t * NP + i] = xr[i];
     }
   }
   __syncthreads();
-  if (v.valid) {
+  double xc[NP], gy[NP];
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
 #pragma unroll
     for (int l = 0; l < NP; ++l) xc[l] = s_x[e][l * NP + t];
 #pragma unroll
     for (int l = 0; l < NP; ++l) gy[l] = dot_row<NP>(B, l, xc);
     s_gyf[e][t][0] = gy[0]; s_gyf[e][t][1] = gy[L];
-
-    // ---- xi-phase part 2: x-faces of row t and the x-stiffness transpose
+  }
+  if (vr.valid) {
+    // ---- xi-phase part 2: x faces of the row and the x-stiffness transpose
+    const int t = vr.t, e = vr.e;
     double kxr[NP];
 #pragma unroll
-    for (int i = 0; i < NP; ++i) kxr[i] = a.ckx[v.base + t * NP + i];
-    // partner values across the left (s = 0) and right (s = 1) faces
-    double px_[2], pd_[2], pk_[2];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int i = 0; i < NP; ++i) kxr[i] = a.ckx[vr.base + t * NP + i];
+    auto fetch = [&](int s) {
+      Partner1 P;
       int it;
-      const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, s == 0 ? -1 : 1, 0, &it);
+      const long long pb = neighbour<NP>(tl, I, vr.ex, vr.ey, s == 0 ? -1 : 1, 0, &it);
       const int pi = s == 0 ? L : 0;  // partner face node index along x
-      pk_[s] = a.ckx[pb + t * NP + pi];
+      P.k = a.ckx[pb + t * NP + pi];
       if (it >= 0) {
-        px_[s] = s_x[it][t * NP + pi];
-        pd_[s] = s_gxf[it][t][s == 0 ? 1 : 0];
+        P.x = s_x[it][t * NP + pi];
+        P.d = s_gxf[it][t][s == 0 ? 1 : 0];
       } else {
         double pr[NP];
 #pragma unroll
         for (int k = 0; k < NP; ++k) pr[k] = a.x[pb + t * NP + k];
-        px_[s] = pr[pi];
-        pd_[s] = dot_row<NP>(B, pi, pr);
+        P.x = s == 0 ? pr[L] : pr[0];
+        P.d = dot_end<NP>(B, s == 0, pr);
       }
-    }
+      return P;
+    };
+    const int sf = first_side(vr.ext, TX);
+    const Partner1 pA = fetch(sf), pB = fetch(1 - sf);
+    const Partner1 pl = sf == 0 ? pA : pB, prt = sf == 0 ? pB : pA;
     // left face: own node (0,t) is the R side; right face: own node (L,t) is the L side
-    const double jl = px_[0] - xr[0];
-    const double Fl = fma(a.cpx[v.base + t * NP], jl, hw * fma(pk_[0], pd_[0], kxr[0] * gx[0]));
-    const double jr = xr[L] - px_[1];
-    const double Fr = fma(a.cpx[v.base + t * NP + L], jr, hw * fma(kxr[L], gx[L], pk_[1] * pd_[1]));
+    const double jl = pl.x - xr[0];
+    const double Fl = fma(a.cpx[vr.base + t * NP], jl, hw * fma(pl.k, pl.d, kxr[0] * gx[0]));
+    const double jr = xr[L] - prt.x;
+    const double Fr = fma(a.cpx[vr.base + t * NP + L], jr, hw * fma(kxr[L], gx[L], prt.k * prt.d));
     double sx[NP];
 #pragma unroll
-    for (int i = 0; i < NP; ++i) sx[i] = kxr[i] * gx[i];
+    for (int i = 1; i < L; ++i) sx[i] = kxr[i] * gx[i];
     sx[0] = kxr[0] * fma(hw, jl, gx[0]);
     sx[L] = kxr[L] * fma(hw, jr, gx[L]);
 #pragma unroll
@@ -312,42 +361,46 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
     }
   }
   __syncthreads();
-  if (!v.valid) return;
+  if (!vc.valid) return;
 
-  // ---- eta-phase: y-faces of column t, y-stiffness transpose, mass, epilogue
+  // ---- eta-phase: y faces of the column, y-stiffness transpose, mass, epilogue
+  const int t = vc.t, e = vc.e;
   double kyc[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) kyc[l] = a.cky[v.base + l * NP + t];
-  double qx_[2], qd_[2], qk_[2];
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
+  for (int l = 0; l < NP; ++l) kyc[l] = a.cky[vc.base + l * NP + t];
+  auto fetchy = [&](int s) {
+    Partner1 P;
     int it;
-    const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, 0, s == 0 ? -1 : 1, &it);
+    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
     const int pl = s == 0 ? L : 0;
-    qk_[s] = a.cky[pb + pl * NP + t];
+    P.k = a.cky[pb + pl * NP + t];
     if (it >= 0) {
-      qx_[s] = s_x[it][pl * NP + t];
-      qd_[s] = s_gyf[it][t][s == 0 ? 1 : 0];
+      P.x = s_x[it][pl * NP + t];
+      P.d = s_gyf[it][t][s == 0 ? 1 : 0];
     } else {
       double pc[NP];
 #pragma unroll
       for (int k = 0; k < NP; ++k) pc[k] = a.x[pb + k * NP + t];
-      qx_[s] = pc[pl];
-      qd_[s] = dot_row<NP>(B, pl, pc);
+      P.x = s == 0 ? pc[L] : pc[0];
+      P.d = dot_end<NP>(B, s == 0, pc);
     }
-  }
-  const double jb = qx_[0] - xc[0];
-  const double Fb = fma(a.cpy[v.base + t], jb, hw * fma(qk_[0], qd_[0], kyc[0] * gy[0]));
-  const double jt = xc[L] - qx_[1];
-  const double Ft = fma(a.cpy[v.base + L * NP + t], jt, hw * fma(kyc[L], gy[L], qk_[1] * qd_[1]));
+    return P;
+  };
+  const int sf = first_side(vc.eyt, TY);
+  const Partner1 qA = fetchy(sf), qB = fetchy(1 - sf);
+  const Partner1 qb = sf == 0 ? qA : qB, qt = sf == 0 ? qB : qA;
+  const double jb = qb.x - xc[0];
+  const double Fb = fma(a.cpy[vc.base + t], jb, hw * fma(qb.k, qb.d, kyc[0] * gy[0]));
+  const double jt = xc[L] - qt.x;
+  const double Ft = fma(a.cpy[vc.base + L * NP + t], jt, hw * fma(kyc[L], gy[L], qt.k * qt.d));
   double sy[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) sy[l] = kyc[l] * gy[l];
+  for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gy[l];
   sy[0] = kyc[0] * fma(hw, jb, gy[0]);
   sy[L] = kyc[L] * fma(hw, jt, gy[L]);
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
+    const long long n = vc.base + l * NP + t;
     double y = fma(a.cm[n], xc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
     y = dot_col<NP>(B, l, sy, y);
     if (EPI == EPI_RESID) { a.y_out[n] = y; continue; }
@@ -367,8 +420,9 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
 // ---------------------------------------------------------------------------
 // Hyperbolic DG RHS (hyperbolic.jl:27-119) fused with the SSP-RK3 stage
 // combination (forward.jl:53-68):  q_out = c0*q^n + c1*q_s + c2*dt*k(q_s, Sigma).
-// Also writes 1/rho of q_out for the next stage's setup and flags non-finite
-// values or rho <= 0 in the status word.
+// Also writes 1/rho of q_out for the next stage's setup, optionally the LLF
+// wave speeds at face nodes (the reverse reads them instead of recomputing
+// square roots), and flags non-finite values or rho <= 0 in the status word.
 // ---------------------------------------------------------------------------
 struct HypArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
@@ -377,104 +431,123 @@ struct HypArgs2D {
   double c0, c1, c2;
   double *qo[4], *invro;           // stage output (may alias qn: pointwise)
   double *k_out[4];                // optional: raw RHS k (compute_hyperbolic_rhs!)
+  double *ws_x, *ws_y;             // optional: |u_n| + c at x-face / y-face nodes
   int* status;
 };
 
-template <int NP>
 struct FaceState { double q[4], f[4], ws; };
 
-// Physical flux in direction dir at one node (euler.jl:156-186) and |u_n| + c.
-__device__ __forceinline__ void node_flux(int dir, double g, double mx, double my, double r, double E, double S, double ir,
-                                          double f[4], double* ws) {
-  const double ux = mx * ir, uy = my * ir;
+// Pointwise physics at one node (euler.jl:145-214): both directional fluxes
+// with P_bar = P + Sigma from one evaluation of the pressure.
+struct NodePhys {
+  double ux, uy, P, pb;
+  double fx[4], fy[4];
+};
+__device__ __forceinline__ NodePhys node_phys(double g, double mx, double my, double E, double S, double ir) {
+  NodePhys p;
+  p.ux = mx * ir; p.uy = my * ir;
   const double kin = fma(mx, mx, my * my) * (0.5 * ir);
-  const double P = (g - 1.0) * (E - kin);
-  const double pb = P + S;
-  const double un = dir == 0 ? ux : uy;
-  if (dir == 0) { f[0] = fma(mx, ux, pb); f[1] = my * ux; f[2] = mx; }
-  else { f[0] = mx * uy; f[1] = fma(my, uy, pb); f[2] = my; }
-  f[3] = (E + pb) * un;
-  if (ws) *ws = fabs(un) + sqrt(g * P * ir);
+  p.P = (g - 1.0) * (E - kin);
+  p.pb = p.P + S;
+  const double epb = E + p.pb;
+  p.fx[0] = fma(mx, p.ux, p.pb); p.fx[1] = my * p.ux; p.fx[2] = mx; p.fx[3] = epb * p.ux;
+  p.fy[0] = mx * p.uy; p.fy[1] = fma(my, p.uy, p.pb); p.fy[2] = my; p.fy[3] = epb * p.uy;
+  return p;
+}
+// |u_n| + c, c = sqrt(gamma P / rho)
+__device__ __forceinline__ double wavespeed(double g, double un, double P, double ir) {
+  return fabs(un) + sqrt(g * P * ir);
 }
 
 template <int NP>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
   using TL = Tiling2D<NP>;
-  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L;
+  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
   __shared__ double s_fy[4][TE][NN];    // y fluxes
   __shared__ double s_k[4][TE][NN];     // x part of the RHS
-  __shared__ FaceState<NP> s_xf[TE][NP][2];  // x-face node data (left, right) per row
-  __shared__ FaceState<NP> s_yf[TE][NP][2];  // y-face node data (bottom, top) per column
+  __shared__ double s_q[4][TE][NN];     // state (y-face LLF states)
+  __shared__ double s_pw[TE][NN];       // pressure (y-face wave speeds)
+  __shared__ FaceState s_xf[TE][NP][2]; // x-face node data (left, right) per row
+  __shared__ FaceState s_yf[TE][NP][2]; // y-face node data (bottom, top) per column
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const ElemView v = elem_view<NP>(tl, I);
+  const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
-  const int t = v.t, e = v.e;
   const double g = I.gamma;
   const double invJx = I.ijx, invJy = I.ijy;
 
-  double q[4][NP], fx[4][NP];
-  if (v.valid) {
+  // ---- phase 1 (row of vr): fluxes, x volume term, x-face node data
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
+    double fx[4][NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      const long long n = v.base + t * NP + i;
+      const long long n = vr.base + t * NP + i;
       const double mx = a.q[0][n], my = a.q[1][n], r = a.q[2][n], E = a.q[3][n], S = a.S[n], ir = a.invr[n];
-      q[0][i] = mx; q[1][i] = my; q[2][i] = r; q[3][i] = E;
-      double f[4], fyv[4], ws;
-      node_flux(0, g, mx, my, r, E, S, ir, f, (i == 0 || i == L) ? &ws : nullptr);
+      const NodePhys ph = node_phys(g, mx, my, E, S, ir);
+      s_q[0][e][t * NP + i] = mx; s_q[1][e][t * NP + i] = my; s_q[2][e][t * NP + i] = r; s_q[3][e][t * NP + i] = E;
+      s_pw[e][t * NP + i] = ph.P;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) fx[c][i] = f[c];
-      node_flux(1, g, mx, my, r, E, S, ir, fyv, nullptr);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) s_fy[c][e][t * NP + i] = fyv[c];
+      for (int c = 0; c < 4; ++c) { fx[c][i] = ph.fx[c]; s_fy[c][e][t * NP + i] = ph.fy[c]; }
       if (i == 0 || i == L) {
-        FaceState<NP>& fs = s_xf[e][t][i == 0 ? 0 : 1];
+        FaceState& fs = s_xf[e][t][i == 0 ? 0 : 1];
+        fs.q[0] = mx; fs.q[1] = my; fs.q[2] = r; fs.q[3] = E;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) { fs.q[c] = q[c][i]; fs.f[c] = f[c]; }
-        fs.ws = ws;
+        for (int c = 0; c < 4; ++c) fs.f[c] = ph.fx[c];
+        fs.ws = wavespeed(g, ph.ux, ph.P, ir);
+        if (a.ws_x) a.ws_x[n] = fs.ws;
       }
     }
-  }
-  __syncthreads();
-  if (v.valid) {
-    // y-face node data of column t (bottom l = 0, top l = L)
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const int l = s == 0 ? 0 : L;
-      const long long n = v.base + l * NP + t;
-      double f[4], ws;
-      node_flux(1, g, a.q[0][n], a.q[1][n], a.q[2][n], a.q[3][n], a.S[n], a.invr[n], f, &ws);
-      FaceState<NP>& fs = s_yf[e][t][s];
-      fs.q[0] = a.q[0][n]; fs.q[1] = a.q[1][n]; fs.q[2] = a.q[2][n]; fs.q[3] = a.q[3][n];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) fs.f[c] = f[c];
-      fs.ws = ws;
-    }
-    // ---- x volume term of row t
 #pragma unroll
     for (int c = 0; c < 4; ++c)
 #pragma unroll
       for (int i = 0; i < NP; ++i) s_k[c][e][t * NP + i] = -invJx * dot_row<NP>(B, i, fx[c]);
   }
   __syncthreads();
-  if (v.valid) {
-    // ---- x faces of row t (LLF, euler.jl:222-236), owner computes its side
+  // ---- phase 2 (column of vc): y-face node data
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
+      const int l = s == 0 ? 0 : L;
+      const int nd = l * NP + t;
+      FaceState& fs = s_yf[e][t][s];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) { fs.q[c] = s_q[c][e][nd]; fs.f[c] = s_fy[c][e][nd]; }
+      const double ir = a.invr[vc.base + nd];
+      fs.ws = wavespeed(g, fs.q[1] * ir, s_pw[e][nd], ir);
+      if (a.ws_y) a.ws_y[vc.base + nd] = fs.ws;
+    }
+  }
+  __syncthreads();
+  // ---- phase 3 (row of vr): x faces (LLF, euler.jl:222-236), owner computes its side
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
+    auto fetch = [&](int s) {
       int it;
-      const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, s == 0 ? -1 : 1, 0, &it);
-      const int pi = s == 0 ? L : 0;
-      FaceState<NP> pf;
+      const long long pb = neighbour<NP>(tl, I, vr.ex, vr.ey, s == 0 ? -1 : 1, 0, &it);
+      FaceState pf;
       if (it >= 0) {
         pf = s_xf[it][t][s == 0 ? 1 : 0];
       } else {
-        const long long n = pb + t * NP + pi;
+        const long long n = pb + t * NP + (s == 0 ? L : 0);
         pf.q[0] = a.q[0][n]; pf.q[1] = a.q[1][n]; pf.q[2] = a.q[2][n]; pf.q[3] = a.q[3][n];
-        node_flux(0, g, pf.q[0], pf.q[1], pf.q[2], pf.q[3], a.S[n], a.invr[n], pf.f, &pf.ws);
+        const double ir = a.invr[n];
+        const NodePhys ph = node_phys(g, pf.q[0], pf.q[1], pf.q[3], a.S[n], ir);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) pf.f[c] = ph.fx[c];
+        pf.ws = wavespeed(g, ph.ux, ph.P, ir);
       }
-      const FaceState<NP>& of = s_xf[e][t][s];
-      const FaceState<NP>& Ls = s == 0 ? pf : of;
-      const FaceState<NP>& Rs = s == 0 ? of : pf;
+      return pf;
+    };
+    const int sf = first_side(vr.ext, TX);
+    const FaceState pA = fetch(sf), pB = fetch(1 - sf);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const FaceState& pf = (s == sf) ? pA : pB;
+      const FaceState& of = s_xf[e][t][s];
+      const FaceState& Ls = s == 0 ? pf : of;
+      const FaceState& Rs = s == 0 ? of : pf;
       const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
       const int io = s == 0 ? 0 : L;
       const double cf = s == 0 ? invJx * B.iw0 : -invJx * B.iwL;
@@ -486,8 +559,9 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
     }
   }
   __syncthreads();
-  if (!v.valid) return;
-  // ---- column t: y volume term, y faces, RK combination
+  if (!vc.valid) return;
+  // ---- phase 4 (column of vc): y volume term, y faces, RK combination
+  const int t = vc.t, e = vc.e;
   double kc[4][NP];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
@@ -497,22 +571,31 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
 #pragma unroll
     for (int l = 0; l < NP; ++l) kc[c][l] = fma(-invJy, dot_row<NP>(B, l, fyc), s_k[c][e][l * NP + t]);
   }
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
+  auto fetchy = [&](int s) {
     int it;
-    const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, 0, s == 0 ? -1 : 1, &it);
-    const int pl = s == 0 ? L : 0;
-    FaceState<NP> pf;
+    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
+    FaceState pf;
     if (it >= 0) {
       pf = s_yf[it][t][s == 0 ? 1 : 0];
     } else {
-      const long long n = pb + pl * NP + t;
+      const long long n = pb + (s == 0 ? L : 0) * NP + t;
       pf.q[0] = a.q[0][n]; pf.q[1] = a.q[1][n]; pf.q[2] = a.q[2][n]; pf.q[3] = a.q[3][n];
-      node_flux(1, g, pf.q[0], pf.q[1], pf.q[2], pf.q[3], a.S[n], a.invr[n], pf.f, &pf.ws);
+      const double ir = a.invr[n];
+      const NodePhys ph = node_phys(g, pf.q[0], pf.q[1], pf.q[3], a.S[n], ir);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) pf.f[c] = ph.fy[c];
+      pf.ws = wavespeed(g, ph.uy, ph.P, ir);
     }
-    const FaceState<NP>& of = s_yf[e][t][s];
-    const FaceState<NP>& Ls = s == 0 ? pf : of;
-    const FaceState<NP>& Rs = s == 0 ? of : pf;
+    return pf;
+  };
+  const int sf = first_side(vc.eyt, TY);
+  const FaceState qA = fetchy(sf), qB = fetchy(1 - sf);
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const FaceState& pf = (s == sf) ? qA : qB;
+    const FaceState& of = s_yf[e][t][s];
+    const FaceState& Ls = s == 0 ? pf : of;
+    const FaceState& Rs = s == 0 ? of : pf;
     const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
     const int lo = s == 0 ? 0 : L;
     const double cf = s == 0 ? invJy * B.iw0 : -invJy * B.iwL;
@@ -526,12 +609,12 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
   bool bad = false;
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
+    const long long n = vc.base + l * NP + t;
     double qo[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       if (a.k_out[c]) a.k_out[c][n] = kc[c][l];
-      const double qs = a.q[c][n];
+      const double qs = s_q[c][e][l * NP + t];
       double val = fma(c2dt, kc[c][l], a.c1 * qs);
       if (a.c0 != 0.0) val = fma(a.c0, a.qn[c][n], val);
       qo[c] = val;

@@ -1,5 +1,6 @@
 // 2D discrete-adjoint (reverse-mode) kernels: the transpose of every forward
-// kernel in igr2d_kernels.cuh, in the same tile / line-per-thread layout.
+// kernel in igr2d_kernels.cuh, in the same tile / line-per-thread layout and
+// with the same phase-dependent thread mapping (elem_view).
 //
 // What the reference gets from Enzyme (IGR_adjoints_2d/enzyme_adjoint.jl:270-296)
 // is built here by hand, primitive by primitive:
@@ -24,44 +25,41 @@
 
 namespace igrgpu {
 
-// Reverse of node_flux (one direction) at one node: fb = adjoint of the 4 flux
-// components; accumulates into qb[4], Sb and gb.
-__device__ __forceinline__ void node_flux_rev(int dir, double g, double mx, double my, double E, double S, double ir,
-                                              const double fb[4], double qb[4], double& Sb, double& gb) {
+// Reverse of node_phys for both flux directions at one node: fbx, fby are
+// the adjoints of the x and y flux components; accumulates into qb[4]
+// (mx, my, rho, E), Sb and gb.
+__device__ __forceinline__ void node_phys_rev(double g, double mx, double my, double E, double S, double ir,
+                                              const double fbx[4], const double fby[4], double qb[4], double& Sb,
+                                              double& gb) {
   const double ux = mx * ir, uy = my * ir;
   const double kin = fma(mx, mx, my * my) * (0.5 * ir);
-  const double P = (g - 1.0) * (E - kin);
-  const double pb = P + S;
-  const double un = dir == 0 ? ux : uy;
-  const double unb = fma(fb[0], mx, fma(fb[1], my, fb[3] * (E + pb)));
-  double pbb;
-  if (dir == 0) {
-    pbb = fma(fb[3], un, fb[0]);
-    qb[0] += fma(fb[0], un, fb[2]);
-    qb[1] += fb[1] * un;
-  } else {
-    pbb = fma(fb[3], un, fb[1]);
-    qb[0] += fb[0] * un;
-    qb[1] += fma(fb[1], un, fb[2]);
-  }
-  qb[3] += fb[3] * un;
-  Sb += pbb;
-  // un = m_n / rho
-  qb[dir] += unb * ir;
-  qb[2] -= unb * un * ir;
-  // P = (g-1)(E - kin), kin = |m|^2 / (2 rho)
-  gb += pbb * (E - kin);
   const double gm1 = g - 1.0;
-  qb[3] += pbb * gm1;
+  const double P = gm1 * (E - kin), pb = P + S, epb = E + pb;
+  // fx = (mx ux + pb, my ux, mx, (E+pb) ux), fy = (mx uy, my uy + pb, my, (E+pb) uy)
+  const double uxb = fma(fbx[0], mx, fma(fbx[1], my, fbx[3] * epb));
+  const double uyb = fma(fby[0], mx, fma(fby[1], my, fby[3] * epb));
+  const double e3 = fma(fbx[3], ux, fby[3] * uy);   // d/dE through E + pb, and part of d/d pb
+  const double pbb = fbx[0] + fby[1] + e3;
+  qb[0] += fma(fbx[0], ux, fma(fby[0], uy, fbx[2]));
+  qb[1] += fma(fby[1], uy, fma(fbx[1], ux, fby[2]));
+  qb[3] += e3;
+  Sb += pbb;
+  // u = m / rho
+  qb[0] += uxb * ir;
+  qb[1] += uyb * ir;
+  qb[2] -= fma(uxb, ux, uyb * uy) * ir;
+  // P = (g-1)(E - kin), kin = |m|^2 / (2 rho)
+  gb = fma(pbb, E - kin, gb);
+  qb[3] = fma(pbb, gm1, qb[3]);
   const double kb = -pbb * gm1;
-  qb[0] += kb * ux;
-  qb[1] += kb * uy;
+  qb[0] = fma(kb, ux, qb[0]);
+  qb[1] = fma(kb, uy, qb[1]);
   qb[2] -= kb * kin * ir;
 }
 
-// Reverse of |u_n| + sqrt(g P / rho) at one node with adjoint wb.
-__device__ __forceinline__ void wavespeed_rev(int dir, double g, double mx, double my, double E, double ir, double wb,
-                                              double qb[4], double& gb) {
+// Reverse of |u_n| + sqrt(g P / rho) at one node with adjoint wb; c is the sound speed.
+__device__ __forceinline__ void wavespeed_rev(int dir, double g, double mx, double my, double E, double ir, double c,
+                                              double wb, double qb[4], double& gb) {
   const double ux = mx * ir, uy = my * ir;
   const double kin = fma(mx, mx, my * my) * (0.5 * ir);
   const double P = (g - 1.0) * (E - kin);
@@ -69,16 +67,17 @@ __device__ __forceinline__ void wavespeed_rev(int dir, double g, double mx, doub
   const double unb = signbit(un) ? -wb : wb;
   qb[dir] += unb * ir;
   qb[2] -= unb * un * ir;
-  const double X = g * P * ir;
-  const double Xb = wb * 0.5 * rsqrt(X);
-  gb += Xb * P * ir;
+  // c = sqrt(X), X = g P / rho:  dX = wb / (2 c)
+  const double Xb = wb * 0.5 / c;
+  const double X = c * c;
+  gb = fma(Xb, P * ir, gb);
   const double Pb = Xb * g * ir;
   qb[2] -= Xb * X * ir;
-  gb += Pb * (E - kin);
-  qb[3] += Pb * (g - 1.0);
+  gb = fma(Pb, E - kin, gb);
+  qb[3] = fma(Pb, g - 1.0, qb[3]);
   const double kb = -Pb * (g - 1.0);
-  qb[0] += kb * ux;
-  qb[1] += kb * uy;
+  qb[0] = fma(kb, ux, qb[0]);
+  qb[1] = fma(kb, uy, qb[1]);
   qb[2] -= kb * kin * ir;
 }
 
@@ -99,6 +98,7 @@ enum { SREV_NONE = 0, SREV_CHEB = 1, SREV_JACOBI = 2 };
 struct HypRevArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
   const double *q[4], *invr, *S;     // taped stage input and Sigma_out
+  const double *ws_x, *ws_y;         // taped LLF wave speeds at face nodes
   const double *A[4];                // adjoint of the stage output
   double c0, c1, c2;
   double *Qn[4]; int qn_mode;
@@ -115,184 +115,175 @@ struct HypRevArgs2D {
 template <int NP>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rev(HypRevArgs2D a) {
   using TL = Tiling2D<NP>;
-  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L;
+  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
   __shared__ double s_kb[4][TE][NN];      // kbar = c2 dt A
-  __shared__ double s_pq[6][TE][NN];      // row-phase partials: q (4), S, gamma
+  __shared__ double s_q[4][TE][NN];       // taped stage state
+  __shared__ double s_fbx[4][TE][NN];     // adjoint of the x fluxes (row phase)
+  __shared__ double s_qbx[4][TE][NN];     // q adjoint from the x faces (row phase)
   __shared__ double s_xw[TE][NP][2];      // x wave speed at x-face nodes
   __shared__ double s_yw[TE][NP][2];
+  __shared__ double s_grow[TE][NP];       // row-phase d/dgamma partials
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const ElemView v = elem_view<NP>(tl, I);
+  const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
-  const int t = v.t, e = v.e;
   const double g = I.gamma;
   const double invJx = I.ijx, invJy = I.ijy;
   const double c2dt = a.c2 * I.dt;
 
-  double q[4][NP], S[NP], ir[NP], kb[4][NP];
-  if (v.valid) {
+  // ---- phase 1: row data of vr into smem; face wave speeds
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      const long long n = v.base + t * NP + i;
+      const long long n = vr.base + t * NP + i;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) { q[c][i] = a.q[c][n]; kb[c][i] = c2dt * a.A[c][n]; s_kb[c][e][t * NP + i] = kb[c][i]; }
-      S[i] = a.S[n]; ir[i] = a.invr[n];
+      for (int c = 0; c < 4; ++c) { s_q[c][e][t * NP + i] = a.q[c][n]; s_kb[c][e][t * NP + i] = c2dt * a.A[c][n]; }
     }
-    {
-      double f[4], ws;
-      node_flux(0, g, q[0][0], q[1][0], q[2][0], q[3][0], S[0], ir[0], f, &ws); s_xw[e][t][0] = ws;
-      node_flux(0, g, q[0][L], q[1][L], q[2][L], q[3][L], S[L], ir[L], f, &ws); s_xw[e][t][1] = ws;
-    }
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const long long n = v.base + (s == 0 ? 0 : L) * NP + t;
-      double f[4], ws;
-      node_flux(1, g, a.q[0][n], a.q[1][n], a.q[2][n], a.q[3][n], a.S[n], a.invr[n], f, &ws);
-      s_yw[e][t][s] = ws;
-    }
+    s_xw[e][t][0] = a.ws_x[vr.base + t * NP];
+    s_xw[e][t][1] = a.ws_x[vr.base + t * NP + L];
+  }
+  if (vc.valid) {
+    s_yw[vc.e][vc.t][0] = a.ws_y[vc.base + vc.t];
+    s_yw[vc.e][vc.t][1] = a.ws_y[vc.base + L * NP + vc.t];
   }
   __syncthreads();
-  if (v.valid) {
-    // ---- row t: F̄x = transpose of the x volume term, x-face LLF reverse, flux reverse
-    double Fb[4][NP];
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-      for (int k = 0; k < NP; ++k) Fb[c][k] = -invJx * dot_col<NP>(B, k, kb[c], 0.0);
-    double qbr[4][NP], Sbr[NP], gb = 0.0;
-#pragma unroll
-    for (int i = 0; i < NP; ++i) { Sbr[i] = 0.0;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) qbr[c][i] = 0.0; }
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const int io = s == 0 ? 0 : L;            // own face node
-      int it;
-      const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, s == 0 ? -1 : 1, 0, &it);
-      const int pi = s == 0 ? L : 0;
-      const long long pn = pb + t * NP + pi;
-      double pq[4], pkb[4], pws;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) pq[c] = a.q[c][pn];
-      if (it >= 0) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) pkb[c] = s_kb[c][it][t * NP + pi];
-        pws = s_xw[it][t][s == 0 ? 1 : 0];
-      } else {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) pkb[c] = c2dt * a.A[c][pn];
-        double f[4];
-        node_flux(0, g, pq[0], pq[1], pq[2], pq[3], a.S[pn], a.invr[pn], f, &pws);
-      }
-      const double ows = s_xw[e][t][s];
-      // correction coefficients: R side (node 0) +invJx/w0, L side (node L) -invJx/wL
-      const double cfo = s == 0 ? invJx * B.iw0 : -invJx * B.iwL;
-      const double cfp = s == 0 ? -invJx * B.iwL : invJx * B.iw0;
-      const double wsL = s == 0 ? pws : ows, wsR = s == 0 ? ows : pws;
-      const double lam = (wsR > wsL) ? wsR : wsL;
-      const bool own_wins = (s == 0) ? (wsR > wsL) : !(wsR > wsL);
-      double lamb = 0.0;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const double fsb = fma(cfo, kb[c][io], cfp * pkb[c]);
-        Fb[c][io] = fma(-cfo, kb[c][io], Fb[c][io]) + 0.5 * fsb;
-        const double qL = s == 0 ? pq[c] : q[c][io], qR = s == 0 ? q[c][io] : pq[c];
-        qbr[c][io] += (s == 0 ? -0.5 : 0.5) * lam * fsb;
-        lamb = fma(0.5 * fsb, qL - qR, lamb);
-      }
-      if (own_wins) {
-        double qq[4] = {0, 0, 0, 0};
-        wavespeed_rev(0, g, q[0][io], q[1][io], q[3][io], ir[io], lamb, qq, gb);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) qbr[c][io] += qq[c];
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < NP; ++i) {
-      double fb[4] = {Fb[0][i], Fb[1][i], Fb[2][i], Fb[3][i]};
-      double qq[4] = {qbr[0][i], qbr[1][i], qbr[2][i], qbr[3][i]};
-      node_flux_rev(0, g, q[0][i], q[1][i], q[3][i], S[i], ir[i], fb, qq, Sbr[i], gb);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) s_pq[c][e][t * NP + i] = qq[c];
-      s_pq[4][e][t * NP + i] = Sbr[i];
-    }
-#pragma unroll
-    for (int i = 0; i < NP; ++i) s_pq[5][e][t * NP + i] = (i == 0) ? gb : 0.0;
-  }
-  __syncthreads();
-  if (!v.valid) return;
-  // ---- column t: F̄y, y-face LLF reverse, flux reverse, combination, outputs
-  double cq[4][NP], cS[NP], cir[NP], ckb[4][NP];
-#pragma unroll
-  for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) { cq[c][l] = a.q[c][n]; ckb[c][l] = s_kb[c][e][l * NP + t]; }
-    cS[l] = a.S[n]; cir[l] = a.invr[n];
-  }
-  double Fb[4][NP];
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-#pragma unroll
-    for (int k = 0; k < NP; ++k) Fb[c][k] = -invJy * dot_col<NP>(B, k, ckb[c], 0.0);
-  double qbc[4][NP], gb = 0.0;
-#pragma unroll
-  for (int l = 0; l < NP; ++l)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) qbc[c][l] = 0.0;
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const int lo = s == 0 ? 0 : L;
-    int it;
-    const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, 0, s == 0 ? -1 : 1, &it);
-    const int pl = s == 0 ? L : 0;
-    const long long pn = pb + pl * NP + t;
-    double pq[4], pkb[4], pws;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) pq[c] = a.q[c][pn];
-    if (it >= 0) {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) pkb[c] = s_kb[c][it][pl * NP + t];
-      pws = s_yw[it][t][s == 0 ? 1 : 0];
-    } else {
-#pragma unroll
-      for (int c = 0; c < 4; ++c) pkb[c] = c2dt * a.A[c][pn];
-      double f[4];
-      node_flux(1, g, pq[0], pq[1], pq[2], pq[3], a.S[pn], a.invr[pn], f, &pws);
-    }
-    const double ows = s_yw[e][t][s];
-    const double cfo = s == 0 ? invJy * B.iw0 : -invJy * B.iwL;
-    const double cfp = s == 0 ? -invJy * B.iwL : invJy * B.iw0;
+  // Reverse of one face's LLF flux for the own side: kb/pkb are the RHS
+  // adjoints at the own and partner face nodes; returns the flux adjoint
+  // increment and accumulates the own-state adjoint.
+  auto face_rev = [&](int dir, int s, const double oq[4], const double okb[4], double ows, double pws, const double pq[4],
+                      const double pkb[4], double ir_own, double fb[4], double qbo[4], double& gb) {
+    const double invJ = dir == 0 ? invJx : invJy;
+    // correction coefficients: R side (node 0) +invJ/w0, L side (node L) -invJ/wL
+    const double cfo = s == 0 ? invJ * B.iw0 : -invJ * B.iwL;
+    const double cfp = s == 0 ? -invJ * B.iwL : invJ * B.iw0;
     const double wsL = s == 0 ? pws : ows, wsR = s == 0 ? ows : pws;
     const double lam = (wsR > wsL) ? wsR : wsL;
     const bool own_wins = (s == 0) ? (wsR > wsL) : !(wsR > wsL);
     double lamb = 0.0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const double fsb = fma(cfo, ckb[c][lo], cfp * pkb[c]);
-      Fb[c][lo] = fma(-cfo, ckb[c][lo], Fb[c][lo]) + 0.5 * fsb;
-      const double qL = s == 0 ? pq[c] : cq[c][lo], qR = s == 0 ? cq[c][lo] : pq[c];
-      qbc[c][lo] += (s == 0 ? -0.5 : 0.5) * lam * fsb;
-      lamb = fma(0.5 * fsb, qL - qR, lamb);
+      const double fsb = fma(cfo, okb[c], cfp * pkb[c]);
+      fb[c] = fma(-cfo, okb[c], fb[c]) + 0.5 * fsb;
+      const double dq = s == 0 ? pq[c] - oq[c] : oq[c] - pq[c];  // q_L - q_R
+      qbo[c] = fma((s == 0 ? -0.5 : 0.5) * lam, fsb, qbo[c]);
+      lamb = fma(0.5 * fsb, dq, lamb);
     }
     if (own_wins) {
-      double qq[4] = {0, 0, 0, 0};
-      wavespeed_rev(1, g, cq[0][lo], cq[1][lo], cq[3][lo], cir[lo], lamb, qq, gb);
+      const double un = (dir == 0 ? oq[0] : oq[1]) * ir_own;
+      wavespeed_rev(dir, g, oq[0], oq[1], oq[3], ir_own, ows - fabs(un), lamb, qbo, gb);
+    }
+  };
+  double gb = 0.0;
+  // ---- phase 2a (row of vr): x flux adjoint = transpose of the x volume term + x-face LLF reverse
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
+    double kb[4][NP], fb[4][NP], qbo[4][NP];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) qbc[c][lo] += qq[c];
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int i = 0; i < NP; ++i) { kb[c][i] = s_kb[c][e][t * NP + i]; qbo[c][i] = 0.0; }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int k = 0; k < NP; ++k) fb[c][k] = -invJx * dot_col<NP>(B, k, kb[c], 0.0);
+    struct PF { double q[4], kb[4], ws; };
+    auto fetch = [&](int s) {
+      PF P;
+      int it;
+      const long long pb = neighbour<NP>(tl, I, vr.ex, vr.ey, s == 0 ? -1 : 1, 0, &it);
+      const int pi = s == 0 ? L : 0;
+      if (it >= 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) { P.q[c] = s_q[c][it][t * NP + pi]; P.kb[c] = s_kb[c][it][t * NP + pi]; }
+        P.ws = s_xw[it][t][s == 0 ? 1 : 0];
+      } else {
+        const long long pn = pb + t * NP + pi;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) { P.q[c] = a.q[c][pn]; P.kb[c] = c2dt * a.A[c][pn]; }
+        P.ws = a.ws_x[pn];
+      }
+      return P;
+    };
+    const int sf = first_side(vr.ext, TX);
+    const PF pA = fetch(sf), pB = fetch(1 - sf);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const PF& P = (s == sf) ? pA : pB;
+      const int io = s == 0 ? 0 : L;
+      double oq[4], okb[4], f4[4], q4[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) { oq[c] = s_q[c][e][t * NP + io]; okb[c] = kb[c][io]; f4[c] = fb[c][io]; q4[c] = qbo[c][io]; }
+      face_rev(0, s, oq, okb, s_xw[e][t][s], P.ws, P.q, P.kb, a.invr[vr.base + t * NP + io], f4, q4, gb);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) { fb[c][io] = f4[c]; qbo[c][io] = q4[c]; }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int i = 0; i < NP; ++i) { s_fbx[c][e][t * NP + i] = fb[c][i]; s_qbx[c][e][t * NP + i] = qbo[c][i]; }
+    s_grow[e][t] = gb;
+    gb = 0.0;
+  }
+  // ---- phase 2b (column of vc): y flux adjoint + y-face LLF reverse (registers)
+  double fby[4][NP], qby[4][NP];
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
+    double kb[4][NP];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int l = 0; l < NP; ++l) { kb[c][l] = s_kb[c][e][l * NP + t]; qby[c][l] = 0.0; }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int k = 0; k < NP; ++k) fby[c][k] = -invJy * dot_col<NP>(B, k, kb[c], 0.0);
+    struct PF { double q[4], kb[4], ws; };
+    auto fetch = [&](int s) {
+      PF P;
+      int it;
+      const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
+      const int pl = s == 0 ? L : 0;
+      if (it >= 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) { P.q[c] = s_q[c][it][pl * NP + t]; P.kb[c] = s_kb[c][it][pl * NP + t]; }
+        P.ws = s_yw[it][t][s == 0 ? 1 : 0];
+      } else {
+        const long long pn = pb + pl * NP + t;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) { P.q[c] = a.q[c][pn]; P.kb[c] = c2dt * a.A[c][pn]; }
+        P.ws = a.ws_y[pn];
+      }
+      return P;
+    };
+    const int sf = first_side(vc.eyt, TY);
+    const PF pA = fetch(sf), pB = fetch(1 - sf);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const PF& P = (s == sf) ? pA : pB;
+      const int lo = s == 0 ? 0 : L;
+      double oq[4], okb[4], f4[4], q4[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) { oq[c] = s_q[c][e][lo * NP + t]; okb[c] = kb[c][lo]; f4[c] = fby[c][lo]; q4[c] = qby[c][lo]; }
+      face_rev(1, s, oq, okb, s_yw[e][t][s], P.ws, P.q, P.kb, a.invr[vc.base + lo * NP + t], f4, q4, gb);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) { fby[c][lo] = f4[c]; qby[c][lo] = q4[c]; }
     }
   }
-  double gsum = 0.0;
+  __syncthreads();
+  if (!vc.valid) return;
+  // ---- phase 3 (column of vc): merged flux reverse per node, combination, outputs
+  const int t = vc.t, e = vc.e;
+  gb += s_grow[e][t];
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
-    double fb[4] = {Fb[0][l], Fb[1][l], Fb[2][l], Fb[3][l]};
-    double qq[4];
+    const long long n = vc.base + l * NP + t;
+    const int nd = l * NP + t;
+    double fbx[4], fbyl[4], qq[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) qq[c] = qbc[c][l] + s_pq[c][e][l * NP + t];
-    double Sb = s_pq[4][e][l * NP + t];
-    node_flux_rev(1, g, cq[0][l], cq[1][l], cq[3][l], cS[l], cir[l], fb, qq, Sb, gb);
-    gsum += s_pq[5][e][l * NP + t];
+    for (int c = 0; c < 4; ++c) { fbx[c] = s_fbx[c][e][nd]; fbyl[c] = fby[c][l]; qq[c] = qby[c][l] + s_qbx[c][e][nd]; }
+    double Sb = 0.0;
+    node_phys_rev(g, s_q[0][e][nd], s_q[1][e][nd], s_q[3][e][nd], a.S[n], a.invr[n], fbx, fbyl, qq, Sb, gb);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const double Av = a.A[c][n];
@@ -305,8 +296,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rev(HypRevArgs2D a) {
     a.Sb[n] = Sbt;
     if (a.srev == SREV_CHEB) {
       // x_n = x_{n-1} + d_n ; d_n = a_n d_{n-1} + c_n z_n ; z_n = M^-1 r_{n-1}
-      const double zb = a.cc * Sbt;
-      const double u = a.cinvM[n] * zb;
+      const double u = a.cinvM[n] * (a.cc * Sbt);
       a.u_out[n] = u;
       a.Mb[n] = -u * a.r_last[n] * a.cinvM[n];
       a.db[n] = a.ca * Sbt;
@@ -317,7 +307,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rev(HypRevArgs2D a) {
       a.Mb[n] = -u * a.r_last[n] * a.cinvM[n];
     }
   }
-  a.gnode[v.base + t] += gb + gsum;
+  a.gnode[vc.base + t] += gb;
 }
 
 // ---------------------------------------------------------------------------
@@ -339,81 +329,93 @@ struct ApplyRevArgs2D {
   double ca, cc, omega;
 };
 
+// Partner data across one face for the reverse apply: values and end-node
+// derivatives of u and of x_k, the partner's stiffness coefficient and 1/rho.
+struct Partner2 { double u, v, du, dv, k, ir; };
+
 template <int NP, int SREV>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D a) {
   using TL = Tiling2D<NP>;
-  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L;
+  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
   __shared__ double s_u[TE][NN], s_v[TE][NN], s_yx[TE][NN], s_zr[TE][NN];
   __shared__ double s_gxf[2][TE][NP][2], s_gyf[2][TE][NP][2];  // [u|v] face derivatives
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const ElemView v = elem_view<NP>(tl, I);
+  const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
-  const int t = v.t, e = v.e;
   const double hw = B.hw;
 
-  double ur[NP], vr[NP], gxu[NP], gxv[NP];
-  double uc[NP], vc[NP], gyu[NP], gyv[NP];
-  if (v.valid) {
+  double ur[NP], vr_[NP], gxu[NP], gxv[NP];
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      const long long n = v.base + t * NP + i;
-      ur[i] = a.u[n]; vr[i] = a.xk[n];
-      s_u[e][t * NP + i] = ur[i]; s_v[e][t * NP + i] = vr[i];
+      const long long n = vr.base + t * NP + i;
+      ur[i] = a.u[n]; vr_[i] = a.xk[n];
+      s_u[e][t * NP + i] = ur[i]; s_v[e][t * NP + i] = vr_[i];
     }
 #pragma unroll
-    for (int i = 0; i < NP; ++i) { gxu[i] = dot_row<NP>(B, i, ur); gxv[i] = dot_row<NP>(B, i, vr); }
+    for (int i = 0; i < NP; ++i) { gxu[i] = dot_row<NP>(B, i, ur); gxv[i] = dot_row<NP>(B, i, vr_); }
     s_gxf[0][e][t][0] = gxu[0]; s_gxf[0][e][t][1] = gxu[L];
     s_gxf[1][e][t][0] = gxv[0]; s_gxf[1][e][t][1] = gxv[L];
   }
   __syncthreads();
-  if (v.valid) {
+  double uc[NP], vc_[NP], gyu[NP], gyv[NP];
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
 #pragma unroll
-    for (int l = 0; l < NP; ++l) { uc[l] = s_u[e][l * NP + t]; vc[l] = s_v[e][l * NP + t]; }
+    for (int l = 0; l < NP; ++l) { uc[l] = s_u[e][l * NP + t]; vc_[l] = s_v[e][l * NP + t]; }
 #pragma unroll
-    for (int l = 0; l < NP; ++l) { gyu[l] = dot_row<NP>(B, l, uc); gyv[l] = dot_row<NP>(B, l, vc); }
+    for (int l = 0; l < NP; ++l) { gyu[l] = dot_row<NP>(B, l, uc); gyv[l] = dot_row<NP>(B, l, vc_); }
     s_gyf[0][e][t][0] = gyu[0]; s_gyf[0][e][t][1] = gyu[L];
     s_gyf[1][e][t][0] = gyv[0]; s_gyf[1][e][t][1] = gyv[L];
-
-    // ---- row t: x faces
+  }
+  if (vr.valid) {
+    // ---- row of vr: x faces
+    const int t = vr.t, e = vr.e;
     double kxr[NP], zr[NP];
 #pragma unroll
-    for (int i = 0; i < NP; ++i) { kxr[i] = a.ckx[v.base + t * NP + i]; zr[i] = kxr[i] * gxu[i] * gxv[i]; }
-    double pu[2], pv[2], pdu[2], pdv[2], pk[2], pir[2];
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
+    for (int i = 0; i < NP; ++i) { kxr[i] = a.ckx[vr.base + t * NP + i]; zr[i] = kxr[i] * gxu[i] * gxv[i]; }
+    auto fetch = [&](int s) {
+      Partner2 P;
       int it;
-      const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, s == 0 ? -1 : 1, 0, &it);
+      const long long pb = neighbour<NP>(tl, I, vr.ex, vr.ey, s == 0 ? -1 : 1, 0, &it);
       const int pi = s == 0 ? L : 0;
-      pk[s] = a.ckx[pb + t * NP + pi];
-      pir[s] = a.invr[pb + t * NP + pi];
+      P.k = a.ckx[pb + t * NP + pi];
+      P.ir = a.invr[pb + t * NP + pi];
       if (it >= 0) {
-        pu[s] = s_u[it][t * NP + pi]; pv[s] = s_v[it][t * NP + pi];
-        pdu[s] = s_gxf[0][it][t][s == 0 ? 1 : 0]; pdv[s] = s_gxf[1][it][t][s == 0 ? 1 : 0];
+        P.u = s_u[it][t * NP + pi]; P.v = s_v[it][t * NP + pi];
+        P.du = s_gxf[0][it][t][s == 0 ? 1 : 0]; P.dv = s_gxf[1][it][t][s == 0 ? 1 : 0];
       } else {
         double pr[NP], pw[NP];
 #pragma unroll
         for (int k = 0; k < NP; ++k) { pr[k] = a.u[pb + t * NP + k]; pw[k] = a.xk[pb + t * NP + k]; }
-        pu[s] = pr[pi]; pv[s] = pw[pi];
-        pdu[s] = dot_row<NP>(B, pi, pr); pdv[s] = dot_row<NP>(B, pi, pw);
+        P.u = s == 0 ? pr[L] : pr[0];
+        P.v = s == 0 ? pw[L] : pw[0];
+        P.du = dot_end<NP>(B, s == 0, pr);
+        P.dv = dot_end<NP>(B, s == 0, pw);
       }
-    }
-    const double irl0 = a.invr[v.base + t * NP], irlL = a.invr[v.base + t * NP + L];
+      return P;
+    };
+    const int sf = first_side(vr.ext, TX);
+    const Partner2 pA = fetch(sf), pB = fetch(1 - sf);
+    const Partner2 pl = sf == 0 ? pA : pB, prt = sf == 0 ? pB : pA;
+    const double irl0 = a.invr[vr.base + t * NP], irlL = a.invr[vr.base + t * NP + L];
     // left face (own R side, node 0)
-    const double jul = pu[0] - ur[0], jvl = pv[0] - vr[0];
-    const double pl_ = a.cpx[v.base + t * NP];
-    const double Fl = fma(pl_, jul, hw * fma(pk[0], pdu[0], kxr[0] * gxu[0]));
+    const double jul = pl.u - ur[0], jvl = pl.v - vr_[0];
+    const double pl_ = a.cpx[vr.base + t * NP];
+    const double Fl = fma(pl_, jul, hw * fma(pl.k, pl.du, kxr[0] * gxu[0]));
     zr[0] = fma(hw * kxr[0], fma(gxv[0], jul, gxu[0] * jvl), zr[0]);
-    if (irl0 > pir[0]) zr[0] = fma(pl_ * jvl, jul, zr[0]);  // R wins only when strictly larger
+    if (irl0 > pl.ir) zr[0] = fma(pl_ * jvl, jul, zr[0]);  // R wins only when strictly larger
     // right face (own L side, node L)
-    const double jur = ur[L] - pu[1], jvr = vr[L] - pv[1];
-    const double pr_ = a.cpx[v.base + t * NP + L];
-    const double Fr = fma(pr_, jur, hw * fma(kxr[L], gxu[L], pk[1] * pdu[1]));
+    const double jur = ur[L] - prt.u, jvr = vr_[L] - prt.v;
+    const double pr_ = a.cpx[vr.base + t * NP + L];
+    const double Fr = fma(pr_, jur, hw * fma(kxr[L], gxu[L], prt.k * prt.du));
     zr[L] = fma(hw * kxr[L], fma(gxv[L], jur, gxu[L] * jvr), zr[L]);
-    if (!(pir[1] > irlL)) zr[L] = fma(pr_ * jvr, jur, zr[L]);
+    if (!(prt.ir > irlL)) zr[L] = fma(pr_ * jvr, jur, zr[L]);
     double sx[NP];
 #pragma unroll
-    for (int i = 0; i < NP; ++i) sx[i] = kxr[i] * gxu[i];
+    for (int i = 1; i < L; ++i) sx[i] = kxr[i] * gxu[i];
     sx[0] = kxr[0] * fma(hw, jul, gxu[0]);
     sx[L] = kxr[L] * fma(hw, jur, gxu[L]);
 #pragma unroll
@@ -424,53 +426,59 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
     }
   }
   __syncthreads();
-  if (!v.valid) return;
-  // ---- column t: y faces, transposes, outputs
+  if (!vc.valid) return;
+  // ---- column of vc: y faces, transposes, outputs
+  const int t = vc.t, e = vc.e;
   double kyc[NP], zc[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) { kyc[l] = a.cky[v.base + l * NP + t]; zc[l] = kyc[l] * gyu[l] * gyv[l]; }
-  double qu[2], qv[2], qdu[2], qdv[2], qk[2], qir[2];
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
+  for (int l = 0; l < NP; ++l) { kyc[l] = a.cky[vc.base + l * NP + t]; zc[l] = kyc[l] * gyu[l] * gyv[l]; }
+  auto fetchy = [&](int s) {
+    Partner2 P;
     int it;
-    const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, 0, s == 0 ? -1 : 1, &it);
+    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
     const int pl = s == 0 ? L : 0;
-    qk[s] = a.cky[pb + pl * NP + t];
-    qir[s] = a.invr[pb + pl * NP + t];
+    P.k = a.cky[pb + pl * NP + t];
+    P.ir = a.invr[pb + pl * NP + t];
     if (it >= 0) {
-      qu[s] = s_u[it][pl * NP + t]; qv[s] = s_v[it][pl * NP + t];
-      qdu[s] = s_gyf[0][it][t][s == 0 ? 1 : 0]; qdv[s] = s_gyf[1][it][t][s == 0 ? 1 : 0];
+      P.u = s_u[it][pl * NP + t]; P.v = s_v[it][pl * NP + t];
+      P.du = s_gyf[0][it][t][s == 0 ? 1 : 0]; P.dv = s_gyf[1][it][t][s == 0 ? 1 : 0];
     } else {
       double pc[NP], pw[NP];
 #pragma unroll
       for (int k = 0; k < NP; ++k) { pc[k] = a.u[pb + k * NP + t]; pw[k] = a.xk[pb + k * NP + t]; }
-      qu[s] = pc[pl]; qv[s] = pw[pl];
-      qdu[s] = dot_row<NP>(B, pl, pc); qdv[s] = dot_row<NP>(B, pl, pw);
+      P.u = s == 0 ? pc[L] : pc[0];
+      P.v = s == 0 ? pw[L] : pw[0];
+      P.du = dot_end<NP>(B, s == 0, pc);
+      P.dv = dot_end<NP>(B, s == 0, pw);
     }
-  }
-  const double ic0 = a.invr[v.base + t], icL = a.invr[v.base + L * NP + t];
-  const double jub = qu[0] - uc[0], jvb = qv[0] - vc[0];
-  const double pbot = a.cpy[v.base + t];
-  const double Fb = fma(pbot, jub, hw * fma(qk[0], qdu[0], kyc[0] * gyu[0]));
+    return P;
+  };
+  const int sf = first_side(vc.eyt, TY);
+  const Partner2 qA = fetchy(sf), qB = fetchy(1 - sf);
+  const Partner2 qb = sf == 0 ? qA : qB, qt = sf == 0 ? qB : qA;
+  const double ic0 = a.invr[vc.base + t], icL = a.invr[vc.base + L * NP + t];
+  const double jub = qb.u - uc[0], jvb = qb.v - vc_[0];
+  const double pbot = a.cpy[vc.base + t];
+  const double Fb = fma(pbot, jub, hw * fma(qb.k, qb.du, kyc[0] * gyu[0]));
   zc[0] = fma(hw * kyc[0], fma(gyv[0], jub, gyu[0] * jvb), zc[0]);
-  if (ic0 > qir[0]) zc[0] = fma(pbot * jvb, jub, zc[0]);
-  const double jut = uc[L] - qu[1], jvt = vc[L] - qv[1];
-  const double ptop = a.cpy[v.base + L * NP + t];
-  const double Ft = fma(ptop, jut, hw * fma(kyc[L], gyu[L], qk[1] * qdu[1]));
+  if (ic0 > qb.ir) zc[0] = fma(pbot * jvb, jub, zc[0]);
+  const double jut = uc[L] - qt.u, jvt = vc_[L] - qt.v;
+  const double ptop = a.cpy[vc.base + L * NP + t];
+  const double Ft = fma(ptop, jut, hw * fma(kyc[L], gyu[L], qt.k * qt.du));
   zc[L] = fma(hw * kyc[L], fma(gyv[L], jut, gyu[L] * jvt), zc[L]);
-  if (!(qir[1] > icL)) zc[L] = fma(ptop * jvt, jut, zc[L]);
+  if (!(qt.ir > icL)) zc[L] = fma(ptop * jvt, jut, zc[L]);
   double sy[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) sy[l] = kyc[l] * gyu[l];
+  for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gyu[l];
   sy[0] = kyc[0] * fma(hw, jub, gyu[0]);
   sy[L] = kyc[L] * fma(hw, jut, gyu[L]);
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
+    const long long n = vc.base + l * NP + t;
     const double cmn = a.cm[n];
     double w = fma(cmn, uc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
     w = dot_col<NP>(B, l, sy, w);
-    const double zm = a.zscale * (cmn * uc[l] * vc[l]);
+    const double zm = a.zscale * (cmn * uc[l] * vc_[l]);
     const double zs = a.zscale * (zc[l] + s_zr[e][l * NP + t]);
     const double xb = a.xb[n] - w;
     a.xb[n] = xb;
@@ -514,20 +522,20 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
   __shared__ double s_ir[TE][NN], s_ib[TE][NN];         // 1/rho; row-phase d/d(1/rho) from diag(A)
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const ElemView v = elem_view<NP>(tl, I);
+  const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
-  const int t = v.t, e = v.e;
   const double invJx = I.ijx, invJy = I.ijy;
   const double alpha = I.alpha;
   if (alpha <= 0.0) return;
   const double eta = (double)(NP * NP);
 
-  double ux[NP], uy[NP], Mbr[NP];
-  if (v.valid) {
+  if (vr.valid) {
+    const int t = vr.t, e = vr.e;
+    double ux[NP], uy[NP], Mbr[NP];
     const double cxs = alpha * B.w[t] * I.jy * invJx;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      const long long n = v.base + t * NP + i;
+      const long long n = vr.base + t * NP + i;
       const double ir = a.invr[n];
       ux[i] = a.mx[n] * ir; uy[i] = a.my[n] * ir; Mbr[i] = a.Mb[n];
       s_ux[e][t * NP + i] = ux[i]; s_uy[e][t * NP + i] = uy[i]; s_Mb[e][t * NP + i] = Mbr[i]; s_ir[e][t * NP + i] = ir;
@@ -544,28 +552,28 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
     }
   }
   __syncthreads();
-  // ---- column t: y derivatives, source adjoint, y transposes, diag(A) y part and faces
+  // ---- column of vc: y derivatives, source adjoint, y transposes, diag(A) y part and faces
   double cux[NP], cuy[NP], cMb[NP], cir[NP];
   double uxb[NP], uyb[NP], ib[NP];
-  if (v.valid) {
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
 #pragma unroll
     for (int l = 0; l < NP; ++l) {
       cux[l] = s_ux[e][l * NP + t]; cuy[l] = s_uy[e][l * NP + t]; cMb[l] = s_Mb[e][l * NP + t]; cir[l] = s_ir[e][l * NP + t];
-      uxb[l] = 0.0; uyb[l] = 0.0;
     }
     const double cys = alpha * B.w[t] * I.jx * invJy;
     double bxy[NP], byy[NP];
 #pragma unroll
     for (int l = 0; l < NP; ++l) {
-      const long long n = v.base + l * NP + t;
+      const long long n = vc.base + l * NP + t;
       const double uxy = dot_row<NP>(B, l, cux) * invJy, uyy = dot_row<NP>(B, l, cuy) * invJy;
       const double uxx = s_uxx[e][l * NP + t], uyx = s_uyx[e][l * NP + t];
       const double s = uxx + uyy;
-      const double Qb = a.bb[n] * (B.w[t] * B.w[l] * I.jx * I.jy * alpha);
-      s_bxx[e][l * NP + t] = Qb * 2.0 * (s + uxx);
-      s_byx[e][l * NP + t] = Qb * 2.0 * uxy;
-      bxy[l] = Qb * 2.0 * uyx * invJy;
-      byy[l] = Qb * 2.0 * (s + uyy) * invJy;
+      const double Qb2 = 2.0 * a.bb[n] * (B.w[t] * B.w[l] * I.jx * I.jy * alpha);
+      s_bxx[e][l * NP + t] = Qb2 * (s + uxx);
+      s_byx[e][l * NP + t] = Qb2 * uxy;
+      bxy[l] = Qb2 * uyx * invJy;
+      byy[l] = Qb2 * (s + uyy) * invJy;
       // y stiffness self-coupling of diag(A)
       double sm = B.W2[l][0] * cMb[0];
 #pragma unroll
@@ -574,57 +582,59 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
     }
     // y transposes of the source adjoint: ux[t,k] gets D[l][k] * bxy[l]
 #pragma unroll
-    for (int k = 0; k < NP; ++k) { uxb[k] = dot_col<NP>(B, k, bxy, uxb[k]); uyb[k] = dot_col<NP>(B, k, byy, uyb[k]); }
+    for (int k = 0; k < NP; ++k) { uxb[k] = dot_col<NP>(B, k, bxy, 0.0); uyb[k] = dot_col<NP>(B, k, byy, 0.0); }
     // diag(A) face terms, x faces (t == 0: own R side; t == L: own L side)
     if (t == 0 || t == L) {
       int it;
-      const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, t == 0 ? -1 : 1, 0, &it);
+      const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, t == 0 ? -1 : 1, 0, &it);
       const int pi = t == 0 ? L : 0;
+      const double cself = (t == L ? -alpha * invJx * B.D[L][L] : alpha * invJx * B.D[0][0]);
 #pragma unroll
       for (int l = 0; l < NP; ++l) {
         const double pir = it >= 0 ? s_ir[it][l * NP + pi] : a.invr[pb + l * NP + pi];
         const double pMb = it >= 0 ? s_Mb[it][l * NP + pi] : a.Mb[pb + l * NP + pi];
         const double wf = B.w[l] * I.jy;
-        ib[l] += cMb[l] * (t == L ? -alpha * invJx * B.D[L][L] : alpha * invJx * B.D[0][0]) * wf;
+        ib[l] = fma(cMb[l] * cself, wf, ib[l]);
         const double iL = t == L ? cir[l] : pir, iR = t == L ? pir : cir[l];
         const bool own_wins = (t == L) ? !(iR > iL) : (iR > iL);
-        if (own_wins) ib[l] += (cMb[l] + pMb) * alpha * wf * eta * I.idx;
+        if (own_wins) ib[l] = fma((cMb[l] + pMb) * alpha * wf, eta * I.idx, ib[l]);
       }
     }
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
       const int l = s == 0 ? 0 : L;
       int it;
-      const long long pb = neighbour<NP>(tl, I, v.ex, v.ey, 0, s == 0 ? -1 : 1, &it);
+      const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
       const int pl = s == 0 ? L : 0;
       const double pir = it >= 0 ? s_ir[it][pl * NP + t] : a.invr[pb + pl * NP + t];
       const double pMb = it >= 0 ? s_Mb[it][pl * NP + t] : a.Mb[pb + pl * NP + t];
       const double wf = B.w[t] * I.jx;
-      ib[l] += cMb[l] * (l == L ? -alpha * invJy * B.D[L][L] : alpha * invJy * B.D[0][0]) * wf;
+      ib[l] = fma(cMb[l] * (l == L ? -alpha * invJy * B.D[L][L] : alpha * invJy * B.D[0][0]), wf, ib[l]);
       const double iL = l == L ? cir[l] : pir, iR = l == L ? pir : cir[l];
       const bool own_wins = (l == L) ? !(iR > iL) : (iR > iL);
-      if (own_wins) ib[l] += (cMb[l] + pMb) * alpha * wf * eta * I.idy;
+      if (own_wins) ib[l] = fma((cMb[l] + pMb) * alpha * wf, eta * I.idy, ib[l]);
     }
   }
   __syncthreads();
-  if (!v.valid) return;
-  // ---- column t, final: x transposes of the source adjoint (need row data),
+  if (!vc.valid) return;
+  // ---- column of vc, final: x transposes of the source adjoint (need row data),
   // mass part of diag(A), conversion to d/d rho and d/d alpha
+  const int t = vc.t, e = vc.e;
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
     // ux[t,l] gets sum_i D[i][t] * bxx[i,l] * invJx (row l, x transpose at node t)
-    double rx[NP], ry[NP];
-#pragma unroll
-    for (int i = 0; i < NP; ++i) { rx[i] = s_bxx[e][l * NP + i]; ry[i] = s_byx[e][l * NP + i]; }
     double sxv = 0.0, syv = 0.0;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) { sxv = fma(B.D[i][t], rx[i], sxv); syv = fma(B.D[i][t], ry[i], syv); }
+    for (int i = 0; i < NP; ++i) {
+      sxv = fma(B.D[i][t], s_bxx[e][l * NP + i], sxv);
+      syv = fma(B.D[i][t], s_byx[e][l * NP + i], syv);
+    }
     uxb[l] = fma(invJx, sxv, uxb[l]);
     uyb[l] = fma(invJx, syv, uyb[l]);
   }
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
-    const long long n = v.base + l * NP + t;
+    const long long n = vc.base + l * NP + t;
     const double ir = cir[l];
     const double Mb = cMb[l];
     const double cmn = a.cm[n];

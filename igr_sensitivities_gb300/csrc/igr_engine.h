@@ -30,6 +30,7 @@ class Workspace {
   double* dbl(const std::string& name, size_t n) { return static_cast<double*>(get(name, n * sizeof(double))); }
   void release_all();
   size_t bytes() const;
+  size_t held(const std::string& name) const;  // current capacity of one named buffer (0 if absent)
 
  private:
   struct Buf { void* p = nullptr; size_t n = 0; };
@@ -66,6 +67,9 @@ struct Ctx {
   size_t tape_budget = 0;       // 0: derive from free device memory
   long long launches = 0;       // kernels launched by the last call (host-side count)
   long long cur_nodes = 0;      // nodes of the plan being executed (profiler bookkeeping)
+  // memory plan of the last adjoint call: instance groups, instances per group,
+  // steps taped per segment and segments per group (1 = no forward recompute)
+  int plan_groups = 0, plan_group_size = 0, plan_seg = 0, plan_nseg = 0;
   Profiler prof;
 };
 

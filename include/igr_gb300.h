@@ -87,6 +87,10 @@ int igr_profile_reset(igr_ctx* ctx);
 int igr_profile_read(igr_ctx* ctx, int kernel_family, double* total_ms, long long* launches);
 /* Nodes processed by the timed launches of a family (sum over launches). */
 int igr_profile_nodes(igr_ctx* ctx, int kernel_family, double* nodes);
+/* Memory plan of the last adjoint call: instance groups run one after the
+ * other, instances per group, RK steps taped per segment and segments per
+ * group (segments > 1 means the forward is recomputed from checkpoints). */
+int igr_last_adjoint_plan(const igr_ctx* ctx, int* groups, int* group_size, int* segment_steps, int* segments);
 /* Measured FP64 FMA throughput of the device in TFLOP/s (the roofline
  * denominator of this FP64-bound path; no reference counterpart). */
 int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops);

@@ -190,7 +190,7 @@ def test_checkpointed_adjoint_equals_full_tape(igr, oracle):
     full = igr.enzyme_adjoint_ic(*q0, 11, dt, basis, mesh, g, alpha, n_iter=5, solver="chebyshev", objective="l2_density",
                                  with_params=True, ctx=ctx)
     n = mesh.x.size
-    step_bytes = 3 * (14 + 2 * 5) * n * 8
+    step_bytes = 3 * (16 + 2 * 5) * n * 8
     ctx.set_tape_budget(3 * step_bytes + 10 * 6 * n * 8)
     seg = igr.enzyme_adjoint_ic(*q0, 11, dt, basis, mesh, g, alpha, n_iter=5, solver="chebyshev", objective="l2_density",
                                 with_params=True, ctx=ctx)
