@@ -68,6 +68,13 @@ class Context:
         check(self, lib().igr_last_launch_count(self.handle, C.byref(n)))
         return n.value
 
+    def last_adjoint_plan(self):
+        """Memory plan of the last adjoint call: instance groups, instances per
+        group, steps taped per segment and segments (recomputed from checkpoints)."""
+        v = [C.c_int(0) for _ in range(4)]
+        check(self, lib().igr_last_adjoint_plan(self.handle, *[C.byref(x) for x in v]))
+        return dict(zip(("groups", "instances_per_group", "steps_per_segment", "segments"), (x.value for x in v)))
+
 
 _default = None
 

@@ -223,20 +223,21 @@ static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const do
     const size_t avail = fr + c.ws.bytes();  // workspace buffers are reused or regrown
     const size_t reserve = (size_t)4 << 30;
     const bool apos = alphas[0] > 0;
-    const size_t F = 16 + (apos ? 2 * (size_t)n_iter : 0);
+    const size_t F = (size_t)stage_fields2d(Solve2DOpts{n_iter, solver}, apos, N, 1);
     // full tape (3 stages x F fields per step) + checkpoints + ~110 working fields per instance
     const size_t per_inst = ((size_t)3 * F * std::max(n_steps, 1) + 6 + 110) * N * sizeof(double);
     const size_t fit = avail > reserve ? (size_t)((avail - reserve) * 0.92) / per_inst : 0;
     G = (int)std::max<size_t>(1, std::min<size_t>((size_t)n_inst, fit));
-    if (G < n_inst) {  // equal-sized groups keep the workspace shapes identical across groups
-      const int ngroups = (n_inst + G - 1) / G;
-      G = (n_inst + ngroups - 1) / ngroups;
-    }
   }
-  c.plan_groups = (n_inst + G - 1) / G;
+  // balanced groups: sizes differ by at most one (workspace sized for the largest)
+  const int ngroups = (n_inst + G - 1) / G;
+  std::vector<int> gstart(ngroups + 1, 0);
+  for (int g = 0; g < ngroups; ++g) gstart[g + 1] = gstart[g] + n_inst / ngroups + (g < n_inst % ngroups ? 1 : 0);
+  G = gstart[1];
+  c.plan_groups = ngroups;
   c.plan_group_size = G;
-  for (int g0 = 0; g0 < n_inst; g0 += G) {
-    const int gn = std::min(G, n_inst - g0);
+  for (int gi = 0; gi < ngroups; ++gi) {
+    const int g0 = gstart[gi], gn = gstart[gi + 1] - gstart[gi];
     std::vector<Inst2DDesc> insts;
     for (int b = g0; b < g0 + gn; ++b) insts.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], alphas[b], dts[b]});
     Plan2D P = make_plan2d(c, B, insts, "adj");

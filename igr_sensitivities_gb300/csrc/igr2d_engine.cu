@@ -6,6 +6,7 @@
 
 #include "igr2d_kernels.cuh"
 #include "igr2d_launch.h"
+#include "igr2d_pcg_kernels.cuh"
 #include "igr2d_rev_kernels.cuh"
 #include "igr_engine.h"
 
@@ -139,12 +140,14 @@ Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& ins
     I.gamma = d.gamma; I.alpha = d.alpha; I.dt = d.dt;
     I.ijx = 1.0 / I.jx; I.ijy = 1.0 / I.jy; I.idx = 1.0 / I.dx; I.idy = 1.0 / I.dy;
     I.ialpha = d.alpha > 0 ? 1.0 / d.alpha : 0.0;
+    I.tile0 = (int)P.tiles.size();
+    for (int ey0 = 0; ey0 < d.ney; ey0 += ty)
+      for (int ex0 = 0; ex0 < d.nex; ex0 += tx) P.tiles.push_back(Tile2D{(int)i, ex0, ey0, 0});
+    I.ntiles = (int)P.tiles.size() - I.tile0;
     P.inst.push_back(I);
     const long long n = (long long)P.np * P.np * d.nex * d.ney;
     P.inst_nodes.push_back(n);
     off += n;
-    for (int ey0 = 0; ey0 < d.ney; ey0 += ty)
-      for (int ex0 = 0; ex0 < d.nex; ex0 += tx) P.tiles.push_back(Tile2D{(int)i, ex0, ey0, 0});
   }
   P.NG = off;
   c.cur_nodes = off;
@@ -312,16 +315,36 @@ struct StageBuf {
   double* Sout = nullptr;
   double *b = nullptr, *cm = nullptr, *ckx = nullptr, *cky = nullptr, *cinvM = nullptr, *cpx = nullptr, *cpy = nullptr, *cM = nullptr;
   double *wsx = nullptr, *wsy = nullptr;  // LLF wave speeds at face nodes
-  std::vector<double*> xk, rk;  // taped iterates (empty when untaped)
+  // taped solver iterates (empty when untaped). Jacobi / Chebyshev: xk = x_k,
+  // rk = r_k (k < n). PCG: x0t = x_0, rk = r_0..r_n, pk = p_k, apk = A p_k,
+  // scal = per-instance rz_0..rz_n then pAp_0..pAp_{n-1}.
+  std::vector<double*> xk, rk;
+  std::vector<double*> gxk, gyk;  // taped reference derivatives of the iterates (optional)
+  std::vector<double*> pk, apk;
+  double* x0t = nullptr;
+  double* scal = nullptr;
 };
 
 constexpr int STAGE_FIXED_FIELDS = 16;  // q(4) invr Sout b cm ckx cky cinvM cpx cpy cM wsx wsy
+// Taping the reference derivatives of the Jacobi / Chebyshev iterates saves
+// two line contractions per reverse apply but adds two fields per iteration to
+// the tape; on the 32 x 128^2 P3 Chebyshev-5 adjoint the smaller tape (more
+// instances per group) measured faster (3.77 vs 3.59 gradients/s), so the
+// reverse recomputes them.
+constexpr bool TAPE_ITERATE_DERIVATIVES = false;
 
-static int stage_fields(const Solve2DOpts& o, bool alpha_pos) {
-  return STAGE_FIXED_FIELDS + (alpha_pos ? 2 * o.n_iter : 0);
+static int pcg_scal_fields(const Solve2DOpts& o, long long NG, int ni) {
+  const long long need = (long long)(2 * o.n_iter + 1) * ni;
+  return (int)((need + NG - 1) / NG);
 }
 
-static StageBuf stage_from(double* base, long long NG, const Solve2DOpts& o, bool alpha_pos, bool taped) {
+int stage_fields2d(const Solve2DOpts& o, bool alpha_pos, long long NG, int ni) {
+  if (!alpha_pos) return STAGE_FIXED_FIELDS;
+  if (o.solver == SOLVER_PCG) return STAGE_FIXED_FIELDS + 1 + (o.n_iter + 1) + 2 * o.n_iter + pcg_scal_fields(o, NG, ni);
+  return STAGE_FIXED_FIELDS + (TAPE_ITERATE_DERIVATIVES ? 4 : 2) * o.n_iter;
+}
+
+static StageBuf stage_from(double* base, long long NG, const Solve2DOpts& o, bool alpha_pos, bool taped, int ni) {
   StageBuf s;
   int f = 0;
   auto nxt = [&]() { return base + (long long)(f++) * NG; };
@@ -330,8 +353,21 @@ static StageBuf stage_from(double* base, long long NG, const Solve2DOpts& o, boo
   s.cinvM = nxt(); s.cpx = nxt(); s.cpy = nxt(); s.cM = nxt();
   s.wsx = nxt(); s.wsy = nxt();
   if (taped && alpha_pos) {
-    for (int k = 0; k < o.n_iter; ++k) s.xk.push_back(nxt());
-    for (int k = 0; k < o.n_iter; ++k) s.rk.push_back(nxt());
+    if (o.solver == SOLVER_PCG) {
+      s.x0t = nxt();
+      for (int k = 0; k <= o.n_iter; ++k) s.rk.push_back(nxt());
+      for (int k = 0; k < o.n_iter; ++k) s.pk.push_back(nxt());
+      for (int k = 0; k < o.n_iter; ++k) s.apk.push_back(nxt());
+      s.scal = base + (long long)f * NG;
+      f += pcg_scal_fields(o, NG, ni);
+    } else {
+      for (int k = 0; k < o.n_iter; ++k) s.xk.push_back(nxt());
+      for (int k = 0; k < o.n_iter; ++k) s.rk.push_back(nxt());
+      if (TAPE_ITERATE_DERIVATIVES) {
+        for (int k = 0; k < o.n_iter; ++k) s.gxk.push_back(nxt());
+        for (int k = 0; k < o.n_iter; ++k) s.gyk.push_back(nxt());
+      }
+    }
   }
   return s;
 }
@@ -345,6 +381,75 @@ static bool all_alpha_pos(const Plan2D& P) {
   return true;
 }
 
+// Per-tile partial sums and per-instance arrival counters of the in-kernel
+// reductions (the counters are left at zero by every reduction).
+static void reduction_scratch(Ctx& c, const Plan2D& P, double** partials, int** counters) {
+  *partials = c.ws.dbl("red:part", P.ntiles());
+  *counters = static_cast<int*>(c.ws.get("red:cnt", sizeof(int) * P.inst.size()));
+  cuda_check(cudaMemsetAsync(*counters, 0, sizeof(int) * P.inst.size(), c.stream), "reset counters");
+}
+
+static void tile_geometry(const Plan2D& P, int* tx, int* ty) { tile_shape(P.np, tx, ty); }
+
+// Fixed-count Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347) on
+// the stage's operator: x_0 = warm start, result in st.Sout. Per iteration
+// one operator kernel (A p_k and p_k . A p_k, with p_k formed on load) and one
+// pointwise kernel (x, r and r . M^-1 r). With a tape slot, r_k, p_k, A p_k
+// and the scalars are written straight into it.
+static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* x0, double* xa, double* xb,
+                      double* dbuf) {
+  const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
+  const long long NG = P.NG;
+  const bool taped = st.x0t != nullptr;
+  double* part;
+  int* cnt;
+  reduction_scratch(c, P, &part, &cnt);
+  double* scal = taped ? st.scal : c.ws.dbl("pcg:scal", (size_t)(2 * n + 1) * ni);
+  double* apbuf = taped ? nullptr : c.ws.dbl("pcg:ap", NG);
+  auto RZ = [&](int k) { return scal + (long long)k * ni; };
+  auto PAP = [&](int k) { return scal + (long long)(n + 1 + k) * ni; };
+  auto R = [&](int k) { return taped ? st.rk[k] : xa; };
+  auto PK = [&](int k) { return taped ? st.pk[k] : ((k % 2 == 0) ? xb : dbuf); };
+  auto AP = [&](int k) { return taped ? st.apk[k] : apbuf; };
+  int tx, ty;
+  tile_geometry(P, &tx, &ty);
+  ApplyArgs2D base;
+  std::memset(&base, 0, sizeof(base));
+  base.tiles = P.d_tiles; base.inst = P.d_inst; base.B = P.B;
+  base.cm = st.cm; base.ckx = st.ckx; base.cky = st.cky; base.cpx = st.cpx; base.cpy = st.cpy; base.b = st.b; base.cinvM = st.cinvM;
+  base.partials = part; base.counters = cnt;
+  {  // r_0 = b - A x_0, p_0 = M^-1 r_0, rz_0
+    ApplyArgs2D a = base;
+    a.x = x0;
+    a.tape_x = taped ? st.x0t : nullptr;
+    a.r_out = R(0); a.p_out = PK(0); a.red_out = RZ(0);
+    LaunchScope ls(c, KID_APPLY);
+    NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG0, a, nb, c.stream));
+  }
+  for (int k = 0; k < n; ++k) {
+    {
+      ApplyArgs2D a = base;
+      if (k == 0) {
+        a.x = PK(0);
+      } else {
+        a.pcg_r = R(k); a.pcg_p = PK(k - 1); a.rz_cur = RZ(k); a.rz_prev = RZ(k - 1);
+        a.p_out = PK(k);
+      }
+      a.ap_out = AP(k); a.red_out = PAP(k);
+      LaunchScope ls(c, KID_APPLY);
+      NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG, a, nb, c.stream));
+    }
+    PcgUpdateArgs u;
+    u.tiles = P.d_tiles; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
+    u.x_in = k == 0 ? x0 : st.Sout; u.x_out = st.Sout;
+    u.p = PK(k); u.ap = AP(k); u.r_in = R(k); u.r_out = R(k + 1); u.cinvM = st.cinvM;
+    u.rz = RZ(k); u.pap = PAP(k); u.rz_out = RZ(k + 1);
+    u.partials = part; u.counters = cnt;
+    LaunchScope ls(c, KID_OTHER);
+    k2_pcg_update<<<nb, PCG_THREADS, 0, c.stream>>>(u);
+  }
+}
+
 // Setup + fixed-count solve of one stage. x0: warm start (read only);
 // result in st.Sout; xa/xb/dbuf: scratch.
 static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* x0, double* xa,
@@ -356,7 +461,10 @@ static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf&
   sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
   sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = st.cM;
   { LaunchScope ls(c, KID_SETUP); NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, nb, c.stream)); }
-  if (o.solver == SOLVER_PCG) throw Error(1, "PCG is not available in this build of the 2D engine");
+  if (o.solver == SOLVER_PCG) {
+    pcg_solve(c, P, o, st, x0, xa, xb, dbuf);
+    return;
+  }
   const int epi = o.solver == SOLVER_CHEBYSHEV ? EPI_CHEB : EPI_JACOBI;
   std::vector<double> ca, cc;
   cheb_coeffs(P.B, o.n_iter, ca, cc);
@@ -373,6 +481,8 @@ static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf&
     a.x_out = xo;
     a.tape_x = st.xk.empty() ? nullptr : st.xk[k];
     a.tape_r = st.rk.empty() ? nullptr : st.rk[k];
+    a.tape_gx = st.gxk.empty() ? nullptr : st.gxk[k];
+    a.tape_gy = st.gyk.empty() ? nullptr : st.gyk[k];
     a.ca = ca[k + 1]; a.cc = cc[k + 1];
     a.omega = 2.0 / 3.0;
     { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(epi, a, nb, c.stream)); }
@@ -423,7 +533,7 @@ void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_s
   const bool apos = any_alpha_pos(P);
   double* scratch = c.ws.dbl("fwd:stages", (size_t)NG * 3 * STAGE_FIXED_FIELDS);
   StageBuf st[3];
-  for (int s = 0; s < 3; ++s) st[s] = stage_from(scratch + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false);
+  for (int s = 0; s < 3; ++s) st[s] = stage_from(scratch + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false, (int)P.inst.size());
   double* xa = c.ws.dbl("fwd:xa", NG);
   double* xb = c.ws.dbl("fwd:xb", NG);
   double* db = c.ws.dbl("fwd:d", NG);
@@ -449,7 +559,7 @@ void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double*
   if (!any_alpha_pos(P)) return;
   check_alpha_uniform(P);
   double* scratch = c.ws.dbl("sol:stage", (size_t)NG * STAGE_FIXED_FIELDS);
-  StageBuf st = stage_from(scratch, NG, o, true, false);
+  StageBuf st = stage_from(scratch, NG, o, true, false, (int)P.inst.size());
   for (int v = 0; v < 4; ++v) st.q[v] = const_cast<double*>(q[v]);
   recip(c, q[2], st.invr, NG);
   double* x0 = c.ws.dbl("sol:x0", NG);
@@ -478,7 +588,7 @@ void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, do
   const long long NG = P.NG;
   double* scratch = c.ws.dbl("sip:stage", (size_t)NG * STAGE_FIXED_FIELDS);
   Solve2DOpts o;
-  StageBuf st = stage_from(scratch, NG, o, true, false);
+  StageBuf st = stage_from(scratch, NG, o, true, false, (int)P.inst.size());
   double* zeros = c.ws.dbl("sip:zero", NG);
   cuda_check(cudaMemsetAsync(zeros, 0, NG * sizeof(double), c.stream), "zero");
   st.q[0] = zeros; st.q[1] = zeros; st.q[2] = const_cast<double*>(rho); st.q[3] = zeros;
@@ -570,11 +680,11 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   const long long NG = P.NG;
   const int ni = (int)P.inst.size();
   const bool apos = any_alpha_pos(P);
-  const int F = stage_fields(o, apos);
+  const int F = stage_fields2d(o, apos, NG, ni);
   // scratch for untaped steps and final state
   double* scr = c.ws.dbl("adj:scr", (size_t)NG * 3 * STAGE_FIXED_FIELDS);
   StageBuf ust[3];
-  for (int s = 0; s < 3; ++s) ust[s] = stage_from(scr + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false);
+  for (int s = 0; s < 3; ++s) ust[s] = stage_from(scr + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false, ni);
   double* xa = c.ws.dbl("adj:xa", NG);
   double* xb = c.ws.dbl("adj:xb", NG);
   double* dbuf = c.ws.dbl("adj:d", NG);
@@ -614,7 +724,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   double* ckpt = c.ws.dbl("adj:ckpt", (size_t)n_seg * 6 * NG);
   double* tape = c.ws.dbl("adj:tape", (size_t)seg * 3 * F * NG);
   auto slot = [&](int local_step, int stage) {
-    return stage_from(tape + ((long long)local_step * 3 + stage) * F * NG, NG, o, apos, true);
+    return stage_from(tape + ((long long)local_step * 3 + stage) * F * NG, NG, o, apos, true, ni);
   };
 
   cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
@@ -699,9 +809,72 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   cuda_check(cudaMemsetAsync(anode, 0, NG * sizeof(double), c.stream), "zero anode");
   std::vector<double> ca, cc;
   cheb_coeffs(P.B, o.n_iter, ca, cc);
-  const int srev = !apos ? SREV_NONE : (o.solver == SOLVER_CHEBYSHEV ? SREV_CHEB : SREV_JACOBI);
+  const int srev = !apos ? SREV_NONE : (o.solver == SOLVER_CHEBYSHEV ? SREV_CHEB : (o.solver == SOLVER_JACOBI ? SREV_JACOBI : SREV_PCG));
+  int tx, ty;
+  tile_geometry(P, &tx, &ty);
+  double* part = nullptr;
+  int* cnt = nullptr;
+  if (srev == SREV_PCG) reduction_scratch(c, P, &part, &cnt);
+  double* pscal = c.ws.dbl("adj:pcgscal", (size_t)3 * ni);  // BET, RZB, PAPB per instance
   const int nb = P.ntiles();
   const double c0s[3] = {0.0, 3.0 / 4, 1.0 / 3}, c1s[3] = {1.0, 1.0 / 4, 2.0 / 3}, c2s[3] = {1.0, 1.0 / 4, 2.0 / 3};
+
+  // Reverse of one stage's PCG solve (the tape of pcg_solve), given Sb = the
+  // adjoint of its result: leaves the adjoint of the warm start in Sb and
+  // bb, iMb (Mb), Zm, Zs for the setup reverse.
+  auto pcg_reverse = [&](StageBuf& sb) {
+    const int n = o.n_iter;
+    double* PB = U[0];
+    double* RB = U[1];
+    double* BET = pscal; double* RZB = pscal + ni; double* PAPB = pscal + 2 * ni;
+    const double* RZ = sb.scal;
+    const double* PAP = sb.scal + (long long)(n + 1) * ni;
+    for (int it = n - 1; it >= 0; --it) {
+      PcgRevArgs g;
+      g.tiles = P.d_tiles; g.inst = P.d_inst; g.np = P.np; g.tx = tx; g.ty = ty;
+      g.first = it == n - 1 ? 1 : 0; g.it = it; g.ni = ni;
+      g.pb = PB; g.rb = RB; g.iMb = Mb;
+      g.r1 = sb.rk[it + 1]; g.cinvM = sb.cinvM; g.ap = sb.apk[it]; g.p = sb.pk[it]; g.xb = Sb;
+      g.RZ = RZ; g.PAP = PAP; g.BET = BET; g.RZB = RZB; g.PAPB = PAPB;
+      g.partials = part; g.counters = cnt;
+      { LaunchScope ls(c, KID_OTHER); k2_pcg_rev_update<<<nb, PCG_THREADS, 0, c.stream>>>(g); }
+      ApplyRevArgs2D r;
+      std::memset(&r, 0, sizeof(r));
+      r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
+      r.u = RB; r.xk = sb.pk[it];
+      r.cm = sb.cm; r.ckx = sb.ckx; r.cky = sb.cky; r.cpx = sb.cpx; r.cpy = sb.cpy; r.cinvM = sb.cinvM;
+      r.invr = sb.invr;
+      r.xb = PB; r.bb = bb; r.Zm = Zm; r.Zs = Zs;
+      r.first = it == n - 1 ? 1 : 0;
+      r.bb_op = 0;
+      r.zscale = -1.0;
+      r.has_next = it > 0 ? 1 : 0;
+      r.rz_it = RZ + (long long)it * ni; r.pap_it = PAP + (long long)it * ni; r.papb = PAPB;
+      r.xconst = Sb; r.apk = sb.apk[it]; r.p_next = it > 0 ? sb.pk[it - 1] : nullptr;
+      r.red_out = BET; r.partials = part; r.counters = cnt;
+      { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(SREV_PCG, r, nb, c.stream)); }
+    }
+    {
+      PcgRevFinalArgs f;
+      f.tiles = P.d_tiles; f.inst = P.d_inst; f.np = P.np; f.tx = tx; f.ty = ty;
+      f.pb = PB; f.r0 = sb.rk[0]; f.cinvM = sb.cinvM; f.RZB = RZB; f.rb = RB; f.iMb = Mb;
+      LaunchScope ls(c, KID_OTHER);
+      k2_pcg_rev_final<<<nb, PCG_THREADS, 0, c.stream>>>(f);
+    }
+    // r_0 = b - A x_0
+    ApplyRevArgs2D r;
+    std::memset(&r, 0, sizeof(r));
+    r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
+    r.u = RB; r.xk = sb.x0t;
+    r.cm = sb.cm; r.ckx = sb.ckx; r.cky = sb.cky; r.cpx = sb.cpx; r.cpy = sb.cpy; r.cinvM = sb.cinvM;
+    r.invr = sb.invr;
+    r.xb = Sb; r.bb = bb; r.Zm = Zm; r.Zs = Zs;
+    r.first = 0; r.bb_op = 1;
+    r.zscale = -1.0;
+    r.has_next = 0;
+    LaunchScope ls(c, KID_APPLY_REV);
+    NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(SREV_NONE, r, nb, c.stream));
+  };
 
   auto reverse_step = [&](int local) {
     StageBuf st[3] = {slot(local, 0), slot(local, 1), slot(local, 2)};
@@ -722,37 +895,44 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       h.qs_add = s == 0 ? 1 : 0;
       h.Sb = Sb; h.Sb_add = 1;
       h.gnode = gnode;
-      h.srev = srev;
+      h.srev = srev == SREV_PCG ? SREV_NONE : srev;
       h.cinvM = st[s].cinvM;
-      h.r_last = apos ? st[s].rk[o.n_iter - 1] : nullptr;
-      h.u_out = U[0]; h.db = db; h.Mb = Mb;
+      h.r_last = (apos && srev != SREV_PCG) ? st[s].rk[o.n_iter - 1] : nullptr;
+      h.u_out = U[0]; h.db = db; h.iMb = Mb;
       h.ca = ca[o.n_iter]; h.cc = cc[o.n_iter]; h.omega = 2.0 / 3.0;
       { LaunchScope ls(c, KID_HYP_REV); NP_DISPATCH(P.np, launch_k2_hyp_rev<NPV>(h, nb, c.stream)); }
       if (!apos) continue;
+      if (srev == SREV_PCG) {
+        pcg_reverse(st[s]);
+      } else {
       int cur = 0;
       for (int m = o.n_iter - 1; m >= 0; --m) {
         ApplyRevArgs2D r;
         std::memset(&r, 0, sizeof(r));
         r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
         r.u = U[cur]; r.xk = st[s].xk[m];
+        r.gxk = st[s].gxk.empty() ? nullptr : st[s].gxk[m];
+        r.gyk = st[s].gyk.empty() ? nullptr : st[s].gyk[m];
         r.cm = st[s].cm; r.ckx = st[s].ckx; r.cky = st[s].cky; r.cpx = st[s].cpx; r.cpy = st[s].cpy; r.cinvM = st[s].cinvM;
         r.invr = st[s].invr;
         r.xb = Sb; r.bb = bb; r.Zm = Zm; r.Zs = Zs;
         r.first = (m == o.n_iter - 1) ? 1 : 0;
+        r.bb_op = r.first ? 1 : 2;
         r.zscale = -1.0;
         r.has_next = m > 0 ? 1 : 0;
         r.r_prev = m > 0 ? st[s].rk[m - 1] : nullptr;
-        r.u_out = U[1 - cur]; r.db = db; r.Mb = Mb;
+        r.u_out = U[1 - cur]; r.db = db; r.iMb = Mb;
         r.ca = ca[m > 0 ? m : 1]; r.cc = cc[m > 0 ? m : 1]; r.omega = 2.0 / 3.0;
         { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(srev, r, nb, c.stream)); }
         cur = 1 - cur;
+      }
       }
       SetupRevArgs2D sr;
       std::memset(&sr, 0, sizeof(sr));
       sr.tiles = P.d_tiles; sr.inst = P.d_inst; sr.B = P.B;
       sr.mx = st[s].q[0]; sr.my = st[s].q[1]; sr.invr = st[s].invr;
-      sr.b = st[s].b; sr.cm = st[s].cm; sr.cM = st[s].cM;
-      sr.bb = bb; sr.Mb = Mb; sr.Zm = Zm; sr.Zs = Zs;
+      sr.b = st[s].b; sr.cm = st[s].cm; sr.cM = st[s].cM; sr.cinvM = st[s].cinvM;
+      sr.bb = bb; sr.iMb = Mb; sr.Zm = Zm; sr.Zs = Zs;
       double* const* QsP = s == 2 ? Q2b : (s == 1 ? Q1b : QN);
       sr.Qs[0] = QsP[0]; sr.Qs[1] = QsP[1]; sr.Qs[2] = QsP[2];
       sr.anode = anode;

@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
 // where d is the reference derivative of x at the face node on each side.
 // Each side computes F itself (owner computes), so no atomics are needed.
 // ---------------------------------------------------------------------------
-enum { EPI_CHEB = 0, EPI_JACOBI = 1, EPI_RESID = 2 };
+enum { EPI_CHEB = 0, EPI_JACOBI = 1, EPI_RESID = 2, EPI_PCG0 = 3, EPI_PCG = 4 };
 
 struct ApplyArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
@@ -275,8 +275,17 @@ struct ApplyArgs2D {
   const double* d_in;                    // Chebyshev d_k (null on the first iteration)
   double *d_out, *x_out;                 // d_{k+1}, x_{k+1}
   double *tape_x, *tape_r;               // optional tape of x_k and r_k = b - A x_k
+  double *tape_gx, *tape_gy;             // optional tape of the reference derivatives of x_k
   double *y_out;                         // EPI_RESID: raw y = A x
   double ca, cc, omega;                  // d_{k+1} = ca d_k + cc M^-1 r_k ; Jacobi omega
+  // Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347):
+  //  EPI_PCG0: x = x_0; r_0 = b - A x_0 -> r_out, p_0 = M^-1 r_0 -> p_out, red_out = r_0 . p_0
+  //  EPI_PCG : x = p_k; with pcg_p set, p_k = M^-1 r_k + beta p_{k-1} is formed on load from
+  //            (pcg_r, pcg_p), beta = rz_cur / (rz_prev + 1e-30), and stored to p_out;
+  //            A p_k -> ap_out, red_out = p_k . A p_k
+  const double *pcg_r, *pcg_p, *rz_cur, *rz_prev;
+  double *p_out, *r_out, *ap_out, *red_out;
+  double* partials; int* counters;       // per-tile partial sums, per-instance arrival counters
 };
 
 // Partner data across one face: its value and end-node derivative of x, and its stiffness coefficient.
@@ -286,25 +295,44 @@ template <int NP, int EPI>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
   using TL = Tiling2D<NP>;
   constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
+  constexpr bool PCG = EPI == EPI_PCG0 || EPI == EPI_PCG;
+  constexpr int P2 = pow2_at_least(TL::NT);
   __shared__ double s_x[TE][NN], s_yx[TE][NN], s_gxf[TE][NP][2], s_gyf[TE][NP][2];
+  __shared__ double s_red[PCG ? P2 : 1];
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
   const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
   const double hw = B.hw;
+  // PCG direction update fused into the loads (p_k is pointwise in r_k, p_{k-1})
+  const bool form_p = EPI == EPI_PCG && a.pcg_p != nullptr;
+  double beta = 0.0;
+  if (form_p) beta = a.rz_cur[tl.inst] / (a.rz_prev[tl.inst] + 1e-30);
+  auto ldx = [&](long long n) -> double {
+    if (form_p) return fma(beta, a.pcg_p[n], a.pcg_r[n] * a.cinvM[n]);
+    return a.x[n];
+  };
 
   // ---- xi-phase part 1: row derivatives
   double xr[NP], gx[NP];
   if (vr.valid) {
     const int t = vr.t, e = vr.e;
 #pragma unroll
-    for (int i = 0; i < NP; ++i) { xr[i] = a.x[vr.base + t * NP + i]; s_x[e][t * NP + i] = xr[i]; }
+    for (int i = 0; i < NP; ++i) { xr[i] = ldx(vr.base + t * NP + i); s_x[e][t * NP + i] = xr[i]; }
+    if (form_p) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) a.p_out[vr.base + t * NP + i] = xr[i];
+    }
 #pragma unroll
     for (int i = 0; i < NP; ++i) gx[i] = dot_row<NP>(B, i, xr);
     s_gxf[e][t][0] = gx[0]; s_gxf[e][t][1] = gx[L];
     if (a.tape_x) {
 #pragma unroll
       for (int i = 0; i < NP; ++i) a.tape_x[vr.base + t * NP + i] = xr[i];
+    }
+    if (a.tape_gx) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) a.tape_gx[vr.base + t * NP + i] = gx[i];
     }
   }
   __syncthreads();
@@ -316,6 +344,10 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
 #pragma unroll
     for (int l = 0; l < NP; ++l) gy[l] = dot_row<NP>(B, l, xc);
     s_gyf[e][t][0] = gy[0]; s_gyf[e][t][1] = gy[L];
+    if (a.tape_gy) {
+#pragma unroll
+      for (int l = 0; l < NP; ++l) a.tape_gy[vc.base + l * NP + t] = gy[l];
+    }
   }
   if (vr.valid) {
     // ---- xi-phase part 2: x faces of the row and the x-stiffness transpose
@@ -335,7 +367,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
       } else {
         double pr[NP];
 #pragma unroll
-        for (int k = 0; k < NP; ++k) pr[k] = a.x[pb + t * NP + k];
+        for (int k = 0; k < NP; ++k) pr[k] = ldx(pb + t * NP + k);
         P.x = s == 0 ? pr[L] : pr[0];
         P.d = dot_end<NP>(B, s == 0, pr);
       }
@@ -361,59 +393,81 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
     }
   }
   __syncthreads();
-  if (!vc.valid) return;
+  if (!PCG && !vc.valid) return;
+  double part = 0.0;  // PCG inner-product partial of this thread
 
   // ---- eta-phase: y faces of the column, y-stiffness transpose, mass, epilogue
-  const int t = vc.t, e = vc.e;
-  double kyc[NP];
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
+    double kyc[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) kyc[l] = a.cky[vc.base + l * NP + t];
-  auto fetchy = [&](int s) {
-    Partner1 P;
-    int it;
-    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
-    const int pl = s == 0 ? L : 0;
-    P.k = a.cky[pb + pl * NP + t];
-    if (it >= 0) {
-      P.x = s_x[it][pl * NP + t];
-      P.d = s_gyf[it][t][s == 0 ? 1 : 0];
-    } else {
-      double pc[NP];
+    for (int l = 0; l < NP; ++l) kyc[l] = a.cky[vc.base + l * NP + t];
+    auto fetchy = [&](int s) {
+      Partner1 P;
+      int it;
+      const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
+      const int pl = s == 0 ? L : 0;
+      P.k = a.cky[pb + pl * NP + t];
+      if (it >= 0) {
+        P.x = s_x[it][pl * NP + t];
+        P.d = s_gyf[it][t][s == 0 ? 1 : 0];
+      } else {
+        double pc[NP];
 #pragma unroll
-      for (int k = 0; k < NP; ++k) pc[k] = a.x[pb + k * NP + t];
-      P.x = s == 0 ? pc[L] : pc[0];
-      P.d = dot_end<NP>(B, s == 0, pc);
+        for (int k = 0; k < NP; ++k) pc[k] = ldx(pb + k * NP + t);
+        P.x = s == 0 ? pc[L] : pc[0];
+        P.d = dot_end<NP>(B, s == 0, pc);
+      }
+      return P;
+    };
+    const int sf = first_side(vc.eyt, TY);
+    const Partner1 qA = fetchy(sf), qB = fetchy(1 - sf);
+    const Partner1 qb = sf == 0 ? qA : qB, qt = sf == 0 ? qB : qA;
+    const double jb = qb.x - xc[0];
+    const double Fb = fma(a.cpy[vc.base + t], jb, hw * fma(qb.k, qb.d, kyc[0] * gy[0]));
+    const double jt = xc[L] - qt.x;
+    const double Ft = fma(a.cpy[vc.base + L * NP + t], jt, hw * fma(kyc[L], gy[L], qt.k * qt.d));
+    double sy[NP];
+#pragma unroll
+    for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gy[l];
+    sy[0] = kyc[0] * fma(hw, jb, gy[0]);
+    sy[L] = kyc[L] * fma(hw, jt, gy[L]);
+#pragma unroll
+    for (int l = 0; l < NP; ++l) {
+      const long long n = vc.base + l * NP + t;
+      double y = fma(a.cm[n], xc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
+      y = dot_col<NP>(B, l, sy, y);
+      if (EPI == EPI_RESID) { a.y_out[n] = y; continue; }
+      if (EPI == EPI_PCG) {
+        a.ap_out[n] = y;
+        part = fma(xc[l], y, part);
+        continue;
+      }
+      if (EPI == EPI_PCG0) {
+        const double r0 = a.b[n] - y;
+        const double z0 = r0 * a.cinvM[n];
+        a.r_out[n] = r0;
+        a.p_out[n] = z0;
+        part = fma(r0, z0, part);
+        continue;
+      }
+      const double r = a.b[n] - y;
+      if (a.tape_r) a.tape_r[n] = r;
+      if (EPI == EPI_CHEB) {
+        const double z = r * a.cinvM[n];
+        const double d = a.d_in ? fma(a.ca, a.d_in[n], a.cc * z) : a.cc * z;
+        a.d_out[n] = d;
+        a.x_out[n] = xc[l] + d;
+      } else {  // EPI_JACOBI: x + omega (b - A x) / M   (elliptic.jl:358)
+        a.x_out[n] = fma(a.omega * r, a.cinvM[n], xc[l]);
+      }
     }
-    return P;
-  };
-  const int sf = first_side(vc.eyt, TY);
-  const Partner1 qA = fetchy(sf), qB = fetchy(1 - sf);
-  const Partner1 qb = sf == 0 ? qA : qB, qt = sf == 0 ? qB : qA;
-  const double jb = qb.x - xc[0];
-  const double Fb = fma(a.cpy[vc.base + t], jb, hw * fma(qb.k, qb.d, kyc[0] * gy[0]));
-  const double jt = xc[L] - qt.x;
-  const double Ft = fma(a.cpy[vc.base + L * NP + t], jt, hw * fma(kyc[L], gy[L], qt.k * qt.d));
-  double sy[NP];
-#pragma unroll
-  for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gy[l];
-  sy[0] = kyc[0] * fma(hw, jb, gy[0]);
-  sy[L] = kyc[L] * fma(hw, jt, gy[L]);
-#pragma unroll
-  for (int l = 0; l < NP; ++l) {
-    const long long n = vc.base + l * NP + t;
-    double y = fma(a.cm[n], xc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
-    y = dot_col<NP>(B, l, sy, y);
-    if (EPI == EPI_RESID) { a.y_out[n] = y; continue; }
-    const double r = a.b[n] - y;
-    if (a.tape_r) a.tape_r[n] = r;
-    if (EPI == EPI_CHEB) {
-      const double z = r * a.cinvM[n];
-      const double d = a.d_in ? fma(a.ca, a.d_in[n], a.cc * z) : a.cc * z;
-      a.d_out[n] = d;
-      a.x_out[n] = xc[l] + d;
-    } else {  // EPI_JACOBI: x + omega (b - A x) / M   (elliptic.jl:358)
-      a.x_out[n] = fma(a.omega * r, a.cinvM[n], xc[l]);
-    }
+  }
+  if (PCG) {
+    const double tot = block_sum<P2>(part, s_red);
+    double inst_tot = 0.0;
+    if (instance_sum<P2>(tot, tl.inst, I.tile0, I.ntiles, a.partials, a.counters, s_red, &inst_tot) && threadIdx.x == 0)
+      a.red_out[tl.inst] = inst_tot;
   }
 }
 

@@ -15,6 +15,8 @@ template <int NP> void launch_k2_setup(const SetupArgs2D& a, int nb, cudaStream_
 template <int NP> void launch_k2_apply(int epi, const ApplyArgs2D& a, int nb, cudaStream_t s) {
   if (epi == EPI_CHEB) k2_apply<NP, EPI_CHEB><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
   else if (epi == EPI_JACOBI) k2_apply<NP, EPI_JACOBI><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else if (epi == EPI_PCG0) k2_apply<NP, EPI_PCG0><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else if (epi == EPI_PCG) k2_apply<NP, EPI_PCG><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
   else k2_apply<NP, EPI_RESID><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
 }
 template <int NP> void launch_k2_hyp_rk(const HypArgs2D& a, int nb, cudaStream_t s) {
@@ -26,6 +28,7 @@ template <int NP> void launch_k2_hyp_rev(const HypRevArgs2D& a, int nb, cudaStre
 template <int NP> void launch_k2_apply_rev(int srev, const ApplyRevArgs2D& a, int nb, cudaStream_t s) {
   if (srev == SREV_CHEB) k2_apply_rev<NP, SREV_CHEB><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
   else if (srev == SREV_JACOBI) k2_apply_rev<NP, SREV_JACOBI><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+  else if (srev == SREV_PCG) k2_apply_rev<NP, SREV_PCG><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
   else k2_apply_rev<NP, SREV_NONE><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
 }
 template <int NP> void launch_k2_setup_rev(const SetupRevArgs2D& a, int nb, cudaStream_t s) {

@@ -81,7 +81,7 @@ __device__ __forceinline__ void wavespeed_rev(int dir, double g, double mx, doub
   qb[2] -= kb * kin * ir;
 }
 
-enum { SREV_NONE = 0, SREV_CHEB = 1, SREV_JACOBI = 2 };
+enum { SREV_NONE = 0, SREV_CHEB = 1, SREV_JACOBI = 2, SREV_PCG = 3 };
 
 // ---------------------------------------------------------------------------
 // Reverse of k2_hyp_rk for one stage.
@@ -93,7 +93,8 @@ enum { SREV_NONE = 0, SREV_CHEB = 1, SREV_JACOBI = 2 };
 //     gnode += d/dgamma
 // Solver prologue (SREV_CHEB / SREV_JACOBI) with xb = Sb total: produces the
 // residual adjoint u = rb_{n-1} for the first k2_apply_rev, initialises the
-// diag(A) adjoint Mb, and (Chebyshev) the direction adjoint db.
+// adjoint iMb of 1/diag(A) (the forward multiplies by the stored reciprocal),
+// and (Chebyshev) the direction adjoint db.
 // ---------------------------------------------------------------------------
 struct HypRevArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
@@ -108,7 +109,7 @@ struct HypRevArgs2D {
   // solver prologue
   int srev;
   const double *cinvM, *r_last;      // taped r_{n-1}
-  double *u_out, *db, *Mb;
+  double *u_out, *db, *iMb;
   double ca, cc, omega;              // Chebyshev a_n, c_n ; Jacobi omega
 };
 
@@ -295,16 +296,16 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rev(HypRevArgs2D a) {
     const double Sbt = a.Sb_add ? a.Sb[n] + Sb : Sb;
     a.Sb[n] = Sbt;
     if (a.srev == SREV_CHEB) {
-      // x_n = x_{n-1} + d_n ; d_n = a_n d_{n-1} + c_n z_n ; z_n = M^-1 r_{n-1}
-      const double u = a.cinvM[n] * (a.cc * Sbt);
-      a.u_out[n] = u;
-      a.Mb[n] = -u * a.r_last[n] * a.cinvM[n];
+      // x_n = x_{n-1} + d_n ; d_n = a_n d_{n-1} + c_n z_n ; z_n = (1/M) r_{n-1}
+      const double zb = a.cc * Sbt;
+      a.u_out[n] = a.cinvM[n] * zb;
+      a.iMb[n] = zb * a.r_last[n];
       a.db[n] = a.ca * Sbt;
     } else if (a.srev == SREV_JACOBI) {
-      // x_n = x_{n-1} + omega M^-1 r_{n-1}
-      const double u = a.omega * Sbt * a.cinvM[n];
-      a.u_out[n] = u;
-      a.Mb[n] = -u * a.r_last[n] * a.cinvM[n];
+      // x_n = x_{n-1} + (omega r_{n-1}) (1/M)
+      const double tb = a.omega * Sbt;
+      a.u_out[n] = tb * a.cinvM[n];
+      a.iMb[n] = tb * a.r_last[n];
     }
   }
   a.gnode[vc.base + t] += gb;
@@ -318,15 +319,25 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rev(HypRevArgs2D a) {
 struct ApplyRevArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
   const double *u, *xk;               // residual adjoint and taped iterate
+  const double *gxk, *gyk;            // taped reference derivatives of x_k (null: recompute)
   const double *cm, *ckx, *cky, *cpx, *cpy, *cinvM, *invr;
   double *xb, *bb, *Zm, *Zs;
-  int first;                          // first reverse iteration of this solve: write bb, Zm, Zs
+  int first;                          // first reverse apply of this solve: write Zm, Zs (else add)
+  int bb_op;                          // bb: 0 untouched, 1 write u, 2 add u
   double zscale;                      // -1 for r = b - A x terms
   // epilogue (when has_next): r̄_{m-1}
   int has_next;
   const double* r_prev;               // taped r_{m-1}
-  double *u_out, *db, *Mb;
+  double *u_out, *db, *iMb;
   double ca, cc, omega;
+  // SREV_PCG (reverse of A p_it, second half of the iteration reverse):
+  //   u = -(adjoint of A p_it) = alpha_it rb - pApb p_it, formed on load from
+  //   (u = rb, xk = p_it); xb = pb: pb += alpha_it xconst + pApb apk + A(adjoint of A p_it);
+  //   with has_next, red_out = pb . p_next (betab of the next reverse iteration)
+  const double *rz_it, *pap_it, *papb;  // per-instance scalars
+  const double *xconst, *apk, *p_next;
+  double* red_out;
+  double* partials; int* counters;
 };
 
 // Partner data across one face for the reverse apply: values and end-node
@@ -337,25 +348,42 @@ template <int NP, int SREV>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D a) {
   using TL = Tiling2D<NP>;
   constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
+  constexpr bool PCG = SREV == SREV_PCG;
+  constexpr int P2 = pow2_at_least(TL::NT);
   __shared__ double s_u[TE][NN], s_v[TE][NN], s_yx[TE][NN], s_zr[TE][NN];
   __shared__ double s_gxf[2][TE][NP][2], s_gyf[2][TE][NP][2];  // [u|v] face derivatives
+  __shared__ double s_red[PCG ? P2 : 1];
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
   const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
   const double hw = B.hw;
+  double pal = 0.0, ppb = 0.0;  // PCG: alpha_it and the adjoint of pAp_it
+  if (PCG) {
+    pal = a.rz_it[tl.inst] / (a.pap_it[tl.inst] + 1e-30);
+    ppb = a.papb[tl.inst];
+  }
+  // u at node n, given x_k there (PCG forms it from rb and p_it)
+  auto ldu = [&](long long n, double xkv) -> double {
+    if (PCG) return fma(pal, a.u[n], -ppb * xkv);
+    return a.u[n];
+  };
 
   double ur[NP], vr_[NP], gxu[NP], gxv[NP];
+  const bool taped_g = !PCG && a.gxk != nullptr;
   if (vr.valid) {
     const int t = vr.t, e = vr.e;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
       const long long n = vr.base + t * NP + i;
-      ur[i] = a.u[n]; vr_[i] = a.xk[n];
+      vr_[i] = a.xk[n]; ur[i] = ldu(n, vr_[i]);
       s_u[e][t * NP + i] = ur[i]; s_v[e][t * NP + i] = vr_[i];
     }
 #pragma unroll
-    for (int i = 0; i < NP; ++i) { gxu[i] = dot_row<NP>(B, i, ur); gxv[i] = dot_row<NP>(B, i, vr_); }
+    for (int i = 0; i < NP; ++i) {
+      gxu[i] = dot_row<NP>(B, i, ur);
+      gxv[i] = taped_g ? a.gxk[vr.base + t * NP + i] : dot_row<NP>(B, i, vr_);
+    }
     s_gxf[0][e][t][0] = gxu[0]; s_gxf[0][e][t][1] = gxu[L];
     s_gxf[1][e][t][0] = gxv[0]; s_gxf[1][e][t][1] = gxv[L];
   }
@@ -366,7 +394,10 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
 #pragma unroll
     for (int l = 0; l < NP; ++l) { uc[l] = s_u[e][l * NP + t]; vc_[l] = s_v[e][l * NP + t]; }
 #pragma unroll
-    for (int l = 0; l < NP; ++l) { gyu[l] = dot_row<NP>(B, l, uc); gyv[l] = dot_row<NP>(B, l, vc_); }
+    for (int l = 0; l < NP; ++l) {
+      gyu[l] = dot_row<NP>(B, l, uc);
+      gyv[l] = taped_g ? a.gyk[vc.base + l * NP + t] : dot_row<NP>(B, l, vc_);
+    }
     s_gyf[0][e][t][0] = gyu[0]; s_gyf[0][e][t][1] = gyu[L];
     s_gyf[1][e][t][0] = gyv[0]; s_gyf[1][e][t][1] = gyv[L];
   }
@@ -387,13 +418,21 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
         P.u = s_u[it][t * NP + pi]; P.v = s_v[it][t * NP + pi];
         P.du = s_gxf[0][it][t][s == 0 ? 1 : 0]; P.dv = s_gxf[1][it][t][s == 0 ? 1 : 0];
       } else {
-        double pr[NP], pw[NP];
+        double pr[NP];
+        if (taped_g) {
 #pragma unroll
-        for (int k = 0; k < NP; ++k) { pr[k] = a.u[pb + t * NP + k]; pw[k] = a.xk[pb + t * NP + k]; }
+          for (int k = 0; k < NP; ++k) pr[k] = a.u[pb + t * NP + k];
+          P.v = a.xk[pb + t * NP + pi];
+          P.dv = a.gxk[pb + t * NP + pi];
+        } else {
+          double pw[NP];
+#pragma unroll
+          for (int k = 0; k < NP; ++k) { pw[k] = a.xk[pb + t * NP + k]; pr[k] = ldu(pb + t * NP + k, pw[k]); }
+          P.v = s == 0 ? pw[L] : pw[0];
+          P.dv = dot_end<NP>(B, s == 0, pw);
+        }
         P.u = s == 0 ? pr[L] : pr[0];
-        P.v = s == 0 ? pw[L] : pw[0];
         P.du = dot_end<NP>(B, s == 0, pr);
-        P.dv = dot_end<NP>(B, s == 0, pw);
       }
       return P;
     };
@@ -426,75 +465,97 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
     }
   }
   __syncthreads();
-  if (!vc.valid) return;
+  if (!PCG && !vc.valid) return;
+  double part = 0.0;  // PCG: betab partial of this thread
   // ---- column of vc: y faces, transposes, outputs
-  const int t = vc.t, e = vc.e;
-  double kyc[NP], zc[NP];
+  if (vc.valid) {
+    const int t = vc.t, e = vc.e;
+    double kyc[NP], zc[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) { kyc[l] = a.cky[vc.base + l * NP + t]; zc[l] = kyc[l] * gyu[l] * gyv[l]; }
-  auto fetchy = [&](int s) {
-    Partner2 P;
-    int it;
-    const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
-    const int pl = s == 0 ? L : 0;
-    P.k = a.cky[pb + pl * NP + t];
-    P.ir = a.invr[pb + pl * NP + t];
-    if (it >= 0) {
-      P.u = s_u[it][pl * NP + t]; P.v = s_v[it][pl * NP + t];
-      P.du = s_gyf[0][it][t][s == 0 ? 1 : 0]; P.dv = s_gyf[1][it][t][s == 0 ? 1 : 0];
-    } else {
-      double pc[NP], pw[NP];
+    for (int l = 0; l < NP; ++l) { kyc[l] = a.cky[vc.base + l * NP + t]; zc[l] = kyc[l] * gyu[l] * gyv[l]; }
+    auto fetchy = [&](int s) {
+      Partner2 P;
+      int it;
+      const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
+      const int pl = s == 0 ? L : 0;
+      P.k = a.cky[pb + pl * NP + t];
+      P.ir = a.invr[pb + pl * NP + t];
+      if (it >= 0) {
+        P.u = s_u[it][pl * NP + t]; P.v = s_v[it][pl * NP + t];
+        P.du = s_gyf[0][it][t][s == 0 ? 1 : 0]; P.dv = s_gyf[1][it][t][s == 0 ? 1 : 0];
+      } else {
+        double pc[NP];
+        if (taped_g) {
 #pragma unroll
-      for (int k = 0; k < NP; ++k) { pc[k] = a.u[pb + k * NP + t]; pw[k] = a.xk[pb + k * NP + t]; }
-      P.u = s == 0 ? pc[L] : pc[0];
-      P.v = s == 0 ? pw[L] : pw[0];
-      P.du = dot_end<NP>(B, s == 0, pc);
-      P.dv = dot_end<NP>(B, s == 0, pw);
+          for (int k = 0; k < NP; ++k) pc[k] = a.u[pb + k * NP + t];
+          P.v = a.xk[pb + pl * NP + t];
+          P.dv = a.gyk[pb + pl * NP + t];
+        } else {
+          double pw[NP];
+#pragma unroll
+          for (int k = 0; k < NP; ++k) { pw[k] = a.xk[pb + k * NP + t]; pc[k] = ldu(pb + k * NP + t, pw[k]); }
+          P.v = s == 0 ? pw[L] : pw[0];
+          P.dv = dot_end<NP>(B, s == 0, pw);
+        }
+        P.u = s == 0 ? pc[L] : pc[0];
+        P.du = dot_end<NP>(B, s == 0, pc);
+      }
+      return P;
+    };
+    const int sf = first_side(vc.eyt, TY);
+    const Partner2 qA = fetchy(sf), qB = fetchy(1 - sf);
+    const Partner2 qb = sf == 0 ? qA : qB, qt = sf == 0 ? qB : qA;
+    const double ic0 = a.invr[vc.base + t], icL = a.invr[vc.base + L * NP + t];
+    const double jub = qb.u - uc[0], jvb = qb.v - vc_[0];
+    const double pbot = a.cpy[vc.base + t];
+    const double Fb = fma(pbot, jub, hw * fma(qb.k, qb.du, kyc[0] * gyu[0]));
+    zc[0] = fma(hw * kyc[0], fma(gyv[0], jub, gyu[0] * jvb), zc[0]);
+    if (ic0 > qb.ir) zc[0] = fma(pbot * jvb, jub, zc[0]);
+    const double jut = uc[L] - qt.u, jvt = vc_[L] - qt.v;
+    const double ptop = a.cpy[vc.base + L * NP + t];
+    const double Ft = fma(ptop, jut, hw * fma(kyc[L], gyu[L], qt.k * qt.du));
+    zc[L] = fma(hw * kyc[L], fma(gyv[L], jut, gyu[L] * jvt), zc[L]);
+    if (!(qt.ir > icL)) zc[L] = fma(ptop * jvt, jut, zc[L]);
+    double sy[NP];
+#pragma unroll
+    for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gyu[l];
+    sy[0] = kyc[0] * fma(hw, jub, gyu[0]);
+    sy[L] = kyc[L] * fma(hw, jut, gyu[L]);
+#pragma unroll
+    for (int l = 0; l < NP; ++l) {
+      const long long n = vc.base + l * NP + t;
+      const double cmn = a.cm[n];
+      double w = fma(cmn, uc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
+      w = dot_col<NP>(B, l, sy, w);
+      // zscale is -1 (r = b - A x) or +1 (A p): applied through fma signs, not a multiply
+      const double zm = a.zscale > 0 ? (cmn * uc[l]) * vc_[l] : -(cmn * uc[l]) * vc_[l];
+      const double zs = a.zscale > 0 ? zc[l] + s_zr[e][l * NP + t] : -(zc[l] + s_zr[e][l * NP + t]);
+      double xb = a.xb[n] - w;
+      if (PCG) xb = fma(ppb, a.apk[n], fma(pal, a.xconst[n], xb));
+      a.xb[n] = xb;
+      if (a.bb_op == 1) a.bb[n] = uc[l];
+      else if (a.bb_op == 2) a.bb[n] += uc[l];
+      if (a.first) { a.Zm[n] = zm; a.Zs[n] = zs; }
+      else { a.Zm[n] += zm; a.Zs[n] += zs; }
+      if (PCG && a.has_next) part = fma(xb, a.p_next[n], part);
+      if (SREV == SREV_CHEB && a.has_next) {
+        const double dbv = a.db[n] + xb;
+        const double zb = a.cc * dbv;
+        a.u_out[n] = a.cinvM[n] * zb;
+        a.iMb[n] = fma(zb, a.r_prev[n], a.iMb[n]);
+        a.db[n] = a.ca * dbv;
+      } else if (SREV == SREV_JACOBI && a.has_next) {
+        const double tb = a.omega * xb;
+        a.u_out[n] = tb * a.cinvM[n];
+        a.iMb[n] = fma(tb, a.r_prev[n], a.iMb[n]);
+      }
     }
-    return P;
-  };
-  const int sf = first_side(vc.eyt, TY);
-  const Partner2 qA = fetchy(sf), qB = fetchy(1 - sf);
-  const Partner2 qb = sf == 0 ? qA : qB, qt = sf == 0 ? qB : qA;
-  const double ic0 = a.invr[vc.base + t], icL = a.invr[vc.base + L * NP + t];
-  const double jub = qb.u - uc[0], jvb = qb.v - vc_[0];
-  const double pbot = a.cpy[vc.base + t];
-  const double Fb = fma(pbot, jub, hw * fma(qb.k, qb.du, kyc[0] * gyu[0]));
-  zc[0] = fma(hw * kyc[0], fma(gyv[0], jub, gyu[0] * jvb), zc[0]);
-  if (ic0 > qb.ir) zc[0] = fma(pbot * jvb, jub, zc[0]);
-  const double jut = uc[L] - qt.u, jvt = vc_[L] - qt.v;
-  const double ptop = a.cpy[vc.base + L * NP + t];
-  const double Ft = fma(ptop, jut, hw * fma(kyc[L], gyu[L], qt.k * qt.du));
-  zc[L] = fma(hw * kyc[L], fma(gyv[L], jut, gyu[L] * jvt), zc[L]);
-  if (!(qt.ir > icL)) zc[L] = fma(ptop * jvt, jut, zc[L]);
-  double sy[NP];
-#pragma unroll
-  for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gyu[l];
-  sy[0] = kyc[0] * fma(hw, jub, gyu[0]);
-  sy[L] = kyc[L] * fma(hw, jut, gyu[L]);
-#pragma unroll
-  for (int l = 0; l < NP; ++l) {
-    const long long n = vc.base + l * NP + t;
-    const double cmn = a.cm[n];
-    double w = fma(cmn, uc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
-    w = dot_col<NP>(B, l, sy, w);
-    const double zm = a.zscale * (cmn * uc[l] * vc_[l]);
-    const double zs = a.zscale * (zc[l] + s_zr[e][l * NP + t]);
-    const double xb = a.xb[n] - w;
-    a.xb[n] = xb;
-    if (a.first) { a.bb[n] = uc[l]; a.Zm[n] = zm; a.Zs[n] = zs; }
-    else { a.bb[n] += uc[l]; a.Zm[n] += zm; a.Zs[n] += zs; }
-    if (SREV == SREV_CHEB && a.has_next) {
-      const double dbv = a.db[n] + xb;
-      const double u = a.cinvM[n] * (a.cc * dbv);
-      a.u_out[n] = u;
-      a.Mb[n] -= u * a.r_prev[n] * a.cinvM[n];
-      a.db[n] = a.ca * dbv;
-    } else if (SREV == SREV_JACOBI && a.has_next) {
-      const double u = a.omega * xb * a.cinvM[n];
-      a.u_out[n] = u;
-      a.Mb[n] -= u * a.r_prev[n] * a.cinvM[n];
-    }
+  }
+  if (PCG && a.has_next) {
+    const double tot = block_sum<P2>(part, s_red);
+    double inst_tot = 0.0;
+    if (instance_sum<P2>(tot, tl.inst, I.tile0, I.ntiles, a.partials, a.counters, s_red, &inst_tot) && threadIdx.x == 0)
+      a.red_out[tl.inst] = inst_tot;
   }
 }
 
@@ -506,8 +567,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
 struct SetupRevArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
   const double *mx, *my, *invr;       // taped stage input
-  const double *b, *cm, *cM;          // taped source, mass coefficient, diag(A)
-  const double *bb, *Mb, *Zm, *Zs;
+  const double *b, *cm, *cM, *cinvM;  // taped source, mass coefficient, diag(A), 1/diag(A)
+  const double *bb, *iMb, *Zm, *Zs;   // iMb: adjoint of 1/diag(A)
   double *Qs[3];                      // adjoints of (mx, my, rho) of the stage input
   double *anode;
 };
@@ -537,7 +598,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
     for (int i = 0; i < NP; ++i) {
       const long long n = vr.base + t * NP + i;
       const double ir = a.invr[n];
-      ux[i] = a.mx[n] * ir; uy[i] = a.my[n] * ir; Mbr[i] = a.Mb[n];
+      const double im = a.cinvM[n];
+      ux[i] = a.mx[n] * ir; uy[i] = a.my[n] * ir; Mbr[i] = -(a.iMb[n] * im) * im;  // d/dM = -d/d(1/M) / M^2
       s_ux[e][t * NP + i] = ux[i]; s_uy[e][t * NP + i] = uy[i]; s_Mb[e][t * NP + i] = Mbr[i]; s_ir[e][t * NP + i] = ir;
     }
 #pragma unroll
@@ -592,7 +654,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
 #pragma unroll
       for (int l = 0; l < NP; ++l) {
         const double pir = it >= 0 ? s_ir[it][l * NP + pi] : a.invr[pb + l * NP + pi];
-        const double pMb = it >= 0 ? s_Mb[it][l * NP + pi] : a.Mb[pb + l * NP + pi];
+        const long long pn = pb + l * NP + pi;
+        const double pMb = it >= 0 ? s_Mb[it][l * NP + pi] : -(a.iMb[pn] * a.cinvM[pn]) * a.cinvM[pn];
         const double wf = B.w[l] * I.jy;
         ib[l] = fma(cMb[l] * cself, wf, ib[l]);
         const double iL = t == L ? cir[l] : pir, iR = t == L ? pir : cir[l];
@@ -607,7 +670,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
       const long long pb = neighbour<NP>(tl, I, vc.ex, vc.ey, 0, s == 0 ? -1 : 1, &it);
       const int pl = s == 0 ? L : 0;
       const double pir = it >= 0 ? s_ir[it][pl * NP + t] : a.invr[pb + pl * NP + t];
-      const double pMb = it >= 0 ? s_Mb[it][pl * NP + t] : a.Mb[pb + pl * NP + t];
+      const long long pn = pb + pl * NP + t;
+      const double pMb = it >= 0 ? s_Mb[it][pl * NP + t] : -(a.iMb[pn] * a.cinvM[pn]) * a.cinvM[pn];
       const double wf = B.w[t] * I.jx;
       ib[l] = fma(cMb[l] * (l == L ? -alpha * invJy * B.D[L][L] : alpha * invJy * B.D[0][0]), wf, ib[l]);
       const double iL = l == L ? cir[l] : pir, iR = l == L ? pir : cir[l];

@@ -36,6 +36,7 @@ struct Inst2D {
   double gamma, alpha, dt;
   // reciprocals precomputed on the host (an FP64 divide costs ~9 FMA slots)
   double ijx, ijy, idx, idy, ialpha;
+  int tile0, ntiles;  // this instance's tiles in the tile list (contiguous)
 };
 
 struct Inst1D {
@@ -53,6 +54,56 @@ enum : int { DEV_OK = 0, DEV_NONFINITE = 1 };
 
 __device__ __forceinline__ void flag_nonfinite(int* status) {
   if (status) atomicOr(status, DEV_NONFINITE);
+}
+
+// Deterministic sum over the threads of a block (fixed tree order). P2 is a
+// power of two >= blockDim.x; every thread must call it; s_red holds P2
+// doubles. Returns the sum to every thread.
+template <int P2>
+__device__ __forceinline__ double block_sum(double v, double* s_red) {
+  const int tid = threadIdx.x;
+  s_red[tid] = v;
+  for (int k = tid + blockDim.x; k < P2; k += blockDim.x) s_red[k] = 0.0;
+  __syncthreads();
+#pragma unroll
+  for (int w = P2 / 2; w > 0; w >>= 1) {
+    if (tid < w) s_red[tid] += s_red[tid + w];
+    __syncthreads();
+  }
+  const double r = s_red[0];
+  __syncthreads();
+  return r;
+}
+
+// Per-instance sum of one value per tile (block), deterministic: each block
+// stores its partial; the last block of the instance to arrive (atomic
+// counter) adds the instance's partials in tile order. Returns true in every
+// thread of that last block, with the instance total in *total; the counter
+// is reset there for the next reduction on the stream. Every thread calls it.
+template <int P2>
+__device__ __forceinline__ bool instance_sum(double block_partial, int inst, int tile0, int ntiles, double* partials,
+                                             int* counters, double* s_red, double* total) {
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = block_partial;
+    __threadfence();
+    const int prev = atomicAdd(&counters[inst], 1);
+    s_last = (prev == ntiles - 1);
+  }
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < ntiles; k += blockDim.x) acc += __ldcg(&partials[tile0 + k]);
+  *total = block_sum<P2>(acc, s_red);
+  if (threadIdx.x == 0) counters[inst] = 0;
+  return true;
+}
+
+// Smallest power of two >= n (n <= 1024), for block_sum's scratch size.
+__host__ __device__ constexpr int pow2_at_least(int n) {
+  return n <= 1 ? 1 : (n <= 2 ? 2 : (n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : (n <= 32 ? 32 : (n <= 64 ? 64 :
+         (n <= 128 ? 128 : (n <= 256 ? 256 : (n <= 512 ? 512 : 1024)))))))));
 }
 
 }  // namespace igrgpu

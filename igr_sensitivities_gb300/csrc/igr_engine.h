@@ -112,6 +112,8 @@ Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& ins
 // Drivers. Field pointers are device pointers to NG doubles each, in the
 // instance-major Julia layout.
 struct Solve2DOpts { int n_iter = 10; int solver = SOLVER_PCG; };
+// FP64 fields (of NG nodes) one taped RK stage holds for this solver setup.
+int stage_fields2d(const Solve2DOpts& o, bool alpha_pos, long long NG, int ni);
 
 // In-place forward over n_steps fixed steps (dt per instance), Sigma in/out
 // (warm start carried across stages and steps as forward.jl:41-75 does).

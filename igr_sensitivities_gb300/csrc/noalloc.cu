@@ -105,6 +105,8 @@ extern "C" int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const 
   int nt = 0;
   for (int ey0 = 0; ey0 < d->n_ey; ey0 += ty)
     for (int ex0 = 0; ex0 < d->n_ex; ex0 += tx) tiles[nt++] = Tile2D{0, ex0, ey0, 0};
+  I.tile0 = 0;
+  I.ntiles = nt;
   Inst2D* d_inst = reinterpret_cast<Inst2D*>(base);
   Tile2D* d_tiles = reinterpret_cast<Tile2D*>(base + 256);
   double* f = reinterpret_cast<double*>(base + NOALLOC_META);

@@ -95,7 +95,7 @@ def test_freestream_preservation(igr, oracle, p):
     assert max(np.max(np.abs(a)) for a in out) < 1e-11
 
 
-@pytest.mark.parametrize("solver", ["chebyshev", "jacobi"])
+@pytest.mark.parametrize("solver", ["chebyshev", "jacobi", "pcg"])
 def test_solve_elliptic_matches_oracle(igr, oracle, solver):
     basis, mesh, G = setup(igr, oracle, 3, 8, 6)
     q = random_state(mesh, 11)
@@ -107,7 +107,8 @@ def test_solve_elliptic_matches_oracle(igr, oracle, solver):
 
 
 @pytest.mark.parametrize("solver,alpha,n_iter", [("chebyshev", 3.0 * (1 / 8) ** 2, 5), ("jacobi", 3.0 * (1 / 8) ** 2, 6),
-                                                 ("chebyshev", 0.0, 5)])
+                                                 ("chebyshev", 0.0, 5), ("pcg", 3.0 * (1 / 8) ** 2, 12),
+                                                 ("pcg", 3.0 * (1 / 8) ** 2, 1)])
 def test_run_forward_matches_oracle(igr, oracle, solver, alpha, n_iter):
     g = 1.4
     basis, mesh, G = setup(igr, oracle, 3, 8, 8)
@@ -124,7 +125,8 @@ def test_run_forward_matches_oracle(igr, oracle, solver, alpha, n_iter):
 
 @pytest.mark.parametrize("solver,objective", [("chebyshev", "window_rho2"), ("jacobi", "l2_density"),
                                               ("chebyshev", "kinetic_energy"), ("chebyshev", "l2_pressure"),
-                                              ("jacobi", "weighted_momentum"), ("chebyshev", "windowed_kinetic_energy")])
+                                              ("jacobi", "weighted_momentum"), ("chebyshev", "windowed_kinetic_energy"),
+                                              ("pcg", "window_rho2"), ("pcg", "l2_pressure"), ("pcg", "kinetic_energy")])
 def test_adjoint_matches_oracle(igr, oracle, solver, objective):
     g = 1.4
     basis, mesh, G = setup(igr, oracle, 3, 6, 5)
@@ -178,7 +180,8 @@ def test_adjoint_degrees_and_ics(igr, oracle, p, ic, alpha, nex):
     assert abs(res[5] - dgr) <= RTOL_GRAD * abs(dgr)
 
 
-def test_checkpointed_adjoint_equals_full_tape(igr, oracle):
+@pytest.mark.parametrize("solver", ["chebyshev", "pcg"])
+def test_checkpointed_adjoint_equals_full_tape(igr, oracle, solver):
     """A tape budget of a few steps forces segment checkpointing + recompute;
     the gradient must be bitwise the one of the full tape."""
     g = 1.4
@@ -187,20 +190,24 @@ def test_checkpointed_adjoint_equals_full_tape(igr, oracle):
     q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(3, 2), width=0.12)
     dt = W.cfl_dt_2d(mesh, 3, q0, g, 0.1)
     ctx = igr.Context(0)
-    full = igr.enzyme_adjoint_ic(*q0, 11, dt, basis, mesh, g, alpha, n_iter=5, solver="chebyshev", objective="l2_density",
+    full = igr.enzyme_adjoint_ic(*q0, 11, dt, basis, mesh, g, alpha, n_iter=5, solver=solver, objective="l2_density",
                                  with_params=True, ctx=ctx)
     n = mesh.x.size
-    step_bytes = 3 * (16 + 2 * 5) * n * 8
+    # fields of one taped stage (upper bound for either solver at n_iter = 5)
+    step_bytes = 3 * (16 + 1 + 6 + 2 * 5 + 1) * n * 8
     ctx.set_tape_budget(3 * step_bytes + 10 * 6 * n * 8)
-    seg = igr.enzyme_adjoint_ic(*q0, 11, dt, basis, mesh, g, alpha, n_iter=5, solver="chebyshev", objective="l2_density",
+    seg = igr.enzyme_adjoint_ic(*q0, 11, dt, basis, mesh, g, alpha, n_iter=5, solver=solver, objective="l2_density",
                                 with_params=True, ctx=ctx)
+    plan = ctx.last_adjoint_plan()
+    assert plan["segments"] > 1
     assert full[0] == seg[0]
     for a, b in zip(full[1:5], seg[1:5]):
         assert np.array_equal(a, b)
     assert full[5] == seg[5] and full[6] == seg[6]
 
 
-def test_batched_adjoint_matches_single(igr, oracle):
+@pytest.mark.parametrize("solver", ["chebyshev", "pcg"])
+def test_batched_adjoint_matches_single(igr, oracle, solver):
     g0 = 1.4
     basis, mesh, G = setup(igr, oracle, 3, 4, 4)
     B = 3
@@ -214,11 +221,18 @@ def test_batched_adjoint_matches_single(igr, oracle):
         dts.append(W.cfl_dt_2d(mesh, 3, q0, gam, 0.1))
     q0 = np.stack(qs)
     prm = (0.1, 0.2, 0.5)
-    J, dq, dg, da = igr.adjoint_batch(q0, gammas, alphas, dts, 5, basis, mesh, n_iter=5, solver="chebyshev",
+    J, dq, dg, da = igr.adjoint_batch(q0, gammas, alphas, dts, 5, basis, mesh, n_iter=5, solver=solver,
                                       objective="window_rho2", obj_params=prm)
     for b in range(B):
-        Jr, dqr, dgr, dar = oracle.adjoint_2d(G, gammas[b], alphas[b], 5, dts[b], 5, "chebyshev", "window_rho2", list(q0[b]),
+        Jr, dqr, dgr, dar = oracle.adjoint_2d(G, gammas[b], alphas[b], 5, dts[b], 5, solver, "window_rho2", list(q0[b]),
                                               prm)
+        # batching does not change any reduction order: bitwise equal to the single-instance call
+        one = igr.enzyme_adjoint_ic(*[np.asfortranarray(q0[b, v].reshape(mesh.x.shape, order="F")) for v in range(4)], 5,
+                                    dts[b], basis, mesh, gammas[b], alphas[b], n_iter=5, solver=solver,
+                                    objective="window_rho2", obj_params=prm, with_params=True)
+        assert one[0] == J[b] and one[5] == dg[b] and one[6] == da[b]
+        for v in range(4):
+            assert np.array_equal(flat(one[1 + v]), dq[b, v])
         assert abs(J[b] - Jr) <= 1e-12 * abs(Jr)
         num = np.sqrt(sum(np.sum((dq[b, v] - dqr[v]) ** 2) for v in range(4)))
         den = np.sqrt(sum(np.sum(dqr[v] ** 2) for v in range(4)))
