@@ -20,7 +20,7 @@ from ._lib import Context, check, default_context, lib
 
 __all__ = [
     "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
-    "run_forward", "run_forward_", "enzyme_adjoint_ic", "adjoint_batch", "objective_value",
+    "run_forward", "run_forward_", "run_sensitivity", "enzyme_adjoint_ic", "adjoint_batch", "objective_value",
     "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
 ]
 
@@ -190,6 +190,29 @@ def run_forward(mux0, muy0, rho0, E0, dt, T, basis, mesh, gamma, alpha, n_iter=1
     S = np.zeros(shape, order="F")
     run_forward_(*out, S, dt, T, basis, mesh, gamma, alpha, n_iter, solver, ctx)
     return (*out, S)
+
+
+def run_sensitivity(mux0, muy0, rho0, E0, zetax0, zetay0, sigma0, eta0, dt, T, basis, mesh, gamma, alpha, n_iter=10,
+                    solver="pcg", s_gamma=0.0, ctx=None):
+    """run_sensitivity (IGR_adjoints_2d/sensitivity.jl:353-413).
+
+    Advances the state and its tangent (zeta_x, zeta_y, sigma, eta) together
+    to time T; returns (mux, muy, rho, E, Sigma, zetax, zetay, sigma, eta,
+    varsigma). s_gamma adds the direct dP/dgamma tangent source (0 in the
+    reference's 2D package).
+    """
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n).copy() for a in (mux0, muy0, rho0, E0)]
+    s = [_flat(a, n).copy() for a in (zetax0, zetay0, sigma0, eta0)]
+    S, V = np.zeros(n), np.zeros(n)
+    check(ctx, lib().igr2d_run_sensitivity(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma),
+                                           C.c_double(alpha), C.c_double(dt), C.c_double(T), C.c_int(n_iter),
+                                           C.c_int(_solver(solver)), C.c_double(s_gamma), *[_ptr(a) for a in q], _ptr(S),
+                                           *[_ptr(a) for a in s], _ptr(V)))
+    r = lambda a: np.asfortranarray(a.reshape(shape, order="F"))
+    return tuple(r(a) for a in q) + (r(S),) + tuple(r(a) for a in s) + (r(V),)
 
 
 def enzyme_adjoint_ic(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",

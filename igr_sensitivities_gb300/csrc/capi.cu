@@ -186,6 +186,35 @@ int igr2d_run_forward(igr_ctx* ctx, const igr_disc2d* d, double gamma, double al
   });
 }
 
+int igr2d_run_sensitivity(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
+                          int n_iter, int solver, double s_gamma, double* mux, double* muy, double* rho, double* E,
+                          double* sigma, double* zetax, double* zetay, double* srho, double* eta, double* varsigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+    // sensitivity.jl:361-362 (same re-rounding as run_forward!)
+    const int n_steps = (int)std::ceil(t_end / dt);
+    const double dtr = t_end / n_steps;
+    Plan2D P = plan_single(c, d, gamma, alpha, dtr, "sen");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:qs", 10 * N);
+    double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* sv[4] = {buf + 4 * N, buf + 5 * N, buf + 6 * N, buf + 7 * N};
+    double* S = buf + 8 * N;
+    double* V = buf + 9 * N;
+    double* qh[4] = {mux, muy, rho, E};
+    double* sh[4] = {zetax, zetay, srho, eta};
+    for (int v = 0; v < 4; ++v) { h2d(c, q[v], qh[v], N); h2d(c, sv[v], sh[v], N); }
+    Solve2DOpts o{n_iter, solver};
+    sensitivity2d(c, P, q, S, sv, V, n_steps, o, s_gamma);
+    for (int v = 0; v < 4; ++v) { d2h(c, qh[v], q[v], N); d2h(c, sh[v], sv[v], N); }
+    d2h(c, sigma, S, N);
+    d2h(c, varsigma, V, N);
+    sync(c);
+  });
+}
+
 int igr2d_objective(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_steps, double dt,
                     int n_iter, int solver, int objective, const double* obj_params, double* mux, double* muy,
                     double* rho, double* E, double* J) {

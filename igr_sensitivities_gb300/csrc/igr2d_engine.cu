@@ -8,6 +8,7 @@
 #include "igr2d_launch.h"
 #include "igr2d_pcg_kernels.cuh"
 #include "igr2d_rev_kernels.cuh"
+#include "igr2d_sens_kernels.cuh"
 #include "igr_engine.h"
 
 namespace igrgpu {
@@ -396,11 +397,10 @@ static void tile_geometry(const Plan2D& P, int* tx, int* ty) { tile_shape(P.np, 
 // one operator kernel (A p_k and p_k . A p_k, with p_k formed on load) and one
 // pointwise kernel (x, r and r . M^-1 r). With a tape slot, r_k, p_k, A p_k
 // and the scalars are written straight into it.
-static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* x0, double* xa, double* xb,
-                      double* dbuf) {
+static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b, const double* x0,
+                      double* xout, bool taped, double* xa, double* xb, double* dbuf) {
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
-  const bool taped = st.x0t != nullptr;
   double* part;
   int* cnt;
   reduction_scratch(c, P, &part, &cnt);
@@ -416,7 +416,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
   ApplyArgs2D base;
   std::memset(&base, 0, sizeof(base));
   base.tiles = P.d_tiles; base.inst = P.d_inst; base.B = P.B;
-  base.cm = st.cm; base.ckx = st.ckx; base.cky = st.cky; base.cpx = st.cpx; base.cpy = st.cpy; base.b = st.b; base.cinvM = st.cinvM;
+  base.cm = st.cm; base.ckx = st.ckx; base.cky = st.cky; base.cpx = st.cpx; base.cpy = st.cpy; base.b = b; base.cinvM = st.cinvM;
   base.partials = part; base.counters = cnt;
   {  // r_0 = b - A x_0, p_0 = M^-1 r_0, rz_0
     ApplyArgs2D a = base;
@@ -441,7 +441,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
     }
     PcgUpdateArgs u;
     u.tiles = P.d_tiles; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
-    u.x_in = k == 0 ? x0 : st.Sout; u.x_out = st.Sout;
+    u.x_in = k == 0 ? x0 : xout; u.x_out = xout;
     u.p = PK(k); u.ap = AP(k); u.r_in = R(k); u.r_out = R(k + 1); u.cinvM = st.cinvM;
     u.rz = RZ(k); u.pap = PAP(k); u.rz_out = RZ(k + 1);
     u.partials = part; u.counters = cnt;
@@ -450,21 +450,28 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
   }
 }
 
-// Setup + fixed-count solve of one stage. x0: warm start (read only);
-// result in st.Sout; xa/xb/dbuf: scratch.
-static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* x0, double* xa,
-                        double* xb, double* dbuf) {
-  const int nb = P.ntiles();
+// Operator coefficients, IGR source b and diag(A) of one stage (the setup
+// part of solve_elliptic!, elliptic.jl:413-416).
+static void stage_setup(Ctx& c, const Plan2D& P, StageBuf& st) {
   SetupArgs2D sa;
   std::memset(&sa, 0, sizeof(sa));
   sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
   sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
   sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = st.cM;
-  { LaunchScope ls(c, KID_SETUP); NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, nb, c.stream)); }
+  LaunchScope ls(c, KID_SETUP);
+  NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, P.ntiles(), c.stream));
+}
+
+// Fixed-count solve A x = b on the stage's operator (set up by stage_setup):
+// x0 = warm start (read only), result in xout (!= x0). taped: record the
+// iterates into the stage's tape slots. xa/xb/dbuf: scratch.
+static void stage_solve_b(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b, const double* x0,
+                          double* xout, bool taped, double* xa, double* xb, double* dbuf) {
   if (o.solver == SOLVER_PCG) {
-    pcg_solve(c, P, o, st, x0, xa, xb, dbuf);
+    pcg_solve(c, P, o, st, b, x0, xout, taped, xa, xb, dbuf);
     return;
   }
+  const int nb = P.ntiles();
   const int epi = o.solver == SOLVER_CHEBYSHEV ? EPI_CHEB : EPI_JACOBI;
   std::vector<double> ca, cc;
   cheb_coeffs(P.B, o.n_iter, ca, cc);
@@ -474,15 +481,17 @@ static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf&
     std::memset(&a, 0, sizeof(a));
     a.tiles = P.d_tiles; a.inst = P.d_inst; a.B = P.B;
     a.x = x;
-    a.cm = st.cm; a.ckx = st.ckx; a.cky = st.cky; a.cpx = st.cpx; a.cpy = st.cpy; a.b = st.b; a.cinvM = st.cinvM;
+    a.cm = st.cm; a.ckx = st.ckx; a.cky = st.cky; a.cpx = st.cpx; a.cpy = st.cpy; a.b = b; a.cinvM = st.cinvM;
     a.d_in = k == 0 ? nullptr : dbuf;
     a.d_out = dbuf;
-    double* xo = (k == o.n_iter - 1) ? st.Sout : ((k % 2 == 0) ? xa : xb);
+    double* xo = (k == o.n_iter - 1) ? xout : ((k % 2 == 0) ? xa : xb);
     a.x_out = xo;
-    a.tape_x = st.xk.empty() ? nullptr : st.xk[k];
-    a.tape_r = st.rk.empty() ? nullptr : st.rk[k];
-    a.tape_gx = st.gxk.empty() ? nullptr : st.gxk[k];
-    a.tape_gy = st.gyk.empty() ? nullptr : st.gyk[k];
+    if (taped) {
+      a.tape_x = st.xk.empty() ? nullptr : st.xk[k];
+      a.tape_r = st.rk.empty() ? nullptr : st.rk[k];
+      a.tape_gx = st.gxk.empty() ? nullptr : st.gxk[k];
+      a.tape_gy = st.gyk.empty() ? nullptr : st.gyk[k];
+    }
     a.ca = ca[k + 1]; a.cc = cc[k + 1];
     a.omega = 2.0 / 3.0;
     { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(epi, a, nb, c.stream)); }
@@ -490,28 +499,44 @@ static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf&
   }
 }
 
+// Setup + fixed-count solve of one stage: x0 = warm start, result in st.Sout
+// (taped when the stage buffer carries tape slots).
+static void stage_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* x0, double* xa,
+                        double* xb, double* dbuf) {
+  stage_setup(c, P, st);
+  const bool taped = st.x0t != nullptr || !st.xk.empty();
+  stage_solve_b(c, P, o, st, st.b, x0, st.Sout, taped, xa, xb, dbuf);
+}
+
 // One SSP-RK3 step: stage inputs st[0..2] (st[0].q holds q^n), warm start
 // Sin, output state into (qout, invrout) (may alias st[0].q: pointwise).
+// SSP-RK3 stage coefficients (forward.jl:53-68): q_out = c0 q^n + c1 q_s + c2 dt k(q_s)
+static const double RK_C0[3] = {0.0, 3.0 / 4, 1.0 / 3}, RK_C1[3] = {1.0, 1.0 / 4, 2.0 / 3}, RK_C2[3] = {1.0, 1.0 / 4, 2.0 / 3};
+
+// Hyperbolic RHS + RK combination of stage s (inputs st[s], step start st[0]).
+static void hyp_stage(Ctx& c, const Plan2D& P, StageBuf st[3], int s, double* const qout[4], double* invrout) {
+  HypArgs2D h;
+  std::memset(&h, 0, sizeof(h));
+  h.tiles = P.d_tiles; h.inst = P.d_inst; h.B = P.B;
+  for (int v = 0; v < 4; ++v) { h.q[v] = st[s].q[v]; h.qn[v] = st[0].q[v]; }
+  h.invr = st[s].invr;
+  h.S = st[s].Sout;
+  h.c0 = RK_C0[s]; h.c1 = RK_C1[s]; h.c2 = RK_C2[s];
+  for (int v = 0; v < 4; ++v) h.qo[v] = s < 2 ? st[s + 1].q[v] : qout[v];
+  h.invro = s < 2 ? st[s + 1].invr : invrout;
+  h.ws_x = st[s].wsx; h.ws_y = st[s].wsy;
+  h.status = c.d_status;
+  LaunchScope ls(c, KID_HYP);
+  NP_DISPATCH(P.np, launch_k2_hyp_rk<NPV>(h, P.ntiles(), c.stream));
+}
+
 static void step_forward(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf st[3], const double* Sin, double* const qout[4],
                          double* invrout, double* xa, double* xb, double* dbuf) {
-  const int nb = P.ntiles();
   const bool apos = any_alpha_pos(P);
-  const double c0s[3] = {0.0, 3.0 / 4, 1.0 / 3}, c1s[3] = {1.0, 1.0 / 4, 2.0 / 3}, c2s[3] = {1.0, 1.0 / 4, 2.0 / 3};
   const double* sprev = Sin;
   for (int s = 0; s < 3; ++s) {
     if (apos) stage_solve(c, P, o, st[s], sprev, xa, xb, dbuf);
-    HypArgs2D h;
-    std::memset(&h, 0, sizeof(h));
-    h.tiles = P.d_tiles; h.inst = P.d_inst; h.B = P.B;
-    for (int v = 0; v < 4; ++v) { h.q[v] = st[s].q[v]; h.qn[v] = st[0].q[v]; }
-    h.invr = st[s].invr;
-    h.S = st[s].Sout;
-    h.c0 = c0s[s]; h.c1 = c1s[s]; h.c2 = c2s[s];
-    for (int v = 0; v < 4; ++v) h.qo[v] = s < 2 ? st[s + 1].q[v] : qout[v];
-    h.invro = s < 2 ? st[s + 1].invr : invrout;
-    h.ws_x = st[s].wsx; h.ws_y = st[s].wsy;
-    h.status = c.d_status;
-    { LaunchScope ls(c, KID_HYP); NP_DISPATCH(P.np, launch_k2_hyp_rk<NPV>(h, nb, c.stream)); }
+    hyp_stage(c, P, st, s, qout, invrout);
     sprev = st[s].Sout;
   }
 }
@@ -551,6 +576,85 @@ void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_s
       sig_cur = Sig;
     }
   }
+  check_status(c);
+}
+
+// ------------------------------------------------------------------------------------------
+// Tangent (run_sensitivity, sensitivity.jl:353-413)
+// ------------------------------------------------------------------------------------------
+static void sens_rhs(Ctx& c, const Plan2D& P, const StageBuf& st, double* const s[4], double* b) {
+  SensRhsArgs2D a;
+  std::memset(&a, 0, sizeof(a));
+  a.tiles = P.d_tiles; a.inst = P.d_inst; a.B = P.B;
+  for (int v = 0; v < 3; ++v) { a.q[v] = st.q[v]; a.s[v] = s[v]; }
+  a.invr = st.invr; a.S = st.Sout;
+  a.b_out = b;
+  LaunchScope ls(c, KID_TAN);
+  NP_DISPATCH(P.np, launch_k2_sens_rhs<NPV>(a, P.ntiles(), c.stream));
+}
+
+void sensitivity2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, double* const s[4], double* vs, int n_steps,
+                   const Solve2DOpts& o, double s_gamma) {
+  check_alpha_uniform(P);
+  const long long NG = P.NG;
+  const bool apos = any_alpha_pos(P);
+  const int ni = (int)P.inst.size();
+  double* scratch = c.ws.dbl("sen:stages", (size_t)NG * 3 * STAGE_FIXED_FIELDS);
+  StageBuf st[3];
+  for (int k = 0; k < 3; ++k) st[k] = stage_from(scratch + (long long)k * STAGE_FIXED_FIELDS * NG, NG, o, apos, false, ni);
+  double* tsb = c.ws.dbl("sen:tan", (size_t)NG * 8);
+  double* ts[3][4];
+  for (int v = 0; v < 4; ++v) { ts[0][v] = s[v]; ts[1][v] = tsb + v * NG; ts[2][v] = tsb + (4 + v) * NG; }
+  double* bs = c.ws.dbl("sen:bs", NG);
+  double* xa = c.ws.dbl("sen:xa", NG);
+  double* xb = c.ws.dbl("sen:xb", NG);
+  double* db = c.ws.dbl("sen:d", NG);
+  double* sigAlt = c.ws.dbl("sen:sig", NG);
+  double* vsAlt = c.ws.dbl("sen:vs", NG);
+  for (int v = 0; v < 4; ++v) st[0].q[v] = q[v];
+  recip(c, q[2], st[0].invr, NG);
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  cuda_check(cudaMemsetAsync(Sig, 0, NG * sizeof(double), c.stream), "zero Sigma");      // sensitivity.jl:364
+  cuda_check(cudaMemsetAsync(vs, 0, NG * sizeof(double), c.stream), "zero varsigma");
+  // Sigma and varsigma chains: warm start in *_cur, solution into the other buffer
+  double* sig_cur = Sig; double* sig_nxt = sigAlt;
+  double* vs_cur = vs; double* vs_nxt = vsAlt;
+  for (int step = 0; step < n_steps; ++step) {
+    for (int k = 0; k < 3; ++k) {
+      if (apos) {
+        st[k].Sout = sig_nxt;
+        stage_solve(c, P, o, st[k], sig_cur, xa, xb, db);
+        std::swap(sig_cur, sig_nxt);
+        sens_rhs(c, P, st[k], ts[k], bs);
+        stage_solve_b(c, P, o, st[k], bs, vs_cur, vs_nxt, false, xa, xb, db);
+        std::swap(vs_cur, vs_nxt);
+      } else {
+        st[k].Sout = sig_cur;  // zero
+      }
+      hyp_stage(c, P, st, k, q, st[0].invr);
+      SensHypArgs2D h;
+      std::memset(&h, 0, sizeof(h));
+      h.tiles = P.d_tiles; h.inst = P.d_inst; h.B = P.B;
+      for (int v = 0; v < 4; ++v) { h.q[v] = st[k].q[v]; h.s[v] = ts[k][v]; h.sn[v] = ts[0][v]; h.so[v] = k < 2 ? ts[k + 1][v] : s[v]; }
+      h.invr = st[k].invr; h.S = st[k].Sout; h.vs = vs_cur;
+      h.ws_x = st[k].wsx; h.ws_y = st[k].wsy;
+      h.c0 = RK_C0[k]; h.c1 = RK_C1[k]; h.c2 = RK_C2[k]; h.s_gamma = s_gamma;
+      h.status = c.d_status;
+      LaunchScope ls(c, KID_TAN);
+      NP_DISPATCH(P.np, launch_k2_sens_hyp_rk<NPV>(h, P.ntiles(), c.stream));
+    }
+  }
+  if (apos) {  // sensitivity.jl:404-409: Sigma and varsigma at the final state
+    recip(c, q[2], st[0].invr, NG);
+    st[0].Sout = sig_nxt;
+    stage_solve(c, P, o, st[0], sig_cur, xa, xb, db);
+    std::swap(sig_cur, sig_nxt);
+    sens_rhs(c, P, st[0], s, bs);
+    stage_solve_b(c, P, o, st[0], bs, vs_cur, vs_nxt, false, xa, xb, db);
+    std::swap(vs_cur, vs_nxt);
+  }
+  if (sig_cur != Sig) cuda_check(cudaMemcpyAsync(Sig, sig_cur, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Sigma");
+  if (vs_cur != vs) cuda_check(cudaMemcpyAsync(vs, vs_cur, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "varsigma");
   check_status(c);
 }
 

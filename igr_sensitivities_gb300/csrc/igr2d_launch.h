@@ -14,6 +14,8 @@ struct HypArgs2D;
 struct HypRevArgs2D;
 struct ApplyRevArgs2D;
 struct SetupRevArgs2D;
+struct SensRhsArgs2D;
+struct SensHypArgs2D;
 
 template <int NP> int threads2d();
 template <int NP> void launch_k2_setup(const SetupArgs2D& a, int nblocks, cudaStream_t s);
@@ -22,6 +24,8 @@ template <int NP> void launch_k2_hyp_rk(const HypArgs2D& a, int nblocks, cudaStr
 template <int NP> void launch_k2_hyp_rev(const HypRevArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void launch_k2_apply_rev(int srev, const ApplyRevArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void launch_k2_setup_rev(const SetupRevArgs2D& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k2_sens_rhs(const SensRhsArgs2D& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k2_sens_hyp_rk(const SensHypArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void tile_shape2d(int* tx, int* ty);
 
 }  // namespace igrgpu

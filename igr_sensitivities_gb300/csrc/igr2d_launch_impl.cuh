@@ -3,6 +3,7 @@
 #pragma once
 #include "igr2d_launch.h"
 #include "igr2d_rev_kernels.cuh"
+#include "igr2d_sens_kernels.cuh"
 
 namespace igrgpu {
 
@@ -35,6 +36,13 @@ template <int NP> void launch_k2_setup_rev(const SetupRevArgs2D& a, int nb, cuda
   k2_setup_rev<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
 }
 
+template <int NP> void launch_k2_sens_rhs(const SensRhsArgs2D& a, int nb, cudaStream_t s) {
+  k2_sens_rhs<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_sens_hyp_rk(const SensHypArgs2D& a, int nb, cudaStream_t s) {
+  k2_sens_hyp_rk<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+
 #define IGR2D_INSTANTIATE(NP)                                                                        \
   template int threads2d<NP>();                                                                      \
   template void tile_shape2d<NP>(int*, int*);                                                        \
@@ -43,6 +51,8 @@ template <int NP> void launch_k2_setup_rev(const SetupRevArgs2D& a, int nb, cuda
   template void launch_k2_hyp_rk<NP>(const HypArgs2D&, int, cudaStream_t);                           \
   template void launch_k2_hyp_rev<NP>(const HypRevArgs2D&, int, cudaStream_t);                       \
   template void launch_k2_apply_rev<NP>(int, const ApplyRevArgs2D&, int, cudaStream_t);              \
-  template void launch_k2_setup_rev<NP>(const SetupRevArgs2D&, int, cudaStream_t);
+  template void launch_k2_setup_rev<NP>(const SetupRevArgs2D&, int, cudaStream_t);                    \
+  template void launch_k2_sens_rhs<NP>(const SensRhsArgs2D&, int, cudaStream_t);                      \
+  template void launch_k2_sens_hyp_rk<NP>(const SensHypArgs2D&, int, cudaStream_t);
 
 }  // namespace igrgpu

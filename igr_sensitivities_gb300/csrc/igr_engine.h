@@ -118,6 +118,11 @@ int stage_fields2d(const Solve2DOpts& o, bool alpha_pos, long long NG, int ni);
 // In-place forward over n_steps fixed steps (dt per instance), Sigma in/out
 // (warm start carried across stages and steps as forward.jl:41-75 does).
 void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_steps, const Solve2DOpts& o);
+// Coupled primal + tangent SSP-RK3 (run_sensitivity, sensitivity.jl:353-413):
+// q and the tangent s in place; Sigma and varsigma zeroed at entry and
+// returned for the final state. s_gamma adds the direct dP/dgamma source.
+void sensitivity2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, double* const s[4], double* vs, int n_steps,
+                   const Solve2DOpts& o, double s_gamma);
 // One elliptic solve (solve_elliptic!, elliptic.jl:413-427) with Sigma as warm start.
 void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o);
 // One hyperbolic RHS evaluation (compute_hyperbolic_rhs!, hyperbolic.jl:27).

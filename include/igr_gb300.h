@@ -102,6 +102,17 @@ int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops);
 int igr2d_run_forward(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
                       int n_iter, int solver, double* mux, double* muy, double* rho, double* E, double* sigma);
 
+/* run_sensitivity (IGR_adjoints_2d/sensitivity.jl:353-413): the coupled
+ * primal + tangent SSP-RK3 to time T, in place. On entry (mux..E) is the
+ * initial state and (zetax, zetay, srho, eta) its tangent direction; on exit
+ * both are at T, with sigma = Sigma(T) and varsigma = its tangent. Same dt
+ * re-rounding as run_forward!. s_gamma != 0 adds the direct dP/dgamma source
+ * s_gamma * rho e to the tangent pressure, as the 1D package does
+ * (IGR_adjoints_1d/sensitivity.jl:36-41); the 2D reference has none (pass 0). */
+int igr2d_run_sensitivity(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
+                          int n_iter, int solver, double s_gamma, double* mux, double* muy, double* rho, double* E,
+                          double* sigma, double* zetax, double* zetay, double* srho, double* eta, double* varsigma);
+
 /* enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:428-454): J and
  * dJ/dq0 of the objective after n_steps SSP-RK3 steps of size dt (no dt
  * re-rounding, Sigma warm start from zero). dgamma/dalpha (may be NULL) are
