@@ -393,3 +393,66 @@ int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_
 }
 
 }  // extern "C"
+
+namespace {
+
+void check_disc1(int p, const double* xi, const double* w, const double* D) {
+  if (!xi || !w || !D) throw Error(IGR_EINVAL, "null basis arrays");
+  if (p < 1 || p > 4) throw Error(IGR_EINVAL, "polynomial degree p must be in 1..4");
+}
+
+}  // namespace
+
+extern "C" {
+
+int igr1d_run_forward(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
+                      int n_iter, int solver, double* mu, double* rho, double* E, double* sigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!d) throw Error(IGR_EINVAL, "null discretisation");
+    check_disc1(d->p, d->xi, d->w, d->D);
+    check_solver(solver, n_iter);
+    if (d->n_e < 1 || !(d->L > 0)) throw Error(IGR_EINVAL, "bad mesh");
+    if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+    const int n_steps = (int)std::ceil(t_end / dt);  // IGR_adjoints_1d/forward.jl:58-59
+    const double dtr = t_end / n_steps;
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    Plan1D P = make_plan1d(c, B, {Inst1DDesc{d->n_e, d->L, gamma, alpha, dtr, n_steps}}, forward1d_scratch_fields(), "f1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:q", 4 * N);
+    double* in[3] = {mu, rho, E};
+    for (int v = 0; v < 3; ++v) h2d(c, buf + v * N, in[v], N);
+    Solve2DOpts o{n_iter, solver};
+    forward1d(c, P, buf, buf + 3 * N, o, true);
+    for (int v = 0; v < 3; ++v) d2h(c, in[v], buf + v * N, N);
+    d2h(c, sigma, buf + 3 * N, N);
+    sync(c);
+  });
+}
+
+int igr1d_forward_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                        const int* n_e, const double* L, const double* gammas, const double* alphas,
+                        const double* dts, const int* n_steps, int n_iter, int solver, int final_solve, double* q,
+                        double* sigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc1(p, xi, w, D);
+    check_solver(solver, n_iter);
+    if (n_inst < 1 || !n_e || !L || !gammas || !alphas || !dts || !n_steps || !q || !sigma)
+      throw Error(IGR_EINVAL, "bad batch arguments");
+    BasisDev B = make_basis_dev(p, xi, w, D);
+    std::vector<Inst1DDesc> insts;
+    for (int i = 0; i < n_inst; ++i) insts.push_back(Inst1DDesc{n_e[i], L[i], gammas[i], alphas[i], dts[i], n_steps[i]});
+    Plan1D P = make_plan1d(c, B, insts, forward1d_scratch_fields(), "f1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:qb", 4 * N);
+    h2d(c, buf, q, 3 * N);
+    Solve2DOpts o{n_iter, solver};
+    forward1d(c, P, buf, buf + 3 * N, o, final_solve != 0);
+    d2h(c, q, buf, 3 * N);
+    d2h(c, sigma, buf + 3 * N, N);
+    sync(c);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,425 @@
+// 1D IGR-Euler kernels (IGR_adjoints_1d): one CTA per instance, persistent
+// over the whole trajectory.
+//
+// A 1D instance is small (N_e <= a few thousand elements, 4 nodes each at
+// P3), so instead of one launch per operator application (whose launch
+// latency would dominate) each CTA advances its own instance through every
+// RK stage, solver iteration and step, with __syncthreads() between phases
+// and deterministic block reductions for the solver inner products. A batch
+// of instances with different N_e, gamma, alpha, dt and step counts is one
+// launch; instances are independent, so no grid-wide synchronisation exists.
+//
+// Thread mapping: one thread per element (strided over the CTA), the
+// element's NP nodes in registers; face partners are read from the
+// neighbouring elements' nodes (L1/L2 resident: an instance's fields are a
+// few tens of KB). Node order is the reference's Julia (n_p, N_e) layout.
+#pragma once
+#include "igr2d_kernels.cuh"  // line contractions dot_row / dot_end / dot_col
+
+namespace igrgpu {
+
+constexpr int T1 = 256;  // threads per 1D CTA (power of two: block_sum scratch size)
+
+// Per-CTA view of one instance.
+template <int NP>
+struct View1 {
+  Inst1D I;
+  int N;          // nodes
+  double* scr;    // this instance's scratch (fields of N doubles)
+  __device__ double* f(int k) const { return scr + (long long)k * N; }
+};
+
+__device__ __forceinline__ int wrap_left(int e, int ne) { return e == 0 ? ne - 1 : e - 1; }
+__device__ __forceinline__ int wrap_right(int e, int ne) { return e == ne - 1 ? 0 : e + 1; }
+
+// ---------------------------------------------------------------------------
+// Physics at one node (IGR_adjoints_1d/euler.jl:46-111)
+//   P = (gamma-1)(E - mu^2/(2 rho)),  P_bar = P + Sigma
+//   f = (mu^2/rho + P_bar, mu, (E + P_bar) mu/rho),  |u| + sqrt(gamma P / rho)
+// ---------------------------------------------------------------------------
+struct Node1 { double f[3], P, u; };
+__device__ __forceinline__ Node1 node1(double g, double mu, double E, double S, double ir) {
+  Node1 o;
+  o.u = mu * ir;
+  o.P = (g - 1.0) * (E - 0.5 * mu * o.u);
+  const double pb = o.P + S;
+  o.f[0] = fma(mu, o.u, pb); o.f[1] = mu; o.f[2] = (E + pb) * o.u;
+  return o;
+}
+__device__ __forceinline__ double ws1(double g, const Node1& o, double ir) { return fabs(o.u) + sqrt(g * o.P * ir); }
+
+// ---------------------------------------------------------------------------
+// Stage setup (IGR_adjoints_1d/elliptic.jl:126-154, 206-253): IGR source
+// b = w_i J 2 alpha (d_x u)^2, diag(A), and the operator coefficients
+//   cm = w_i J / rho, ck = alpha w_i / (J rho), cpR[e] = alpha eta max(1/rho_L, 1/rho_R) / dx
+// (cpR: the penalty of element e's right face). All threads call it.
+// ---------------------------------------------------------------------------
+template <int NP>
+__device__ void d1_setup(const View1<NP>& v, const BasisDev& B, const double* mu, const double* ir, double* b, double* cm,
+                         double* ck, double* cpR, double* cinvM, double* cM) {
+  constexpr int L = NP - 1;
+  const Inst1D& I = v.I;
+  const double eta = (double)(NP * NP);
+  const double al = I.alpha;
+  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+    const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
+    const int base = e * NP;
+    double r[NP], u[NP], kk[NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) { r[i] = ir[base + i]; u[i] = mu[base + i] * r[i]; }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const double du = I.iJ * dot_row<NP>(B, i, u);
+      b[base + i] = (B.w[i] * I.J) * (2.0 * al * (du * du));
+      cm[base + i] = (B.w[i] * I.J) * r[i];
+      kk[i] = (al * B.w[i] * I.iJ) * r[i];
+      ck[base + i] = kk[i];
+    }
+    const double irLL = ir[eL * NP + L], irR0 = ir[eR * NP];
+    const double cpr = al * eta * I.idx * ((irR0 > r[L]) ? irR0 : r[L]);
+    const double cpl = al * eta * I.idx * ((r[0] > irLL) ? r[0] : irLL);
+    cpR[e] = cpr;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      double M = cm[base + k];
+#pragma unroll
+      for (int i = 0; i < NP; ++i) M = fma(kk[i], B.D[i][k] * B.D[i][k], M);
+      if (k == L) M = fma(-kk[L] * B.iwL, B.D[L][L], M) + cpr;
+      if (k == 0) M = fma(kk[0] * B.iw0, B.D[0][0], M) + cpl;
+      cinvM[base + k] = 1.0 / M;
+      if (cM) cM[base + k] = M;
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// SIP operator y = A x (IGR_adjoints_1d/elliptic.jl:32-116) per element, with
+// the face terms folded as in the 2D kernels:
+//   F = hw (ck_L d_L + ck_R d_R) + cp (x_L - x_R),  hw = -1/(2 w_0)
+//   y_L-side += F, y_R-side -= F, symmetry term into the stiffness transpose.
+// ldx(n) supplies x at node n; epi(e, x[], y[]) consumes the element's result.
+// Does not synchronise (the epilogue decides what it writes).
+// ---------------------------------------------------------------------------
+template <int NP, class LDX, class EPI>
+__device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm, const double* ck,
+                                         const double* cpR, EPI epi) {
+  constexpr int L = NP - 1;
+  const int ne = v.I.ne;
+  const double hw = B.hw;
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const int eL = wrap_left(e, ne), eR = wrap_right(e, ne);
+    const int base = e * NP;
+    double x[NP], g[NP], xl[NP], xr[NP], kc[NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) { x[i] = ldx(base + i); kc[i] = ck[base + i]; }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) { xl[i] = ldx(eL * NP + i); xr[i] = ldx(eR * NP + i); }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) g[i] = dot_row<NP>(B, i, x);
+    const double gl = dot_end<NP>(B, true, xl), gr = dot_end<NP>(B, false, xr);
+    const double ckl = ck[eL * NP + L], ckr = ck[eR * NP];
+    const double jl = xl[L] - x[0];
+    const double Fl = fma(cpR[eL], jl, hw * fma(ckl, gl, kc[0] * g[0]));
+    const double jr = x[L] - xr[0];
+    const double Fr = fma(cpR[e], jr, hw * fma(kc[L], g[L], ckr * gr));
+    double sx[NP];
+#pragma unroll
+    for (int i = 1; i < L; ++i) sx[i] = kc[i] * g[i];
+    sx[0] = kc[0] * fma(hw, jl, g[0]);
+    sx[L] = kc[L] * fma(hw, jr, g[L]);
+    double y[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k)
+      y[k] = dot_col<NP>(B, k, sx, fma(cm[base + k], x[k], (k == 0) ? -Fl : ((k == L) ? Fr : 0.0)));
+    epi(e, x, y);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Solver tape of one stage (adjoint only). Jacobi / Chebyshev: x_k, r_k for
+// k < n. PCG: x_0, r_0..r_n, p_k, A p_k (k < n) and the scalars rz_0..rz_n,
+// pAp_0..pAp_{n-1}.
+// ---------------------------------------------------------------------------
+struct SolveTape1 {
+  double* base = nullptr;  // null: untaped
+  int N = 0, n = 0, pcg = 0;
+  __device__ double* x(int k) const { return base + (long long)k * N; }                  // Jac/Cheb x_k, PCG x_0
+  __device__ double* r(int k) const { return base + (long long)((pcg ? 1 : n) + k) * N; }
+  __device__ double* p(int k) const { return base + (long long)(n + 2 + k) * N; }
+  __device__ double* ap(int k) const { return base + (long long)(2 * n + 2 + k) * N; }
+  __device__ double* scal() const { return base + (long long)(3 * n + 2) * N; }          // rz[0..n], pAp[0..n-1]
+};
+__host__ __device__ inline int solve_tape_fields1(int solver, int n, int N) {
+  if (solver == 0) return 3 * n + 2 + (2 * n + 1 + N - 1) / N;
+  return 2 * n;
+}
+
+// Chebyshev recurrence coefficients for iteration it = 1..n (elliptic.jl:383-391)
+__device__ __forceinline__ void cheb_coef(const BasisDev& B, int it, double& rc, double* ca, double* cc) {
+  if (it == 1) { *ca = 0.0; *cc = 1.0 / B.cheb_theta; rc = 1.0 / B.cheb_sigma; return; }
+  const double rn = 1.0 / (2.0 * B.cheb_sigma - rc);
+  *ca = rn * rc; *cc = 2.0 * rn / B.cheb_delta;
+  rc = rn;
+}
+
+// Fixed-count solve A x = b on the instance (pcg_fixed! / jacobi_fixed! /
+// chebyshev_fixed!, elliptic.jl:307-430): x0 warm start, result in xout
+// (!= x0); w0..w3: scratch fields. All threads call it; ends synchronised.
+template <int NP>
+__device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int n, const double* b, const double* x0,
+                         double* xout, const double* cm, const double* ck, const double* cpR, const double* cinvM,
+                         double* w0, double* w1, double* w2, double* w3, const SolveTape1& tp, double* s_red) {
+  const int N = v.N;
+  const bool taped = tp.base != nullptr;
+  if (solver == 0) {
+    // ---- PCG: w0 = r, w1 = p, w2 = A p
+    double* r = w0; double* p = w1; double* ap = w2;
+    double part = 0.0;
+    d1_apply<NP>(v, B, [&](int m) { return x0[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        const int m = e * NP + i;
+        const double rr = b[m] - y[i], z = rr * cinvM[m];
+        r[m] = rr; p[m] = z;
+        part = fma(rr, z, part);
+        if (taped) { tp.x(0)[m] = xx[i]; tp.r(0)[m] = rr; }
+      }
+    });
+    double rz = block_sum<T1>(part, s_red);
+    if (taped && threadIdx.x == 0) tp.scal()[0] = rz;
+    for (int k = 0; k < n; ++k) {
+      part = 0.0;
+      d1_apply<NP>(v, B, [&](int m) { return p[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+          const int m = e * NP + i;
+          ap[m] = y[i];
+          part = fma(xx[i], y[i], part);
+          if (taped) { tp.p(k)[m] = xx[i]; tp.ap(k)[m] = y[i]; }
+        }
+      });
+      const double pAp = block_sum<T1>(part, s_red);
+      if (taped && threadIdx.x == 0) tp.scal()[n + 1 + k] = pAp;
+      const double a = rz / (pAp + 1e-30);
+      part = 0.0;
+      const double* xin = k == 0 ? x0 : xout;
+      for (int m = threadIdx.x; m < N; m += blockDim.x) {
+        xout[m] = fma(a, p[m], xin[m]);
+        const double rr = fma(-a, ap[m], r[m]);
+        r[m] = rr;
+        part = fma(rr, rr * cinvM[m], part);
+        if (taped) tp.r(k + 1)[m] = rr;
+      }
+      const double rzn = block_sum<T1>(part, s_red);
+      if (taped && threadIdx.x == 0) tp.scal()[k + 1] = rzn;
+      const double beta = rzn / (rz + 1e-30);
+      for (int m = threadIdx.x; m < N; m += blockDim.x) p[m] = fma(beta, p[m], r[m] * cinvM[m]);
+      rz = rzn;
+      __syncthreads();
+    }
+    return;
+  }
+  // ---- Jacobi / Chebyshev: one apply per iteration, x ping-pong in w0/w1, d in w2
+  double rc = 0.0;
+  const double* x = x0;
+  for (int k = 0; k < n; ++k) {
+    double* xo = (k == n - 1) ? xout : ((k % 2 == 0) ? w0 : w1);
+    double ca = 0.0, cc = 0.0;
+    if (solver == 2) cheb_coef(B, k + 1, rc, &ca, &cc);
+    double* d = w2;
+    d1_apply<NP>(v, B, [&](int m) { return x[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        const int m = e * NP + i;
+        const double rr = b[m] - y[i];
+        if (taped) { tp.x(k)[m] = xx[i]; tp.r(k)[m] = rr; }
+        if (solver == 2) {
+          const double z = rr * cinvM[m];
+          const double dn = k == 0 ? cc * z : fma(ca, d[m], cc * z);
+          d[m] = dn;
+          xo[m] = xx[i] + dn;
+        } else {
+          xo[m] = fma((2.0 / 3.0) * rr, cinvM[m], xx[i]);
+        }
+      }
+    });
+    __syncthreads();
+    x = xo;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Hyperbolic DG RHS (IGR_adjoints_1d/hyperbolic.jl:134-194) fused with the
+// SSP-RK3 stage combination q_out = c0 q^n + c1 q_s + c2 dt k(q_s, Sigma),
+// plus 1/rho of q_out. Optional raw RHS output (kout). All threads call it.
+// ---------------------------------------------------------------------------
+template <int NP>
+__device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* const q[3], const double* ir,
+                          const double* S, const double* const qn[3], double c0, double c1, double c2,
+                          double* const qo[3], double* iro, double* const kout[3], int* status) {
+  constexpr int L = NP - 1;
+  const Inst1D& I = v.I;
+  const double g = I.gamma, iJ = I.iJ, c2dt = c2 * I.dt;
+  bool bad = false;
+  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+    const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
+    const int base = e * NP;
+    double qq[3][NP], f[3][NP], k[3][NP];
+    Node1 n0, nL;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const int m = base + i;
+      qq[0][i] = q[0][m]; qq[1][i] = q[1][m]; qq[2][i] = q[2][m];
+      const Node1 o = node1(g, qq[0][i], qq[2][i], S[m], ir[m]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c][i] = o.f[c];
+      if (i == 0) n0 = o;
+      if (i == L) nL = o;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int i = 0; i < NP; ++i) k[c][i] = -iJ * dot_row<NP>(B, i, f[c]);
+    // right face (own node L | node 0 of eR)
+    {
+      const int m = eR * NP;
+      const double pq[3] = {q[0][m], q[1][m], q[2][m]};
+      const double pir = ir[m];
+      const Node1 o = node1(g, pq[0], pq[2], S[m], pir);
+      const double wl = ws1(g, nL, ir[base + L]), wr = ws1(g, o, pir);
+      const double lam = (wr > wl) ? wr : wl;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const double fs = 0.5 * fma(lam, qq[c][L] - pq[c], f[c][L] + o.f[c]);
+        k[c][L] = fma(-iJ * B.iwL, fs - f[c][L], k[c][L]);
+      }
+    }
+    // left face (node L of eL | own node 0)
+    {
+      const int m = eL * NP + L;
+      const double pq[3] = {q[0][m], q[1][m], q[2][m]};
+      const double pir = ir[m];
+      const Node1 o = node1(g, pq[0], pq[2], S[m], pir);
+      const double wl = ws1(g, o, pir), wr = ws1(g, n0, ir[base]);
+      const double lam = (wr > wl) ? wr : wl;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const double fs = 0.5 * fma(lam, pq[c] - qq[c][0], o.f[c] + f[c][0]);
+        k[c][0] = fma(iJ * B.iw0, fs - f[c][0], k[c][0]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const int m = base + i;
+      double out[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (kout) kout[c][m] = k[c][i];
+        double val = fma(c2dt, k[c][i], c1 * qq[c][i]);
+        if (c0 != 0.0) val = fma(c0, qn[c][m], val);
+        out[c] = val;
+      }
+      if (qo) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) qo[c][m] = out[c];
+        iro[m] = 1.0 / out[1];
+      }
+      bad |= !(out[1] > 0.0) || !isfinite(out[0]) || !isfinite(out[1]) || !isfinite(out[2]);
+    }
+  }
+  if (bad) flag_nonfinite(status);
+  __syncthreads();
+}
+
+template <int NP>
+__device__ void d1_recip(const View1<NP>& v, const double* x, double* y) {
+  for (int m = threadIdx.x; m < v.N; m += blockDim.x) y[m] = 1.0 / x[m];
+  __syncthreads();
+}
+template <int NP>
+__device__ void d1_copy(const View1<NP>& v, const double* x, double* y) {
+  for (int m = threadIdx.x; m < v.N; m += blockDim.x) y[m] = x[m];
+  __syncthreads();
+}
+template <int NP>
+__device__ void d1_zero(const View1<NP>& v, double* y) {
+  for (int m = threadIdx.x; m < v.N; m += blockDim.x) y[m] = 0.0;
+  __syncthreads();
+}
+
+// SSP-RK3 stage coefficients (IGR_adjoints_1d/forward.jl:61-79):
+// q_out = c0 q^n + c1 q_s + c2 dt k(q_s)
+__device__ __forceinline__ void rk1_coef(int s, double* c0, double* c1, double* c2) {
+  *c0 = s == 0 ? 0.0 : (s == 1 ? 0.75 : 1.0 / 3.0);
+  *c1 = s == 0 ? 1.0 : (s == 1 ? 0.25 : 2.0 / 3.0);
+  *c2 = *c1;
+}
+
+// Scratch fields of the forward (per instance, N doubles each)
+enum : int {
+  F1_Q1 = 0, F1_Q2 = 3, F1_IR0 = 6, F1_IR1 = 7, F1_IR2 = 8, F1_SA = 9, F1_B = 10, F1_CM = 11, F1_CK = 12,
+  F1_CINVM = 13, F1_CPR = 14, F1_W0 = 15, F1_W1 = 16, F1_W2 = 17, F1_W3 = 18, F1_FIELDS = 19
+};
+
+// Batch layout: instance i's state is the block q + 3 off_i = (mu, rho, E),
+// N_i doubles each, and its Sigma is sig + off_i.
+struct Fwd1DArgs {
+  const Inst1D* inst; const int* order; BasisDev B;
+  double* q;          // batch state, in place
+  double* sig;        // batch Sigma out
+  double* scr;        // scratch arena
+  int solver, n_iter, final_solve;
+  int* status;
+};
+
+// run_forward! (IGR_adjoints_1d/forward.jl:50-87) for one instance per CTA:
+// n_steps SSP-RK3 steps of size dt with the Sigma warm-start chain, then the
+// final solve at T when final_solve and alpha > 0.
+template <int NP>
+__global__ void __launch_bounds__(T1) k1_forward(Fwd1DArgs a) {
+  __shared__ double s_red[T1];
+  View1<NP> v;
+  v.I = a.inst[a.order[blockIdx.x]];
+  v.N = NP * v.I.ne;
+  v.scr = a.scr + v.I.soff;
+  const BasisDev& B = a.B;
+  const Inst1D& I = v.I;
+  const bool apos = I.alpha > 0;
+  double* q[3] = {a.q + 3 * I.off, a.q + 3 * I.off + v.N, a.q + 3 * I.off + 2 * v.N};
+  double* q1[3] = {v.f(F1_Q1), v.f(F1_Q1 + 1), v.f(F1_Q1 + 2)};
+  double* q2[3] = {v.f(F1_Q2), v.f(F1_Q2 + 1), v.f(F1_Q2 + 2)};
+  double* irs[3] = {v.f(F1_IR0), v.f(F1_IR1), v.f(F1_IR2)};
+  double* sig = a.sig + I.off;
+  double* Sx = sig;          // Sigma chain: current solution
+  double* Sy = v.f(F1_SA);   // the other buffer
+  const SolveTape1 none;
+  d1_zero(v, Sx);
+  d1_recip(v, q[1], irs[0]);
+  for (int step = 0; step < I.n_steps; ++step) {
+    for (int s = 0; s < 3; ++s) {
+      double* const* qs = s == 0 ? q : (s == 1 ? q1 : q2);
+      if (apos) {
+        d1_setup(v, B, qs[0], irs[s], v.f(F1_B), v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), nullptr);
+        d1_solve(v, B, a.solver, a.n_iter, v.f(F1_B), Sx, Sy, v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM),
+                 v.f(F1_W0), v.f(F1_W1), v.f(F1_W2), v.f(F1_W3), none, s_red);
+        double* t = Sx; Sx = Sy; Sy = t;
+      }
+      const double* qsc[3] = {qs[0], qs[1], qs[2]};
+      const double* qnc[3] = {q[0], q[1], q[2]};
+      double* const* qo = s == 0 ? q1 : (s == 1 ? q2 : q);
+      double c0, c1, c2;
+      rk1_coef(s, &c0, &c1, &c2);
+      d1_hyp_rk(v, B, qsc, irs[s], Sx, qnc, c0, c1, c2, qo, s < 2 ? irs[s + 1] : irs[0], nullptr, a.status);
+    }
+  }
+  if (apos && a.final_solve) {
+    d1_setup(v, B, q[0], irs[0], v.f(F1_B), v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), nullptr);
+    d1_solve(v, B, a.solver, a.n_iter, v.f(F1_B), Sx, Sy, v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), v.f(F1_W0),
+             v.f(F1_W1), v.f(F1_W2), v.f(F1_W3), none, s_red);
+    double* t = Sx; Sx = Sy; Sy = t;
+  }
+  if (Sx != sig) d1_copy(v, Sx, sig);
+}
+
+}  // namespace igrgpu

@@ -39,10 +39,13 @@ struct Inst2D {
   int tile0, ntiles;  // this instance's tiles in the tile list (contiguous)
 };
 
+// One 1D instance (IGR_adjoints_1d/mesh.jl:21-33): its nodes start at `off`
+// in every batch field; its private scratch (tapes, solver vectors) is
+// `scr_fields` arrays of NP*ne doubles starting at `soff` in the scratch arena.
 struct Inst1D {
-  long long off;
-  int ne, pad;
-  double dx, jac;
+  long long off, soff;
+  int ne, n_steps;
+  double L, dx, J, iJ, idx;  // dx = L / ne, J = dx / 2, iJ = 1/J, idx = 1/dx
   double gamma, alpha, dt;
 };
 

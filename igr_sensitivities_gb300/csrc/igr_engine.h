@@ -135,6 +135,32 @@ void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, do
 void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, const Solve2DOpts& o, int objective,
                const double* obj_params, double* J, double* const dq0[4], double* dgamma, double* dalpha);
 
+// ---- 1D ---------------------------------------------------------------------
+struct Inst1DDesc {
+  int ne;
+  double L, gamma, alpha, dt;
+  int n_steps;
+};
+// A batch of 1D instances. State layout on the device: instance i's block of
+// 3 N_i doubles (mu, rho, E) starts at 3 * inst[i].off; Sigma at inst[i].off.
+struct Plan1D {
+  BasisDev B;
+  int np = 4;
+  std::vector<Inst1D> inst;
+  std::vector<long long> inst_nodes;
+  std::vector<int> order;      // launch order (largest work first)
+  long long NG = 0;            // total nodes
+  long long scratch = 0;       // scratch doubles
+  Inst1D* d_inst = nullptr;
+  int* d_order = nullptr;
+};
+Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& insts, int scratch_fields,
+                   const std::string& tag);
+int forward1d_scratch_fields();
+// run_forward! (IGR_adjoints_1d/forward.jl:50-87) for every instance: n_steps
+// steps of size dt each (the caller re-rounds dt), final solve when asked.
+void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpts& o, bool final_solve);
+
 double probe_fp64_tflops(Ctx& c);
 // y = 1 / x elementwise on stream s (no bookkeeping).
 void launch_recip(const double* x, double* y, long long n, cudaStream_t s);

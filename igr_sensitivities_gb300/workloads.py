@@ -77,3 +77,39 @@ def max_wavespeed_2d(mux, muy, rho, E, gamma):
 def cfl_dt_2d(mesh, p, q, gamma, cfl):
     """dt = CFL min(dx, dy) / ((2p+1) max wavespeed) (IGR_adjoints_2d/tests/run_euler_test.jl:100-106)."""
     return cfl * min(mesh.dx, mesh.dy) / ((2 * p + 1) * max_wavespeed_2d(*q, gamma))
+
+
+# ----------------------------------------------------------------------------- 1D
+def pulse_ic_1d(mesh, gamma, amps, centers, width, p_bg=0.1):
+    """1D pressure pulses at rest: rho = 1, u = 0, p = p_bg + sum A exp(-(x-c)^2/width^2);
+    returns (mu, rho, E) shaped (n_p, N_e)."""
+    x = mesh.x
+    p = np.full(x.shape, p_bg)
+    for A, c in zip(amps, centers):
+        p = p + A * np.exp(-((x - c) ** 2) / width ** 2)
+    return (np.asfortranarray(np.zeros(x.shape)), np.asfortranarray(np.ones(x.shape)),
+            np.asfortranarray(p / (gamma - 1)))
+
+
+def seeded_pulses_1d(mesh, gamma, seed, n_pulses=2, width=0.02, amp=(1.0, 10.0), lo=0.2, hi=0.8):
+    rng = SplitMix64(seed)
+    amps = [rng.uniform(*amp) for _ in range(n_pulses)]
+    centers = [rng.uniform(lo, hi) for _ in range(n_pulses)]
+    return pulse_ic_1d(mesh, gamma, amps, centers, width)
+
+
+def seeded_interval(seed):
+    """Interval [a, b] for the interval_rho objective."""
+    rng = SplitMix64(seed ^ 0x2545F4914F6CDD1D)
+    a = rng.uniform(0.1, 0.6)
+    return (a, a + rng.uniform(0.1, 0.3))
+
+
+def max_wavespeed_1d(mu, rho, E, gamma):
+    P = (gamma - 1) * (E - mu ** 2 / (2 * rho))
+    return float(np.max(np.abs(mu / rho) + np.sqrt(gamma * P / rho)))
+
+
+def cfl_dt_1d(mesh, p, q, gamma, cfl):
+    """dt = CFL dx / ((2p+1) max wavespeed), the 1D form of the tests' CFL rule."""
+    return cfl * mesh.dx / ((2 * p + 1) * max_wavespeed_1d(*q, gamma))

@@ -68,6 +68,17 @@ typedef struct {
   const double* D;  /* (p+1)^2, column-major */
 } igr_disc2d;
 
+/* Discretisation of one 1D instance: DGBasis + PeriodicMesh1D
+ * (IGR_adjoints_1d/basis.jl, mesh.jl:7-33). */
+typedef struct {
+  int p;
+  int n_e;
+  double L;
+  const double* xi; /* p+1 */
+  const double* w;  /* p+1 */
+  const double* D;  /* (p+1)^2, column-major */
+} igr_disc1d;
+
 /* ---- context -------------------------------------------------------------- */
 int igr_ctx_create(int device, igr_ctx** out);
 int igr_ctx_destroy(igr_ctx* ctx);
@@ -166,6 +177,26 @@ int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_
  * looks up the array's address; make it before any stream capture. */
 int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const double* x_dev, const double* rho_dev,
                             double* y_dev, void* stream);
+
+/* ---- 1D ------------------------------------------------------------------- */
+
+/* run_forward! (IGR_adjoints_1d/forward.jl:50-87): in place, Sigma zeroed at
+ * entry, n_steps = ceil(T/dt), dt = T/n_steps, final solve at T when alpha > 0.
+ * State ordering (mu, rho, E) as IGR_adjoints_1d/euler.jl:23. */
+int igr1d_run_forward(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
+                      int n_iter, int solver, double* mu, double* rho, double* E, double* sigma);
+
+/* Batched 1D forward: n_inst instances sharing the basis (p, xi, w, D), each
+ * with its own n_e, L, gamma, alpha, dt and step count, advanced in one
+ * launch (one CTA per instance). Fixed steps (no dt re-rounding; callers that
+ * want run_forward! semantics pass n_steps = ceil(T/dt) and dt = T/n_steps).
+ * q is the concatenation over instances of (mu, rho, E), N_i = (p+1) n_e[i]
+ * doubles each, in place; sigma is the concatenation of Sigma (N_i each).
+ * final_solve != 0 adds the solve at the final state (forward.jl:83-85). */
+int igr1d_forward_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                        const int* n_e, const double* L, const double* gammas, const double* alphas,
+                        const double* dts, const int* n_steps, int n_iter, int solver, int final_solve, double* q,
+                        double* sigma);
 
 #ifdef __cplusplus
 }
