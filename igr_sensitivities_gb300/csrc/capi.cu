@@ -417,7 +417,7 @@ int igr1d_run_forward(igr_ctx* ctx, const igr_disc1d* d, double gamma, double al
     const int n_steps = (int)std::ceil(t_end / dt);  // IGR_adjoints_1d/forward.jl:58-59
     const double dtr = t_end / n_steps;
     BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
-    Plan1D P = make_plan1d(c, B, {Inst1DDesc{d->n_e, d->L, gamma, alpha, dtr, n_steps}}, forward1d_scratch_fields(), "f1");
+    Plan1D P = make_plan1d(c, B, {Inst1DDesc{d->n_e, d->L, gamma, alpha, dtr, n_steps}}, forward1d_scratch_fields, "f1");
     const long long N = P.NG;
     double* buf = c.ws.dbl("capi1:q", 4 * N);
     double* in[3] = {mu, rho, E};
@@ -443,7 +443,7 @@ int igr1d_forward_batch(igr_ctx* ctx, int p, const double* xi, const double* w, 
     BasisDev B = make_basis_dev(p, xi, w, D);
     std::vector<Inst1DDesc> insts;
     for (int i = 0; i < n_inst; ++i) insts.push_back(Inst1DDesc{n_e[i], L[i], gammas[i], alphas[i], dts[i], n_steps[i]});
-    Plan1D P = make_plan1d(c, B, insts, forward1d_scratch_fields(), "f1");
+    Plan1D P = make_plan1d(c, B, insts, forward1d_scratch_fields, "f1");
     const long long N = P.NG;
     double* buf = c.ws.dbl("capi1:qb", 4 * N);
     h2d(c, buf, q, 3 * N);
@@ -451,6 +451,108 @@ int igr1d_forward_batch(igr_ctx* ctx, int p, const double* xi, const double* w, 
     forward1d(c, P, buf, buf + 3 * N, o, final_solve != 0);
     d2h(c, q, buf, 3 * N);
     d2h(c, sigma, buf + 3 * N, N);
+    sync(c);
+  });
+}
+
+int igr1d_adjoint_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                        const int* n_e, const double* L, const double* gammas, const double* alphas,
+                        const double* dts, const int* n_steps, int n_iter, int solver, int objective,
+                        const double* obj_params, const double* q0, double* J, double* dq0, double* dgamma,
+                        double* dalpha) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc1(p, xi, w, D);
+    check_solver(solver, n_iter);
+    if (n_inst < 1 || !n_e || !L || !gammas || !alphas || !dts || !n_steps || !q0 || !J || !dq0)
+      throw Error(IGR_EINVAL, "bad batch arguments");
+    if (objective != 0 && objective != 1 && objective != 2 && objective != 4 && objective != 6)
+      throw Error(IGR_EINVAL, "Unknown objective");
+    if (objective == 6 && !obj_params) throw Error(IGR_EINVAL, "interval objective needs obj_params = {a, b}");
+    BasisDev B = make_basis_dev(p, xi, w, D);
+    std::vector<Inst1DDesc> insts;
+    for (int i = 0; i < n_inst; ++i) insts.push_back(Inst1DDesc{n_e[i], L[i], gammas[i], alphas[i], dts[i], n_steps[i]});
+    Solve2DOpts o{n_iter, solver};
+    size_t budget = c.tape_budget;
+    if (budget == 0) {
+      size_t fr = 0, tot = 0;
+      cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+      const size_t avail = fr + c.ws.held("a1:scr");
+      budget = avail > ((size_t)2 << 30) ? avail - ((size_t)2 << 30) : 0;
+    }
+    const int seg = adjoint1d_segment(insts, p + 1, o, budget);
+    Plan1D P = make_plan1d(c, B, insts,
+                           [&](const Inst1DDesc& d, int N) { return adjoint1d_scratch_fields(d, N, o, seg); }, "a1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:adj", 6 * N);
+    h2d(c, buf, q0, 3 * N);
+    adjoint1d(c, P, buf, buf + 3 * N, o, objective, obj_params, seg, J, dgamma, dalpha);
+    d2h(c, dq0, buf + 3 * N, 3 * N);
+    sync(c);
+  });
+}
+
+int igr1d_run_sensitivity(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
+                          int n_iter, int solver, int elliptic_rhs, double s_gamma, double* mu, double* rho, double* E,
+                          double* sigma, double* smu, double* srho, double* sE, double* ssigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!d) throw Error(IGR_EINVAL, "null discretisation");
+    check_disc1(d->p, d->xi, d->w, d->D);
+    check_solver(solver, n_iter);
+    if (elliptic_rhs != 1 && elliptic_rhs != 2) throw Error(IGR_EINVAL, "Unknown elliptic_rhs (use :form1 or :form2)");
+    if (d->n_e < 1 || !(d->L > 0)) throw Error(IGR_EINVAL, "bad mesh");
+    if (!(dt > 0) || !(t_end >= 0)) throw Error(IGR_EINVAL, "dt must be positive and T non-negative");
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    Inst1DDesc desc{d->n_e, d->L, gamma, alpha, dt, 0};
+    desc.t_end = t_end;
+    Plan1D P = make_plan1d(c, B, {desc}, tangent1d_scratch_fields, "t1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:tan", 8 * N);
+    double* qh[3] = {mu, rho, E};
+    double* sh[3] = {smu, srho, sE};
+    for (int v = 0; v < 3; ++v) { h2d(c, buf + v * N, qh[v], N); h2d(c, buf + (3 + v) * N, sh[v], N); }
+    Solve2DOpts o{n_iter, solver};
+    tangent1d(c, P, buf, buf + 3 * N, buf + 6 * N, buf + 7 * N, o, elliptic_rhs, s_gamma);
+    for (int v = 0; v < 3; ++v) { d2h(c, qh[v], buf + v * N, N); d2h(c, sh[v], buf + (3 + v) * N, N); }
+    d2h(c, sigma, buf + 6 * N, N);
+    d2h(c, ssigma, buf + 7 * N, N);
+    sync(c);
+  });
+}
+
+int igr1d_sensitivity_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                            const int* n_e, const double* L, const double* gammas, const double* alphas,
+                            const double* dts, const double* t_ends, int n_iter, int solver, int elliptic_rhs,
+                            const double* s_gammas, double* q, double* s, double* sigma, double* ssigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc1(p, xi, w, D);
+    check_solver(solver, n_iter);
+    if (n_inst < 1 || !n_e || !L || !gammas || !alphas || !dts || !t_ends || !q || !s || !sigma || !ssigma)
+      throw Error(IGR_EINVAL, "bad batch arguments");
+    if (s_gammas) {
+      for (int i = 1; i < n_inst; ++i)
+        if (s_gammas[i] != s_gammas[0]) throw Error(IGR_EINVAL, "s_gamma must be the same for every instance of a batch");
+    }
+    BasisDev B = make_basis_dev(p, xi, w, D);
+    std::vector<Inst1DDesc> insts;
+    for (int i = 0; i < n_inst; ++i) {
+      Inst1DDesc dsc{n_e[i], L[i], gammas[i], alphas[i], dts[i], 0};
+      dsc.t_end = t_ends[i];
+      insts.push_back(dsc);
+    }
+    Plan1D P = make_plan1d(c, B, insts, tangent1d_scratch_fields, "t1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:tanb", 8 * N);
+    h2d(c, buf, q, 3 * N);
+    h2d(c, buf + 3 * N, s, 3 * N);
+    Solve2DOpts o{n_iter, solver};
+    tangent1d(c, P, buf, buf + 3 * N, buf + 6 * N, buf + 7 * N, o, elliptic_rhs, s_gammas ? s_gammas[0] : 0.0);
+    d2h(c, q, buf, 3 * N);
+    d2h(c, s, buf + 3 * N, 3 * N);
+    d2h(c, sigma, buf + 6 * N, N);
+    d2h(c, ssigma, buf + 7 * N, N);
     sync(c);
   });
 }

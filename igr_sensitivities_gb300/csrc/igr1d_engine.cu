@@ -3,9 +3,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 
-#include "igr1d_kernels.cuh"
+#include "igr1d_launch.h"
+#include "igr1d_rev_kernels.cuh"
+#include "igr1d_sens_kernels.cuh"
 #include "igr_engine.h"
 
 namespace igrgpu {
@@ -19,8 +22,8 @@ namespace igrgpu {
     default: throw Error(1, "unsupported polynomial degree"); \
   }
 
-Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& insts, int scratch_fields,
-                   const std::string& tag) {
+Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& insts,
+                   const std::function<long long(const Inst1DDesc&, int)>& scratch_fields, const std::string& tag) {
   Plan1D P;
   P.B = B;
   P.np = B.np;
@@ -42,11 +45,12 @@ Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& ins
     I.iJ = 1.0 / I.J;
     I.idx = 1.0 / I.dx;
     I.gamma = d.gamma; I.alpha = d.alpha; I.dt = d.dt;
+    I.t_end = d.t_end;
     P.inst.push_back(I);
     const long long n = (long long)P.np * d.ne;
     P.inst_nodes.push_back(n);
     off += n;
-    soff += (long long)scratch_fields * n;
+    soff += scratch_fields(d, (int)n) * n;
     cost.push_back((double)n * std::max(d.n_steps, 1));
   }
   P.NG = off;
@@ -65,7 +69,7 @@ Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& ins
   return P;
 }
 
-int forward1d_scratch_fields() { return F1_FIELDS; }
+long long forward1d_scratch_fields(const Inst1DDesc&, int) { return F1_FIELDS; }
 
 void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpts& o, bool final_solve) {
   double* scr = c.ws.dbl("f1:scr", (size_t)std::max<long long>(P.scratch, 1));
@@ -78,9 +82,93 @@ void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpt
   a.status = c.d_status;
   {
     LaunchScope ls(c, KID_1D);
-    NP1_DISPATCH(P.np, (k1_forward<NPV><<<(int)P.inst.size(), T1, 0, c.stream>>>(a)));
+    NP1_DISPATCH(P.np, launch_k1_forward<NPV>(a, (int)P.inst.size(), c.stream));
   }
   cuda_check(cudaGetLastError(), "k1_forward launch");
+  int st = 0;
+  cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
+  cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
+  if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
+}
+
+int adjoint1d_segment(const std::vector<Inst1DDesc>& insts, int np, const Solve2DOpts& o, size_t budget) {
+  int nmax = 0;
+  for (auto& d : insts) nmax = std::max(nmax, d.n_steps);
+  if (nmax <= 1) return 1;
+  auto bytes = [&](int seg) {
+    long long t = 0;
+    for (auto& d : insts) {
+      const int N = np * d.ne;
+      t += adjoint1d_fields(o.solver, o.n_iter, N, d.n_steps, seg) * N;
+    }
+    return (size_t)t * sizeof(double);
+  };
+  // every step's state kept (one forward re-run) when it fits in half the
+  // budget, else sqrt(n)-long segments (two re-runs, O(sqrt n) snapshots)
+  if (bytes(nmax) <= budget / 2) return nmax;
+  const int s = (int)std::ceil(std::sqrt((double)nmax));
+  if (bytes(s) > budget) throw Error(5, "device memory too small for the 1D adjoint of this batch");
+  return s;
+}
+
+void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Solve2DOpts& o, int objective,
+               const double* prm, int seg, double* J, double* dgamma, double* dalpha) {
+  const int ni = (int)P.inst.size();
+  double* scr = c.ws.dbl("a1:scr", (size_t)std::max<long long>(P.scratch, 1));
+  double* outs = c.ws.dbl("a1:out", (size_t)3 * ni);
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  Adj1DArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.inst = P.d_inst; a.order = P.d_order; a.B = P.B;
+  a.q0 = q0; a.dq0 = dq0;
+  a.J = outs; a.dgamma = outs + ni; a.dalpha = outs + 2 * ni;
+  a.scr = scr;
+  a.solver = o.solver; a.n_iter = o.n_iter; a.objective = objective; a.seg = seg;
+  for (int k = 0; k < 4; ++k) a.prm[k] = prm ? prm[k] : 0.0;
+  a.status = c.d_status;
+  c.plan_seg = seg;
+  c.plan_groups = 1;
+  c.plan_group_size = ni;
+  {
+    LaunchScope ls(c, KID_1D);
+    NP1_DISPATCH(P.np, launch_k1_adjoint<NPV>(a, ni, c.stream));
+  }
+  cuda_check(cudaGetLastError(), "k1_adjoint launch");
+  std::vector<double> h(3 * ni);
+  int st = 0;
+  cuda_check(cudaMemcpyAsync(h.data(), outs, sizeof(double) * 3 * ni, cudaMemcpyDeviceToHost, c.stream), "readback");
+  cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
+  cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
+  if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
+  for (int i = 0; i < ni; ++i) {
+    J[i] = h[i];
+    if (dgamma) dgamma[i] = h[ni + i];
+    if (dalpha) dalpha[i] = h[2 * ni + i];
+  }
+}
+
+long long adjoint1d_scratch_fields(const Inst1DDesc& d, int N, const Solve2DOpts& o, int seg) {
+  return adjoint1d_fields(o.solver, o.n_iter, N, d.n_steps, seg);
+}
+
+long long tangent1d_scratch_fields(const Inst1DDesc&, int) { return T1_FIELDS; }
+
+void tangent1d(Ctx& c, const Plan1D& P, double* q, double* s, double* sig, double* vs, const Solve2DOpts& o, int form,
+               double s_gamma) {
+  if (form != 1 && form != 2) throw Error(1, "Unknown elliptic_rhs (use :form1 or :form2)");
+  double* scr = c.ws.dbl("t1:scr", (size_t)std::max<long long>(P.scratch, 1));
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  Tan1DArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.inst = P.d_inst; a.order = P.d_order; a.B = P.B;
+  a.q = q; a.s = s; a.sig = sig; a.vs = vs; a.scr = scr;
+  a.solver = o.solver; a.n_iter = o.n_iter; a.form = form; a.s_gamma = s_gamma;
+  a.status = c.d_status;
+  {
+    LaunchScope ls(c, KID_1D);
+    NP1_DISPATCH(P.np, launch_k1_tangent<NPV>(a, (int)P.inst.size(), c.stream));
+  }
+  cuda_check(cudaGetLastError(), "k1_tangent launch");
   int st = 0;
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");

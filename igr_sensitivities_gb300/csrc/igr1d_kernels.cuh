@@ -256,11 +256,11 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
 // ---------------------------------------------------------------------------
 template <int NP>
 __device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* const q[3], const double* ir,
-                          const double* S, const double* const qn[3], double c0, double c1, double c2,
+                          const double* S, const double* const qn[3], double c0, double c1, double c2, double dt,
                           double* const qo[3], double* iro, double* const kout[3], int* status) {
   constexpr int L = NP - 1;
   const Inst1D& I = v.I;
-  const double g = I.gamma, iJ = I.iJ, c2dt = c2 * I.dt;
+  const double g = I.gamma, iJ = I.iJ, c2dt = c2 * dt;
   bool bad = false;
   for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
     const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
@@ -356,11 +356,82 @@ __device__ __forceinline__ void rk1_coef(int s, double* c0, double* c1, double* 
   *c2 = *c1;
 }
 
-// Scratch fields of the forward (per instance, N doubles each)
+// Scratch fields of one untaped step (per instance, N doubles each)
 enum : int {
-  F1_Q1 = 0, F1_Q2 = 3, F1_IR0 = 6, F1_IR1 = 7, F1_IR2 = 8, F1_SA = 9, F1_B = 10, F1_CM = 11, F1_CK = 12,
-  F1_CINVM = 13, F1_CPR = 14, F1_W0 = 15, F1_W1 = 16, F1_W2 = 17, F1_W3 = 18, F1_FIELDS = 19
+  F1_Q1 = 0, F1_Q2 = 3, F1_IR1 = 6, F1_IR2 = 7, F1_B = 8, F1_CM = 9, F1_CK = 10, F1_CINVM = 11, F1_CPR = 12,
+  F1_W0 = 13, F1_W1 = 14, F1_W2 = 15, F1_W3 = 16, F1_STEP_FIELDS = 17
 };
+
+// Tape of one RK stage (adjoint): stage input, Sigma in/out, setup outputs
+// and the solver tape.
+struct StageTape1 {
+  double *q[3], *ir, *sin, *sout, *b, *cm, *ck, *cpR, *cinvM, *cM;
+  SolveTape1 st;
+};
+constexpr int STAGE1_FIELDS = 12;
+
+// Lay a stage tape over `fields` consecutive fields starting at base.
+template <int NP>
+__device__ StageTape1 stage_tape1(const View1<NP>& v, double* base, int solver, int n) {
+  StageTape1 t;
+  auto f = [&](int k) { return base + (long long)k * v.N; };
+  t.q[0] = f(0); t.q[1] = f(1); t.q[2] = f(2);
+  t.ir = f(3); t.sin = f(4); t.sout = f(5); t.b = f(6); t.cm = f(7); t.ck = f(8); t.cpR = f(9); t.cinvM = f(10); t.cM = f(11);
+  t.st.base = f(STAGE1_FIELDS); t.st.N = v.N; t.st.n = n; t.st.pcg = solver == 0 ? 1 : 0;
+  return t;
+}
+
+// One SSP-RK3 step of IGR_adjoints_1d/forward.jl:61-79 (compute_igr_euler_rhs!
+// per stage: Sigma solve with the warm-start chain, then the DG RHS).
+// q (3 fields) and ir = 1/rho are advanced in place; Sx is the current Sigma
+// (warm start in, solution out), Sy a spare buffer (the two may be swapped).
+// wk: F1_STEP_FIELDS work fields. tp: 3 stage tapes or null.
+template <int NP>
+__device__ void d1_step(const View1<NP>& v, const BasisDev& B, int solver, int n_iter, double* const q[3], double* ir,
+                        double*& Sx, double*& Sy, double* wk, StageTape1* tp, int* status, double* s_red) {
+  const Inst1D& I = v.I;
+  const bool apos = I.alpha > 0;
+  auto W = [&](int k) { return wk + (long long)k * v.N; };
+  double* q1[3] = {W(F1_Q1), W(F1_Q1 + 1), W(F1_Q1 + 2)};
+  double* q2[3] = {W(F1_Q2), W(F1_Q2 + 1), W(F1_Q2 + 2)};
+  double* irs[3] = {ir, W(F1_IR1), W(F1_IR2)};
+  const SolveTape1 none;
+  for (int s = 0; s < 3; ++s) {
+    double* const* qs = s == 0 ? q : (s == 1 ? q1 : q2);
+    StageTape1* t = tp ? &tp[s] : nullptr;
+    if (t) {
+      for (int m = threadIdx.x; m < v.N; m += blockDim.x) {
+        t->q[0][m] = qs[0][m]; t->q[1][m] = qs[1][m]; t->q[2][m] = qs[2][m];
+        t->ir[m] = irs[s][m]; t->sin[m] = Sx[m];
+      }
+      __syncthreads();
+    }
+    if (apos) {
+      double* b = t ? t->b : W(F1_B);
+      double* cm = t ? t->cm : W(F1_CM);
+      double* ck = t ? t->ck : W(F1_CK);
+      double* cpR = t ? t->cpR : W(F1_CPR);
+      double* ci = t ? t->cinvM : W(F1_CINVM);
+      d1_setup(v, B, qs[0], irs[s], b, cm, ck, cpR, ci, t ? t->cM : nullptr);
+      d1_solve(v, B, solver, n_iter, b, Sx, Sy, cm, ck, cpR, ci, W(F1_W0), W(F1_W1), W(F1_W2), W(F1_W3),
+               t ? t->st : none, s_red);
+      double* tmp = Sx; Sx = Sy; Sy = tmp;
+    }
+    if (t) {
+      for (int m = threadIdx.x; m < v.N; m += blockDim.x) t->sout[m] = Sx[m];
+      __syncthreads();
+    }
+    const double* qsc[3] = {qs[0], qs[1], qs[2]};
+    const double* qnc[3] = {q[0], q[1], q[2]};
+    double* const* qo = s == 0 ? q1 : (s == 1 ? q2 : q);
+    double c0, c1, c2;
+    rk1_coef(s, &c0, &c1, &c2);
+    d1_hyp_rk(v, B, qsc, irs[s], Sx, qnc, c0, c1, c2, I.dt, qo, s < 2 ? irs[s + 1] : irs[0], nullptr, status);
+  }
+}
+
+// Forward kernel scratch: the step work fields, 1/rho and the spare Sigma.
+enum : int { F1_IR0 = F1_STEP_FIELDS, F1_SA = F1_STEP_FIELDS + 1, F1_FIELDS = F1_STEP_FIELDS + 2 };
 
 // Batch layout: instance i's state is the block q + 3 off_i = (mu, rho, E),
 // N_i doubles each, and its Sigma is sig + off_i.
@@ -385,36 +456,17 @@ __global__ void __launch_bounds__(T1) k1_forward(Fwd1DArgs a) {
   v.scr = a.scr + v.I.soff;
   const BasisDev& B = a.B;
   const Inst1D& I = v.I;
-  const bool apos = I.alpha > 0;
   double* q[3] = {a.q + 3 * I.off, a.q + 3 * I.off + v.N, a.q + 3 * I.off + 2 * v.N};
-  double* q1[3] = {v.f(F1_Q1), v.f(F1_Q1 + 1), v.f(F1_Q1 + 2)};
-  double* q2[3] = {v.f(F1_Q2), v.f(F1_Q2 + 1), v.f(F1_Q2 + 2)};
-  double* irs[3] = {v.f(F1_IR0), v.f(F1_IR1), v.f(F1_IR2)};
+  double* ir = v.f(F1_IR0);
   double* sig = a.sig + I.off;
-  double* Sx = sig;          // Sigma chain: current solution
-  double* Sy = v.f(F1_SA);   // the other buffer
-  const SolveTape1 none;
+  double* Sx = sig;
+  double* Sy = v.f(F1_SA);
   d1_zero(v, Sx);
-  d1_recip(v, q[1], irs[0]);
-  for (int step = 0; step < I.n_steps; ++step) {
-    for (int s = 0; s < 3; ++s) {
-      double* const* qs = s == 0 ? q : (s == 1 ? q1 : q2);
-      if (apos) {
-        d1_setup(v, B, qs[0], irs[s], v.f(F1_B), v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), nullptr);
-        d1_solve(v, B, a.solver, a.n_iter, v.f(F1_B), Sx, Sy, v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM),
-                 v.f(F1_W0), v.f(F1_W1), v.f(F1_W2), v.f(F1_W3), none, s_red);
-        double* t = Sx; Sx = Sy; Sy = t;
-      }
-      const double* qsc[3] = {qs[0], qs[1], qs[2]};
-      const double* qnc[3] = {q[0], q[1], q[2]};
-      double* const* qo = s == 0 ? q1 : (s == 1 ? q2 : q);
-      double c0, c1, c2;
-      rk1_coef(s, &c0, &c1, &c2);
-      d1_hyp_rk(v, B, qsc, irs[s], Sx, qnc, c0, c1, c2, qo, s < 2 ? irs[s + 1] : irs[0], nullptr, a.status);
-    }
-  }
-  if (apos && a.final_solve) {
-    d1_setup(v, B, q[0], irs[0], v.f(F1_B), v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), nullptr);
+  d1_recip(v, q[1], ir);
+  for (int step = 0; step < I.n_steps; ++step) d1_step(v, B, a.solver, a.n_iter, q, ir, Sx, Sy, v.scr, nullptr, a.status, s_red);
+  if (I.alpha > 0 && a.final_solve) {
+    const SolveTape1 none;
+    d1_setup(v, B, q[0], ir, v.f(F1_B), v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), nullptr);
     d1_solve(v, B, a.solver, a.n_iter, v.f(F1_B), Sx, Sy, v.f(F1_CM), v.f(F1_CK), v.f(F1_CPR), v.f(F1_CINVM), v.f(F1_W0),
              v.f(F1_W1), v.f(F1_W2), v.f(F1_W3), none, s_red);
     double* t = Sx; Sx = Sy; Sy = t;

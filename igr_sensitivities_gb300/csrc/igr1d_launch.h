@@ -1,0 +1,16 @@
+// Host-side launchers of the 1D per-instance kernels, explicitly
+// instantiated for NP = 2..5 in igr1d_np<NP>.cu (compiled in parallel).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace igrgpu {
+
+struct Fwd1DArgs;
+struct Adj1DArgs;
+struct Tan1DArgs;
+
+template <int NP> void launch_k1_forward(const Fwd1DArgs& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k1_adjoint(const Adj1DArgs& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k1_tangent(const Tan1DArgs& a, int nblocks, cudaStream_t s);
+
+}  // namespace igrgpu

@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -140,6 +141,7 @@ struct Inst1DDesc {
   int ne;
   double L, gamma, alpha, dt;
   int n_steps;
+  double t_end = 0.0;  // tangent only: final time of the `while t < T` stepping
 };
 // A batch of 1D instances. State layout on the device: instance i's block of
 // 3 N_i doubles (mu, rho, E) starts at 3 * inst[i].off; Sigma at inst[i].off.
@@ -154,12 +156,27 @@ struct Plan1D {
   Inst1D* d_inst = nullptr;
   int* d_order = nullptr;
 };
-Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& insts, int scratch_fields,
-                   const std::string& tag);
-int forward1d_scratch_fields();
+// scratch_fields(desc, N): scratch fields (of N doubles) the instance needs.
+Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& insts,
+                   const std::function<long long(const Inst1DDesc&, int)>& scratch_fields, const std::string& tag);
+long long forward1d_scratch_fields(const Inst1DDesc& d, int N);
 // run_forward! (IGR_adjoints_1d/forward.jl:50-87) for every instance: n_steps
 // steps of size dt each (the caller re-rounds dt), final solve when asked.
 void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpts& o, bool final_solve);
+long long tangent1d_scratch_fields(const Inst1DDesc& d, int N);
+// run_sensitivity (IGR_adjoints_1d/sensitivity.jl:401-515) for every
+// instance: q and the tangent s in place, Sigma and varsigma out; form = 1 or 2
+// selects the tangent elliptic source; s_gamma the direct dP/dgamma source.
+void tangent1d(Ctx& c, const Plan1D& P, double* q, double* s, double* sig, double* vs, const Solve2DOpts& o, int form,
+               double s_gamma);
+// Snapshot segment length of the 1D adjoint for this batch within `budget` bytes.
+int adjoint1d_segment(const std::vector<Inst1DDesc>& insts, int np, const Solve2DOpts& o, size_t budget);
+long long adjoint1d_scratch_fields(const Inst1DDesc& d, int N, const Solve2DOpts& o, int seg);
+// Gradient of the objective after each instance's n_steps fixed steps
+// (enzyme_adjoint_ic, IGR_adjoints_1d/enzyme_adjoint.jl:267-314, in
+// conservative variables): J, dq0 (same layout as q0), dgamma, dalpha.
+void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Solve2DOpts& o, int objective,
+               const double* prm, int seg, double* J, double* dgamma, double* dalpha);
 
 double probe_fp64_tflops(Ctx& c);
 // y = 1 / x elementwise on stream s (no bookkeeping).

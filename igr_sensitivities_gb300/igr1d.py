@@ -12,7 +12,8 @@ import numpy as np
 from . import DGBasis, PeriodicMesh1D, _flat, _ptr, _solver
 from ._lib import check, default_context, lib
 
-__all__ = ["DGBasis", "PeriodicMesh1D", "run_forward", "run_forward_", "forward_batch"]
+__all__ = ["DGBasis", "PeriodicMesh1D", "run_forward", "run_forward_", "forward_batch", "run_sensitivity",
+           "enzyme_adjoint_ic", "enzyme_dJ_dA", "adjoint_batch", "IC_BUILDERS", "ic_dA_weights"]
 
 
 class _Disc1D(C.Structure):
@@ -83,3 +84,143 @@ def forward_batch(states, basis, n_e, L, gammas, alphas, dts, n_steps, n_iter=10
         o3 += 3 * n
         o1 += n
     return out
+
+
+# ----------------------------------------------------------------------------- initial conditions
+def _ic(rho_fn, u_fn, p_fn):
+    def build(mu0, rho0, E0, A, mesh_x, L, gamma):
+        s = np.sin(2 * np.pi * np.asarray(mesh_x) / L)
+        rho, u, p = rho_fn(A, s), u_fn(A, s), p_fn(A, s)
+        rho0[...] = rho
+        mu0[...] = rho * u
+        E0[...] = p / (gamma - 1) + 0.5 * rho * u ** 2
+    return build
+
+
+_one = lambda A, s: np.ones_like(s)
+_zero = lambda A, s: np.zeros_like(s)
+_pert = lambda A, s: 1 + A * s
+# IC_BUILDERS of IGR_adjoints_1d/initial_conditions.jl:218-224 (builders :94-204)
+IC_BUILDERS = {
+    "acoustic_pulse": (_ic(_pert, lambda A, s: A * s, _pert), "rho=1+A sin, u=A sin, p=1+A sin"),
+    "entropy_wave": (_ic(_pert, _one, _one), "rho=1+A sin, u=1, p=1"),
+    "density_pulse": (_ic(_pert, _zero, _one), "rho=1+A sin, u=0, p=1"),
+    "pressure_pulse": (_ic(_one, _zero, _pert), "rho=1, u=0, p=1+A sin"),
+    "velocity_pulse": (_ic(_one, lambda A, s: A * s, _one), "rho=1, u=A sin, p=1"),
+}
+
+
+def ic_dA_weights(ic_type):
+    """ic_dA_weights (initial_conditions.jl:232-246)."""
+    w = {"acoustic_pulse": (1.0, 1.0, 1.0), "entropy_wave": (1.0, 0.0, 0.0), "density_pulse": (1.0, 0.0, 0.0),
+         "pressure_pulse": (0.0, 0.0, 1.0), "velocity_pulse": (0.0, 1.0, 0.0)}
+    key = ic_type.lstrip(":")
+    if key not in w:
+        raise ValueError("Unknown IC type: %s" % ic_type)
+    return w[key]
+
+
+# ----------------------------------------------------------------------------- tangent
+def run_sensitivity(mu0, rho0, E0, smu0, srho0, sE0, dt, T, basis, mesh, gamma, alpha, n_iter=10, elliptic_rhs="form2",
+                    solver="pcg", s_gamma=0.0, ctx=None):
+    """run_sensitivity (IGR_adjoints_1d/sensitivity.jl:475-515): returns
+    (mu, rho, E, Sigma, smu, srho, sE, sSigma) at time T."""
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    form = {"form1": 1, "form2": 2}.get(str(elliptic_rhs).lstrip(":"))
+    if form is None:
+        raise ValueError("Unknown elliptic_rhs: %s (use :form1 or :form2)" % elliptic_rhs)
+    q = [_flat(a, n).copy() for a in (mu0, rho0, E0)]
+    s = [_flat(a, n).copy() for a in (smu0, srho0, sE0)]
+    S, V = np.zeros(n), np.zeros(n)
+    check(ctx, lib().igr1d_run_sensitivity(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(gamma),
+                                           C.c_double(alpha), C.c_double(dt), C.c_double(T), C.c_int(n_iter),
+                                           C.c_int(_solver(solver)), C.c_int(form), C.c_double(s_gamma),
+                                           *[_ptr(a) for a in q], _ptr(S), *[_ptr(a) for a in s], _ptr(V)))
+    r = lambda a: np.asfortranarray(a.reshape(shape, order="F"))
+    return tuple(r(a) for a in q) + (r(S),) + tuple(r(a) for a in s) + (r(V),)
+
+
+# ----------------------------------------------------------------------------- adjoint
+_OBJ1 = {"l2_density": 0, "l2_pressure": 1, "kinetic_energy": 2, "weighted_momentum": 4, "interval_rho": 6}
+
+
+def adjoint_batch(states, basis, n_e, L, gammas, alphas, dts, n_steps, n_iter=10, solver="pcg", objective="l2_density",
+                  obj_params=None, ctx=None):
+    """Batched discrete adjoint in conservative variables, one CTA per instance.
+
+    states: list of (mu0, rho0, E0) (flat Julia order). Returns
+    (J[n], [(dmu0, drho0, dE0)], dgamma[n], dalpha[n]).
+    """
+    ctx = ctx or default_context()
+    obj = objective.lstrip(":") if isinstance(objective, str) else objective
+    if isinstance(obj, str):
+        if obj not in _OBJ1:
+            raise ValueError("Unknown objective: %s" % objective)
+        obj = _OBJ1[obj]
+    n_e = np.ascontiguousarray(n_e, dtype=np.int32)
+    B = n_e.size
+    sizes = basis.n_p * n_e
+    q = np.concatenate([np.concatenate([_flat(x, int(sizes[i])) for x in states[i]]) for i in range(B)])
+    dq = np.zeros_like(q)
+    f64 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (B,)))
+    i32 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.int32), (B,)))
+    Ls, gs, als, dtv, ns = f64(L), f64(gammas), f64(alphas), f64(dts), i32(n_steps)
+    J, dg, da = np.zeros(B), np.zeros(B), np.zeros(B)
+    prm = np.zeros(4) if obj_params is None else np.ascontiguousarray(np.resize(np.asarray(obj_params, np.float64), 4))
+    IP = C.POINTER(C.c_int)
+    check(ctx, lib().igr1d_adjoint_batch(ctx.handle, C.c_int(basis.p), _ptr(basis.xi), _ptr(basis.w), _ptr(basis._Dcol),
+                                         C.c_int(B), n_e.ctypes.data_as(IP), _ptr(Ls), _ptr(gs), _ptr(als), _ptr(dtv),
+                                         ns.ctypes.data_as(IP), C.c_int(n_iter), C.c_int(_solver(solver)), C.c_int(obj),
+                                         _ptr(prm), _ptr(q), _ptr(J), _ptr(dq), _ptr(dg), _ptr(da)))
+    out, o3 = [], 0
+    for i in range(B):
+        n = int(sizes[i])
+        out.append((dq[o3:o3 + n], dq[o3 + n:o3 + 2 * n], dq[o3 + 2 * n:o3 + 3 * n]))
+        o3 += 3 * n
+    return J, out, dg, da
+
+
+def enzyme_adjoint_ic(A, p, N_e, L, gamma, alpha, CFL, T, n_iter=10, ic_type="acoustic_pulse", solver="pcg",
+                      objective="l2_density", ctx=None):
+    """enzyme_adjoint_ic (IGR_adjoints_1d/enzyme_adjoint.jl:267-314).
+
+    Builds the initial condition of family `ic_type` with amplitude A, runs
+    n_steps = ceil(T / dt) steps of dt = T / n_steps (dt from the CFL rule
+    CFL dx / ((2p+1) 2.5)), and returns (J, adj_rho, adj_u, adj_p): the
+    gradient of J with respect to the primitive initial state.
+    """
+    obj = objective.lstrip(":")
+    if obj not in ("l2_density", "l2_pressure"):
+        raise ValueError("Unknown objective: %s (use :l2_density or :l2_pressure)" % objective)
+    key = ic_type.lstrip(":")
+    if key not in IC_BUILDERS:
+        raise ValueError("Unknown IC type: %s" % ic_type)
+    basis = DGBasis(p)
+    mesh = PeriodicMesh1D(N_e, L, basis)
+    dt = CFL * mesh.dx / ((2 * p + 1) * 2.5)
+    n_steps = int(np.ceil(T / dt))
+    dt = T / n_steps
+    shape = (basis.n_p, N_e)
+    mu0, rho0, E0 = np.zeros(shape, order="F"), np.zeros(shape, order="F"), np.zeros(shape, order="F")
+    IC_BUILDERS[key][0](mu0, rho0, E0, A, mesh.x, L, gamma)
+    J, dq, _, _ = adjoint_batch([(mu0, rho0, E0)], basis, [N_e], L, gamma, alpha, dt, n_steps, n_iter=max(n_iter, 1),
+                                solver=solver, objective=obj, ctx=ctx)
+    dmu, drho, dE = (a.reshape(shape, order="F") for a in dq[0])
+    u0 = mu0 / rho0
+    adj_rho = drho + u0 * dmu + (u0 ** 2 / 2) * dE
+    adj_u = rho0 * dmu + rho0 * u0 * dE
+    adj_p = dE / (gamma - 1)
+    return J[0], adj_rho, adj_u, adj_p
+
+
+def enzyme_dJ_dA(A0, p, N_e, L, gamma, alpha, CFL, T, n_iter=10, ic_type="acoustic_pulse", solver="pcg", ctx=None):
+    """enzyme_dJ_dA (IGR_adjoints_1d/enzyme_adjoint.jl:232-248): (J, dJ/dA)."""
+    J, ar, au, ap = enzyme_adjoint_ic(A0, p, N_e, L, gamma, alpha, CFL, T, n_iter=n_iter, ic_type=ic_type, solver=solver,
+                                      ctx=ctx)
+    basis = DGBasis(p)
+    mesh = PeriodicMesh1D(N_e, L, basis)
+    wr, wu, wp = ic_dA_weights(ic_type)
+    s = np.sin(2 * np.pi * mesh.x / L)
+    return J, float(np.sum((wr * ar + wu * au + wp * ap) * s))

@@ -198,6 +198,44 @@ int igr1d_forward_batch(igr_ctx* ctx, int p, const double* xi, const double* w, 
                         const double* dts, const int* n_steps, int n_iter, int solver, int final_solve, double* q,
                         double* sigma);
 
+/* run_sensitivity (IGR_adjoints_1d/sensitivity.jl:475-515): the coupled primal
+ * + tangent SSP-RK3 to time T with the reference's stepping (`while t < T -
+ * 1e-14`, h = min(dt, T - t), no re-rounding), in place: (mu, rho, E) and the
+ * tangent (smu, srho, sE) on entry are the initial state and direction; on
+ * exit both are at T with sigma = Sigma(T) and ssigma its tangent.
+ * elliptic_rhs: 1 = :form1, 2 = :form2 (sensitivity.jl:168-314). s_gamma: the
+ * direct dP/dgamma source (sensitivity.jl:36-48). The reference's optional
+ * per-step callback has no counterpart. */
+int igr1d_run_sensitivity(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
+                          int n_iter, int solver, int elliptic_rhs, double s_gamma, double* mu, double* rho, double* E,
+                          double* sigma, double* smu, double* srho, double* sE, double* ssigma);
+
+/* Batched run_sensitivity: per-instance n_e, L, gamma, alpha, dt, T; one
+ * s_gamma for the batch (s_gammas may be NULL = 0; all entries must be equal).
+ * q and s: concatenations of (mu, rho, E) / (smu, srho, sE) per instance as in
+ * igr1d_forward_batch; sigma, ssigma: N_i each. */
+int igr1d_sensitivity_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                            const int* n_e, const double* L, const double* gammas, const double* alphas,
+                            const double* dts, const double* t_ends, int n_iter, int solver, int elliptic_rhs,
+                            const double* s_gammas, double* q, double* s, double* sigma, double* ssigma);
+
+/* Batched 1D discrete adjoint: for each instance, J and dJ/d(mu0, rho0, E0)
+ * (conservative variables) of the objective after n_steps[i] fixed SSP-RK3
+ * steps of size dts[i] from q0 (layout as igr1d_forward_batch), plus
+ * dJ/dgamma and dJ/dalpha (may be NULL). The gradient enzyme_adjoint_ic
+ * returns (IGR_adjoints_1d/enzyme_adjoint.jl:267-314) before its
+ * conservative-to-primitive transform, which the host-side mirror applies.
+ * Objectives: IGR_OBJ_L2_DENSITY, _L2_PRESSURE, _KINETIC_ENERGY,
+ * _WEIGHTED_MOMENTUM (enzyme_adjoint.jl:34-215) and IGR_OBJ_INTERVAL_RHO
+ * (obj_params = {a, b}). One CTA per instance; the step history is kept as
+ * snapshots (all steps, or sqrt(n)-step segments when memory is short) and
+ * every step is re-run with full stage tapes before its reverse. */
+int igr1d_adjoint_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                        const int* n_e, const double* L, const double* gammas, const double* alphas,
+                        const double* dts, const int* n_steps, int n_iter, int solver, int objective,
+                        const double* obj_params, const double* q0, double* J, double* dq0, double* dgamma,
+                        double* dalpha);
+
 #ifdef __cplusplus
 }
 #endif
