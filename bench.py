@@ -34,14 +34,34 @@ P, NE, N_STEPS, N_ITER, SOLVER, OBJ = 3, 128, 200, 5, "chebyshev", "window_rho2"
 GAMMA = 1.4
 METRIC = "2D P3 128² adjoint gradients/s: batched vs plain, same GPU, rel err ≤1e-9"
 
-# FP64 operations per node executed by each kernel family (FMA = 2), P3,
-# counted from the kernels' instruction mix (ncu FP64 instruction counts of
-# one launch divided by nodes; see profiles/). Used for the live roofline.
-FLOPS_PER_NODE = {0: 110.0, 1: 56.0, 2: 230.0, 3: 330.0, 4: 110.0, 5: 150.0}
-# FP64 bytes moved per node per launch by each family (reads + writes of
-# whole fields, halo re-reads excluded), for the HBM fraction.
-BYTES_PER_NODE = {0: 8 * 13, 1: 8 * 15, 2: 8 * 19, 3: 8 * 27, 4: 8 * 22, 5: 8 * 17}
+# FP64 flops per node executed by each kernel family, P3, Chebyshev epilogues:
+# (2 DFMA + DADD + DMUL) of one ncu capture divided by the launch's nodes
+# (profiles/adjoint2d_kernels_128.md). Used for the live roofline.
+FLOPS_PER_NODE = {0: 86.0, 1: 47.8, 2: 163.0, 3: 233.9, 4: 81.2, 5: 136.9}
+# Algorithmic FP64 bytes per node per launch: one read of every live field and
+# one write of every output field (halo re-reads excluded), for the HBM fraction.
+BYTES_PER_NODE = {0: 8 * 11, 1: 8 * 13, 2: 8 * 17, 3: 8 * 35, 4: 8 * 23, 5: 8 * 19}
+# DRAM bytes per node of one launch of each family, measured with ncu on an
+# 8-instance case whose fields exceed L2 (profiles/adjoint2d_kernels_128.md);
+# scaled by the launch's node count for `roofline.traffic`.
+TRAFFIC_PER_NODE = {0: 61.9, 1: 91.6, 2: 105.6, 3: 209.4, 4: 167.4, 5: 141.2}
 FAMILY = {0: "k2_setup", 1: "k2_apply", 2: "k2_hyp_rk", 3: "k2_hyp_rev", 4: "k2_apply_rev", 5: "k2_setup_rev"}
+
+
+def instance_seeds(rank, B):
+    """Seeds of the B instances rank `rank` runs: ranks shard the instance
+    stream with no overlap (weak scaling, no data exchange)."""
+    return [rank * B + b for b in range(B)]
+
+
+def max_over_ranks(t, dist=None, device=None):
+    """Slowest rank's elapsed time (the job's time); identity on one rank."""
+    if dist is None:
+        return t
+    import torch
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
 
 
 def make_batch(igr, W, B, first=0):
@@ -127,7 +147,7 @@ def reference_arm(args):
         return
     threads = os.cpu_count() or 1
     B_cpu = threads
-    n_sample = 1
+    n_sample = 2
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(B_cpu, n_sample, threads)
@@ -156,6 +176,111 @@ def config_dict(B):
             "l2": "inputs and tape far larger than L2 (no flush needed)", "parallelism": "instances per GPU (no exchange)"}
 
 
+def secondary(args):
+    """Other BASELINE configurations, timed the same way (one JSON line each,
+    not the headline): forward2d_pcg (2D 128^2 P3, PCG 60, 500 steps),
+    forward1d (1D N_e = 256 P3, Jacobi 50, T = 0.1) and batch1d (1024 1D
+    instances, N_e in {64..1024}, PCG 102, forward + adjoint; a bounded
+    sample of the 2000 steps, scaled)."""
+    import torch
+    import igr_sensitivities_gb300 as igr
+    from igr_sensitivities_gb300 import igr1d, workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    ctx = igr.Context(0)
+    threads = os.cpu_count() or 1
+    flat = lambda a: np.ascontiguousarray(np.asarray(a).reshape(-1, order="F"))
+    line = {"impl": "gb300", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic (seeded Gaussian pressure pulses)", "vs_baseline": None}
+    if args.workload == "forward2d_pcg":
+        basis = igr.DGBasis(3)
+        mesh = igr.CartesianMesh2D(128, 128, 1.0, 1.0, basis)
+        q0 = W.seeded_pulses_2d(mesh, GAMMA, W.seed_for(2, 0), n_pulses=3, width=0.03)
+        dt = W.cfl_dt_2d(mesh, 3, q0, GAMMA, 0.1)
+        alpha, nst = 3.0 / 128 ** 2, 500
+        T = nst * dt * 0.999
+        run = lambda: igr.run_forward(*q0, dt, T, basis, mesh, GAMMA, alpha, n_iter=60, solver="pcg", ctx=ctx)
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        t = (time.perf_counter() - t0) / args.steps
+        G = O.Grid2D(3, 128, 128)
+        ns = 2
+        tc0 = time.perf_counter()
+        O.run_forward_2d(G, GAMMA, alpha, dt, ns * dt * 0.999, 60, "pcg", [flat(a) for a in q0])
+        tc = (time.perf_counter() - tc0) * nst / ns
+        line.update(metric="2D P3 128^2 PCG-60 forward solves/s (500 SSP-RK3 steps)", value=1.0 / t,
+                    unit="solves/s", ms_per_step=t * 1e3, gpu_launches=ctx.last_launch_count(),
+                    config={"workload": "2D IGR-Euler forward, P3 128x128, PCG 60 iters/stage, 500 steps", "mesh": "128x128"},
+                    cpu_baseline={"value": 1.0 / tc, "unit": "solves/s", "cores": 1, "kind": "port",
+                                  "sample": "%d of %d steps, single thread, scaled" % (ns, nst)})
+    elif args.workload == "forward1d":
+        basis = igr.DGBasis(3)
+        mesh = igr.PeriodicMesh1D(256, 1.0, basis)
+        q0 = W.seeded_pulses_1d(mesh, GAMMA, W.seed_for(1, 0), n_pulses=2, width=0.02)
+        dt = W.cfl_dt_1d(mesh, 3, q0, GAMMA, 0.1)
+        alpha, T = 3.0 * mesh.dx ** 2, 0.1
+        run = lambda: igr1d.run_forward(*q0, dt, T, basis, mesh, GAMMA, alpha, n_iter=50, solver="jacobi", ctx=ctx)
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        t = (time.perf_counter() - t0) / args.steps
+        G = O.Grid1D(3, 256)
+        nst = int(np.ceil(T / dt))
+        Ts = 0.005
+        tc0 = time.perf_counter()
+        O.run_forward_1d(G, GAMMA, alpha, dt, Ts, 50, "jacobi", [flat(a) for a in q0])
+        tc = (time.perf_counter() - tc0) * T / Ts
+        line.update(metric="1D P3 N_e=256 Jacobi-50 forward solves/s (T = 0.1)", value=1.0 / t, unit="solves/s",
+                    ms_per_step=t * 1e3, config={"workload": "1D IGR-Euler forward, N_e=256 P3, Jacobi 50, T=0.1",
+                                                 "n_steps": nst},
+                    cpu_baseline={"value": 1.0 / tc, "unit": "solves/s", "cores": 1, "kind": "port",
+                                  "sample": "T = %.3f of %.1f, single thread, scaled" % (Ts, T)})
+    elif args.workload == "batch1d":
+        basis = igr.DGBasis(3)
+        rng = W.SplitMix64(W.seed_for(4, 0xB))
+        nes = [64 * 2 ** int(rng.uniform(0, 5)) for _ in range(1024)]
+        gs = [rng.uniform(1.2, 1.8) for _ in range(1024)]
+        states, dts, als = [], [], []
+        for i, ne in enumerate(nes):
+            mesh = igr.PeriodicMesh1D(ne, 1.0, basis)
+            q0 = W.seeded_pulses_1d(mesh, gs[i], W.seed_for(4, i), n_pulses=2, width=0.02)
+            states.append(tuple(flat(a) for a in q0))
+            dts.append(W.cfl_dt_1d(mesh, 3, q0, gs[i], 0.1))
+            als.append(3.0 * mesh.dx ** 2)
+        ns, nfull = args.n_steps if args.n_steps != N_STEPS else 10, 2000
+        prm = W.seeded_interval(W.seed_for(4, 0))
+        run = lambda: igr1d.adjoint_batch(states, basis, nes, 1.0, gs, als, dts, ns, n_iter=102, solver="pcg",
+                                          objective="interval_rho", obj_params=prm, ctx=ctx)
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        t = (time.perf_counter() - t0) / args.steps
+        # CPU: the oracle's 1D adjoint on two instances of each size for 2 steps, single thread
+        tc = 0.0
+        for ne in (64, 128, 256, 512, 1024):
+            G = O.Grid1D(3, ne)
+            i = nes.index(ne)
+            tc0 = time.perf_counter()
+            O.adjoint_1d(G, gs[i], als[i], 2, dts[i], 102, "pcg", "interval_rho", list(states[i]), prm)
+            tc += (time.perf_counter() - tc0) * nes.count(ne) * nfull / 2
+        line.update(metric="1D batch of 1024 (N_e in {64..1024}, P3, PCG 102) forward+adjoint gradients/s",
+                    value=1024 * ns / nfull / t, unit="gradients/s (2000-step equivalents)", ms_per_step=t * 1e3,
+                    config={"workload": "1024 1D instances, N_e ~ U{64..1024}, gamma ~ U[1.2,1.8], PCG 102, "
+                                        "interval rho objective", "sample_steps": ns, "full_steps": nfull},
+                    cpu_baseline={"value": 1024 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
+                                  "sample": "one instance per N_e for 2 steps, scaled by counts and to 2000 steps"})
+    else:
+        raise SystemExit("unknown workload " + args.workload)
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -166,11 +291,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
+    ap.add_argument("--workload", default="adjoint2d",
+                    help="adjoint2d (the headline) | forward2d_pcg | forward1d | batch1d")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload != "adjoint2d":
+        return secondary(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -187,17 +316,19 @@ def main():
 
     ctx = igr.Context(local)
     if args.profile_case:
-        basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, 2)
+        # one instance group of the metric workload (8 instances: fields of 16.8 MB, the
+        # per-kernel working set well above L2) for 2 steps, called twice
+        basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, 8)
         q0d = torch.from_numpy(q0h).to(torch.device("cuda", local))
         for _ in range(2):
-            igr.adjoint_batch(q0d, gam, alp, dts, 4, basis, mesh, n_iter=N_ITER, solver=SOLVER, objective=OBJ,
+            igr.adjoint_batch(q0d, gam, alp, dts, 2, basis, mesh, n_iter=N_ITER, solver=SOLVER, objective=OBJ,
                               obj_params=prm, ctx=ctx, device_arrays=True)
         torch.cuda.synchronize()
         print("profile case done")
         return
     n_steps = args.n_steps
     B = args.batch
-    basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, B, first=rank * B)
+    basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, B, first=instance_seeds(rank, B)[0])
     dev = torch.device("cuda", local)
     q0d = torch.from_numpy(q0h).to(dev)
 
@@ -243,11 +374,7 @@ def main():
         lib.igr_profile_read(ctx.handle, k, C.byref(ms), C.byref(cnt))
         lib.igr_profile_nodes(ctx.handle, k, C.byref(nn))
         fam[k] = (ms.value, cnt.value, nn.value)
-    tmax = t
-    if dist is not None:
-        tt = torch.tensor([t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tmax = float(tt.item())
+    tmax = max_over_ranks(t, dist, dev)
     value = B * world * args.steps / tmax
 
     # end to end: host buffers through the C ABI
@@ -295,8 +422,10 @@ def main():
         hbm_peak, hbm_src = float(peaks["hbm_gbs"]), "measured"
     except Exception:
         hbm_peak, hbm_src = 6800.0, "fallback"
+    traffic = TRAFFIC_PER_NODE[dom] * nodes if dom in TRAFFIC_PER_NODE else None
     roofline = {"bound": "fp64", "kernel": FAMILY[dom], "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
+                "traffic_note": "DRAM bytes per launch (ncu, 8-instance case scaled by nodes)",
                 "peak_source": "measured live (DFMA-chain probe in libigr_gb300.so)",
                 "ms_per_launch": ms_launch, "flops_per_launch": flops, "nodes_per_launch": nodes,
                 "all_kernels_fp64_tflops": all_flops / (all_ms * 1e-3) / 1e12 if all_ms else None,
@@ -316,10 +445,11 @@ def main():
             "gpu_launches": launches, "roofline": roofline, "clocks": clocks}
     if not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
-        v, tcpu = cpu_baseline(threads, 1, threads)
+        n_sample = 5
+        v, tcpu = cpu_baseline(threads, n_sample, threads)
         line["cpu_baseline"] = {"value": v, "unit": "gradients/s", "cores": threads, "kind": "port",
-                                "sample": "%d instances x 1 of %d steps (OpenMP over instances, %.1f s), scaled to full "
-                                          "gradients" % (threads, N_STEPS, tcpu)}
+                                "sample": "%d instances x %d of %d steps (OpenMP over instances, %.1f s), scaled to full "
+                                          "gradients" % (threads, n_sample, N_STEPS, tcpu)}
     print(json.dumps(line))
 
 
