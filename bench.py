@@ -254,6 +254,12 @@ def secondary(args):
             als.append(3.0 * mesh.dx ** 2)
         ns, nfull = args.n_steps if args.n_steps != N_STEPS else 10, 2000
         prm = W.seeded_interval(W.seed_for(4, 0))
+        if args.profile_case:  # the first 152 instances for 2 steps, once (ncu captures; ~2 GB on the device)
+            k = 152
+            igr1d.adjoint_batch(states[:k], basis, nes[:k], 1.0, gs[:k], als[:k], dts[:k], 2, n_iter=102, solver="pcg",
+                                objective="interval_rho", obj_params=prm, ctx=ctx)
+            print("profile case done")
+            return
         run = lambda: igr1d.adjoint_batch(states, basis, nes, 1.0, gs, als, dts, ns, n_iter=102, solver="pcg",
                                           objective="interval_rho", obj_params=prm, ctx=ctx)
         for _ in range(args.warmup):

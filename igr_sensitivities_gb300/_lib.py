@@ -68,6 +68,15 @@ class Context:
         check(self, lib().igr_last_launch_count(self.handle, C.byref(n)))
         return n.value
 
+    def set_cluster_size_1d(self, cs):
+        """1D: CTAs per instance (0 = automatic; 1, 2, 4, 8, 16)."""
+        check(self, lib().igr_set_cluster_size_1d(self.handle, C.c_int(int(cs))))
+
+    def last_cluster_size_1d(self):
+        v = C.c_int(0)
+        check(self, lib().igr_last_cluster_size_1d(self.handle, C.byref(v)))
+        return v.value
+
     def last_adjoint_plan(self):
         """Memory plan of the last adjoint call: instance groups, instances per
         group, steps taped per segment and segments (recomputed from checkpoints)."""

@@ -106,6 +106,18 @@ int igr_set_tape_budget(igr_ctx* ctx, size_t bytes) {
   return IGR_OK;
 }
 
+int igr_set_cluster_size_1d(igr_ctx* ctx, int cs) {
+  if (!ctx || cs < 0 || cs > 16 || (cs & (cs - 1)) != 0) return IGR_EINVAL;
+  ctx->c.cluster1d = cs;
+  return IGR_OK;
+}
+
+int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out) {
+  if (!ctx || !out) return IGR_EINVAL;
+  *out = ctx->c.last_cluster1d;
+  return IGR_OK;
+}
+
 int igr_last_launch_count(const igr_ctx* ctx, long long* out) {
   if (!ctx || !out) return IGR_EINVAL;
   *out = ctx->c.launches;

@@ -69,7 +69,40 @@ Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& ins
   return P;
 }
 
-long long forward1d_scratch_fields(const Inst1DDesc&, int) { return F1_FIELDS; }
+long long forward1d_scratch_fields(const Inst1DDesc&, int) { return E1_FIELDS + F1_FIELDS; }
+
+// CTAs per instance. Results do not depend on it (fixed-order reductions), so
+// it is chosen for speed: small batches spread each instance over a cluster of
+// up to 16 SMs (at least 4 elements per CTA); batches that fill the GPU use one
+// CTA per instance. A context setting overrides the choice.
+static int cluster_size(Ctx& c, const Plan1D& P) {
+  if (c.cluster1d > 0) return c.cluster1d;
+  int sms = 0;
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device), "attr");
+  const long long ni = (long long)P.inst.size();
+  int min_ne = 1 << 30;
+  for (auto& I : P.inst) min_ne = std::min(min_ne, I.ne);
+  int cs = 1;
+  while (cs < 16 && ni * cs * 2 * 2 <= sms && min_ne / (cs * 2) >= 4) cs *= 2;
+  return cs;
+}
+
+// Launch with the chosen cluster size, falling back to smaller clusters when
+// the device refuses one (results are identical for every size).
+template <class Args, class F>
+static void launch_1d(Ctx& c, Args& a, int n_inst, F launch, const char* what) {
+  for (;;) {
+    cudaError_t e;
+    {
+      LaunchScope ls(c, KID_1D);
+      e = launch(a, n_inst);
+    }
+    if (e == cudaSuccess) { c.last_cluster1d = a.cs; return; }
+    if (a.cs <= 1) cuda_check(e, what);
+    (void)cudaGetLastError();  // clear the refused launch
+    a.cs /= 2;
+  }
+}
 
 void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpts& o, bool final_solve) {
   double* scr = c.ws.dbl("f1:scr", (size_t)std::max<long long>(P.scratch, 1));
@@ -80,11 +113,10 @@ void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpt
   a.q = q; a.sig = sig; a.scr = scr;
   a.solver = o.solver; a.n_iter = o.n_iter; a.final_solve = final_solve ? 1 : 0;
   a.status = c.d_status;
-  {
-    LaunchScope ls(c, KID_1D);
-    NP1_DISPATCH(P.np, launch_k1_forward<NPV>(a, (int)P.inst.size(), c.stream));
-  }
-  cuda_check(cudaGetLastError(), "k1_forward launch");
+  a.cs = cluster_size(c, P);
+  NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
+                               [&](const Fwd1DArgs& x, int n) { return launch_k1_forward<NPV>(x, n, c.stream); },
+                               "k1_forward launch"));
   int st = 0;
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
@@ -99,7 +131,7 @@ int adjoint1d_segment(const std::vector<Inst1DDesc>& insts, int np, const Solve2
     long long t = 0;
     for (auto& d : insts) {
       const int N = np * d.ne;
-      t += adjoint1d_fields(o.solver, o.n_iter, N, d.n_steps, seg) * N;
+      t += (E1_FIELDS + adjoint1d_fields(o.solver, o.n_iter, N, d.n_steps, seg)) * N;
     }
     return (size_t)t * sizeof(double);
   };
@@ -129,11 +161,10 @@ void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Sol
   c.plan_seg = seg;
   c.plan_groups = 1;
   c.plan_group_size = ni;
-  {
-    LaunchScope ls(c, KID_1D);
-    NP1_DISPATCH(P.np, launch_k1_adjoint<NPV>(a, ni, c.stream));
-  }
-  cuda_check(cudaGetLastError(), "k1_adjoint launch");
+  a.cs = cluster_size(c, P);
+  NP1_DISPATCH(P.np, launch_1d(c, a, ni,
+                               [&](const Adj1DArgs& x, int n) { return launch_k1_adjoint<NPV>(x, n, c.stream); },
+                               "k1_adjoint launch"));
   std::vector<double> h(3 * ni);
   int st = 0;
   cuda_check(cudaMemcpyAsync(h.data(), outs, sizeof(double) * 3 * ni, cudaMemcpyDeviceToHost, c.stream), "readback");
@@ -148,10 +179,10 @@ void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Sol
 }
 
 long long adjoint1d_scratch_fields(const Inst1DDesc& d, int N, const Solve2DOpts& o, int seg) {
-  return adjoint1d_fields(o.solver, o.n_iter, N, d.n_steps, seg);
+  return E1_FIELDS + adjoint1d_fields(o.solver, o.n_iter, N, d.n_steps, seg);
 }
 
-long long tangent1d_scratch_fields(const Inst1DDesc&, int) { return T1_FIELDS; }
+long long tangent1d_scratch_fields(const Inst1DDesc&, int) { return E1_FIELDS + T1_FIELDS; }
 
 void tangent1d(Ctx& c, const Plan1D& P, double* q, double* s, double* sig, double* vs, const Solve2DOpts& o, int form,
                double s_gamma) {
@@ -164,11 +195,10 @@ void tangent1d(Ctx& c, const Plan1D& P, double* q, double* s, double* sig, doubl
   a.q = q; a.s = s; a.sig = sig; a.vs = vs; a.scr = scr;
   a.solver = o.solver; a.n_iter = o.n_iter; a.form = form; a.s_gamma = s_gamma;
   a.status = c.d_status;
-  {
-    LaunchScope ls(c, KID_1D);
-    NP1_DISPATCH(P.np, launch_k1_tangent<NPV>(a, (int)P.inst.size(), c.stream));
-  }
-  cuda_check(cudaGetLastError(), "k1_tangent launch");
+  a.cs = cluster_size(c, P);
+  NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
+                               [&](const Tan1DArgs& x, int n) { return launch_k1_tangent<NPV>(x, n, c.stream); },
+                               "k1_tangent launch"));
   int st = 0;
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");

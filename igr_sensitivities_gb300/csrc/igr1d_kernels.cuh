@@ -4,7 +4,7 @@
 // A 1D instance is small (N_e <= a few thousand elements, 4 nodes each at
 // P3), so instead of one launch per operator application (whose launch
 // latency would dominate) each CTA advances its own instance through every
-// RK stage, solver iteration and step, with __syncthreads() between phases
+// RK stage, solver iteration and step, with barriers between phases
 // and deterministic block reductions for the solver inner products. A batch
 // of instances with different N_e, gamma, alpha, dt and step counts is one
 // launch; instances are independent, so no grid-wide synchronisation exists.
@@ -14,20 +14,72 @@
 // neighbouring elements' nodes (L1/L2 resident: an instance's fields are a
 // few tens of KB). Node order is the reference's Julia (n_p, N_e) layout.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "igr2d_kernels.cuh"  // line contractions dot_row / dot_end / dot_col
 
 namespace igrgpu {
 
 constexpr int T1 = 256;  // threads per 1D CTA (power of two: block_sum scratch size)
+constexpr int E1_FIELDS = 2;  // per-element work at the start of an instance's scratch
 
-// Per-CTA view of one instance.
+// Per-CTA view of one instance. An instance is advanced by `cs` CTAs (a
+// thread-block cluster when cs > 1, so that one small instance can use up to
+// 16 SMs); CTA rank r owns elements [e0, e1). Phases end with sync() (a CTA
+// or cluster barrier, release/acquire). Inner products are reduced from
+// per-element partials in one fixed order that does not depend on cs, so a
+// result is bitwise the same whatever the cluster size.
 template <int NP>
 struct View1 {
   Inst1D I;
   int N;          // nodes
   double* scr;    // this instance's scratch (fields of N doubles)
+  double* ew;     // per-element work: 2 ne reduction slots, ne d/dgamma, ne d/dalpha accumulators
+  int e0, e1, cs;
+  mutable int flip;
   __device__ double* f(int k) const { return scr + (long long)k * N; }
+  __device__ int m0() const { return e0 * NP; }
+  __device__ int m1() const { return e1 * NP; }
+  __device__ double* slot() const { return ew + (flip & 1) * I.ne; }
+  __device__ double* gbe() const { return ew + 2 * I.ne; }
+  __device__ double* abe() const { return ew + 3 * I.ne; }
+  __device__ void sync() const {
+    if (cs > 1) cooperative_groups::this_cluster().sync();
+    else __syncthreads();
+  }
+  // Sum of per-element values pe[0..ne) written before the call (by any CTA
+  // of the instance); every CTA returns the same value.
+  __device__ double esum(const double* pe, double* s_red) const {
+    sync();
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < I.ne; e += T1) acc += pe[e];
+    return block_sum<T1>(acc, s_red);
+  }
+  // esum of the current slot, then switch slots (ping-pong: between two uses
+  // of one slot there is always another reduction's barrier).
+  __device__ double reduce(double* s_red) const {
+    const double t = esum(slot(), s_red);
+    flip ^= 1;
+    return t;
+  }
 };
+
+// Set up the view of CTA blockIdx.x: instance order[blockIdx.x / cs].
+template <int NP>
+__device__ __forceinline__ View1<NP> make_view1(const Inst1D* inst, const int* order, double* scr_base, int cs, int* idx) {
+  View1<NP> v;
+  const int rank = blockIdx.x % cs;
+  *idx = order[blockIdx.x / cs];
+  v.I = inst[*idx];
+  v.N = NP * v.I.ne;
+  v.ew = scr_base + v.I.soff;
+  v.scr = v.ew + (long long)E1_FIELDS * v.N;
+  v.cs = cs;
+  v.e0 = (int)((long long)v.I.ne * rank / cs);
+  v.e1 = (int)((long long)v.I.ne * (rank + 1) / cs);
+  v.flip = 0;
+  return v;
+}
 
 __device__ __forceinline__ int wrap_left(int e, int ne) { return e == 0 ? ne - 1 : e - 1; }
 __device__ __forceinline__ int wrap_right(int e, int ne) { return e == ne - 1 ? 0 : e + 1; }
@@ -61,7 +113,7 @@ __device__ void d1_setup(const View1<NP>& v, const BasisDev& B, const double* mu
   const Inst1D& I = v.I;
   const double eta = (double)(NP * NP);
   const double al = I.alpha;
-  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
     const int base = e * NP;
     double r[NP], u[NP], kk[NP];
@@ -90,7 +142,7 @@ __device__ void d1_setup(const View1<NP>& v, const BasisDev& B, const double* mu
       if (cM) cM[base + k] = M;
     }
   }
-  __syncthreads();
+  v.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -107,7 +159,7 @@ __device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, 
   constexpr int L = NP - 1;
   const int ne = v.I.ne;
   const double hw = B.hw;
-  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, ne), eR = wrap_right(e, ne);
     const int base = e * NP;
     double x[NP], g[NP], xl[NP], xr[NP], kc[NP];
@@ -175,48 +227,58 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
   if (solver == 0) {
     // ---- PCG: w0 = r, w1 = p, w2 = A p
     double* r = w0; double* p = w1; double* ap = w2;
-    double part = 0.0;
+    double* red = v.slot();
     d1_apply<NP>(v, B, [&](int m) { return x0[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
+      double pe = 0.0;
 #pragma unroll
       for (int i = 0; i < NP; ++i) {
         const int m = e * NP + i;
         const double rr = b[m] - y[i], z = rr * cinvM[m];
         r[m] = rr; p[m] = z;
-        part = fma(rr, z, part);
+        pe = fma(rr, z, pe);
         if (taped) { tp.x(0)[m] = xx[i]; tp.r(0)[m] = rr; }
       }
+      red[e] = pe;
     });
-    double rz = block_sum<T1>(part, s_red);
-    if (taped && threadIdx.x == 0) tp.scal()[0] = rz;
+    double rz = v.reduce(s_red);
+    if (taped && threadIdx.x == 0) tp.scal()[0] = rz;  // every CTA of the instance writes the same value
     for (int k = 0; k < n; ++k) {
-      part = 0.0;
+      red = v.slot();
       d1_apply<NP>(v, B, [&](int m) { return p[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
+        double pe = 0.0;
 #pragma unroll
         for (int i = 0; i < NP; ++i) {
           const int m = e * NP + i;
           ap[m] = y[i];
-          part = fma(xx[i], y[i], part);
+          pe = fma(xx[i], y[i], pe);
           if (taped) { tp.p(k)[m] = xx[i]; tp.ap(k)[m] = y[i]; }
         }
+        red[e] = pe;
       });
-      const double pAp = block_sum<T1>(part, s_red);
+      const double pAp = v.reduce(s_red);
       if (taped && threadIdx.x == 0) tp.scal()[n + 1 + k] = pAp;
       const double a = rz / (pAp + 1e-30);
-      part = 0.0;
       const double* xin = k == 0 ? x0 : xout;
-      for (int m = threadIdx.x; m < N; m += blockDim.x) {
-        xout[m] = fma(a, p[m], xin[m]);
-        const double rr = fma(-a, ap[m], r[m]);
-        r[m] = rr;
-        part = fma(rr, rr * cinvM[m], part);
-        if (taped) tp.r(k + 1)[m] = rr;
+      red = v.slot();
+      for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
+        double pe = 0.0;
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+          const int m = e * NP + i;
+          xout[m] = fma(a, p[m], xin[m]);
+          const double rr = fma(-a, ap[m], r[m]);
+          r[m] = rr;
+          pe = fma(rr, rr * cinvM[m], pe);
+          if (taped) tp.r(k + 1)[m] = rr;
+        }
+        red[e] = pe;
       }
-      const double rzn = block_sum<T1>(part, s_red);
+      const double rzn = v.reduce(s_red);
       if (taped && threadIdx.x == 0) tp.scal()[k + 1] = rzn;
       const double beta = rzn / (rz + 1e-30);
-      for (int m = threadIdx.x; m < N; m += blockDim.x) p[m] = fma(beta, p[m], r[m] * cinvM[m]);
+      for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) p[m] = fma(beta, p[m], r[m] * cinvM[m]);
       rz = rzn;
-      __syncthreads();
+      v.sync();
     }
     return;
   }
@@ -244,7 +306,7 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
         }
       }
     });
-    __syncthreads();
+    v.sync();
     x = xo;
   }
 }
@@ -262,7 +324,7 @@ __device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* c
   const Inst1D& I = v.I;
   const double g = I.gamma, iJ = I.iJ, c2dt = c2 * dt;
   bool bad = false;
-  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
     const int base = e * NP;
     double qq[3][NP], f[3][NP], k[3][NP];
@@ -329,23 +391,23 @@ __device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* c
     }
   }
   if (bad) flag_nonfinite(status);
-  __syncthreads();
+  v.sync();
 }
 
 template <int NP>
 __device__ void d1_recip(const View1<NP>& v, const double* x, double* y) {
-  for (int m = threadIdx.x; m < v.N; m += blockDim.x) y[m] = 1.0 / x[m];
-  __syncthreads();
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) y[m] = 1.0 / x[m];
+  v.sync();
 }
 template <int NP>
 __device__ void d1_copy(const View1<NP>& v, const double* x, double* y) {
-  for (int m = threadIdx.x; m < v.N; m += blockDim.x) y[m] = x[m];
-  __syncthreads();
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) y[m] = x[m];
+  v.sync();
 }
 template <int NP>
 __device__ void d1_zero(const View1<NP>& v, double* y) {
-  for (int m = threadIdx.x; m < v.N; m += blockDim.x) y[m] = 0.0;
-  __syncthreads();
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) y[m] = 0.0;
+  v.sync();
 }
 
 // SSP-RK3 stage coefficients (IGR_adjoints_1d/forward.jl:61-79):
@@ -400,11 +462,11 @@ __device__ void d1_step(const View1<NP>& v, const BasisDev& B, int solver, int n
     double* const* qs = s == 0 ? q : (s == 1 ? q1 : q2);
     StageTape1* t = tp ? &tp[s] : nullptr;
     if (t) {
-      for (int m = threadIdx.x; m < v.N; m += blockDim.x) {
+      for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) {
         t->q[0][m] = qs[0][m]; t->q[1][m] = qs[1][m]; t->q[2][m] = qs[2][m];
         t->ir[m] = irs[s][m]; t->sin[m] = Sx[m];
       }
-      __syncthreads();
+      v.sync();
     }
     if (apos) {
       double* b = t ? t->b : W(F1_B);
@@ -418,8 +480,8 @@ __device__ void d1_step(const View1<NP>& v, const BasisDev& B, int solver, int n
       double* tmp = Sx; Sx = Sy; Sy = tmp;
     }
     if (t) {
-      for (int m = threadIdx.x; m < v.N; m += blockDim.x) t->sout[m] = Sx[m];
-      __syncthreads();
+      for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) t->sout[m] = Sx[m];
+      v.sync();
     }
     const double* qsc[3] = {qs[0], qs[1], qs[2]};
     const double* qnc[3] = {q[0], q[1], q[2]};
@@ -441,6 +503,7 @@ struct Fwd1DArgs {
   double* sig;        // batch Sigma out
   double* scr;        // scratch arena
   int solver, n_iter, final_solve;
+  int cs;             // CTAs per instance (cluster size)
   int* status;
 };
 
@@ -448,12 +511,10 @@ struct Fwd1DArgs {
 // n_steps SSP-RK3 steps of size dt with the Sigma warm-start chain, then the
 // final solve at T when final_solve and alpha > 0.
 template <int NP>
-__global__ void __launch_bounds__(T1) k1_forward(Fwd1DArgs a) {
+__global__ void __launch_bounds__(T1, 2) k1_forward(Fwd1DArgs a) {
   __shared__ double s_red[T1];
-  View1<NP> v;
-  v.I = a.inst[a.order[blockIdx.x]];
-  v.N = NP * v.I.ne;
-  v.scr = a.scr + v.I.soff;
+  int inst;
+  const View1<NP> v = make_view1<NP>(a.inst, a.order, a.scr, a.cs, &inst);
   const BasisDev& B = a.B;
   const Inst1D& I = v.I;
   double* q[3] = {a.q + 3 * I.off, a.q + 3 * I.off + v.N, a.q + 3 * I.off + 2 * v.N};

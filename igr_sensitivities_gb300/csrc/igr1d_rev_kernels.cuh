@@ -8,8 +8,8 @@
 // Every element's thread accumulates into its own nodes only ("owner
 // computes"): face terms that touch two elements are evaluated by both, so no
 // atomics are needed and results do not depend on scheduling. The gamma and
-// alpha derivatives accumulate in registers per thread and are reduced at the
-// end in a fixed order.
+// alpha derivatives accumulate per element (View1::gbe / abe) and are reduced
+// at the end in a fixed order.
 #pragma once
 #include "igr1d_kernels.cuh"
 
@@ -62,13 +62,14 @@ __device__ __forceinline__ void ws1_rev(double g, double mu, double ir, double E
 template <int NP>
 __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* const q[3], const double* ir,
                            const double* S, const double* const A[3], double c0, double c1, double c2, double* const Qn[3],
-                           int qn_mode, double* const Qs[3], int qs_add, double* Sb, double& gb) {
+                           int qn_mode, double* const Qs[3], int qs_add, double* Sb) {
   constexpr int L = NP - 1;
   const Inst1D& I = v.I;
   const double g = I.gamma, iJ = I.iJ, c2dt = c2 * I.dt;
-  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
     const int base = e * NP;
+    double gb = 0.0;  // this element's d/dgamma
     double kb[3][NP], Fb[3][NP], qb[3][NP];
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -153,8 +154,9 @@ __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* 
         Qs[c][m] = qs_add ? Qs[c][m] + val : val;
       }
     }
+    v.gbe()[e] += gb;
   }
-  __syncthreads();
+  v.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -167,13 +169,13 @@ __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* 
 template <int NP, class LDU, class EPI>
 __device__ __forceinline__ void d1_apply_rev(const View1<NP>& v, const BasisDev& B, LDU ldu, const double* vt,
                                              const double* ir, const double* cm, const double* ck, const double* cpR,
-                                             double zscale, double* Zinv, int z_first, double& ab, EPI epi) {
+                                             double zscale, double* Zinv, int z_first, EPI epi) {
   constexpr int L = NP - 1;
   const Inst1D& I = v.I;
   const int ne = I.ne;
   const double hw = B.hw, al = I.alpha, iJ = I.iJ;
   const double eta = (double)(NP * NP);
-  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, ne), eR = wrap_right(e, ne);
     const int base = e * NP;
     double u[NP], w[NP], ul[NP], ur[NP], wl[NP], wr[NP], kc[NP];
@@ -232,7 +234,7 @@ __device__ __forceinline__ void d1_apply_rev(const View1<NP>& v, const BasisDev&
     }
 #pragma unroll
     for (int i = 0; i < NP; ++i) Zinv[base + i] = z_first ? zscale * z[i] : fma(zscale, z[i], Zinv[base + i]);
-    ab = fma(zscale, abl, ab);
+    v.abe()[e] = fma(zscale, abl, v.abe()[e]);
   }
 }
 
@@ -245,7 +247,7 @@ __device__ __forceinline__ void d1_apply_rev(const View1<NP>& v, const BasisDev&
 template <int NP>
 __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, int n, const StageTape1& t, double* xb,
                              double* bb, double* iMb, double* Zinv, double* w0, double* w1, double* w2, double* w3,
-                             double& ab, double* s_red) {
+                             double* s_red) {
   const int N = v.N;
   const SolveTape1& tp = t.st;
   const double* cinvM = t.cinvM;
@@ -261,7 +263,7 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
     double can = 0.0, ccn = 0.0;
     if (solver == 2) coef(n, &can, &ccn);
     // last iteration's x_n = x_{n-1} + (...) r_{n-1}: r̄_{n-1} from xb
-    for (int m = threadIdx.x; m < N; m += blockDim.x) {
+    for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) {
       const double xbv = xb[m];
       if (solver == 2) {
         const double zb = ccn * xbv;
@@ -274,7 +276,7 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
         iMb[m] = tb * tp.r(n - 1)[m];
       }
     }
-    __syncthreads();
+    v.sync();
     int cur = 0;
     for (int k = n - 1; k >= 0; --k) {
       // r_k = b - A x_k : bb += u, xb -= A u, Z += -(u, x_k); then r̄_{k-1}
@@ -284,7 +286,7 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
       double cak = 0.0, cck = 0.0;
       if (solver == 2 && k > 0) coef(k, &cak, &cck);
       d1_apply_rev<NP>(v, B, [&](int m, double) { return u[m]; }, tp.x(k), t.ir, t.cm, t.ck, t.cpR, -1.0, Zinv,
-                       first ? 1 : 0, ab, [&](int e, const double* uu, const double* y) {
+                       first ? 1 : 0, [&](int e, const double* uu, const double* y) {
 #pragma unroll
         for (int i = 0; i < NP; ++i) {
           const int m = e * NP + i;
@@ -306,7 +308,7 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
           }
         }
       });
-      __syncthreads();
+      v.sync();
       cur = 1 - cur;
     }
     return;
@@ -318,58 +320,66 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
   const double* PAP = tp.scal() + n + 1;
   double rzb = 0.0;   // running adjoint of rz_{it+1} (then rz_it)
   double betab = 0.0; // pb . p_it from the previous reverse apply
-  for (int m = threadIdx.x; m < N; m += blockDim.x) { pb[m] = 0.0; rb[m] = 0.0; }
-  __syncthreads();
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) { pb[m] = 0.0; rb[m] = 0.0; }
+  v.sync();
   bool first_z = true;
   for (int it = n - 1; it >= 0; --it) {
     const double rz0 = RZ[it], rz1 = RZ[it + 1], pap = PAP[it];
     const double e0 = rz0 + 1e-30, den = pap + 1e-30;
     const double beta = rz1 / e0, al = rz0 / den;
     const double rzb1 = rzb + betab / e0;
-    double part = 0.0;
     const double* r1 = tp.r(it + 1);
     const double* ap = tp.ap(it);
     const double* p = tp.p(it);
-    for (int m = threadIdx.x; m < N; m += blockDim.x) {
-      const double pbv = pb[m], im = cinvM[m], rr = r1[m];
-      pb[m] = beta * pbv;
-      const double zb = fma(rzb1, rr, pbv);
-      double rbv = fma(rzb1, rr * im, rb[m]);
-      rbv = fma(zb, im, rbv);
-      rb[m] = rbv;
-      iMb[m] = (it == n - 1) ? zb * rr : fma(zb, rr, iMb[m]);
-      part = fma(xb[m], p[m], fma(-rbv, ap[m], part));
+    double* red = v.slot();
+    for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
+      double pe = 0.0;
+#pragma unroll
+      for (int i = 0; i < NP; ++i) {
+        const int m = e * NP + i;
+        const double pbv = pb[m], im = cinvM[m], rr = r1[m];
+        pb[m] = beta * pbv;
+        const double zb = fma(rzb1, rr, pbv);
+        double rbv = fma(rzb1, rr * im, rb[m]);
+        rbv = fma(zb, im, rbv);
+        rb[m] = rbv;
+        iMb[m] = (it == n - 1) ? zb * rr : fma(zb, rr, iMb[m]);
+        pe = fma(xb[m], p[m], fma(-rbv, ap[m], pe));
+      }
+      red[e] = pe;
     }
-    const double abv = block_sum<T1>(part, s_red);
+    const double abv = v.reduce(s_red);
     rzb = -betab * rz1 / (e0 * e0) + abv / den;
     const double papb = -abv * rz0 / (den * den);
     // Ap = A p: pb += alpha xb + papb Ap + A (adjoint of Ap); u = -(adjoint of Ap) = alpha rb - papb p
-    part = 0.0;
     const double* pn = it > 0 ? tp.p(it - 1) : nullptr;
+    red = v.slot();
     d1_apply_rev<NP>(v, B, [&](int m, double pv) { return fma(al, rb[m], -papb * pv); }, p, t.ir, t.cm, t.ck, t.cpR, -1.0,
-                     Zinv, first_z ? 1 : 0, ab, [&](int e, const double*, const double* y) {
+                     Zinv, first_z ? 1 : 0, [&](int e, const double*, const double* y) {
+      double pe = 0.0;
 #pragma unroll
       for (int i = 0; i < NP; ++i) {
         const int m = e * NP + i;
         const double pbv = fma(papb, ap[m], fma(al, xb[m], pb[m] - y[i]));
         pb[m] = pbv;
-        if (pn) part = fma(pbv, pn[m], part);
+        if (pn) pe = fma(pbv, pn[m], pe);
       }
+      red[e] = pe;
     });
     first_z = false;
-    betab = block_sum<T1>(part, s_red);  // also synchronises the pb / rb updates
+    betab = v.reduce(s_red);  // also synchronises the pb / rb updates
   }
   // p_0 = z_0, rz_0 = r_0 . z_0, z_0 = M^-1 r_0
   const double* r0 = tp.r(0);
-  for (int m = threadIdx.x; m < N; m += blockDim.x) {
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) {
     const double rr = r0[m], im = cinvM[m];
     const double z0b = fma(rzb, rr, pb[m]);
     rb[m] = rb[m] + fma(rzb, rr * im, z0b * im);
     iMb[m] = fma(z0b, rr, iMb[m]);
   }
-  __syncthreads();
+  v.sync();
   // r_0 = b - A x_0
-  d1_apply_rev<NP>(v, B, [&](int m, double) { return rb[m]; }, tp.x(0), t.ir, t.cm, t.ck, t.cpR, -1.0, Zinv, 0, ab,
+  d1_apply_rev<NP>(v, B, [&](int m, double) { return rb[m]; }, tp.x(0), t.ir, t.cm, t.ck, t.cpR, -1.0, Zinv, 0,
                    [&](int e, const double* uu, const double* y) {
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
@@ -378,7 +388,7 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
       bb[m] = uu[i];
     }
   });
-  __syncthreads();
+  v.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -388,14 +398,15 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
 // ---------------------------------------------------------------------------
 template <int NP>
 __device__ void d1_setup_rev(const View1<NP>& v, const BasisDev& B, const StageTape1& t, const double* bb,
-                             const double* iMb, const double* Zinv, double* const Qs[3], double& ab) {
+                             const double* iMb, const double* Zinv, double* const Qs[3]) {
   constexpr int L = NP - 1;
   const Inst1D& I = v.I;
   const double al = I.alpha, iJ = I.iJ, eta = (double)(NP * NP);
   auto Mb = [&](int m) { const double im = t.cinvM[m]; return -(iMb[m] * im) * im; };
-  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
     const int base = e * NP;
+    double ab = 0.0;  // this element's d/dalpha
     double r[NP], mu[NP], u[NP], mb[NP], invb[NP], dub[NP];
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
@@ -443,8 +454,9 @@ __device__ void d1_setup_rev(const View1<NP>& v, const BasisDev& B, const StageT
       Qs[0][base + j] += ub * r[j];
       Qs[1][base + j] += -(ub * mu[j]) * r[j] * r[j] - invb[j] * r[j] * r[j];
     }
+    v.abe()[e] += ab;
   }
-  __syncthreads();
+  v.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -456,56 +468,70 @@ __device__ double d1_objective(const View1<NP>& v, const BasisDev& B, int obj, c
                                double* s_red, double* ke_out, double* ms_out) {
   const Inst1D& I = v.I;
   const double g = I.gamma, pi = 3.14159265358979323846;
-  double acc = 0.0, ms = 0.0;
-  for (int m = threadIdx.x; m < v.N; m += blockDim.x) {
-    const int i = m % NP, e = m / NP;
-    const double c = B.w[i] * I.J;
-    const double x = e * I.dx + I.J * (1.0 + B.xi[i]);
-    const double mu = q[0][m], r = q[1][m], E = q[2][m];
-    switch (obj) {
-      case 0: acc = fma(c, r * r, acc); break;
-      case 1: { const double P = (g - 1.0) * (E - mu * mu / (2.0 * r)); acc = fma(c, P * P, acc); break; }
-      case 2: acc += c * (mu * mu) / (2.0 * r); ms = fma(c, r, ms); break;
-      case 4: acc += c * mu * sin(2.0 * pi * x / (I.ne * I.dx)); break;
-      case 6: acc += (x >= prm[0] && x <= prm[1]) ? c * r : 0.0; break;
-      default: break;
+  double* red = v.slot();
+  double* red2 = v.gbe();  // unused until the reverse starts: holds the mass partials
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
+    double acc = 0.0, ms = 0.0;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const int m = e * NP + i;
+      const double c = B.w[i] * I.J;
+      const double x = e * I.dx + I.J * (1.0 + B.xi[i]);
+      const double mu = q[0][m], r = q[1][m], E = q[2][m];
+      switch (obj) {
+        case 0: acc = fma(c, r * r, acc); break;
+        case 1: { const double P = (g - 1.0) * (E - mu * mu / (2.0 * r)); acc = fma(c, P * P, acc); break; }
+        case 2: acc += c * (mu * mu) / (2.0 * r); ms = fma(c, r, ms); break;
+        case 4: acc += c * mu * sin(2.0 * pi * x / (I.ne * I.dx)); break;
+        case 6: acc += (x >= prm[0] && x <= prm[1]) ? c * r : 0.0; break;
+        default: break;
+      }
     }
+    red[e] = acc;
+    red2[e] = ms;
   }
-  const double J = block_sum<T1>(acc, s_red);
-  const double M = obj == 2 ? block_sum<T1>(ms, s_red) : 1.0;
+  const double J = v.reduce(s_red);
+  const double M = obj == 2 ? v.esum(red2, s_red) : 1.0;
   *ke_out = J;
   *ms_out = M;
+  v.sync();  // every CTA has read the partials before they are overwritten
   return obj == 2 ? J / M : J;
 }
 
 template <int NP>
 __device__ void d1_objective_grad(const View1<NP>& v, const BasisDev& B, int obj, const double* prm, const double* const q[3],
-                                  double KE, double Ms, double* const qb[3], double& gb) {
+                                  double KE, double Ms, double* const qb[3]) {
   const Inst1D& I = v.I;
   const double g = I.gamma, pi = 3.14159265358979323846;
-  for (int m = threadIdx.x; m < v.N; m += blockDim.x) {
-    const int i = m % NP, e = m / NP;
-    const double c = B.w[i] * I.J;
-    const double x = e * I.dx + I.J * (1.0 + B.xi[i]);
-    const double mu = q[0][m], r = q[1][m], E = q[2][m];
-    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
-    switch (obj) {
-      case 0: b1 = 2.0 * c * r; break;
-      case 1: {
-        const double K = mu * mu / (2.0 * r), P = (g - 1.0) * (E - K), Pb = 2.0 * c * P, Kb = -Pb * (g - 1.0);
-        gb += Pb * (E - K); b2 = Pb * (g - 1.0); b0 = Kb * mu / r; b1 = -Kb * K / r; break;
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
+    double gb = 0.0;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const int m = e * NP + i;
+      const double c = B.w[i] * I.J;
+      const double x = e * I.dx + I.J * (1.0 + B.xi[i]);
+      const double mu = q[0][m], r = q[1][m], E = q[2][m];
+      double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+      switch (obj) {
+        case 0: b1 = 2.0 * c * r; break;
+        case 1: {
+          const double K = mu * mu / (2.0 * r), P = (g - 1.0) * (E - K), Pb = 2.0 * c * P, Kb = -Pb * (g - 1.0);
+          gb += Pb * (E - K); b2 = Pb * (g - 1.0); b0 = Kb * mu / r; b1 = -Kb * K / r; break;
+        }
+        case 2: {
+          const double KEb = 1.0 / Ms, Mb = -KE / (Ms * Ms);
+          b0 = KEb * c * mu / r; b1 = -KEb * c * mu * mu / (2.0 * r * r) + Mb * c; break;
+        }
+        case 4: b0 = c * sin(2.0 * pi * x / (I.ne * I.dx)); break;
+        case 6: b1 = (x >= prm[0] && x <= prm[1]) ? c : 0.0; break;
+        default: break;
       }
-      case 2: {
-        const double KEb = 1.0 / Ms, Mb = -KE / (Ms * Ms);
-        b0 = KEb * c * mu / r; b1 = -KEb * c * mu * mu / (2.0 * r * r) + Mb * c; break;
-      }
-      case 4: b0 = c * sin(2.0 * pi * x / (I.ne * I.dx)); break;
-      case 6: b1 = (x >= prm[0] && x <= prm[1]) ? c : 0.0; break;
-      default: break;
+      qb[0][m] = b0; qb[1][m] = b1; qb[2][m] = b2;
     }
-    qb[0][m] = b0; qb[1][m] = b1; qb[2][m] = b2;
+    v.gbe()[e] = gb;  // starts the per-element d/dgamma accumulators
+    v.abe()[e] = 0.0;
   }
-  __syncthreads();
+  v.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -516,11 +542,10 @@ __device__ void d1_objective_grad(const View1<NP>& v, const BasisDev& B, int obj
 template <int NP>
 __device__ void d1_stage_rev(const View1<NP>& v, const BasisDev& B, int solver, int n, const StageTape1& t,
                              const double* const A[3], double c0, double c1, double c2, double* const Qn[3], int qn_mode,
-                             double* const Qs[3], int qs_add, double* Sb, double* wk, double& gb, double& ab,
-                             double* s_red) {
+                             double* const Qs[3], int qs_add, double* Sb, double* wk, double* s_red) {
   auto W = [&](int k) { return wk + (long long)k * v.N; };
   const double* qc[3] = {t.q[0], t.q[1], t.q[2]};
-  d1_hyp_rev(v, B, qc, t.ir, t.sout, A, c0, c1, c2, Qn, qn_mode, Qs, qs_add, Sb, gb);
+  d1_hyp_rev(v, B, qc, t.ir, t.sout, A, c0, c1, c2, Qn, qn_mode, Qs, qs_add, Sb);
   if (!(v.I.alpha > 0)) {
     d1_zero(v, Sb);  // Sigma = 0: nothing flows to the warm start
     return;
@@ -528,8 +553,8 @@ __device__ void d1_stage_rev(const View1<NP>& v, const BasisDev& B, int solver, 
   double* bb = W(0);
   double* iMb = W(1);
   double* Zinv = W(2);
-  d1_solve_rev(v, B, solver, n, t, Sb, bb, iMb, Zinv, W(3), W(4), W(5), W(6), ab, s_red);
-  d1_setup_rev(v, B, t, bb, iMb, Zinv, Qs, ab);
+  d1_solve_rev(v, B, solver, n, t, Sb, bb, iMb, Zinv, W(3), W(4), W(5), W(6), s_red);
+  d1_setup_rev(v, B, t, bb, iMb, Zinv, Qs);
 }
 
 // ---------------------------------------------------------------------------
@@ -558,17 +583,15 @@ struct Adj1DArgs {
   double* scr;
   int solver, n_iter, objective, seg;
   double prm[4];
+  int cs;               // CTAs per instance (cluster size)
   int* status;
 };
 
 template <int NP>
-__global__ void __launch_bounds__(T1) k1_adjoint(Adj1DArgs a) {
+__global__ void __launch_bounds__(T1, 2) k1_adjoint(Adj1DArgs a) {
   __shared__ double s_red[T1];
-  const int inst = a.order[blockIdx.x];
-  View1<NP> v;
-  v.I = a.inst[inst];
-  v.N = NP * v.I.ne;
-  v.scr = a.scr + v.I.soff;
+  int inst;
+  const View1<NP> v = make_view1<NP>(a.inst, a.order, a.scr, a.cs, &inst);
   const BasisDev& B = a.B;
   const Inst1D& I = v.I;
   const int N = v.N, n = I.n_steps, seg = a.seg;
@@ -582,33 +605,33 @@ __global__ void __launch_bounds__(T1) k1_adjoint(Adj1DArgs a) {
   double* ck2 = v.f(A1_TAPE + 3 * tf);
   double* ck1 = ck2 + 4LL * seg * N;
   auto snap = [&](double* dst, const double* S) {
-    for (int m = threadIdx.x; m < N; m += blockDim.x) {
+    for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) {
       dst[m] = X[0][m]; dst[N + m] = X[1][m]; dst[2 * N + m] = X[2][m]; dst[3 * N + m] = S[m];
     }
-    __syncthreads();
+    v.sync();
   };
   double* Sx = v.f(A1_SA);
   double* Sy = v.f(A1_SB);
   auto restore = [&](const double* src) {
     Sx = v.f(A1_SA); Sy = v.f(A1_SB);
-    for (int m = threadIdx.x; m < N; m += blockDim.x) {
+    for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) {
       X[0][m] = src[m]; X[1][m] = src[N + m]; X[2][m] = src[2 * N + m]; Sx[m] = src[3 * N + m];
       ir[m] = 1.0 / src[N + m];
     }
-    __syncthreads();
+    v.sync();
   };
   // ---- forward with level-1 snapshots
   const double* q0 = a.q0 + 3 * I.off;
-  for (int m = threadIdx.x; m < N; m += blockDim.x) {
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) {
     X[0][m] = q0[m]; X[1][m] = q0[N + m]; X[2][m] = q0[2 * N + m]; ir[m] = 1.0 / q0[N + m]; Sx[m] = 0.0;
   }
-  __syncthreads();
+  v.sync();
   for (int s = 0; s < n; ++s) {
     if (s % seg == 0) snap(ck1 + 4LL * (s / seg) * N, Sx);
     d1_step(v, B, a.solver, a.n_iter, X, ir, Sx, Sy, wk, nullptr, a.status, s_red);
   }
   // ---- objective and its gradient
-  double gb = 0.0, ab = 0.0, KE = 0.0, Ms = 0.0;
+  double KE = 0.0, Ms = 0.0;
   const double* Xc[3] = {X[0], X[1], X[2]};
   const double J = d1_objective(v, B, a.objective, a.prm, Xc, s_red, &KE, &Ms);
   double* QB[3] = {v.f(A1_QB), v.f(A1_QB + 1), v.f(A1_QB + 2)};
@@ -616,7 +639,7 @@ __global__ void __launch_bounds__(T1) k1_adjoint(Adj1DArgs a) {
   double* Q2b[3] = {v.f(A1_Q2B), v.f(A1_Q2B + 1), v.f(A1_Q2B + 2)};
   double* Q1b[3] = {v.f(A1_Q1B), v.f(A1_Q1B + 1), v.f(A1_Q1B + 2)};
   double* Sb = v.f(A1_SBAR);
-  d1_objective_grad(v, B, a.objective, a.prm, Xc, KE, Ms, QB, gb);
+  d1_objective_grad(v, B, a.objective, a.prm, Xc, KE, Ms, QB);
   d1_zero(v, Sb);
   // ---- reverse, segment by segment
   for (int j = nseg - 1; j >= 0; --j) {
@@ -631,19 +654,19 @@ __global__ void __launch_bounds__(T1) k1_adjoint(Adj1DArgs a) {
       d1_step(v, B, a.solver, a.n_iter, X, ir, Sx, Sy, wk, tp, a.status, s_red);
       const double* A2[3] = {QB[0], QB[1], QB[2]};
       d1_stage_rev(v, B, a.solver, a.n_iter, tp[2], A2, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, QN, 1, Q2b, 0, Sb, v.f(A1_RW),
-                   gb, ab, s_red);
+                   s_red);
       const double* A1[3] = {Q2b[0], Q2b[1], Q2b[2]};
-      d1_stage_rev(v, B, a.solver, a.n_iter, tp[1], A1, 0.75, 0.25, 0.25, QN, 2, Q1b, 0, Sb, v.f(A1_RW), gb, ab, s_red);
+      d1_stage_rev(v, B, a.solver, a.n_iter, tp[1], A1, 0.75, 0.25, 0.25, QN, 2, Q1b, 0, Sb, v.f(A1_RW), s_red);
       const double* A0[3] = {Q1b[0], Q1b[1], Q1b[2]};
-      d1_stage_rev(v, B, a.solver, a.n_iter, tp[0], A0, 0.0, 1.0, 1.0, QN, 0, QN, 1, Sb, v.f(A1_RW), gb, ab, s_red);
+      d1_stage_rev(v, B, a.solver, a.n_iter, tp[0], A0, 0.0, 1.0, 1.0, QN, 0, QN, 1, Sb, v.f(A1_RW), s_red);
       for (int c = 0; c < 3; ++c) { double* t = QB[c]; QB[c] = QN[c]; QN[c] = t; }
     }
   }
   double* dq = a.dq0 + 3 * I.off;
-  for (int m = threadIdx.x; m < N; m += blockDim.x) { dq[m] = QB[0][m]; dq[N + m] = QB[1][m]; dq[2 * N + m] = QB[2][m]; }
-  const double gsum = block_sum<T1>(gb, s_red);
-  const double asum = block_sum<T1>(ab, s_red);
-  if (threadIdx.x == 0) {
+  for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) { dq[m] = QB[0][m]; dq[N + m] = QB[1][m]; dq[2 * N + m] = QB[2][m]; }
+  const double gsum = v.esum(v.gbe(), s_red);
+  const double asum = v.esum(v.abe(), s_red);
+  if (threadIdx.x == 0 && v.e0 == 0) {
     a.J[inst] = J;
     a.dgamma[inst] = gsum;
     a.dalpha[inst] = asum;

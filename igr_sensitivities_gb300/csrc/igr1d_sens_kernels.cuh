@@ -40,7 +40,7 @@ __device__ void d1_sens_hyp_rk(const View1<NP>& v, const BasisDev& B, double sg,
     sens_flux1(g, sg, q[0][m], q[1][m], q[2][m], S[m], ir[m], s[0][m], s[1][m], s[2][m], vs[m], f);
   };
   auto wsp = [&](int m) { return ws1(g, node1(g, q[0][m], q[2][m], S[m], ir[m]), ir[m]); };
-  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eL = wrap_left(e, I.ne), eR = wrap_right(e, I.ne);
     const int base = e * NP;
     double f[3][NP], k[3][NP], ss[3][NP];
@@ -92,7 +92,7 @@ __device__ void d1_sens_hyp_rk(const View1<NP>& v, const BasisDev& B, double sg,
     }
   }
   if (bad) flag_nonfinite(status);
-  __syncthreads();
+  v.sync();
 }
 
 // Tangent elliptic source.
@@ -107,7 +107,7 @@ __device__ void d1_sens_rhs(const View1<NP>& v, const BasisDev& B, int form, con
   constexpr int L = NP - 1;
   const Inst1D& I = v.I;
   const double al = I.alpha, iJ = I.iJ, eta = (double)(NP * NP);
-  for (int e = threadIdx.x; e < I.ne; e += blockDim.x) {
+  for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
     const int eR = wrap_right(e, I.ne);
     const int base = e * NP;
     double u[NP], su[NP], rs[NP], Sv[NP];
@@ -139,13 +139,13 @@ __device__ void d1_sens_rhs(const View1<NP>& v, const BasisDev& B, int form, con
       cpR[e] = al * eta * I.idx * ((kR > kL) ? kR : kL);
     }
   }
-  __syncthreads();
+  v.sync();
   if (form == 2) return;
   d1_apply<NP>(v, B, [&](int m) { return S[m]; }, cm, ck, cpR, [&](int e, const double*, const double* y) {
 #pragma unroll
     for (int i = 0; i < NP; ++i) b[e * NP + i] += y[i];
   });
-  __syncthreads();
+  v.sync();
 }
 
 // Scratch of the tangent kernel (fields of N doubles, after the step work).
@@ -163,16 +163,15 @@ struct Tan1DArgs {
   double* scr;
   int solver, n_iter, form;
   double s_gamma;
+  int cs;         // CTAs per instance (cluster size)
   int* status;
 };
 
 template <int NP>
-__global__ void __launch_bounds__(T1) k1_tangent(Tan1DArgs a) {
+__global__ void __launch_bounds__(T1, 2) k1_tangent(Tan1DArgs a) {
   __shared__ double s_red[T1];
-  View1<NP> v;
-  v.I = a.inst[a.order[blockIdx.x]];
-  v.N = NP * v.I.ne;
-  v.scr = a.scr + v.I.soff;
+  int inst;
+  const View1<NP> v = make_view1<NP>(a.inst, a.order, a.scr, a.cs, &inst);
   const BasisDev& B = a.B;
   const Inst1D& I = v.I;
   const int N = v.N;

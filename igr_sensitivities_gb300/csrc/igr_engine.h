@@ -71,6 +71,8 @@ struct Ctx {
   // memory plan of the last adjoint call: instance groups, instances per group,
   // steps taped per segment and segments per group (1 = no forward recompute)
   int plan_groups = 0, plan_group_size = 0, plan_seg = 0, plan_nseg = 0;
+  int cluster1d = 0;            // 1D: CTAs per instance (0 = chosen per launch)
+  int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
   Profiler prof;
 };
 

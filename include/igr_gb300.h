@@ -86,6 +86,13 @@ const char* igr_last_error(const igr_ctx* ctx);
 /* Device bytes the adjoint may use for its tape; 0 (default) = most of the
  * free memory. A smaller budget turns on segment checkpointing. */
 int igr_set_tape_budget(igr_ctx* ctx, size_t bytes);
+/* 1D: CTAs that advance one instance (a thread-block cluster when > 1):
+ * 0 (default) = chosen per launch (small batches spread each instance over up
+ * to 16 SMs); 1, 2, 4, 8 or 16 force it. Results do not depend on it.
+ * No reference counterpart. */
+int igr_set_cluster_size_1d(igr_ctx* ctx, int cs);
+/* CTAs per instance used by the last 1D launch on this context. */
+int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out);
 /* Kernels launched by the last call on this context. */
 int igr_last_launch_count(const igr_ctx* ctx, long long* out);
 

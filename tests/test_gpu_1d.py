@@ -222,3 +222,41 @@ def test_run_sensitivity_1d_matches_oracle(igr, igr1d, oracle, p, ne, solver, n_
         assert rel(a, b) <= RTOL_FWD
     if alpha > 0:
         assert rel(out[3], Sr) <= RTOL_FWD and rel(out[7], vr) <= RTOL_FWD
+
+
+@pytest.mark.parametrize("solver", ["pcg", "chebyshev"])
+def test_cluster_size_does_not_change_results(igr, igr1d, oracle, solver):
+    """One instance spread over a cluster of 2..16 CTAs gives bitwise the
+    results of one CTA (forward, tangent and adjoint): every reduction runs
+    over per-element partials in one fixed order."""
+    from igr_sensitivities_gb300 import Context
+    g = 1.4
+    basis, mesh, G = setup1(igr, oracle, 3, 64)
+    q0 = W.seeded_pulses_1d(mesh, g, W.seed_for(1, 900), width=0.08)
+    dt = W.cfl_dt_1d(mesh, 3, q0, g, 0.1)
+    alpha = 3.0 * mesh.dx ** 2
+    rng = np.random.default_rng(3)
+    s0 = [np.asfortranarray(0.1 * rng.standard_normal(mesh.x.shape)) for _ in range(3)]
+    ctx = Context(0)
+    out = {}
+    for cs in (1, 2, 16):
+        ctx.set_cluster_size_1d(cs)
+        f = igr1d.run_forward(*q0, dt, 6 * dt, basis, mesh, g, alpha, n_iter=7, solver=solver, ctx=ctx)
+        assert ctx.last_cluster_size_1d() == cs
+        t = igr1d.run_sensitivity(*q0, *s0, dt, 5.5 * dt, basis, mesh, g, alpha, n_iter=7, solver=solver, ctx=ctx)
+        a = igr1d.adjoint_batch([tuple(flat(x) for x in q0)], basis, [64], 1.0, g, alpha, dt, 5, n_iter=7, solver=solver,
+                                objective="l2_pressure", ctx=ctx)
+        out[cs] = (f, t, a)
+    ctx.set_cluster_size_1d(0)
+    igr1d.run_forward(*q0, dt, 6 * dt, basis, mesh, g, alpha, n_iter=7, solver=solver, ctx=ctx)
+    assert ctx.last_cluster_size_1d() == 16  # automatic choice for one 64-element instance
+    for cs in (2, 16):
+        for x, y in zip(out[1][0] + out[1][1], out[cs][0] + out[cs][1]):
+            assert np.array_equal(x, y)
+        a1, ac = out[1][2], out[cs][2]
+        assert a1[0][0] == ac[0][0] and a1[2][0] == ac[2][0] and a1[3][0] == ac[3][0]
+        for x, y in zip(a1[1][0], ac[1][0]):
+            assert np.array_equal(x, y)
+    ref, _ = oracle.run_forward_1d(G, g, alpha, dt, 6 * dt, 7, solver, [flat(x) for x in q0])
+    for x, y in zip(out[16][0][:3], ref):
+        assert rel(x, y) <= RTOL_FWD
