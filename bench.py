@@ -198,8 +198,15 @@ def secondary(args):
         q0 = W.seeded_pulses_2d(mesh, GAMMA, W.seed_for(2, 0), n_pulses=3, width=0.03)
         dt = W.cfl_dt_2d(mesh, 3, q0, GAMMA, 0.1)
         alpha, nst = 3.0 / 128 ** 2, 500
+        if args.profile_case:  # 2 steps (ncu captures)
+            nst = 2
         T = nst * dt * 0.999
         run = lambda: igr.run_forward(*q0, dt, T, basis, mesh, GAMMA, alpha, n_iter=60, solver="pcg", ctx=ctx)
+        if args.profile_case:
+            run()
+            run()
+            print("profile case done")
+            return
         for _ in range(args.warmup):
             run()
         t0 = time.perf_counter()

@@ -382,12 +382,14 @@ static bool all_alpha_pos(const Plan2D& P) {
   return true;
 }
 
-// Per-tile partial sums and per-instance arrival counters of the in-kernel
-// reductions (the counters are left at zero by every reduction).
-static void reduction_scratch(Ctx& c, const Plan2D& P, double** partials, int** counters) {
-  *partials = c.ws.dbl("red:part", P.ntiles());
-  *counters = static_cast<int*>(c.ws.get("red:cnt", sizeof(int) * P.inst.size()));
-  cuda_check(cudaMemsetAsync(*counters, 0, sizeof(int) * P.inst.size(), c.stream), "reset counters");
+// Per-instance sum of per-tile partials: out[inst] (mode 0) or the PCG
+// reverse scalars (mode 1, see k2_tile_sum).
+static void tile_sum(Ctx& c, const Plan2D& P, const double* partials, double* out) {
+  TileSumArgs t;
+  std::memset(&t, 0, sizeof(t));
+  t.inst = P.d_inst; t.partials = partials; t.out = out; t.mode = 0;
+  LaunchScope ls(c, KID_OTHER);
+  k2_tile_sum<<<(int)P.inst.size(), PCG_THREADS, 0, c.stream>>>(t);
 }
 
 static void tile_geometry(const Plan2D& P, int* tx, int* ty) { tile_shape(P.np, tx, ty); }
@@ -401,9 +403,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
                       double* xout, bool taped, double* xa, double* xb, double* dbuf) {
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
-  double* part;
-  int* cnt;
-  reduction_scratch(c, P, &part, &cnt);
+  double* part = c.ws.dbl("red:part", nb);
   double* scal = taped ? st.scal : c.ws.dbl("pcg:scal", (size_t)(2 * n + 1) * ni);
   double* apbuf = taped ? nullptr : c.ws.dbl("pcg:ap", NG);
   auto RZ = [&](int k) { return scal + (long long)k * ni; };
@@ -417,14 +417,17 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
   std::memset(&base, 0, sizeof(base));
   base.tiles = P.d_tiles; base.inst = P.d_inst; base.B = P.B;
   base.cm = st.cm; base.ckx = st.ckx; base.cky = st.cky; base.cpx = st.cpx; base.cpy = st.cpy; base.b = b; base.cinvM = st.cinvM;
-  base.partials = part; base.counters = cnt;
+  base.partials = part;
   {  // r_0 = b - A x_0, p_0 = M^-1 r_0, rz_0
     ApplyArgs2D a = base;
     a.x = x0;
     a.tape_x = taped ? st.x0t : nullptr;
-    a.r_out = R(0); a.p_out = PK(0); a.red_out = RZ(0);
-    LaunchScope ls(c, KID_APPLY);
-    NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG0, a, nb, c.stream));
+    a.r_out = R(0); a.p_out = PK(0);
+    {
+      LaunchScope ls(c, KID_APPLY);
+      NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG0, a, nb, c.stream));
+    }
+    tile_sum(c, P, part, RZ(0));
   }
   for (int k = 0; k < n; ++k) {
     {
@@ -435,18 +438,24 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
         a.pcg_r = R(k); a.pcg_p = PK(k - 1); a.rz_cur = RZ(k); a.rz_prev = RZ(k - 1);
         a.p_out = PK(k);
       }
-      a.ap_out = AP(k); a.red_out = PAP(k);
-      LaunchScope ls(c, KID_APPLY);
-      NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG, a, nb, c.stream));
+      a.ap_out = AP(k);
+      {
+        LaunchScope ls(c, KID_APPLY);
+        NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG, a, nb, c.stream));
+      }
+      tile_sum(c, P, part, PAP(k));
     }
     PcgUpdateArgs u;
     u.tiles = P.d_tiles; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
     u.x_in = k == 0 ? x0 : xout; u.x_out = xout;
     u.p = PK(k); u.ap = AP(k); u.r_in = R(k); u.r_out = R(k + 1); u.cinvM = st.cinvM;
-    u.rz = RZ(k); u.pap = PAP(k); u.rz_out = RZ(k + 1);
-    u.partials = part; u.counters = cnt;
-    LaunchScope ls(c, KID_OTHER);
-    k2_pcg_update<<<nb, PCG_THREADS, 0, c.stream>>>(u);
+    u.rz = RZ(k); u.pap = PAP(k);
+    u.partials = part;
+    {
+      LaunchScope ls(c, KID_OTHER);
+      k2_pcg_update<<<nb, PCG_THREADS, 0, c.stream>>>(u);
+    }
+    tile_sum(c, P, part, RZ(k + 1));
   }
 }
 
@@ -916,9 +925,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   const int srev = !apos ? SREV_NONE : (o.solver == SOLVER_CHEBYSHEV ? SREV_CHEB : (o.solver == SOLVER_JACOBI ? SREV_JACOBI : SREV_PCG));
   int tx, ty;
   tile_geometry(P, &tx, &ty);
-  double* part = nullptr;
-  int* cnt = nullptr;
-  if (srev == SREV_PCG) reduction_scratch(c, P, &part, &cnt);
+  double* part = srev == SREV_PCG ? c.ws.dbl("red:part", P.ntiles()) : nullptr;
   double* pscal = c.ws.dbl("adj:pcgscal", (size_t)3 * ni);  // BET, RZB, PAPB per instance
   const int nb = P.ntiles();
   const double c0s[3] = {0.0, 3.0 / 4, 1.0 / 3}, c1s[3] = {1.0, 1.0 / 4, 2.0 / 3}, c2s[3] = {1.0, 1.0 / 4, 2.0 / 3};
@@ -939,9 +946,17 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       g.first = it == n - 1 ? 1 : 0; g.it = it; g.ni = ni;
       g.pb = PB; g.rb = RB; g.iMb = Mb;
       g.r1 = sb.rk[it + 1]; g.cinvM = sb.cinvM; g.ap = sb.apk[it]; g.p = sb.pk[it]; g.xb = Sb;
-      g.RZ = RZ; g.PAP = PAP; g.BET = BET; g.RZB = RZB; g.PAPB = PAPB;
-      g.partials = part; g.counters = cnt;
+      g.RZ = RZ; g.BET = BET; g.RZB = RZB;
+      g.partials = part;
       { LaunchScope ls(c, KID_OTHER); k2_pcg_rev_update<<<nb, PCG_THREADS, 0, c.stream>>>(g); }
+      {
+        TileSumArgs ts;
+        std::memset(&ts, 0, sizeof(ts));
+        ts.inst = P.d_inst; ts.partials = part; ts.mode = 1; ts.first = g.first; ts.it = it; ts.ni = ni;
+        ts.RZ = RZ; ts.PAP = PAP; ts.BET = BET; ts.RZB = RZB; ts.PAPB = PAPB;
+        LaunchScope ls(c, KID_OTHER);
+        k2_tile_sum<<<ni, PCG_THREADS, 0, c.stream>>>(ts);
+      }
       ApplyRevArgs2D r;
       std::memset(&r, 0, sizeof(r));
       r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
@@ -955,8 +970,9 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       r.has_next = it > 0 ? 1 : 0;
       r.rz_it = RZ + (long long)it * ni; r.pap_it = PAP + (long long)it * ni; r.papb = PAPB;
       r.xconst = Sb; r.apk = sb.apk[it]; r.p_next = it > 0 ? sb.pk[it - 1] : nullptr;
-      r.red_out = BET; r.partials = part; r.counters = cnt;
+      r.partials = part;
       { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(SREV_PCG, r, nb, c.stream)); }
+      if (it > 0) tile_sum(c, P, part, BET);
     }
     {
       PcgRevFinalArgs f;

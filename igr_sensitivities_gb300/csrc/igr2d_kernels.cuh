@@ -279,13 +279,14 @@ struct ApplyArgs2D {
   double *y_out;                         // EPI_RESID: raw y = A x
   double ca, cc, omega;                  // d_{k+1} = ca d_k + cc M^-1 r_k ; Jacobi omega
   // Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347):
-  //  EPI_PCG0: x = x_0; r_0 = b - A x_0 -> r_out, p_0 = M^-1 r_0 -> p_out, red_out = r_0 . p_0
+  //  EPI_PCG0: x = x_0; r_0 = b - A x_0 -> r_out, p_0 = M^-1 r_0 -> p_out, partial of r_0 . p_0
   //  EPI_PCG : x = p_k; with pcg_p set, p_k = M^-1 r_k + beta p_{k-1} is formed on load from
   //            (pcg_r, pcg_p), beta = rz_cur / (rz_prev + 1e-30), and stored to p_out;
-  //            A p_k -> ap_out, red_out = p_k . A p_k
+  //            A p_k -> ap_out, partial of p_k . A p_k
+  // The inner-product partial of each tile goes to partials[tile]; k2_tile_sum adds them per instance.
   const double *pcg_r, *pcg_p, *rz_cur, *rz_prev;
-  double *p_out, *r_out, *ap_out, *red_out;
-  double* partials; int* counters;       // per-tile partial sums, per-instance arrival counters
+  double *p_out, *r_out, *ap_out;
+  double* partials;
 };
 
 // Partner data across one face: its value and end-node derivative of x, and its stiffness coefficient.
@@ -465,9 +466,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
   }
   if (PCG) {
     const double tot = block_sum<P2>(part, s_red);
-    double inst_tot = 0.0;
-    if (instance_sum<P2>(tot, tl.inst, I.tile0, I.ntiles, a.partials, a.counters, s_red, &inst_tot) && threadIdx.x == 0)
-      a.red_out[tl.inst] = inst_tot;
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
   }
 }
 

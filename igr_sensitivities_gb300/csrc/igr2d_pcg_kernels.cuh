@@ -5,8 +5,9 @@
 // k2_apply_rev (SREV_PCG); these kernels do the vector updates between them.
 // Each block covers one tile of elements (the same tile list as the operator
 // kernels), so the per-instance inner products reduce deterministically:
-// block tree sum -> one partial per tile -> the instance's last block adds
-// its tiles' partials in tile order (instance_sum). The results are therefore
+// block tree sum -> one partial per tile -> k2_tile_sum adds an instance's
+// partials in tile order (a separate launch: ordering across blocks comes from
+// the kernel boundary, with no fences or atomics). The results are therefore
 // identical from run to run and independent of the batch composition.
 //
 // Scalars live on the device, one per instance: rz_k = r_k . M^-1 r_k and
@@ -39,8 +40,7 @@ struct PcgUpdateArgs {
   const double *x_in, *p, *ap, *r_in, *cinvM;
   double *x_out, *r_out;
   const double *rz, *pap;   // per-instance rz_k, pAp_k
-  double* rz_out;           // per-instance rz_{k+1}
-  double* partials; int* counters;
+  double* partials;         // per-tile partials of rz_{k+1}
 };
 
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
@@ -60,9 +60,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
     part = fma(r, r * a.cinvM[n], part);
   }
   const double tot = block_sum<P2>(part, s_red);
-  double it = 0.0;
-  if (instance_sum<P2>(tot, tl.inst, I.tile0, I.ntiles, a.partials, a.counters, s_red, &it) && threadIdx.x == 0)
-    a.rz_out[tl.inst] = it;
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
 }
 
 // ---------------------------------------------------------------------------
@@ -73,18 +71,19 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
 //                                           -> rb += rzb_{it+1} z + M^-1 zb', iMb += zb' r
 //   ab = -(rb . A p_it) + (xb . p_it)       (reduced; stored through RZB, PAPB)
 // betab = pb . p_it arrives from the previous reverse apply (BET), or is 0 on
-// the first reverse iteration, where pb = rb = 0.
-// Afterwards RZB = rzb_it (its part known so far) and PAPB = the adjoint of
-// pAp_it; k2_apply_rev<SREV_PCG> finishes the iteration.
+// the first reverse iteration, where pb = rb = 0. The tile partials of ab go
+// to partials; k2_tile_sum (PCG-reverse mode) then sets RZB = rzb_it (its part
+// known so far) and PAPB = the adjoint of pAp_it, and k2_apply_rev<SREV_PCG>
+// finishes the iteration.
 // ---------------------------------------------------------------------------
 struct PcgRevArgs {
   const Tile2D* tiles; const Inst2D* inst; int np, tx, ty;
   int first, it, ni;
   double *pb, *rb, *iMb;
   const double *r1, *cinvM, *ap, *p, *xb;
-  const double *RZ, *PAP;          // taped scalars: RZ[k*ni+i], PAP[k*ni+i]
-  double *BET, *RZB, *PAPB;        // per-instance adjoint scalars
-  double* partials; int* counters;
+  const double *RZ;                // taped scalars: RZ[k*ni+i]
+  const double *BET, *RZB;         // per-instance adjoint scalars
+  double* partials;
 };
 
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
@@ -115,12 +114,41 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
     part = fma(a.xb[n], a.p[n], fma(-rbv, a.ap[n], part));
   }
   const double tot = block_sum<P2>(part, s_red);
-  double ab = 0.0;
-  if (instance_sum<P2>(tot, i, I.tile0, I.ntiles, a.partials, a.counters, s_red, &ab) && threadIdx.x == 0) {
-    const double den = a.PAP[(long long)a.it * a.ni + i] + 1e-30;
-    a.RZB[i] = -betab * rz1 / (e0 * e0) + ab / den;
-    a.PAPB[i] = -ab * rz0 / (den * den);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
+}
+
+// Per-instance sum of the tile partials (one block per instance, fixed
+// order: thread t adds tiles t, t + 256, ..., then a block tree).
+// mode 0: out[i] = sum. mode 1 (after k2_pcg_rev_update of iteration it):
+// ab = sum, RZB[i] = -betab rz_{it+1} / (rz_it + eps)^2 + ab / (pAp_it + eps),
+// PAPB[i] = -ab rz_it / (pAp_it + eps)^2, betab = BET[i] (0 when first).
+struct TileSumArgs {
+  const Inst2D* inst; const double* partials;
+  double* out;
+  int mode, first, it, ni;
+  const double *RZ, *PAP, *BET;
+  double *RZB, *PAPB;
+};
+
+__global__ void __launch_bounds__(PCG_THREADS) k2_tile_sum(TileSumArgs a) {
+  constexpr int P2 = PCG_THREADS;
+  __shared__ double s_red[P2];
+  const int i = blockIdx.x;
+  const Inst2D I = a.inst[i];
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < I.ntiles; k += blockDim.x) acc += a.partials[I.tile0 + k];
+  const double tot = block_sum<P2>(acc, s_red);
+  if (threadIdx.x != 0) return;
+  if (a.mode == 0) {
+    a.out[i] = tot;
+    return;
   }
+  const double rz0 = a.RZ[(long long)a.it * a.ni + i], rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
+  const double e0 = rz0 + 1e-30;
+  const double betab = a.first ? 0.0 : a.BET[i];
+  const double den = a.PAP[(long long)a.it * a.ni + i] + 1e-30;
+  a.RZB[i] = -betab * rz1 / (e0 * e0) + tot / den;
+  a.PAPB[i] = -tot * rz0 / (den * den);
 }
 
 // Reverse of the PCG start (p_0 = z_0, rz_0 = r_0 . z_0, z_0 = M^-1 r_0):

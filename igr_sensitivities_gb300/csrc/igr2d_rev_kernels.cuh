@@ -333,11 +333,11 @@ struct ApplyRevArgs2D {
   // SREV_PCG (reverse of A p_it, second half of the iteration reverse):
   //   u = -(adjoint of A p_it) = alpha_it rb - pApb p_it, formed on load from
   //   (u = rb, xk = p_it); xb = pb: pb += alpha_it xconst + pApb apk + A(adjoint of A p_it);
-  //   with has_next, red_out = pb . p_next (betab of the next reverse iteration)
+  //   with has_next, the tile's partial of pb . p_next (betab of the next reverse
+  //   iteration) goes to partials[tile]
   const double *rz_it, *pap_it, *papb;  // per-instance scalars
   const double *xconst, *apk, *p_next;
-  double* red_out;
-  double* partials; int* counters;
+  double* partials;
 };
 
 // Partner data across one face for the reverse apply: values and end-node
@@ -553,9 +553,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
   }
   if (PCG && a.has_next) {
     const double tot = block_sum<P2>(part, s_red);
-    double inst_tot = 0.0;
-    if (instance_sum<P2>(tot, tl.inst, I.tile0, I.ntiles, a.partials, a.counters, s_red, &inst_tot) && threadIdx.x == 0)
-      a.red_out[tl.inst] = inst_tot;
+    if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
   }
 }
 

@@ -79,31 +79,6 @@ __device__ __forceinline__ double block_sum(double v, double* s_red) {
   return r;
 }
 
-// Per-instance sum of one value per tile (block), deterministic: each block
-// stores its partial; the last block of the instance to arrive (atomic
-// counter) adds the instance's partials in tile order. Returns true in every
-// thread of that last block, with the instance total in *total; the counter
-// is reset there for the next reduction on the stream. Every thread calls it.
-template <int P2>
-__device__ __forceinline__ bool instance_sum(double block_partial, int inst, int tile0, int ntiles, double* partials,
-                                             int* counters, double* s_red, double* total) {
-  __shared__ int s_last;
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = block_partial;
-    __threadfence();
-    const int prev = atomicAdd(&counters[inst], 1);
-    s_last = (prev == ntiles - 1);
-  }
-  __syncthreads();
-  if (!s_last) return false;
-  __threadfence();
-  double acc = 0.0;
-  for (int k = threadIdx.x; k < ntiles; k += blockDim.x) acc += __ldcg(&partials[tile0 + k]);
-  *total = block_sum<P2>(acc, s_red);
-  if (threadIdx.x == 0) counters[inst] = 0;
-  return true;
-}
-
 // Smallest power of two >= n (n <= 1024), for block_sum's scratch size.
 __host__ __device__ constexpr int pow2_at_least(int n) {
   return n <= 1 ? 1 : (n <= 2 ? 2 : (n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : (n <= 32 ? 32 : (n <= 64 ? 64 :
