@@ -20,7 +20,7 @@ from ._lib import Context, check, default_context, lib
 
 __all__ = [
     "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
-    "run_forward", "run_forward_", "run_sensitivity", "enzyme_adjoint_ic", "adjoint_batch", "objective_value",
+    "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch", "objective_value",
     "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
 ]
 
@@ -213,6 +213,26 @@ def run_sensitivity(mux0, muy0, rho0, E0, zetax0, zetay0, sigma0, eta0, dt, T, b
                                            *[_ptr(a) for a in s], _ptr(V)))
     r = lambda a: np.asfortranarray(a.reshape(shape, order="F"))
     return tuple(r(a) for a in q) + (r(S),) + tuple(r(a) for a in s) + (r(V),)
+
+
+def sensitivity_batch(q0, s0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solver="pcg", s_gamma=0.0, ctx=None):
+    """Batched run_sensitivity for n_steps fixed steps (per-instance gamma, alpha, dt).
+
+    q0, s0: (n_inst, 4, N) float64 (variables mux, muy, rho, E and their
+    tangents, Julia node order). Returns (q, Sigma, s, varsigma) with q, s of
+    shape (n_inst, 4, N) and Sigma, varsigma of shape (n_inst, N).
+    """
+    ctx = ctx or default_context()
+    q = np.array(q0, dtype=np.float64, order="C", copy=True)
+    s = np.array(s0, dtype=np.float64, order="C", copy=True)
+    B, _, n = q.shape
+    f64 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (B,)))
+    gs, als, dtv = f64(gammas), f64(alphas), f64(dts)
+    S, V = np.zeros((B, n)), np.zeros((B, n))
+    check(ctx, lib().igr2d_sensitivity_batch(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_int(B), _ptr(gs), _ptr(als),
+                                             _ptr(dtv), C.c_int(n_steps), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                             C.c_double(s_gamma), _ptr(q), _ptr(s), _ptr(S), _ptr(V)))
+    return q, S, s, V
 
 
 def enzyme_adjoint_ic(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",

@@ -227,6 +227,48 @@ int igr2d_run_sensitivity(igr_ctx* ctx, const igr_disc2d* d, double gamma, doubl
   });
 }
 
+int igr2d_sensitivity_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                            const double* dts, int n_steps, int n_iter, int solver, double s_gamma, double* q,
+                            double* s, double* sigma, double* varsigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc(d);
+    check_solver(solver, n_iter);
+    if (n_inst < 1 || !gammas || !alphas || !dts || !q || !s || !sigma || !varsigma || n_steps < 0)
+      throw Error(IGR_EINVAL, "bad batch arguments");
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    const long long N = nodes2d(d);
+    std::vector<Inst2DDesc> insts;
+    for (int b = 0; b < n_inst; ++b) insts.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], alphas[b], dts[b]});
+    Plan2D P = make_plan2d(c, B, insts, "senb");
+    const long long NG = P.NG;
+    double* buf = c.ws.dbl("capi:senb", 10 * (size_t)NG);
+    double* qd[4];
+    double* sd[4];
+    for (int v = 0; v < 4; ++v) { qd[v] = buf + v * NG; sd[v] = buf + (4 + v) * NG; }
+    double* S = buf + 8 * NG;
+    double* V = buf + 9 * NG;
+    // [inst][var][N] <-> field-major [var][inst*N]
+    for (int v = 0; v < 4; ++v) {
+      cuda_check(cudaMemcpy2DAsync(qd[v], N * sizeof(double), q + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyHostToDevice, c.stream), "gather q");
+      cuda_check(cudaMemcpy2DAsync(sd[v], N * sizeof(double), s + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyHostToDevice, c.stream), "gather s");
+    }
+    Solve2DOpts o{n_iter, solver};
+    sensitivity2d(c, P, qd, S, sd, V, n_steps, o, s_gamma);
+    for (int v = 0; v < 4; ++v) {
+      cuda_check(cudaMemcpy2DAsync(q + v * N, 4 * N * sizeof(double), qd[v], N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyDeviceToHost, c.stream), "scatter q");
+      cuda_check(cudaMemcpy2DAsync(s + v * N, 4 * N * sizeof(double), sd[v], N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyDeviceToHost, c.stream), "scatter s");
+    }
+    d2h(c, sigma, S, NG);
+    d2h(c, varsigma, V, NG);
+    sync(c);
+  });
+}
+
 int igr2d_objective(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_steps, double dt,
                     int n_iter, int solver, int objective, const double* obj_params, double* mux, double* muy,
                     double* rho, double* E, double* J) {

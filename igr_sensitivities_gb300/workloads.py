@@ -113,3 +113,64 @@ def max_wavespeed_1d(mu, rho, E, gamma):
 def cfl_dt_1d(mesh, p, q, gamma, cfl):
     """dt = CFL dx / ((2p+1) max wavespeed), the 1D form of the tests' CFL rule."""
     return cfl * mesh.dx / ((2 * p + 1) * max_wavespeed_1d(*q, gamma))
+
+
+def oseen_pair_pulse_2d(mesh, gamma, seed, a_core=0.05, circ=(0.5, 1.0), amp=(1.0, 10.0), pulse_width=0.05,
+                        n_tab=4000):
+    """Counter-rotating Oseen vortex pair plus one Gaussian pressure pulse
+    (the family of build_oseen_pair_blast_ic!, IGR_adjoints_2d/initial_conditions.jl:175-232):
+    v_theta = G/(2 pi r) (1 - exp(-r^2/a^2)) summed over 3x3 periodic images,
+    homentropic radial equilibrium through the enthalpy defect
+    D(r) = (G/2pi)^2 int_r^inf (1 - e^{-s^2/a^2})^2 / s^3 ds (tabulated,
+    composed additively for the pair), ambient p = rho = 1. The pair (zero net
+    circulation, as the doubly periodic box requires) is centred at a seeded
+    point with separation 0.2; the pulse sits at a seeded point.
+
+    The circulation is drawn as a fraction U[circ] of the strongest vortex
+    that keeps the core enthalpy defect D(0) = (G/2pi)^2 ln2 / a^2 at or below
+    a quarter of the ambient enthalpy gamma/(gamma-1): a literal circulation of
+    order one would drive the core pressure negative at ambient p = 1.
+    """
+    rng = SplitMix64(seed)
+    L = mesh.Lx
+    g_max = 2 * np.pi * a_core * np.sqrt(0.25 * gamma / (gamma - 1) / np.log(2.0))
+    G = rng.uniform(*circ) * g_max
+    xc, yc = rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7)
+    A = rng.uniform(*amp)
+    bx, by = rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8)
+    centers = ((xc, yc + 0.1, +1.0), (xc, yc - 0.1, -1.0))
+    r_max = 2.0 * L
+    r_tab = np.linspace(0.0, r_max, n_tab)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f = np.where(r_tab < 1e-12, 0.0, (1.0 - np.exp(-r_tab ** 2 / a_core ** 2)) ** 2 / r_tab ** 3)
+    seg = 0.5 * (f[:-1] + f[1:]) * np.diff(r_tab)
+    D_tab = np.zeros(n_tab)
+    D_tab[:-1] = (G / (2 * np.pi)) ** 2 * np.cumsum(seg[::-1])[::-1]
+
+    def defect(r):
+        t = np.clip(r / r_max * (n_tab - 1), 0, n_tab - 1 - 1e-12)
+        i = np.floor(t).astype(int)
+        w = t - i
+        return np.where(r >= r_max, 0.0, (1 - w) * D_tab[i] + w * D_tab[np.minimum(i + 1, n_tab - 1)])
+
+    x, y = mesh.x, mesh.y
+    ux, uy = np.zeros(x.shape), np.zeros(x.shape)
+    h = np.full(x.shape, gamma / (gamma - 1))
+    for cx, cy, sgn in centers:
+        for sx in (-1, 0, 1):
+            for sy in (-1, 0, 1):
+                dx, dy = x - (cx + sx * L), y - (cy + sy * L)
+                r2 = dx ** 2 + dy ** 2
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    v = np.where(r2 < 1e-24, 0.0, sgn * G / (2 * np.pi * r2) * (1.0 - np.exp(-r2 / a_core ** 2)))
+                ux += -v * dy
+                uy += v * dx
+        dx, dy = x - cx, y - cy
+        dx -= L * np.round(dx / L)
+        dy -= L * np.round(dy / L)
+        h = h - defect(np.sqrt(dx ** 2 + dy ** 2))
+    p_v = ((gamma - 1) * h / gamma) ** (gamma / (gamma - 1))
+    rho = p_v ** (1.0 / gamma)
+    p = p_v + A * np.exp(-((x - bx) ** 2 + (y - by) ** 2) / pulse_width ** 2)
+    E = p / (gamma - 1) + 0.5 * rho * (ux ** 2 + uy ** 2)
+    return tuple(np.asfortranarray(a) for a in (rho * ux, rho * uy, rho, E))

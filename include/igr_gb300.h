@@ -131,6 +131,17 @@ int igr2d_run_sensitivity(igr_ctx* ctx, const igr_disc2d* d, double gamma, doubl
                           int n_iter, int solver, double s_gamma, double* mux, double* muy, double* rho, double* E,
                           double* sigma, double* zetax, double* zetay, double* srho, double* eta, double* varsigma);
 
+/* Batched run_sensitivity over instances sharing one mesh, each with its own
+ * gamma, alpha and dt, for n_steps fixed steps (no dt re-rounding; a caller
+ * wanting run_sensitivity's semantics passes n_steps = ceil(T/dt) and
+ * dt = T/n_steps). q and s are [n_inst][4][N] (mux, muy, rho, E and their
+ * tangents), in place; sigma and varsigma are [n_inst][N] out. s_gamma is
+ * shared by the batch (the direct dP/dgamma source; 1 with s = 0 gives the
+ * state's derivative with respect to gamma at frozen LLF wave speed). */
+int igr2d_sensitivity_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                            const double* dts, int n_steps, int n_iter, int solver, double s_gamma, double* q,
+                            double* s, double* sigma, double* varsigma);
+
 /* enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:428-454): J and
  * dJ/dq0 of the objective after n_steps SSP-RK3 steps of size dt (no dt
  * re-rounding, Sigma warm start from zero). dgamma/dalpha (may be NULL) are
