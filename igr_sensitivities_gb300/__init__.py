@@ -171,6 +171,7 @@ def _prm(obj_params):
 
 def run_forward_(mux, muy, rho, E, Sigma, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
     """run_forward! (IGR_adjoints_2d/forward.jl:41-75): state arrays updated in place to time T."""
+    _solver(solver)  # validate before touching the device
     ctx = ctx or default_context()
     shape = mesh.shape(basis)
     n = int(np.prod(shape))
@@ -201,6 +202,7 @@ def run_sensitivity(mux0, muy0, rho0, E0, zetax0, zetay0, sigma0, eta0, dt, T, b
     varsigma). s_gamma adds the direct dP/dgamma tangent source (0 in the
     reference's 2D package).
     """
+    _solver(solver)  # validate before touching the device
     ctx = ctx or default_context()
     shape = mesh.shape(basis)
     n = int(np.prod(shape))
@@ -222,6 +224,7 @@ def sensitivity_batch(q0, s0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=
     tangents, Julia node order). Returns (q, Sigma, s, varsigma) with q, s of
     shape (n_inst, 4, N) and Sigma, varsigma of shape (n_inst, N).
     """
+    _solver(solver)  # validate before touching the device
     ctx = ctx or default_context()
     q = np.array(q0, dtype=np.float64, order="C", copy=True)
     s = np.array(s0, dtype=np.float64, order="C", copy=True)
@@ -244,6 +247,8 @@ def enzyme_adjoint_ic(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alp
     size `dt`, computed by the hand-written discrete adjoint on the GPU. With
     with_params=True, (dJ/dgamma, dJ/dalpha) are appended.
     """
+    _solver(solver)  # validate before touching the device
+    _objective(objective)
     ctx = ctx or default_context()
     shape = mesh.shape(basis)
     n = int(np.prod(shape))
@@ -267,6 +272,8 @@ def adjoint_batch(q0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solv
     order. Returns (J[n_inst], dq0 (n_inst, 4, N), dgamma[n_inst], dalpha[n_inst]).
     With device_arrays=True, q0 is a torch CUDA tensor and dq0 is returned as one.
     """
+    _solver(solver)  # validate before touching the device
+    _objective(objective)
     ctx = ctx or default_context()
     gammas = np.ascontiguousarray(gammas, dtype=np.float64)
     alphas = np.ascontiguousarray(alphas, dtype=np.float64)
@@ -297,6 +304,8 @@ def objective_value(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha
                     objective="l2_density", obj_params=None, ctx=None):
     """The primal objective of enzyme_adjoint_ic (the inlined RK3 loop of
     IGR_adjoints_2d/enzyme_adjoint.jl:206-235 and its objective tail)."""
+    _solver(solver)  # validate before touching the device
+    _objective(objective)
     ctx = ctx or default_context()
     shape = mesh.shape(basis)
     n = int(np.prod(shape))
@@ -335,6 +344,7 @@ def compute_hyperbolic_rhs_(dmux, dmuy, drho, dE, mux, muy, rho, E, Sigma, basis
 
 def solve_elliptic_(Sigma, mux, muy, rho, E, basis, mesh, alpha, n_iter=10, solver="pcg", ctx=None):
     """solve_elliptic! (IGR_adjoints_2d/elliptic.jl:413-427); Sigma is the warm start and the result."""
+    _solver(solver)  # validate before touching the device
     ctx = ctx or default_context()
     shape = mesh.shape(basis)
     n = int(np.prod(shape))

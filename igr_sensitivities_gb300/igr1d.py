@@ -35,6 +35,7 @@ def _shape(basis, mesh):
 
 def run_forward_(mu, rho, E, Sigma, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
     """run_forward! (IGR_adjoints_1d/forward.jl:50-87): state updated in place to time T."""
+    _solver(solver)  # validate before touching the device
     ctx = ctx or default_context()
     shape = _shape(basis, mesh)
     n = int(np.prod(shape))
@@ -63,6 +64,7 @@ def forward_batch(states, basis, n_e, L, gammas, alphas, dts, n_steps, n_iter=10
     states: list of (mu, rho, E) per instance (flat Julia order, N_i = n_p n_e[i]
     each). Returns the list of final (mu, rho, E, Sigma).
     """
+    _solver(solver)  # validate before touching the device
     ctx = ctx or default_context()
     n_e = np.ascontiguousarray(n_e, dtype=np.int32)
     B = n_e.size
@@ -125,12 +127,13 @@ def run_sensitivity(mu0, rho0, E0, smu0, srho0, sE0, dt, T, basis, mesh, gamma, 
                     solver="pcg", s_gamma=0.0, ctx=None):
     """run_sensitivity (IGR_adjoints_1d/sensitivity.jl:475-515): returns
     (mu, rho, E, Sigma, smu, srho, sE, sSigma) at time T."""
-    ctx = ctx or default_context()
-    shape = _shape(basis, mesh)
-    n = int(np.prod(shape))
+    _solver(solver)  # validate before touching the device
     form = {"form1": 1, "form2": 2}.get(str(elliptic_rhs).lstrip(":"))
     if form is None:
         raise ValueError("Unknown elliptic_rhs: %s (use :form1 or :form2)" % elliptic_rhs)
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
     q = [_flat(a, n).copy() for a in (mu0, rho0, E0)]
     s = [_flat(a, n).copy() for a in (smu0, srho0, sE0)]
     S, V = np.zeros(n), np.zeros(n)
@@ -153,12 +156,13 @@ def adjoint_batch(states, basis, n_e, L, gammas, alphas, dts, n_steps, n_iter=10
     states: list of (mu0, rho0, E0) (flat Julia order). Returns
     (J[n], [(dmu0, drho0, dE0)], dgamma[n], dalpha[n]).
     """
-    ctx = ctx or default_context()
+    _solver(solver)  # validate before touching the device
     obj = objective.lstrip(":") if isinstance(objective, str) else objective
     if isinstance(obj, str):
         if obj not in _OBJ1:
             raise ValueError("Unknown objective: %s" % objective)
         obj = _OBJ1[obj]
+    ctx = ctx or default_context()
     n_e = np.ascontiguousarray(n_e, dtype=np.int32)
     B = n_e.size
     sizes = basis.n_p * n_e

@@ -55,3 +55,49 @@ def test_mesh_coordinates_match_reference_formula(igr):
     # mesh.jl:116-122: x = (ex-1) dx + Jx (1 + xi_i), y = (ey-1) dy + Jy (1 + xi_j)
     assert m.x[2, 1, 1, 0] == 1 * m.dx + m.Jx * (1.0 + b.xi[2])
     assert m.y[0, 3, 2, 1] == 1 * m.dy + m.Jy * (1.0 + b.xi[3])
+
+
+def test_python_mirror_rejects_bad_symbols_before_any_device_call(igr):
+    """Unknown solver / objective / elliptic_rhs / IC symbols raise with the
+    reference's message before a context (or a GPU) is needed."""
+    from igr_sensitivities_gb300 import igr1d
+    basis = igr.DGBasis(3)
+    m2 = igr.CartesianMesh2D(2, 2, 1.0, 1.0, basis)
+    m1 = igr.PeriodicMesh1D(4, 1.0, basis)
+    z2 = np.zeros(m2.x.shape)
+    z1 = np.zeros(m1.x.shape)
+    with pytest.raises(ValueError, match="Unknown solver"):
+        igr.run_forward(z2, z2, z2, z2, 0.1, 0.2, basis, m2, 1.4, 0.1, solver="gmres")
+    with pytest.raises(ValueError, match="Unknown objective"):
+        igr.enzyme_adjoint_ic(z2, z2, z2, z2, 1, 0.1, basis, m2, 1.4, 0.1, objective="entropy")
+    with pytest.raises(ValueError, match="Unknown elliptic_rhs"):
+        igr1d.run_sensitivity(z1, z1, z1, z1, z1, z1, 0.1, 0.2, basis, m1, 1.4, 0.1, elliptic_rhs="form3")
+    with pytest.raises(ValueError, match="Unknown solver"):
+        igr1d.run_forward(z1, z1, z1, 0.1, 0.2, basis, m1, 1.4, 0.1, solver="cg")
+    with pytest.raises(ValueError, match="Unknown objective"):
+        igr1d.adjoint_batch([(z1, z1, z1)], basis, [4], 1.0, 1.4, 0.1, 0.1, 1, objective="entropy")
+    with pytest.raises(ValueError, match="use :l2_density or :l2_pressure"):
+        igr1d.enzyme_adjoint_ic(0.1, 3, 4, 1.0, 1.4, 0.1, 0.5, 0.1, objective="kinetic_energy")
+    with pytest.raises(ValueError, match="Unknown IC type"):
+        igr1d.enzyme_adjoint_ic(0.1, 3, 4, 1.0, 1.4, 0.1, 0.5, 0.1, ic_type="shock")
+
+
+def test_ic_builders_match_reference_formulas():
+    """IC_BUILDERS (IGR_adjoints_1d/initial_conditions.jl:94-224): the primitive
+    profiles and the conservative conversion."""
+    from igr_sensitivities_gb300 import igr1d
+    import igr_sensitivities_gb300 as igr
+    basis = igr.DGBasis(3)
+    mesh = igr.PeriodicMesh1D(5, 2.0, basis)
+    s = np.sin(2 * np.pi * mesh.x / 2.0)
+    A, g = 0.1, 1.4
+    expect = {"acoustic_pulse": (1 + A * s, A * s, 1 + A * s), "entropy_wave": (1 + A * s, 1 + 0 * s, 1 + 0 * s),
+              "density_pulse": (1 + A * s, 0 * s, 1 + 0 * s), "pressure_pulse": (1 + 0 * s, 0 * s, 1 + A * s),
+              "velocity_pulse": (1 + 0 * s, A * s, 1 + 0 * s)}
+    for name, (rho, u, p) in expect.items():
+        mu0, rho0, E0 = np.zeros(mesh.x.shape), np.zeros(mesh.x.shape), np.zeros(mesh.x.shape)
+        igr1d.IC_BUILDERS[name][0](mu0, rho0, E0, A, mesh.x, 2.0, g)
+        assert np.allclose(rho0, rho, rtol=0, atol=1e-15)
+        assert np.allclose(mu0, rho * u, rtol=0, atol=1e-15)
+        assert np.allclose(E0, p / (g - 1) + 0.5 * rho * u ** 2, rtol=0, atol=1e-14)
+    assert igr1d.ic_dA_weights(":pressure_pulse") == (0.0, 0.0, 1.0)
