@@ -223,6 +223,32 @@ def secondary(args):
                     config={"workload": "2D IGR-Euler forward, P3 128x128, PCG 60 iters/stage, 500 steps", "mesh": "128x128"},
                     cpu_baseline={"value": 1.0 / tc, "unit": "solves/s", "cores": 1, "kind": "port",
                                   "sample": "%d of %d steps, single thread, scaled" % (ns, nst)})
+    elif args.workload == "adjoint2d_64":
+        # one 64^2 P3 gradient (Chebyshev 5, 200 steps, window rho^2), the single-instance adjoint configuration
+        basis = igr.DGBasis(3)
+        mesh = igr.CartesianMesh2D(64, 64, 1.0, 1.0, basis)
+        q0 = W.seeded_pulses_2d(mesh, GAMMA, W.seed_for(3, 0), n_pulses=3, width=0.03)
+        dt = W.cfl_dt_2d(mesh, 3, q0, GAMMA, 0.1)
+        alpha = 3.0 / 64 ** 2
+        prm = W.seeded_window(W.seed_for(3, 0))
+        run = lambda: igr.enzyme_adjoint_ic(*q0, N_STEPS, dt, basis, mesh, GAMMA, alpha, n_iter=N_ITER, solver=SOLVER,
+                                            objective=OBJ, obj_params=prm, with_params=True, ctx=ctx)
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        t = (time.perf_counter() - t0) / args.steps
+        G = O.Grid2D(3, 64, 64)
+        ns = 2
+        tc0 = time.perf_counter()
+        O.adjoint_2d(G, GAMMA, alpha, ns, dt, N_ITER, SOLVER, OBJ, [flat(a) for a in q0], prm)
+        tc = (time.perf_counter() - tc0) * N_STEPS / ns
+        line.update(metric="2D P3 64^2 adjoint gradients/s (Chebyshev 5, 200 steps, one instance)", value=1.0 / t,
+                    unit="gradients/s", ms_per_step=t * 1e3,
+                    config={"workload": "2D IGR-Euler discrete adjoint, P3 64x64, Chebyshev 5, 200 steps, window rho^2"},
+                    cpu_baseline={"value": 1.0 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
+                                  "sample": "%d of %d steps, single thread, scaled" % (ns, N_STEPS)})
     elif args.workload == "forward1d":
         basis = igr.DGBasis(3)
         mesh = igr.PeriodicMesh1D(256, 1.0, basis)
@@ -305,7 +331,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
     ap.add_argument("--workload", default="adjoint2d",
-                    help="adjoint2d (the headline) | forward2d_pcg | forward1d | batch1d")
+                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()

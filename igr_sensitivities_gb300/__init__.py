@@ -20,7 +20,7 @@ from ._lib import Context, check, default_context, lib
 
 __all__ = [
     "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
-    "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch", "objective_value",
+    "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch_meshes", "adjoint_batch", "objective_value",
     "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
 ]
 
@@ -215,6 +215,41 @@ def run_sensitivity(mux0, muy0, rho0, E0, zetax0, zetay0, sigma0, eta0, dt, T, b
                                            *[_ptr(a) for a in s], _ptr(V)))
     r = lambda a: np.asfortranarray(a.reshape(shape, order="F"))
     return tuple(r(a) for a in q) + (r(S),) + tuple(r(a) for a in s) + (r(V),)
+
+
+def adjoint_batch_meshes(states, basis, meshes, gammas, alphas, dts, n_steps, n_iter=10, solver="pcg",
+                         objective="l2_density", obj_params=None, ctx=None):
+    """Batched enzyme_adjoint_ic over instances with their own meshes.
+
+    states: list of (mux0, muy0, rho0, E0) per instance (any array shape with
+    the instance's node count, Julia order). Returns (J, [(dmux0, dmuy0,
+    drho0, dE0)], dgamma, dalpha).
+    """
+    _solver(solver)
+    _objective(objective)
+    ctx = ctx or default_context()
+    B = len(states)
+    n = [int(np.prod(m.shape(basis))) for m in meshes]
+    q = np.concatenate([np.concatenate([_flat(a, n[i]) for a in states[i]]) for i in range(B)])
+    dq = np.zeros_like(q)
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    f64 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (B,)))
+    nex, ney = i32([m.N_ex for m in meshes]), i32([m.N_ey for m in meshes])
+    lx, ly = f64([m.Lx for m in meshes]), f64([m.Ly for m in meshes])
+    gs, als, dtv = f64(gammas), f64(alphas), f64(dts)
+    J, dg, da = np.zeros(B), np.zeros(B), np.zeros(B)
+    IP = C.POINTER(C.c_int)
+    check(ctx, lib().igr2d_adjoint_batch_meshes(ctx.handle, C.c_int(basis.p), _ptr(basis.xi), _ptr(basis.w),
+                                                _ptr(basis._Dcol), C.c_int(B), nex.ctypes.data_as(IP),
+                                                ney.ctypes.data_as(IP), _ptr(lx), _ptr(ly), _ptr(gs), _ptr(als), _ptr(dtv),
+                                                C.c_int(n_steps), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                                C.c_int(_objective(objective)), _ptr(_prm(obj_params)), _ptr(q), _ptr(J),
+                                                _ptr(dq), _ptr(dg), _ptr(da)))
+    out, o = [], 0
+    for i in range(B):
+        out.append(tuple(dq[o + v * n[i]:o + (v + 1) * n[i]] for v in range(4)))
+        o += 4 * n[i]
+    return J, out, dg, da
 
 
 def sensitivity_batch(q0, s0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solver="pcg", s_gamma=0.0, ctx=None):

@@ -227,6 +227,70 @@ int igr2d_run_sensitivity(igr_ctx* ctx, const igr_disc2d* d, double gamma, doubl
   });
 }
 
+int igr2d_adjoint_batch_meshes(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                               const int* n_ex, const int* n_ey, const double* lx, const double* ly,
+                               const double* gammas, const double* alphas, const double* dts, int n_steps, int n_iter,
+                               int solver, int objective, const double* obj_params, const double* q0, double* J,
+                               double* dq0, double* dgamma, double* dalpha) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    if (!xi || !w || !D || p < 1 || p > 4) throw Error(IGR_EINVAL, "bad basis");
+    if (n_inst < 1 || !n_ex || !n_ey || !lx || !ly || !gammas || !alphas || !dts || !q0 || !J || !dq0 || n_steps < 0)
+      throw Error(IGR_EINVAL, "bad batch arguments");
+    BasisDev B = make_basis_dev(p, xi, w, D);
+    const int np = p + 1;
+    std::vector<long long> Ni(n_inst), off(n_inst + 1, 0);
+    for (int i = 0; i < n_inst; ++i) {
+      if (n_ex[i] < 1 || n_ey[i] < 1 || !(lx[i] > 0) || !(ly[i] > 0)) throw Error(IGR_EINVAL, "bad mesh");
+      Ni[i] = (long long)np * np * n_ex[i] * n_ey[i];
+      off[i + 1] = off[i] + 4 * Ni[i];
+    }
+    // groups: consecutive instances while their full tapes fit (an instance that
+    // does not fit alone runs by itself with segment checkpointing)
+    size_t budget = (size_t)-1;
+    if (c.tape_budget == 0) {
+      size_t fr = 0, tot = 0;
+      cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+      const size_t avail = fr + c.ws.bytes();
+      const size_t reserve = (size_t)4 << 30;
+      budget = avail > reserve ? (size_t)((avail - reserve) * 0.92) : 0;
+    }
+    const Solve2DOpts o{n_iter, solver};
+    std::vector<int> gstart{0};
+    size_t used = 0;
+    for (int i = 0; i < n_inst; ++i) {
+      const size_t F = (size_t)stage_fields2d(o, alphas[i] > 0, Ni[i], 1);
+      const size_t bytes = ((size_t)3 * F * std::max(n_steps, 1) + 6 + 110) * Ni[i] * sizeof(double);
+      if (i > gstart.back() && used + bytes > budget) { gstart.push_back(i); used = 0; }
+      used += bytes;
+    }
+    gstart.push_back(n_inst);
+    c.plan_groups = (int)gstart.size() - 1;
+    c.plan_group_size = 0;
+    for (size_t gi = 0; gi + 1 < gstart.size(); ++gi) {
+      const int g0 = gstart[gi], g1 = gstart[gi + 1];
+      c.plan_group_size = std::max(c.plan_group_size, g1 - g0);
+      std::vector<Inst2DDesc> insts;
+      for (int b = g0; b < g1; ++b) insts.push_back(Inst2DDesc{n_ex[b], n_ey[b], lx[b], ly[b], gammas[b], alphas[b], dts[b]});
+      Plan2D P = make_plan2d(c, B, insts, "adjm");
+      const long long NG = P.NG;
+      double* buf = c.ws.dbl("capi:bqm", 8 * (size_t)NG);
+      double* q[4];
+      double* dq[4];
+      for (int v = 0; v < 4; ++v) { q[v] = buf + v * NG; dq[v] = buf + (4 + v) * NG; }
+      for (int b = g0; b < g1; ++b)  // [var][N_b] of instance b -> its slice of each field
+        for (int v = 0; v < 4; ++v) h2d(c, q[v] + P.inst[b - g0].off, q0 + off[b] + v * Ni[b], Ni[b]);
+      const double* qc[4] = {q[0], q[1], q[2], q[3]};
+      adjoint2d(c, P, qc, n_steps, o, objective, obj_params, J + g0, dq, dgamma ? dgamma + g0 : nullptr,
+                dalpha ? dalpha + g0 : nullptr);
+      for (int b = g0; b < g1; ++b)
+        for (int v = 0; v < 4; ++v) d2h(c, dq0 + off[b] + v * Ni[b], dq[v] + P.inst[b - g0].off, Ni[b]);
+      sync(c);
+    }
+  });
+}
+
 int igr2d_sensitivity_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
                             const double* dts, int n_steps, int n_iter, int solver, double s_gamma, double* q,
                             double* s, double* sigma, double* varsigma) {

@@ -158,6 +158,16 @@ int igr2d_adjoint_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const dou
                         const double* dts, int n_steps, int n_iter, int solver, int objective,
                         const double* obj_params, const double* q0, double* J, double* dq0, double* dgamma,
                         double* dalpha);
+/* Batched enzyme_adjoint_ic over instances with their own meshes (n_ex, n_ey,
+ * lx, ly), gamma, alpha and dt, sharing the basis and the step count: one
+ * launch per kernel covers the tiles of every instance of a group. q0 / dq0
+ * are the concatenation over instances of [4][N_i] blocks,
+ * N_i = (p+1)^2 n_ex[i] n_ey[i]. Results equal the single-instance calls. */
+int igr2d_adjoint_batch_meshes(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                               const int* n_ex, const int* n_ey, const double* lx, const double* ly,
+                               const double* gammas, const double* alphas, const double* dts, int n_steps, int n_iter,
+                               int solver, int objective, const double* obj_params, const double* q0, double* J,
+                               double* dq0, double* dgamma, double* dalpha);
 /* Same with q0 and dq0 in device memory (J, dgamma, dalpha stay host arrays). */
 int igr2d_adjoint_batch_dev(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas,
                             const double* alphas, const double* dts, int n_steps, int n_iter, int solver,

@@ -262,3 +262,33 @@ def test_nonfinite_state_is_reported(igr, oracle):
     with pytest.raises(Exception) as ei:
         igr.run_forward(*q0, 0.01, 0.03, basis, mesh, 1.4, 0.01, n_iter=2, solver="chebyshev")
     assert "IGR_ENONFINITE" in str(ei.value)
+
+
+def test_adjoint_batch_of_uneven_meshes_equals_single_calls(igr, oracle):
+    """Instances with different meshes, gammas, alphas and dts in one batch
+    (one launch per kernel over all their tiles) give bitwise the
+    single-instance gradients; one of them is checked against the oracle."""
+    basis = igr.DGBasis(3)
+    meshes = [igr.CartesianMesh2D(6, 4, 1.0, 0.8, basis), igr.CartesianMesh2D(3, 5, 0.6, 1.0, basis),
+              igr.CartesianMesh2D(8, 8, 1.0, 1.0, basis)]
+    gams, states, dts, als = [1.4, 1.3, 1.6], [], [], []
+    for i, m in enumerate(meshes):
+        q = W.seeded_pulses_2d(m, gams[i], W.seed_for(3, 40 + i), width=0.12)
+        states.append(tuple(flat(a) for a in q))
+        dts.append(W.cfl_dt_2d(m, 3, q, gams[i], 0.1))
+        als.append(3.0 * min(m.dx, m.dy) ** 2)
+    prm = (0.1, 0.1, 0.5)
+    J, dq, dg, da = igr.adjoint_batch_meshes(states, basis, meshes, gams, als, dts, 5, n_iter=6, solver="pcg",
+                                             objective="window_rho2", obj_params=prm)
+    for i, m in enumerate(meshes):
+        one = igr.enzyme_adjoint_ic(*[a.reshape(m.shape(basis), order="F") for a in states[i]], 5, dts[i], basis, m,
+                                    gams[i], als[i], n_iter=6, solver="pcg", objective="window_rho2", obj_params=prm,
+                                    with_params=True)
+        assert one[0] == J[i] and one[5] == dg[i] and one[6] == da[i]
+        for v in range(4):
+            assert np.array_equal(flat(one[1 + v]), dq[i][v])
+    G = oracle.Grid2D(3, 3, 5, 0.6, 1.0)
+    Jr, dqr, dgr, dar = oracle.adjoint_2d(G, gams[1], als[1], 5, dts[1], 6, "pcg", "window_rho2", list(states[1]), prm)
+    assert abs(J[1] - Jr) <= 1e-12 * abs(Jr)
+    num = np.sqrt(sum(np.sum((dq[1][v] - dqr[v]) ** 2) for v in range(4)))
+    assert num <= RTOL_GRAD * np.sqrt(sum(np.sum(b ** 2) for b in dqr))
