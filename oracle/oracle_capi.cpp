@@ -9,6 +9,7 @@
 
 #include "igr1d.hpp"
 #include "igr2d_adjoint.hpp"
+#include "igr2d_pde_adjoint.hpp"
 
 using namespace igr;
 
@@ -167,6 +168,83 @@ int orc2d_run_sensitivity(GRID2D_ARGS, double gamma, double alpha, double dt, do
     if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
     Grid2D G = GRID2D; double* q[4] = {mx, my, rho, E}; double* s[4] = {zx, zy, sr, et};
     run_sensitivity(G, q, s, Sig, vs, dt, T_end, gamma, alpha, n_iter, solver, s_gamma);
+  });
+}
+
+// run_forward_store (forward.jl:111-158): snaps = (n_steps + 1) * 5 * N
+// doubles, n_steps = ceil(T / dt) (the caller sizes the buffer).
+int orc2d_run_forward_store(GRID2D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver,
+                            const double* mx, const double* my, const double* rho, const double* E, double* snaps,
+                            long long snaps_len, int* n_steps) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid2D G = GRID2D; const double* q0[4] = {mx, my, rho, E};
+    std::vector<double> s;
+    *n_steps = run_forward_store(G, q0, dt, T_end, gamma, alpha, n_iter, solver, s);
+    if ((long long)s.size() != snaps_len) throw std::invalid_argument("snapshot buffer has the wrong size");
+    std::memcpy(snaps, s.data(), s.size() * sizeof(double));
+  });
+}
+
+// run_adjoint_conservative (adjoint_pde.jl:527-611) over caller-held snapshots.
+int orc2d_run_adjoint_conservative(GRID2D_ARGS, double gamma, double alpha, int n_steps, double dt, double T_end,
+                                   int n_iter, int obj, int solver, const double* prm, const double* snaps,
+                                   double* amx, double* amy, double* arho, double* aE) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    if (obj < 0 || obj > 5) throw std::invalid_argument("Unknown objective");
+    Grid2D G = GRID2D; double* a[4] = {amx, amy, arho, aE};
+    run_adjoint_conservative(G, snaps, n_steps, dt, T_end, gamma, alpha, n_iter, obj, solver, prm, a);
+  });
+}
+
+// compute_adjoint_rhs_conservative! (adjoint_pde.jl:481-516): Pi in-out.
+int orc2d_adjoint_rhs_conservative(GRID2D_ARGS, double gamma, double alpha, int n_iter, int solver, const double* mx,
+                                   const double* my, const double* rho, const double* E, const double* Sig, double* Pi,
+                                   const double* amx, const double* amy, const double* arho, const double* aE,
+                                   double* dmx, double* dmy, double* drho, double* dE) {
+  return guard([&] {
+    Grid2D G = GRID2D; const double* q[4] = {mx, my, rho, E}; const double* a[4] = {amx, amy, arho, aE};
+    double* da[4] = {dmx, dmy, drho, dE};
+    Work2D<double> W; W.alloc(G.N);
+    pde_adjoint_rhs(G, gamma, alpha, n_iter, solver, q, Sig, Pi, a, da, W);
+  });
+}
+
+// Duality of the local adjoint operator (alpha = 0, Sigma frozen): lhs =
+// <a, L dq>_M with L dq the exact directional derivative of the discrete
+// hyperbolic RHS (forward-mode duals), rhs = <L_dag a, dq>_M with L_dag =
+// compute_adjoint_hyperbolic_rhs_local!; M = nodal mass w_i w_j Jx Jy. Equal
+// up to the discretisation error for smooth fields.
+int orc2d_pde_duality(GRID2D_ARGS, double gamma, const double* q_in, const double* Sig, const double* a_in,
+                      const double* dq_in, double* lhs, double* rhs) {
+  return guard([&] {
+    typedef Dual<1> D1;
+    Grid2D G = GRID2D; const size_t N = G.N;
+    std::vector<D1> qd[4], Sd(N), kd[4];
+    for (int v = 0; v < 4; ++v) {
+      qd[v].resize(N); kd[v].resize(N);
+      for (size_t k = 0; k < N; ++k) { qd[v][k].v = q_in[v * N + k]; qd[v][k].d[0] = dq_in[v * N + k]; }
+    }
+    for (size_t k = 0; k < N; ++k) Sd[k] = D1(Sig[k]);
+    const D1* qc[4] = {qd[0].data(), qd[1].data(), qd[2].data(), qd[3].data()};
+    D1* kc[4] = {kd[0].data(), kd[1].data(), kd[2].data(), kd[3].data()};
+    std::vector<D1> F[8];
+    hyperbolic_rhs(G, D1(gamma), qc, Sd.data(), kc, F);
+    const double* q[4] = {q_in, q_in + N, q_in + 2 * N, q_in + 3 * N};
+    const double* a[4] = {a_in, a_in + N, a_in + 2 * N, a_in + 3 * N};
+    std::vector<double> dav(4 * N);
+    double* da[4] = {dav.data(), dav.data() + N, dav.data() + 2 * N, dav.data() + 3 * N};
+    pde_hyperbolic_rhs_local(G, gamma, q, Sig, a, da);
+    double l = 0.0, r = 0.0;
+    const int np = G.np;
+    for (int ey = 0; ey < G.m.Ney; ++ey) for (int ex = 0; ex < G.m.Nex; ++ex)
+      for (int j = 0; j < np; ++j) for (int i = 0; i < np; ++i) {
+        const size_t n = G.id(i, j, ex, ey);
+        const double m = G.b.w[i] * G.b.w[j] * G.m.Jx * G.m.Jy;
+        for (int v = 0; v < 4; ++v) { l += m * a[v][n] * kd[v][n].d[0]; r += m * da[v][n] * dq_in[v * N + n]; }
+      }
+    *lhs = l; *rhs = r;
   });
 }
 

@@ -216,3 +216,86 @@ def test_splitmix_seeds_are_stable():
     assert a == [r2.next_u64() for _ in range(3)]
     u = W.SplitMix64(1).uniform(1.0, 10.0)
     assert 1.0 <= u <= 10.0
+
+
+# ---------------------------------------------------------------------------
+# Continuous adjoint (run_forward_store + run_adjoint_conservative)
+# ---------------------------------------------------------------------------
+def _taylor_green(G, g, A):
+    # build_taylor_green_ic!, IGR_adjoints_2d/initial_conditions.jl:105-121
+    x, y = G.coords()
+    cx, cy = 2 * np.pi * x / G.Lx, 2 * np.pi * y / G.Ly
+    ux, uy = A * np.sin(cx) * np.cos(cy), -A * np.cos(cx) * np.sin(cy)
+    return [ux, uy, np.ones(G.N), 1.0 / (g - 1) + 0.5 * (ux ** 2 + uy ** 2)]
+
+
+def _pde_vs_discrete(oracle, objective, alpha, p=3, Ne=8, T=0.06):
+    """IGR_adjoints_2d/tests/run_adjoint_test.jl:15-78: the discrete gradient
+    divided by the nodal mass against the PDE adjoint at t = 0 (Taylor-Green,
+    A = 0.4, CFL 0.4, Chebyshev, n_iter = 100 if alpha > 0 else 1)."""
+    g = 1.4
+    G = oracle.Grid2D(p, Ne, Ne)
+    q0 = _taylor_green(G, g, 0.4)
+    mws = W.max_wavespeed_2d(*q0, g)
+    dt = 0.4 * min(G.dx, G.dy) / ((2 * p + 1) * mws)
+    n = int(np.ceil(T / dt))
+    dt = T / n
+    nit = 100 if alpha > 0 else 1
+    _, dq, _, _ = oracle.adjoint_2d(G, g, alpha, n, dt, nit, "chebyshev", objective, q0)
+    m = np.tile(np.outer(G.w, G.w).reshape(-1, order="F"), Ne * Ne) * G.Jx * G.Jy
+    enz = [d / m for d in dq]
+    snaps, nf = oracle.run_forward_store_2d(G, g, alpha, dt, T, nit, "chebyshev", q0)
+    assert nf == n and snaps.shape == (n + 1, 5, G.N)
+    pde = oracle.run_adjoint_conservative_2d(G, snaps, nf, dt, T, g, alpha, nit, objective, "chebyshev")
+    return rel(np.concatenate(pde), np.concatenate(enz))
+
+
+@pytest.mark.parametrize("objective", ["l2_density", "weighted_momentum", "kinetic_energy"])
+@pytest.mark.parametrize("alpha", [0.0, 1.5e-3])
+def test_pde_adjoint_within_otd_gap_of_discrete(oracle, objective, alpha):
+    # run_adjoint_test.jl:72 asserts combined < 0.2 (a sign or derivation error
+    # gives O(1)); the restatement measures 5e-5 .. 2e-2 here, bounded at 0.05.
+    e = _pde_vs_discrete(oracle, objective, alpha)
+    assert e < 0.2
+    assert e < 0.05
+
+
+def test_pde_adjoint_otd_gap_does_not_grow(oracle):
+    # run_adjoint_test.jl:90-97: l2_density, alpha = 1.5e-3, N_e 6 -> 12
+    e_coarse = _pde_vs_discrete(oracle, "l2_density", 1.5e-3, Ne=6)
+    e_fine = _pde_vs_discrete(oracle, "l2_density", 1.5e-3, Ne=12)
+    assert e_fine < 2 * e_coarse
+
+
+def test_pde_local_operator_is_the_dual_of_the_linearised_rhs(oracle):
+    """<a, L dq>_M == <L_dag a, dq>_M for smooth periodic fields, L the exact
+    (forward-mode dual) linearisation of the discrete hyperbolic RHS with Sigma
+    frozen and L_dag compute_adjoint_hyperbolic_rhs_local!: it pins the adjoint
+    flux (adjoint_pde.jl:41-80), the flipped LLF faces and the local source
+    (:138-217) to the forward flux. The gap is the LLF jump term; it falls from
+    1e-2 (4^2 elements) to round-off (16^2)."""
+    g = 1.4
+    gaps = []
+    for Ne in (4, 8, 16):
+        G = oracle.Grid2D(3, Ne, Ne)
+        x, y = G.coords()
+
+        def s(kx, ky, ph):
+            return np.sin(2 * np.pi * (kx * x + ky * y) + ph)
+
+        q = [0.3 * s(1, 0, 0.1) + 0.1 * s(0, 1, 0.7), 0.2 * s(0, 1, 0.3) - 0.1 * s(1, 1, 0.2), 1 + 0.2 * s(1, 1, 0.5),
+             2.5 + 0.3 * s(1, 0, 0.9)]
+        a = [s(1, 0, 0.4), s(0, 1, 1.3), s(1, 1, 2.0), s(1, -1, 0.6)]
+        dq = [s(0, 1, 0.2), s(1, 0, 2.2), s(1, 1, 0.8), s(-1, 1, 1.7)]
+        lhs, rhs = oracle.pde_duality_2d(G, g, q, 0.05 * s(1, 1, 1.1), a, dq)
+        gaps.append(abs(lhs - rhs) / abs(lhs))
+    assert gaps[0] > gaps[1] > gaps[2]
+    assert gaps[2] < 1e-12
+
+
+def test_pde_adjoint_unknown_objective_raises(oracle):
+    G = oracle.Grid2D(2, 2, 2)
+    q = [np.zeros(G.N), np.zeros(G.N), np.ones(G.N), np.full(G.N, 2.5)]
+    snaps, n = oracle.run_forward_store_2d(G, 1.4, 0.0, 0.01, 0.02, 1, "pcg", q)
+    with pytest.raises(ValueError):
+        oracle.run_adjoint_conservative_2d(G, snaps, n, 0.01, 0.02, 1.4, 0.0, 1, "entropy", "pcg")
