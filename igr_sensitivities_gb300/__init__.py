@@ -22,6 +22,8 @@ __all__ = [
     "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
     "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch_meshes", "adjoint_batch", "objective_value",
     "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
+    "Snapshots", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
+    "adjoint_conservative_ic", "adjoint_conservative_batch",
 ]
 
 SOLVERS = {"pcg": 0, "jacobi": 1, "chebyshev": 2}
@@ -388,3 +390,137 @@ def solve_elliptic_(Sigma, mux, muy, rho, E, basis, mesh, alpha, n_iter=10, solv
     check(ctx, lib().igr2d_solve_elliptic(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(alpha), C.c_int(n_iter),
                                           C.c_int(_solver(solver)), *[_ptr(a) for a in q], _ptr(S)))
     Sigma[...] = S.reshape(shape, order="F")
+
+
+# ---------------------------------------------------------------------------
+# Continuous adjoint (IGR_adjoints_2d/adjoint_pde.jl, forward.jl:111-158)
+# ---------------------------------------------------------------------------
+class Snapshots:
+    """The snapshot list run_forward_store returns (forward.jl:111-158):
+    snapshots[k] is the tuple (mux, muy, rho, E, Sigma) after step k (k = 0:
+    the initial state), each an (n_p, n_p, N_ex, N_ey) view in Julia order;
+    len() = n_steps + 1 and negative indices count from the end, as
+    snapshots[end] does in Julia. `data` is the flat (n_steps + 1, 5, N)
+    buffer the C ABI reads and writes."""
+
+    def __init__(self, data, shape):
+        self.data = data
+        self.shape = tuple(shape)
+
+    def __len__(self):
+        return self.data.shape[0]
+
+    def __getitem__(self, k):
+        return tuple(self.data[k, v].reshape(self.shape, order="F") for v in range(5))
+
+    @classmethod
+    def from_list(cls, snaps, shape):
+        n = int(np.prod(shape))
+        data = np.stack([np.stack([_flat(a, n) for a in snap]) for snap in snaps])
+        return cls(np.ascontiguousarray(data), shape)
+
+
+def run_forward_store(mux0, muy0, rho0, E0, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
+    """run_forward_store (IGR_adjoints_2d/forward.jl:111-158): returns
+    (snapshots, n_steps) with snapshots[0] at t = 0 and snapshots[-1] at T."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    if not (dt > 0 and T > 0):
+        raise ValueError("dt and T must be positive")
+    steps = int(np.ceil(T / dt))
+    data = np.zeros((steps + 1, 5, n))
+    ns = C.c_int(0)
+    q = [_flat(a, n) for a in (mux0, muy0, rho0, E0)]
+    check(ctx, lib().igr2d_run_forward_store(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma),
+                                             C.c_double(alpha), C.c_double(dt), C.c_double(T), C.c_int(n_iter),
+                                             C.c_int(_solver(solver)), *[_ptr(a) for a in q], _ptr(data),
+                                             C.c_longlong(data.size), C.byref(ns)))
+    return Snapshots(data, shape), ns.value
+
+
+def run_adjoint_conservative(snapshots, n_steps, dt, T, basis, mesh, gamma, alpha, n_iter=10, objective="l2_density",
+                             solver="pcg", obj_params=None, ctx=None):
+    """run_adjoint_conservative (IGR_adjoints_2d/adjoint_pde.jl:527-611):
+    the adjoint (a_mux, a_muy, a_rho, a_E) at t = 0, integrated backward over
+    the snapshots of run_forward_store (a Snapshots or a list of 5-tuples)."""
+    _solver(solver)  # validate before touching the device
+    _objective(objective)
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    if not isinstance(snapshots, Snapshots):
+        snapshots = Snapshots.from_list(snapshots, shape)
+    data = np.ascontiguousarray(snapshots.data, dtype=np.float64)
+    out = [np.zeros(n) for _ in range(4)]
+    check(ctx, lib().igr2d_run_adjoint_conservative(ctx.handle, C.byref(_disc2d(basis, mesh)), _ptr(data),
+                                                    C.c_longlong(data.size), C.c_int(n_steps), C.c_double(dt),
+                                                    C.c_double(T), C.c_double(gamma), C.c_double(alpha),
+                                                    C.c_int(n_iter), C.c_int(_objective(objective)),
+                                                    C.c_int(_solver(solver)), _ptr(_prm(obj_params)),
+                                                    *[_ptr(a) for a in out]))
+    return tuple(np.asfortranarray(a.reshape(shape, order="F")) for a in out)
+
+
+def compute_adjoint_rhs_conservative_(damux, damuy, darho, daE, amux, amuy, arho, aE, mux, muy, rho, E, Sigma, Pi,
+                                      basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
+    """compute_adjoint_rhs_conservative! (IGR_adjoints_2d/adjoint_pde.jl:481-516):
+    the adjoint operator applied to a at the state (q, Sigma); Pi is the warm
+    start of the Pi solve and holds its result on return (alpha > 0)."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(x, n) for x in (mux, muy, rho, E, Sigma)]
+    a = [_flat(x, n) for x in (amux, amuy, arho, aE)]
+    P = _flat(Pi, n).copy()
+    out = [np.zeros(n) for _ in range(4)]
+    check(ctx, lib().igr2d_adjoint_rhs_conservative(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma),
+                                                    C.c_double(alpha), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                                    *[_ptr(x) for x in q], _ptr(P), *[_ptr(x) for x in a],
+                                                    *[_ptr(x) for x in out]))
+    for dst, src in zip((damux, damuy, darho, daE), out):
+        dst[...] = src.reshape(shape, order="F")
+    Pi[...] = P.reshape(shape, order="F")
+
+
+def adjoint_conservative_ic(mux0, muy0, rho0, E0, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",
+                            objective="l2_density", obj_params=None, ctx=None):
+    """run_forward_store followed by run_adjoint_conservative (as
+    IGR_adjoints_2d/tests/run_adjoint_test.jl:59-62 pairs them) with the
+    snapshots kept on the GPU; returns (a_mux, a_muy, a_rho, a_E) at t = 0."""
+    _solver(solver)  # validate before touching the device
+    _objective(objective)
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(x, n) for x in (mux0, muy0, rho0, E0)]
+    out = [np.zeros(n) for _ in range(4)]
+    check(ctx, lib().igr2d_adjoint_conservative_ic(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma),
+                                                   C.c_double(alpha), C.c_double(dt), C.c_double(T), C.c_int(n_iter),
+                                                   C.c_int(_solver(solver)), C.c_int(_objective(objective)),
+                                                   _ptr(_prm(obj_params)), *[_ptr(x) for x in q],
+                                                   *[_ptr(x) for x in out]))
+    return tuple(np.asfortranarray(a.reshape(shape, order="F")) for a in out)
+
+
+def adjoint_conservative_batch(q0, gammas, alphas, dts, T, basis, mesh, n_iter=10, solver="pcg",
+                               objective="l2_density", obj_params=None, ctx=None):
+    """Batched adjoint_conservative_ic over instances on one mesh: q0 is
+    (n_inst, 4, N) in the Julia node order; returns the adjoints at t = 0 in
+    the same layout. ceil(T / dts[i]) must agree across instances."""
+    _solver(solver)  # validate before touching the device
+    _objective(objective)
+    ctx = ctx or default_context()
+    gammas = np.ascontiguousarray(gammas, dtype=np.float64)
+    alphas = np.ascontiguousarray(alphas, dtype=np.float64)
+    dts = np.ascontiguousarray(dts, dtype=np.float64)
+    q0 = np.ascontiguousarray(q0, dtype=np.float64)
+    a0 = np.zeros_like(q0)
+    check(ctx, lib().igr2d_adjoint_conservative_batch(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_int(gammas.size),
+                                                      _ptr(gammas), _ptr(alphas), _ptr(dts), C.c_double(T),
+                                                      C.c_int(n_iter), C.c_int(_solver(solver)),
+                                                      C.c_int(_objective(objective)), _ptr(_prm(obj_params)), _ptr(q0),
+                                                      _ptr(a0)))
+    return a0

@@ -458,6 +458,193 @@ int igr2d_adjoint_batch_dev(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const
   });
 }
 
+namespace {
+// Device memory the continuous adjoint may use for snapshots: the budget set
+// on the context, else free memory (plus what the snapshot buffers already
+// hold) less a reserve.
+size_t snapshot_budget(Ctx& c) {
+  if (c.tape_budget) return c.tape_budget;
+  size_t fr = 0, tot = 0;
+  cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+  const size_t avail = fr + c.ws.held("capi:snaps");
+  const size_t reserve = (size_t)2 << 30;
+  return avail > reserve ? avail - reserve : 0;
+}
+
+int store_steps(double dt, double t_end) {
+  if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+  return (int)std::ceil(t_end / dt);  // forward.jl:131-132
+}
+}  // namespace
+
+int igr2d_run_forward_store(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
+                            int n_iter, int solver, const double* mux0, const double* muy0, const double* rho0,
+                            const double* E0, double* snapshots, long long snapshots_len, int* n_steps) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    const int n = store_steps(dt, t_end);
+    Plan2D P = plan_single(c, d, gamma, alpha, t_end / n, "fst");
+    const long long N = P.NG;
+    if (!snapshots || !n_steps || snapshots_len != (long long)(n + 1) * 5 * N)
+      throw Error(IGR_EINVAL, "snapshots must hold (ceil(T/dt) + 1) * 5 * N doubles");
+    const Solve2DOpts o{n_iter, solver};
+    const double* in[4] = {mux0, muy0, rho0, E0};
+    const size_t bytes = (size_t)(n + 1) * 5 * N * sizeof(double);
+    if (bytes <= snapshot_budget(c)) {
+      double* S = c.ws.dbl("capi:snaps", (size_t)(n + 1) * 5 * N);
+      for (int v = 0; v < 4; ++v) h2d(c, S + v * N, in[v], N);
+      const double* q0[4] = {S, S + N, S + 2 * N, S + 3 * N};
+      forward_store_init2d(c, P, o, q0, S);
+      forward_store_range2d(c, P, o, [&](int k) { return S + (long long)k * 5 * N; }, 0, n);
+      d2h(c, snapshots, S, (long long)(n + 1) * 5 * N);
+    } else {  // two device slots, each snapshot copied out after its step
+      double* S = c.ws.dbl("capi:snaps", (size_t)2 * 5 * N);
+      for (int v = 0; v < 4; ++v) h2d(c, S + v * N, in[v], N);
+      const double* q0[4] = {S, S + N, S + 2 * N, S + 3 * N};
+      forward_store_init2d(c, P, o, q0, S);
+      auto ring = [&](int k) { return S + (long long)(k % 2) * 5 * N; };
+      d2h(c, snapshots, S, 5 * N);
+      for (int k = 0; k < n; ++k) {
+        forward_store_range2d(c, P, o, ring, k, k + 1);
+        d2h(c, snapshots + (long long)(k + 1) * 5 * N, ring(k + 1), 5 * N);
+      }
+    }
+    sync(c);
+    *n_steps = n;
+  });
+}
+
+int igr2d_run_adjoint_conservative(igr_ctx* ctx, const igr_disc2d* d, const double* snapshots, long long snapshots_len,
+                                   int n_steps, double dt, double t_end, double gamma, double alpha, int n_iter,
+                                   int objective, int solver, const double* obj_params, double* amux, double* amuy,
+                                   double* arho, double* aE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    if (objective < 0 || objective > IGR_OBJ_WINDOW_RHO2) throw Error(IGR_EINVAL, "Unknown objective");
+    if (n_steps < 0) throw Error(IGR_EINVAL, "n_steps must be >= 0");
+    if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+    Plan2D P = plan_single(c, d, gamma, alpha, std::min(dt, t_end), "pdea");  // adjoint_pde.jl:587
+    const long long N = P.NG;
+    if (!snapshots || snapshots_len < (long long)(n_steps + 1) * 5 * N)
+      throw Error(IGR_EINVAL, "snapshots must hold (n_steps + 1) * 5 * N doubles");
+    const Solve2DOpts o{n_iter, solver};
+    double* out = c.ws.dbl("capi:aout", 4 * (size_t)N);
+    double* ao[4] = {out, out + N, out + 2 * N, out + 3 * N};
+    const size_t bytes = (size_t)(n_steps + 1) * 5 * N * sizeof(double);
+    if (bytes <= snapshot_budget(c)) {
+      double* S = c.ws.dbl("capi:snaps", (size_t)(n_steps + 1) * 5 * N);
+      h2d(c, S, snapshots, (long long)(n_steps + 1) * 5 * N);
+      pde_adjoint2d(c, P, n_steps, o, objective, obj_params, [&](int k) { return S + (long long)k * 5 * N; }, ao);
+    } else {  // upload each snapshot just before its step (two device slots, stream-ordered)
+      double* S = c.ws.dbl("capi:snaps", (size_t)2 * 5 * N);
+      auto ring = [&](int k) {
+        double* dst = S + (long long)(k % 2) * 5 * N;
+        h2d(c, dst, snapshots + (long long)k * 5 * N, 5 * N);
+        return dst;
+      };
+      pde_adjoint2d(c, P, n_steps, o, objective, obj_params, ring, ao);
+    }
+    double* outs[4] = {amux, amuy, arho, aE};
+    for (int v = 0; v < 4; ++v) d2h(c, outs[v], ao[v], N);
+    sync(c);
+  });
+}
+
+int igr2d_adjoint_conservative_ic(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt,
+                                  double t_end, int n_iter, int solver, int objective, const double* obj_params,
+                                  const double* mux0, const double* muy0, const double* rho0, const double* E0,
+                                  double* amux, double* amuy, double* arho, double* aE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    if (objective < 0 || objective > IGR_OBJ_WINDOW_RHO2) throw Error(IGR_EINVAL, "Unknown objective");
+    const int n = store_steps(dt, t_end);
+    Plan2D Pf = plan_single(c, d, gamma, alpha, t_end / n, "pdef");
+    Plan2D Pa = plan_single(c, d, gamma, alpha, std::min(dt, t_end), "pdea");
+    const long long N = Pf.NG;
+    double* buf = c.ws.dbl("capi:pdeq", 8 * (size_t)N);
+    double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* ao[4] = {buf + 4 * N, buf + 5 * N, buf + 6 * N, buf + 7 * N};
+    const double* in[4] = {mux0, muy0, rho0, E0};
+    for (int v = 0; v < 4; ++v) h2d(c, q[v], in[v], N);
+    const double* qc[4] = {q[0], q[1], q[2], q[3]};
+    const Solve2DOpts o{n_iter, solver};
+    pde_adjoint_ic2d(c, Pf, Pa, qc, n, o, objective, obj_params, ao);
+    double* outs[4] = {amux, amuy, arho, aE};
+    for (int v = 0; v < 4; ++v) d2h(c, outs[v], ao[v], N);
+    sync(c);
+  });
+}
+
+int igr2d_adjoint_conservative_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas,
+                                     const double* alphas, const double* dts, double t_end, int n_iter, int solver,
+                                     int objective, const double* obj_params, const double* q0, double* a0) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc(d);
+    check_solver(solver, n_iter);
+    if (objective < 0 || objective > IGR_OBJ_WINDOW_RHO2) throw Error(IGR_EINVAL, "Unknown objective");
+    if (n_inst < 1 || !gammas || !alphas || !dts || !q0 || !a0) throw Error(IGR_EINVAL, "bad batch arguments");
+    const int n = store_steps(dts[0], t_end);
+    for (int b = 1; b < n_inst; ++b)
+      if (store_steps(dts[b], t_end) != n) throw Error(IGR_EINVAL, "ceil(T/dt) must be the same for every instance");
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    std::vector<Inst2DDesc> fi, ai;
+    for (int b = 0; b < n_inst; ++b) {
+      fi.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], alphas[b], t_end / n});
+      ai.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], alphas[b], std::min(dts[b], t_end)});
+    }
+    Plan2D Pf = make_plan2d(c, B, fi, "pdef");
+    Plan2D Pa = make_plan2d(c, B, ai, "pdea");
+    const long long N = nodes2d(d), NG = Pf.NG;
+    double* buf = c.ws.dbl("capi:pdeq", 8 * (size_t)NG);
+    double* q[4];
+    double* ao[4];
+    for (int v = 0; v < 4; ++v) { q[v] = buf + v * NG; ao[v] = buf + (4 + v) * NG; }
+    for (int v = 0; v < 4; ++v)  // [inst][var][N] -> field-major [var][inst*N]
+      cuda_check(cudaMemcpy2DAsync(q[v], N * sizeof(double), q0 + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyHostToDevice, c.stream), "gather q0");
+    const double* qc[4] = {q[0], q[1], q[2], q[3]};
+    const Solve2DOpts o{n_iter, solver};
+    pde_adjoint_ic2d(c, Pf, Pa, qc, n, o, objective, obj_params, ao);
+    for (int v = 0; v < 4; ++v)
+      cuda_check(cudaMemcpy2DAsync(a0 + v * N, 4 * N * sizeof(double), ao[v], N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyDeviceToHost, c.stream), "scatter a0");
+    sync(c);
+  });
+}
+
+int igr2d_adjoint_rhs_conservative(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_iter,
+                                   int solver, const double* mux, const double* muy, const double* rho,
+                                   const double* E, const double* sigma, double* pi, const double* amux,
+                                   const double* amuy, const double* arho, const double* aE, double* damux,
+                                   double* damuy, double* darho, double* daE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    Plan2D P = plan_single(c, d, gamma, alpha, 0.0, "pder");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:pder", 14 * (size_t)N);
+    const double* qin[5] = {mux, muy, rho, E, sigma};
+    for (int v = 0; v < 5; ++v) h2d(c, buf + v * N, qin[v], N);
+    double* Pi = buf + 5 * N;
+    if (alpha > 0) h2d(c, Pi, pi, N);
+    const double* ain[4] = {amux, amuy, arho, aE};
+    double* a[4];
+    double* da[4];
+    for (int v = 0; v < 4; ++v) { a[v] = buf + (6 + v) * N; da[v] = buf + (10 + v) * N; h2d(c, a[v], ain[v], N); }
+    const double* ac[4] = {a[0], a[1], a[2], a[3]};
+    const Solve2DOpts o{n_iter, solver};
+    pde_adjoint_rhs2d(c, P, o, buf, Pi, ac, da);
+    double* outs[4] = {damux, damuy, darho, daE};
+    for (int v = 0; v < 4; ++v) d2h(c, outs[v], da[v], N);
+    if (alpha > 0) d2h(c, pi, Pi, N);
+    sync(c);
+  });
+}
+
 int igr2d_apply_sip(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* x, const double* rho, double* y) {
   return guarded(ctx, [&] {
     Ctx& c = ctx->c;

@@ -7,6 +7,7 @@
 #include "igr2d_kernels.cuh"
 #include "igr2d_launch.h"
 #include "igr2d_pcg_kernels.cuh"
+#include "igr2d_pde_kernels.cuh"
 #include "igr2d_rev_kernels.cuh"
 #include "igr2d_sens_kernels.cuh"
 #include "igr_engine.h"
@@ -1095,6 +1096,345 @@ __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
   }
   const double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
   if (s == 1234.5) out[threadIdx.x] = s;  // never true; keeps the chains live
+}
+
+// ------------------------------------------------------------------------------------------
+// Continuous adjoint: run_forward_store (forward.jl:111-158) and
+// run_adjoint_conservative (adjoint_pde.jl:527-611)
+// ------------------------------------------------------------------------------------------
+
+// Terminal condition of run_adjoint_conservative (adjoint_pde.jl:542-584): the
+// L2 gradient density of J at t = T (no quadrature weights). s1/s2 hold the
+// per-instance kinetic energy and mass sums for the kinetic-energy objective.
+__global__ void k2_pde_terminal(ObjArgs2D a) {
+  const double pi = 3.14159265358979323846;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < a.NG; n += (long long)gridDim.x * blockDim.x) {
+    const int ii = find_inst(a.inst, a.ninst, n);
+    const Inst2D I = a.inst[ii];
+    double c, x, y;
+    node_coords2d(a.B, I, n - I.off, &c, &x, &y);
+    const double mx = a.q[0][n], my = a.q[1][n], r = a.q[2][n], E = a.q[3][n];
+    const double ux = mx / r, uy = my / r;
+    double g0 = 0, g1 = 0, g2 = 0, g3 = 0;
+    switch (a.obj) {
+      case OBJ_L2_DENSITY: g2 = 2.0 * r; break;
+      case OBJ_L2_PRESSURE: {
+        const double gm = I.gamma - 1.0;
+        const double P = gm * (E - (mx * mx + my * my) / (2.0 * r));
+        g0 = -2.0 * gm * P * ux; g1 = -2.0 * gm * P * uy; g2 = gm * P * (ux * ux + uy * uy); g3 = 2.0 * gm * P;
+        break;
+      }
+      case OBJ_KINETIC_ENERGY: {
+        const double KE = a.s1[ii], Ms = a.s2[ii];
+        g0 = ux / Ms; g1 = uy / Ms;
+        g2 = -(mx * mx + my * my) / (2.0 * (r * r)) / Ms - KE / (Ms * Ms);
+        break;
+      }
+      case OBJ_WINDOWED_KE: {
+        const double wx = exp(-((x - 0.55) * (x - 0.55) + (y - 0.50) * (y - 0.50)) / (0.15 * 0.15));
+        g0 = wx * ux; g1 = wx * uy; g2 = -wx * (ux * ux + uy * uy) / 2.0;
+        break;
+      }
+      case OBJ_WEIGHTED_MOMENTUM: g0 = sin(2 * pi * x / I.lx) * sin(2 * pi * y / I.ly); break;
+      case OBJ_WINDOW_RHO2: {
+        const bool in = x >= a.prm[0] && x <= a.prm[0] + a.prm[2] && y >= a.prm[1] && y <= a.prm[1] + a.prm[2];
+        g2 = in ? 2.0 * r : 0.0;
+        break;
+      }
+      default: break;
+    }
+    a.qb[0][n] = g0; a.qb[1][n] = g1; a.qb[2][n] = g2; a.qb[3][n] = g3;
+  }
+}
+
+void forward_store_init2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const double* const q0[4], double* snap0) {
+  const long long NG = P.NG;
+  for (int v = 0; v < 4; ++v)
+    if (snap0 + v * NG != q0[v])
+      cuda_check(cudaMemcpyAsync(snap0 + v * NG, q0[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "snapshot 0");
+  double* Sig = snap0 + 4 * NG;
+  double* zero = c.ws.dbl("fst:zero", NG);
+  cuda_check(cudaMemsetAsync(zero, 0, NG * sizeof(double), c.stream), "zero");
+  if (!any_alpha_pos(P)) {
+    cuda_check(cudaMemsetAsync(Sig, 0, NG * sizeof(double), c.stream), "zero Sigma");
+    return;
+  }
+  StageBuf st = stage_from(c.ws.dbl("fst:stages", (size_t)NG * 3 * STAGE_FIXED_FIELDS), NG, o, true, false, (int)P.inst.size());
+  for (int v = 0; v < 4; ++v) st.q[v] = snap0 + v * NG;
+  recip(c, st.q[2], st.invr, NG);
+  st.Sout = Sig;
+  stage_solve(c, P, o, st, zero, c.ws.dbl("fst:xa", NG), c.ws.dbl("fst:xb", NG), c.ws.dbl("fst:d", NG));
+}
+
+void forward_store_range2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const SnapSlot& slot, int k0, int k1) {
+  check_alpha_uniform(P);
+  const long long NG = P.NG;
+  const int ni = (int)P.inst.size();
+  const bool apos = any_alpha_pos(P);
+  double* scratch = c.ws.dbl("fst:stages", (size_t)NG * 3 * STAGE_FIXED_FIELDS);
+  StageBuf st[3];
+  for (int s = 0; s < 3; ++s) st[s] = stage_from(scratch + (long long)s * STAGE_FIXED_FIELDS * NG, NG, o, apos, false, ni);
+  double* xa = c.ws.dbl("fst:xa", NG);
+  double* xb = c.ws.dbl("fst:xb", NG);
+  double* db = c.ws.dbl("fst:d", NG);
+  double* sA = c.ws.dbl("fst:sA", NG);
+  double* sB = c.ws.dbl("fst:sB", NG);
+  double* zero = c.ws.dbl("fst:zero", NG);
+  if (k1 <= k0) return;
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  if (!apos) cuda_check(cudaMemsetAsync(zero, 0, NG * sizeof(double), c.stream), "zero");
+  {
+    const double* s0 = slot(k0);
+    recip(c, s0 + 2 * NG, st[0].invr, NG);
+  }
+  for (int k = k0; k < k1; ++k) {
+    double* cur = slot(k);
+    double* nxt = slot(k + 1);
+    for (int v = 0; v < 4; ++v) st[0].q[v] = cur + v * NG;
+    for (int s = 0; s < 3; ++s) st[s].Sout = !apos ? zero : ((s % 2 == 0) ? sA : sB);
+    double* qo[4] = {nxt, nxt + NG, nxt + 2 * NG, nxt + 3 * NG};
+    // the last stage writes 1/rho of the new state into st[0].invr (read by the post-step solve)
+    step_forward(c, P, o, st, cur + 4 * NG, qo, st[0].invr, xa, xb, db);
+    if (apos) {  // forward.jl:152-154: one more solve on the new state, warm start = stage-3 Sigma
+      StageBuf post = st[0];
+      for (int v = 0; v < 4; ++v) post.q[v] = qo[v];
+      post.Sout = nxt + 4 * NG;
+      stage_solve(c, P, o, post, st[2].Sout, xa, xb, db);
+    } else {
+      cuda_check(cudaMemsetAsync(nxt + 4 * NG, 0, NG * sizeof(double), c.stream), "zero Sigma");
+    }
+  }
+  check_status(c);
+}
+
+namespace {
+// Device buffers of the continuous adjoint.
+struct PdeWork {
+  double* a[4]; double* a1[4]; double* a2[4];
+  double* Pi[2];
+  int cur = 0;
+  double* b;
+  double* invr; double* src[PDE_SRC]; double* nl[PDE_NL]; double* wsx; double* wsy;
+  StageBuf st;
+  double *xa, *xb, *db;
+};
+}  // namespace
+
+static PdeWork pde_work(Ctx& c, const Plan2D& P, const Solve2DOpts& o) {
+  const long long NG = P.NG;
+  PdeWork w;
+  double* f = c.ws.dbl("pde:fields", (size_t)NG * (12 + 2 + 1 + 1 + PDE_SRC + PDE_NL + 2 + 3));
+  int k = 0;
+  auto nxt = [&]() { return f + (long long)(k++) * NG; };
+  for (int v = 0; v < 4; ++v) { w.a[v] = nxt(); w.a1[v] = nxt(); w.a2[v] = nxt(); }
+  w.Pi[0] = nxt(); w.Pi[1] = nxt();
+  w.b = nxt(); w.invr = nxt();
+  for (int v = 0; v < PDE_SRC; ++v) w.src[v] = nxt();
+  for (int v = 0; v < PDE_NL; ++v) w.nl[v] = nxt();
+  w.wsx = nxt(); w.wsy = nxt();
+  w.xa = nxt(); w.xb = nxt(); w.db = nxt();
+  w.st = stage_from(c.ws.dbl("pde:stage", (size_t)NG * STAGE_FIXED_FIELDS), NG, o, true, false, (int)P.inst.size());
+  return w;
+}
+
+// Per-step preparation from one snapshot and, with alpha > 0, the SIP
+// operator coefficients of its density (compute_sip_diagonal + the operator
+// the Pi solve applies, adjoint_pde.jl:495-502).
+static void pde_prep(Ctx& c, const Plan2D& P, PdeWork& w, const double* snap, bool apos) {
+  const long long NG = P.NG;
+  PdePrepArgs2D p;
+  std::memset(&p, 0, sizeof(p));
+  p.tiles = P.d_tiles; p.inst = P.d_inst; p.B = P.B;
+  for (int v = 0; v < 4; ++v) p.q[v] = snap + v * NG;
+  p.S = snap + 4 * NG;
+  p.invr = w.invr;
+  for (int v = 0; v < PDE_SRC; ++v) p.src[v] = w.src[v];
+  for (int v = 0; v < PDE_NL; ++v) p.nl[v] = apos ? w.nl[v] : nullptr;
+  p.ws_x = w.wsx; p.ws_y = w.wsy;
+  {
+    LaunchScope ls(c, KID_PDE);
+    NP_DISPATCH(P.np, launch_k2_pde_prep<NPV>(p, P.ntiles(), c.stream));
+  }
+  if (apos) {
+    for (int v = 0; v < 4; ++v) w.st.q[v] = const_cast<double*>(snap + v * NG);
+    w.st.invr = w.invr;
+    stage_setup(c, P, w.st);
+  }
+}
+
+// Pi solve of one stage (adjoint_pde.jl:487-502): b from the stage input,
+// warm start = the current Pi; the result becomes the current Pi.
+static void pde_pi_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, PdeWork& w, const double* snap,
+                         const double* const ain[4]) {
+  const long long NG = P.NG;
+  PdeBArgs2D b;
+  std::memset(&b, 0, sizeof(b));
+  b.tiles = P.d_tiles; b.inst = P.d_inst; b.B = P.B;
+  for (int v = 0; v < 4; ++v) b.a[v] = ain[v];
+  b.mx = snap; b.my = snap + NG; b.invr = w.invr;
+  b.b = w.b;
+  {
+    LaunchScope ls(c, KID_PDE);
+    NP_DISPATCH(P.np, launch_k2_pde_b<NPV>(b, P.ntiles(), c.stream));
+  }
+  stage_solve_b(c, P, o, w.st, w.b, w.Pi[w.cur], w.Pi[1 - w.cur], false, w.xa, w.xb, w.db);
+  w.cur = 1 - w.cur;
+}
+
+static PdeRkArgs2D pde_rk_args(const Plan2D& P, const PdeWork& w, const double* snap, bool apos) {
+  const long long NG = P.NG;
+  PdeRkArgs2D r;
+  std::memset(&r, 0, sizeof(r));
+  r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
+  for (int v = 0; v < 4; ++v) r.q[v] = snap + v * NG;
+  r.S = snap + 4 * NG; r.invr = w.invr; r.ws_x = w.wsx; r.ws_y = w.wsy;
+  for (int v = 0; v < PDE_SRC; ++v) r.src[v] = w.src[v];
+  for (int v = 0; v < PDE_NL; ++v) r.nl[v] = w.nl[v];
+  r.Pi = apos ? w.Pi[w.cur] : nullptr;
+  return r;
+}
+
+// One backward SSP-RK3 step over one snapshot (adjoint_pde.jl:586-608):
+// a -> a1 -> a2 -> a.
+static void pde_step(Ctx& c, const Plan2D& P, const Solve2DOpts& o, PdeWork& w, const double* snap, bool apos) {
+  pde_prep(c, P, w, snap, apos);
+  double* const* ins[3] = {w.a, w.a1, w.a2};
+  double* const* outs[3] = {w.a1, w.a2, w.a};
+  for (int s = 0; s < 3; ++s) {
+    const double* ain[4] = {ins[s][0], ins[s][1], ins[s][2], ins[s][3]};
+    if (apos) pde_pi_solve(c, P, o, w, snap, ain);
+    PdeRkArgs2D r = pde_rk_args(P, w, snap, apos);
+    for (int v = 0; v < 4; ++v) { r.a[v] = ain[v]; r.an[v] = w.a[v]; r.ao[v] = outs[s][v]; }
+    r.c0 = RK_C0[s]; r.c1 = RK_C1[s]; r.c2 = RK_C2[s];
+    LaunchScope ls(c, KID_PDE);
+    NP_DISPATCH(P.np, launch_k2_pde_rk<NPV>(r, P.ntiles(), c.stream));
+  }
+}
+
+static void pde_terminal(Ctx& c, const Plan2D& P, PdeWork& w, const double* snapT, int objective, const double* prm) {
+  const long long NG = P.NG;
+  const int ni = (int)P.inst.size();
+  const double* qT[4] = {snapT, snapT + NG, snapT + 2 * NG, snapT + 3 * NG};
+  ObjArgs2D a = obj_args(P, qT, objective, prm);
+  double* s1 = c.ws.dbl("pde:s1", ni);
+  double* s2 = c.ws.dbl("pde:s2", ni);
+  if (objective == OBJ_KINETIC_ENERGY) {
+    a.j1 = c.ws.dbl("obj:j1", NG);
+    a.j2 = c.ws.dbl("obj:j2", NG);
+    { LaunchScope ls(c, KID_OTHER); k2_obj_nodes<<<grid_for(NG), 256, 0, c.stream>>>(a); }
+    inst_sums(c, P, a.j1, s1);
+    inst_sums(c, P, a.j2, s2);
+  }
+  a.s1 = s1; a.s2 = s2;
+  for (int v = 0; v < 4; ++v) a.qb[v] = w.a[v];
+  LaunchScope ls(c, KID_OTHER);
+  k2_pde_terminal<<<grid_for(NG), 256, 0, c.stream>>>(a);
+}
+
+// Adjoint steps n = n_hi .. n_lo + 1 over slot(n).
+static void pde_steps(Ctx& c, const Plan2D& P, const Solve2DOpts& o, PdeWork& w, const SnapSlot& slot, int n_hi, int n_lo) {
+  const bool apos = any_alpha_pos(P);
+  for (int n = n_hi; n > n_lo; --n) pde_step(c, P, o, w, slot(n), apos);
+}
+
+static void pde_checks(const Plan2D& P, const Solve2DOpts& o, int objective, int n_steps) {
+  check_objective(objective);
+  check_solver(o);
+  check_alpha_uniform(P);
+  if (n_steps < 0) throw Error(1, "n_steps must be >= 0");
+}
+
+void pde_adjoint2d(Ctx& c, const Plan2D& P, int n_steps, const Solve2DOpts& o, int objective, const double* prm,
+                   const SnapSlot& slot, double* const a_out[4]) {
+  pde_checks(P, o, objective, n_steps);
+  const long long NG = P.NG;
+  PdeWork w = pde_work(c, P, o);
+  pde_terminal(c, P, w, slot(n_steps), objective, prm);
+  cuda_check(cudaMemsetAsync(w.Pi[0], 0, NG * sizeof(double), c.stream), "zero Pi");
+  w.cur = 0;
+  pde_steps(c, P, o, w, slot, n_steps, 0);
+  for (int v = 0; v < 4; ++v)
+    cuda_check(cudaMemcpyAsync(a_out[v], w.a[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "adjoint out");
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void pde_adjoint_ic2d(Ctx& c, const Plan2D& Pf, const Plan2D& Pa, const double* const q0[4], int n_steps,
+                      const Solve2DOpts& o, int objective, const double* prm, double* const a_out[4]) {
+  pde_checks(Pa, o, objective, n_steps);
+  check_alpha_uniform(Pf);
+  const long long NG = Pf.NG;
+  const size_t snap = (size_t)5 * NG * sizeof(double);
+  size_t budget = c.tape_budget;
+  if (budget == 0) {
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    const size_t avail = fr + c.ws.held("pde:snaps") + c.ws.held("pde:ckpt") + c.ws.held("pde:seg");
+    const size_t reserve = (size_t)2 << 30;
+    budget = avail > reserve ? avail - reserve : 0;
+  }
+  const int n = n_steps;
+  if ((size_t)(n + 1) * snap <= budget) {  // every snapshot resident
+    c.plan_seg = std::max(n, 1);
+    c.plan_nseg = 1;
+    double* S = c.ws.dbl("pde:snaps", (size_t)(n + 1) * 5 * NG);
+    auto slot = [&](int k) { return S + (long long)k * 5 * NG; };
+    forward_store_init2d(c, Pf, o, q0, slot(0));
+    forward_store_range2d(c, Pf, o, slot, 0, n);
+    pde_adjoint2d(c, Pa, n, o, objective, prm, slot, a_out);
+    return;
+  }
+  // checkpoints at k = 0, K, 2K, ... and one recomputed segment of K snapshots
+  int K = (int)std::ceil(std::sqrt((double)n));
+  const size_t need = ((size_t)(n / K + 1) + (size_t)K + 2) * snap;
+  if (need > budget) throw Error(5, "device memory too small for the snapshots of the continuous adjoint");
+  const int nseg = (n + K - 1) / K;
+  c.plan_seg = K;
+  c.plan_nseg = nseg;
+  double* ck = c.ws.dbl("pde:ckpt", (size_t)(n / K + 1) * 5 * NG);
+  double* sg = c.ws.dbl("pde:seg", (size_t)(K + 2) * 5 * NG);
+  auto pass1 = [&](int k) {
+    return k % K == 0 ? ck + (long long)(k / K) * 5 * NG : sg + (long long)(k % 2) * 5 * NG;
+  };
+  forward_store_init2d(c, Pf, o, q0, pass1(0));
+  forward_store_range2d(c, Pf, o, pass1, 0, n);
+  pde_checks(Pa, o, objective, n);
+  PdeWork w = pde_work(c, Pa, o);
+  pde_terminal(c, Pa, w, pass1(n), objective, prm);
+  cuda_check(cudaMemsetAsync(w.Pi[0], 0, NG * sizeof(double), c.stream), "zero Pi");
+  w.cur = 0;
+  for (int s = nseg - 1; s >= 0; --s) {
+    const int k0 = s * K, k1 = std::min(n, k0 + K);
+    auto seg = [&](int k) { return k == k0 ? ck + (long long)(k0 / K) * 5 * NG : sg + (long long)(k - k0 - 1) * 5 * NG; };
+    forward_store_range2d(c, Pf, o, seg, k0, k1);
+    pde_steps(c, Pa, o, w, seg, k1, k0);
+  }
+  for (int v = 0; v < 4; ++v)
+    cuda_check(cudaMemcpyAsync(a_out[v], w.a[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "adjoint out");
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void pde_adjoint_rhs2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const double* snap, double* Pi,
+                       const double* const a[4], double* const da[4]) {
+  check_solver(o);
+  check_alpha_uniform(P);
+  const long long NG = P.NG;
+  const bool apos = any_alpha_pos(P);
+  PdeWork w = pde_work(c, P, o);
+  pde_prep(c, P, w, snap, apos);
+  if (apos) {
+    cuda_check(cudaMemcpyAsync(w.Pi[0], Pi, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Pi in");
+    w.cur = 0;
+    pde_pi_solve(c, P, o, w, snap, a);
+  }
+  PdeRkArgs2D r = pde_rk_args(P, w, snap, apos);
+  for (int v = 0; v < 4; ++v) { r.a[v] = a[v]; r.an[v] = a[v]; r.ao[v] = nullptr; r.k_out[v] = da[v]; }
+  r.c0 = 0.0; r.c1 = 1.0; r.c2 = 0.0;
+  {
+    LaunchScope ls(c, KID_PDE);
+    NP_DISPATCH(P.np, launch_k2_pde_rk<NPV>(r, P.ntiles(), c.stream));
+  }
+  if (apos) cuda_check(cudaMemcpyAsync(Pi, w.Pi[w.cur], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Pi out");
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
 }
 
 double probe_fp64_tflops(Ctx& c) {

@@ -16,6 +16,9 @@ struct ApplyRevArgs2D;
 struct SetupRevArgs2D;
 struct SensRhsArgs2D;
 struct SensHypArgs2D;
+struct PdePrepArgs2D;
+struct PdeBArgs2D;
+struct PdeRkArgs2D;
 
 template <int NP> int threads2d();
 template <int NP> void launch_k2_setup(const SetupArgs2D& a, int nblocks, cudaStream_t s);
@@ -26,6 +29,9 @@ template <int NP> void launch_k2_apply_rev(int srev, const ApplyRevArgs2D& a, in
 template <int NP> void launch_k2_setup_rev(const SetupRevArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void launch_k2_sens_rhs(const SensRhsArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void launch_k2_sens_hyp_rk(const SensHypArgs2D& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k2_pde_prep(const PdePrepArgs2D& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k2_pde_b(const PdeBArgs2D& a, int nblocks, cudaStream_t s);
+template <int NP> void launch_k2_pde_rk(const PdeRkArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void tile_shape2d(int* tx, int* ty);
 
 }  // namespace igrgpu

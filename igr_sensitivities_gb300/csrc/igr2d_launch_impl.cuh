@@ -4,6 +4,7 @@
 #include "igr2d_launch.h"
 #include "igr2d_rev_kernels.cuh"
 #include "igr2d_sens_kernels.cuh"
+#include "igr2d_pde_kernels.cuh"
 
 namespace igrgpu {
 
@@ -43,6 +44,16 @@ template <int NP> void launch_k2_sens_hyp_rk(const SensHypArgs2D& a, int nb, cud
   k2_sens_hyp_rk<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
 }
 
+template <int NP> void launch_k2_pde_prep(const PdePrepArgs2D& a, int nb, cudaStream_t s) {
+  k2_pde_prep<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_pde_b(const PdeBArgs2D& a, int nb, cudaStream_t s) {
+  k2_pde_b<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+template <int NP> void launch_k2_pde_rk(const PdeRkArgs2D& a, int nb, cudaStream_t s) {
+  k2_pde_rk<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
+}
+
 #define IGR2D_INSTANTIATE(NP)                                                                        \
   template int threads2d<NP>();                                                                      \
   template void tile_shape2d<NP>(int*, int*);                                                        \
@@ -53,6 +64,9 @@ template <int NP> void launch_k2_sens_hyp_rk(const SensHypArgs2D& a, int nb, cud
   template void launch_k2_apply_rev<NP>(int, const ApplyRevArgs2D&, int, cudaStream_t);              \
   template void launch_k2_setup_rev<NP>(const SetupRevArgs2D&, int, cudaStream_t);                    \
   template void launch_k2_sens_rhs<NP>(const SensRhsArgs2D&, int, cudaStream_t);                      \
-  template void launch_k2_sens_hyp_rk<NP>(const SensHypArgs2D&, int, cudaStream_t);
+  template void launch_k2_sens_hyp_rk<NP>(const SensHypArgs2D&, int, cudaStream_t);                   \
+  template void launch_k2_pde_prep<NP>(const PdePrepArgs2D&, int, cudaStream_t);                       \
+  template void launch_k2_pde_b<NP>(const PdeBArgs2D&, int, cudaStream_t);                             \
+  template void launch_k2_pde_rk<NP>(const PdeRkArgs2D&, int, cudaStream_t);
 
 }  // namespace igrgpu

@@ -40,7 +40,7 @@ class Workspace {
 
 // Kernel families timed by the optional per-launch CUDA-event profiler.
 enum KernelId { KID_SETUP = 0, KID_APPLY, KID_HYP, KID_HYP_REV, KID_APPLY_REV, KID_SETUP_REV, KID_TAN, KID_1D, KID_OTHER,
-                KID_COUNT };
+                KID_PDE, KID_COUNT };
 
 struct Profiler {
   bool on = false;
@@ -179,6 +179,32 @@ long long adjoint1d_scratch_fields(const Inst1DDesc& d, int N, const Solve2DOpts
 // conservative variables): J, dq0 (same layout as q0), dgamma, dalpha.
 void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Solve2DOpts& o, int objective,
                const double* prm, int seg, double* J, double* dgamma, double* dalpha);
+
+// ---- continuous adjoint (IGR_adjoints_2d/adjoint_pde.jl, forward.jl:111-158) ----
+// Snapshot k of the forward store: 5 fields of NG doubles (mux, muy, rho, E,
+// Sigma) at a device address given by the caller's slot function.
+using SnapSlot = std::function<double*(int)>;
+// run_forward_store steps k0+1..k1: snapshot k0 must hold a state and its
+// Sigma; every step is followed by one more Sigma solve on the new state,
+// which is stored and is the next step's warm start. P carries the
+// (re-rounded) forward dt.
+void forward_store_range2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const SnapSlot& slot, int k0, int k1);
+// Snapshot 0: q0 and the initial Sigma solve from zero (forward.jl:127-130).
+void forward_store_init2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const double* const q0[4], double* snap0);
+// run_adjoint_conservative (adjoint_pde.jl:527-611) over snapshots 0..n_steps
+// given by slot (each called once per adjoint step, n_steps first; a slot may
+// upload the snapshot on the way). P carries the adjoint step min(dt, T).
+void pde_adjoint2d(Ctx& c, const Plan2D& P, int n_steps, const Solve2DOpts& o, int objective, const double* prm,
+                   const SnapSlot& slot, double* const a_out[4]);
+// Forward store + adjoint with device-resident snapshots: all of them when they
+// fit in the memory budget, else checkpoints every K steps and a recomputed
+// segment of K snapshots at a time (c.plan_seg = K, c.plan_nseg = segments).
+void pde_adjoint_ic2d(Ctx& c, const Plan2D& Pf, const Plan2D& Pa, const double* const q0[4], int n_steps,
+                      const Solve2DOpts& o, int objective, const double* prm, double* const a_out[4]);
+// compute_adjoint_rhs_conservative! (adjoint_pde.jl:481-516): da from a at
+// the state (q, Sigma); Pi is the warm start and returns the new Pi.
+void pde_adjoint_rhs2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const double* snap, double* Pi,
+                       const double* const a[4], double* const da[4]);
 
 double probe_fp64_tflops(Ctx& c);
 // y = 1 / x elementwise on stream s (no bookkeeping).

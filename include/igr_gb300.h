@@ -99,7 +99,8 @@ int igr_last_launch_count(const igr_ctx* ctx, long long* out);
 /* Per-launch CUDA-event timing of the engine's kernel families (no reference
  * counterpart; used by the benchmark for live kernel durations). Families:
  * 0 setup, 1 SIP apply (solver iteration), 2 hyperbolic+RK, 3 hyperbolic
- * reverse, 4 SIP apply reverse, 5 setup reverse, 6 tangent, 7 1D, 8 other. */
+ * reverse, 4 SIP apply reverse, 5 setup reverse, 6 tangent, 7 1D, 8 other,
+ * 9 continuous adjoint (per-step preparation, Pi source, adjoint operator). */
 int igr_profile_enable(igr_ctx* ctx, int on);
 int igr_profile_reset(igr_ctx* ctx);
 int igr_profile_read(igr_ctx* ctx, int kernel_family, double* total_ms, long long* launches);
@@ -205,6 +206,61 @@ int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_
  * looks up the array's address; make it before any stream capture. */
 int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const double* x_dev, const double* rho_dev,
                             double* y_dev, void* stream);
+
+/* ---- 2D continuous adjoint (optimise-then-discretise) ---------------------- */
+
+/* run_forward_store (IGR_adjoints_2d/forward.jl:111-158): the forward with
+ * n_steps = ceil(T/dt), dt = T/n_steps, and one more Sigma solve after every
+ * step (and at t = 0), whose result is stored and is the next step's warm
+ * start. snapshots: (n_steps + 1) x 5 x N doubles, snapshot k (k = 0..n_steps,
+ * the state after step k) = (mux, muy, rho, E, Sigma); snapshots_len must
+ * equal (ceil(T/dt) + 1) * 5 * N. The step count is returned in *n_steps. */
+int igr2d_run_forward_store(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
+                            int n_iter, int solver, const double* mux0, const double* muy0, const double* rho0,
+                            const double* E0, double* snapshots, long long snapshots_len, int* n_steps);
+
+/* run_adjoint_conservative (IGR_adjoints_2d/adjoint_pde.jl:527-611): the
+ * adjoint PDE integrated backward with SSP-RK3 from the L2 gradient of the
+ * objective at T, step n using snapshot n for all three stages, step
+ * min(dt, T), one SIP solve for Pi per stage (warm-started, from zero at T).
+ * snapshots as igr2d_run_forward_store writes them (snapshots_len >=
+ * (n_steps + 1) * 5 * N). Objectives: IGR_OBJ_L2_DENSITY, _L2_PRESSURE,
+ * _KINETIC_ENERGY, _WINDOWED_KE, _WEIGHTED_MOMENTUM (adjoint_pde.jl:542-584)
+ * and IGR_OBJ_WINDOW_RHO2 (no reference counterpart). Output: the adjoint
+ * (a_mux, a_muy, a_rho, a_E) at t = 0. */
+int igr2d_run_adjoint_conservative(igr_ctx* ctx, const igr_disc2d* d, const double* snapshots, long long snapshots_len,
+                                   int n_steps, double dt, double t_end, double gamma, double alpha, int n_iter,
+                                   int objective, int solver, const double* obj_params, double* amux, double* amuy,
+                                   double* arho, double* aE);
+
+/* run_forward_store followed by run_adjoint_conservative (the pairing of
+ * IGR_adjoints_2d/tests/run_adjoint_test.jl:59-62) with the snapshots kept on
+ * the device: all of them when they fit, else checkpoints every K steps and
+ * one recomputed K-step segment at a time (igr_last_adjoint_plan reports K
+ * and the segment count). dt is the caller's step: the forward re-rounds it,
+ * the adjoint steps by min(dt, T), as the two reference calls do. */
+int igr2d_adjoint_conservative_ic(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt,
+                                  double t_end, int n_iter, int solver, int objective, const double* obj_params,
+                                  const double* mux0, const double* muy0, const double* rho0, const double* E0,
+                                  double* amux, double* amuy, double* arho, double* aE);
+
+/* Batched igr2d_adjoint_conservative_ic: n_inst instances on one mesh, each
+ * with its own gamma, alpha, dt and initial state, one final time T for all;
+ * ceil(T/dt[i]) must be the same for every instance. q0 and a0: (n_inst, 4, N)
+ * doubles, instance-major. No counterpart in the reference. */
+int igr2d_adjoint_conservative_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas,
+                                     const double* alphas, const double* dts, double t_end, int n_iter, int solver,
+                                     int objective, const double* obj_params, const double* q0, double* a0);
+
+/* compute_adjoint_rhs_conservative! (IGR_adjoints_2d/adjoint_pde.jl:481-516):
+ * the adjoint operator at the state (q, sigma) applied to a: the local DG
+ * part (adjoint flux with LLF, local source) plus, when alpha > 0, the
+ * nonlocal source of one Pi solve (pi: warm start in, solution out). */
+int igr2d_adjoint_rhs_conservative(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_iter,
+                                   int solver, const double* mux, const double* muy, const double* rho,
+                                   const double* E, const double* sigma, double* pi, const double* amux,
+                                   const double* amuy, const double* arho, const double* aE, double* damux,
+                                   double* damuy, double* darho, double* daE);
 
 /* ---- 1D ------------------------------------------------------------------- */
 

@@ -80,6 +80,30 @@ def test_python_mirror_rejects_bad_symbols_before_any_device_call(igr):
         igr1d.enzyme_adjoint_ic(0.1, 3, 4, 1.0, 1.4, 0.1, 0.5, 0.1, objective="kinetic_energy")
     with pytest.raises(ValueError, match="Unknown IC type"):
         igr1d.enzyme_adjoint_ic(0.1, 3, 4, 1.0, 1.4, 0.1, 0.5, 0.1, ic_type="shock")
+    snaps = [(z2, z2, z2, z2, z2)] * 2
+    with pytest.raises(ValueError, match="Unknown objective"):
+        igr.run_adjoint_conservative(snaps, 1, 0.1, 0.1, basis, m2, 1.4, 0.1, objective="entropy")
+    with pytest.raises(ValueError, match="Unknown solver"):
+        igr.run_forward_store(z2, z2, z2, z2, 0.1, 0.2, basis, m2, 1.4, 0.1, solver="gmres")
+    with pytest.raises(ValueError, match="Unknown solver"):
+        igr.adjoint_conservative_ic(z2, z2, z2, z2, 0.1, 0.2, basis, m2, 1.4, 0.1, solver="gmres")
+
+
+def test_snapshots_index_like_the_reference_list(igr):
+    """Snapshots mirrors the Vector of (mux, muy, rho, E, Sigma) tuples that
+    run_forward_store returns (forward.jl:111-158): snapshots[k] unpacks into
+    five (n_p, n_p, N_ex, N_ey) fields and snapshots[-1] is the state at T."""
+    basis = igr.DGBasis(2)
+    mesh = igr.CartesianMesh2D(3, 2, 1.0, 1.0, basis)
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    data = np.arange(3 * 5 * n, dtype=np.float64).reshape(3, 5, n)
+    s = igr.Snapshots(data, shape)
+    assert len(s) == 3
+    mx, my, rho, E, Sig = s[-1]
+    assert mx.shape == shape and np.array_equal(Sig.reshape(-1, order="F"), data[2, 4])
+    again = igr.Snapshots.from_list([s[k] for k in range(3)], shape)
+    assert np.array_equal(again.data, data)
 
 
 def test_ic_builders_match_reference_formulas():
