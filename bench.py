@@ -315,6 +315,65 @@ def secondary(args):
                                         "interval rho objective", "sample_steps": ns, "full_steps": nfull},
                     cpu_baseline={"value": 1024 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
                                   "sample": "one instance per N_e for 2 steps, scaled by counts and to 2000 steps"})
+    elif args.workload == "pde_adjoint2d":
+        # the headline's batch (32 x 128^2 P3, Chebyshev 5, 200 steps, window rho^2) through the continuous
+        # adjoint: run_forward_store + run_adjoint_conservative with device-resident snapshots
+        B = 8 if args.profile_case else args.batch
+        nst = 2 if args.profile_case else args.n_steps
+        basis, mesh, q0, gs, als, dts, prm = make_batch(igr, W, B)
+        dt = float(dts.min())  # one step for the batch: the most restrictive CFL step
+        T = nst * dt
+        dtv = np.full(B, dt)
+        run = lambda: igr.adjoint_conservative_batch(q0, gs, als, dtv, T, basis, mesh, n_iter=N_ITER, solver=SOLVER,
+                                                     objective=OBJ, obj_params=prm, ctx=ctx)
+        if args.profile_case:
+            run()
+            print("profile case done")
+            return
+        _lib_mod = sys.modules["igr_sensitivities_gb300._lib"]
+        lib = _lib_mod.lib()
+        import ctypes as C
+        for _ in range(args.warmup):
+            run()
+        lib.igr_profile_reset(ctx.handle)
+        lib.igr_profile_enable(ctx.handle, 1)
+        run()
+        lib.igr_profile_enable(ctx.handle, 0)
+        fam = {}
+        for k, nm in ((9, "k2_pde_rk"), (10, "k2_pde_prep+k2_pde_b"), (1, "k2_apply"), (0, "k2_setup"), (2, "k2_hyp_rk"),
+                      (8, "other")):
+            ms, cnt, nodes = C.c_double(0), C.c_longlong(0), C.c_double(0)
+            lib.igr_profile_read(ctx.handle, k, C.byref(ms), C.byref(cnt))
+            lib.igr_profile_nodes(ctx.handle, k, C.byref(nodes))
+            fam[nm] = {"ms": round(ms.value, 2), "launches": cnt.value, "nodes": nodes.value}
+        clocks = ClockSampler(0)
+        clocks.start()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        t = (time.perf_counter() - t0) / args.steps
+        clk = clocks.stop()
+        # CPU: the oracle's forward store + continuous adjoint, one instance for 2 steps, single thread
+        G = O.Grid2D(3, NE, NE)
+        ns = 2
+        qi = [np.ascontiguousarray(q0[0, v]) for v in range(4)]
+        tc0 = time.perf_counter()
+        snaps, n2 = O.run_forward_store_2d(G, GAMMA, als[0], dt, ns * dt, N_ITER, SOLVER, qi)
+        O.run_adjoint_conservative_2d(G, snaps, n2, dt, ns * dt, GAMMA, als[0], N_ITER, OBJ, SOLVER, prm)
+        tc = (time.perf_counter() - tc0) * nst / ns
+        rk = fam["k2_pde_rk"]
+        line.update(metric="2D P3 128^2 continuous-adjoint gradients/s (Chebyshev 5, 200 steps, batch %d)" % B,
+                    value=B / t, unit="gradients/s", ms_per_step=t * 1e3, gpu_launches=ctx.last_launch_count(),
+                    config={"workload": "2D IGR-Euler continuous adjoint (run_forward_store + run_adjoint_conservative), "
+                                        "P3 128x128, Chebyshev 5, 200 steps, window rho^2, snapshots resident in HBM",
+                            "global_batch": B, "n_steps": nst, "l2": "snapshots and fields >> L2"},
+                    e2e={"value": B / t, "unit": "gradients/s", "h2d_bytes_per_step": int(q0.nbytes),
+                         "d2h_bytes_per_step": int(q0.nbytes)},
+                    kernels=fam,
+                    k2_pde_rk_us_per_launch=round(1e3 * rk["ms"] / max(rk["launches"], 1), 1),
+                    clocks=clk,
+                    cpu_baseline={"value": 1.0 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
+                                  "sample": "1 instance, %d of %d steps, single thread, scaled" % (ns, nst)})
     else:
         raise SystemExit("unknown workload " + args.workload)
     print(json.dumps(line))
@@ -331,7 +390,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
     ap.add_argument("--workload", default="adjoint2d",
-                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d")
+                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()

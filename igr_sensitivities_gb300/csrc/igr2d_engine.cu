@@ -1252,7 +1252,7 @@ static void pde_prep(Ctx& c, const Plan2D& P, PdeWork& w, const double* snap, bo
   for (int v = 0; v < PDE_NL; ++v) p.nl[v] = apos ? w.nl[v] : nullptr;
   p.ws_x = w.wsx; p.ws_y = w.wsy;
   {
-    LaunchScope ls(c, KID_PDE);
+    LaunchScope ls(c, KID_PDE_AUX);
     NP_DISPATCH(P.np, launch_k2_pde_prep<NPV>(p, P.ntiles(), c.stream));
   }
   if (apos) {
@@ -1274,7 +1274,7 @@ static void pde_pi_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, PdeWork&
   b.mx = snap; b.my = snap + NG; b.invr = w.invr;
   b.b = w.b;
   {
-    LaunchScope ls(c, KID_PDE);
+    LaunchScope ls(c, KID_PDE_AUX);
     NP_DISPATCH(P.np, launch_k2_pde_b<NPV>(b, P.ntiles(), c.stream));
   }
   stage_solve_b(c, P, o, w.st, w.b, w.Pi[w.cur], w.Pi[1 - w.cur], false, w.xa, w.xb, w.db);

@@ -40,7 +40,7 @@ class Workspace {
 
 // Kernel families timed by the optional per-launch CUDA-event profiler.
 enum KernelId { KID_SETUP = 0, KID_APPLY, KID_HYP, KID_HYP_REV, KID_APPLY_REV, KID_SETUP_REV, KID_TAN, KID_1D, KID_OTHER,
-                KID_PDE, KID_COUNT };
+                KID_PDE, KID_PDE_AUX, KID_COUNT };
 
 struct Profiler {
   bool on = false;

@@ -100,7 +100,8 @@ int igr_last_launch_count(const igr_ctx* ctx, long long* out);
  * counterpart; used by the benchmark for live kernel durations). Families:
  * 0 setup, 1 SIP apply (solver iteration), 2 hyperbolic+RK, 3 hyperbolic
  * reverse, 4 SIP apply reverse, 5 setup reverse, 6 tangent, 7 1D, 8 other,
- * 9 continuous adjoint (per-step preparation, Pi source, adjoint operator). */
+ * 9 continuous-adjoint operator (k2_pde_rk), 10 continuous-adjoint per-step
+ * preparation and Pi source (k2_pde_prep, k2_pde_b). */
 int igr_profile_enable(igr_ctx* ctx, int on);
 int igr_profile_reset(igr_ctx* ctx);
 int igr_profile_read(igr_ctx* ctx, int kernel_family, double* total_ms, long long* launches);
