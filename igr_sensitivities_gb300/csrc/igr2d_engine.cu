@@ -540,12 +540,15 @@ static void hyp_stage(Ctx& c, const Plan2D& P, StageBuf st[3], int s, double* co
   NP_DISPATCH(P.np, launch_k2_hyp_rk<NPV>(h, P.ntiles(), c.stream));
 }
 
+// setup0 = false: st[0] already holds the operator coefficients and IGR
+// source of its state (the caller just solved on it).
 static void step_forward(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf st[3], const double* Sin, double* const qout[4],
-                         double* invrout, double* xa, double* xb, double* dbuf) {
+                         double* invrout, double* xa, double* xb, double* dbuf, bool setup0 = true) {
   const bool apos = any_alpha_pos(P);
   const double* sprev = Sin;
   for (int s = 0; s < 3; ++s) {
-    if (apos) stage_solve(c, P, o, st[s], sprev, xa, xb, dbuf);
+    if (apos && s == 0 && !setup0) stage_solve_b(c, P, o, st[0], st[0].b, sprev, st[0].Sout, false, xa, xb, dbuf);
+    else if (apos) stage_solve(c, P, o, st[s], sprev, xa, xb, dbuf);
     hyp_stage(c, P, st, s, qout, invrout);
     sprev = st[s].Sout;
   }
@@ -1193,8 +1196,9 @@ void forward_store_range2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const 
     for (int v = 0; v < 4; ++v) st[0].q[v] = cur + v * NG;
     for (int s = 0; s < 3; ++s) st[s].Sout = !apos ? zero : ((s % 2 == 0) ? sA : sB);
     double* qo[4] = {nxt, nxt + NG, nxt + 2 * NG, nxt + 3 * NG};
-    // the last stage writes 1/rho of the new state into st[0].invr (read by the post-step solve)
-    step_forward(c, P, o, st, cur + 4 * NG, qo, st[0].invr, xa, xb, db);
+    // the last stage writes 1/rho of the new state into st[0].invr (read by the post-step solve);
+    // the post-step solve leaves st[0]'s coefficients set up for the next step's first stage
+    step_forward(c, P, o, st, cur + 4 * NG, qo, st[0].invr, xa, xb, db, k == k0);
     if (apos) {  // forward.jl:152-154: one more solve on the new state, warm start = stage-3 Sigma
       StageBuf post = st[0];
       for (int v = 0; v < 4; ++v) post.q[v] = qo[v];

@@ -39,8 +39,9 @@ template <int NP>
 __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_prep(PdePrepArgs2D a) {
   using TL = Tiling2D<NP>;
   constexpr int TE = TL::TE, NN = TL::NN;
-  // x-derivatives (physical) of mux, muy, rho, E, Sigma, u_x, u_y
+  // x-derivatives (physical) of mux, muy, rho, E, Sigma, u_x, u_y; 1/rho
   __shared__ double s_dx[7][TE][NN];
+  __shared__ double s_ir[TE][NN];
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
   const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
@@ -52,9 +53,10 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_prep(PdePrepArgs2D a)
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
       const long long n = vr.base + t * NP + i;
-      const double r = a.q[2][n];
+      const double r = a.q[2][n], ir = 1.0 / r;  // one FP64 divide per node, shared by both phases
+      s_ir[e][t * NP + i] = ir;
       f[0][i] = a.q[0][n]; f[1][i] = a.q[1][n]; f[2][i] = r; f[3][i] = a.q[3][n]; f[4][i] = a.S[n];
-      f[5][i] = f[0][i] / r; f[6][i] = f[1][i] / r;
+      f[5][i] = f[0][i] * ir; f[6][i] = f[1][i] * ir;
     }
 #pragma unroll
     for (int v = 0; v < 7; ++v)
@@ -68,9 +70,9 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_prep(PdePrepArgs2D a)
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
     const long long n = vc.base + l * NP + t;
-    const double r = a.q[2][n];
-    f[0][l] = a.q[0][n]; f[1][l] = a.q[1][n]; f[2][l] = r; f[3][l] = a.q[3][n]; f[4][l] = a.S[n];
-    f[5][l] = f[0][l] / r; f[6][l] = f[1][l] / r;
+    const double ir = s_ir[e][l * NP + t];
+    f[0][l] = a.q[0][n]; f[1][l] = a.q[1][n]; f[2][l] = a.q[2][n]; f[3][l] = a.q[3][n]; f[4][l] = a.S[n];
+    f[5][l] = f[0][l] * ir; f[6][l] = f[1][l] * ir;
   }
   const double g = I.gamma, gm = g - 1.0;
 #pragma unroll
@@ -81,8 +83,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_prep(PdePrepArgs2D a)
     const double mxy = dot_row<NP>(B, l, f[0]) * invJy, myy = dot_row<NP>(B, l, f[1]) * invJy;
     const double ry = dot_row<NP>(B, l, f[2]) * invJy, Ey = dot_row<NP>(B, l, f[3]) * invJy;
     const double Sy = dot_row<NP>(B, l, f[4]) * invJy;
-    const double mx = f[0][l], my = f[1][l], r = f[2][l], en = f[3][l], Sg = f[4][l];
-    const double ir = 1.0 / r, ir2 = ir * ir, ir3 = ir2 * ir;
+    const double mx = f[0][l], my = f[1][l], en = f[3][l], Sg = f[4][l];
+    const double ir = s_ir[e][nd], ir2 = ir * ir, ir3 = ir2 * ir;
     const double ux = f[5][l], uy = f[6][l];
     // quotient-rule velocity gradients of the local source (adjoint_pde.jl:163-164)
     const double uxx = (mxx - ux * rx) * ir, uyy = (myy - uy * ry) * ir;
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_prep(PdePrepArgs2D a)
     a.src[0][n] = c0; a.src[1][n] = c1; a.src[2][n] = c2; a.src[3][n] = c3; a.src[4][n] = c4;
     a.src[5][n] = c5; a.src[6][n] = c6; a.src[7][n] = c7; a.src[8][n] = c8; a.src[9][n] = c9;
     a.invr[n] = ir;
-    const double cs = sqrt(g * P / r);
+    const double cs = sqrt(g * P * ir);
     a.ws_x[n] = fabs(ux) + cs;
     a.ws_y[n] = fabs(uy) + cs;
     if (a.nl[0]) {
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_prep(PdePrepArgs2D a)
       R = fma(2.0 * nxy, nyx, R);
       R = fma(nyy, nyy, R);
       a.nl[0][n] = nxx; a.nl[1][n] = nyx; a.nl[2][n] = nxy; a.nl[3][n] = nyy;
-      a.nl[4][n] = Sx / r; a.nl[5][n] = Sy / r; a.nl[6][n] = R;
+      a.nl[4][n] = Sx * ir; a.nl[5][n] = Sy * ir; a.nl[6][n] = R;
     }
   }
 }
