@@ -10,6 +10,7 @@
 #include "igr1d.hpp"
 #include "igr2d_adjoint.hpp"
 #include "igr2d_pde_adjoint.hpp"
+#include "igr1d_pde_adjoint.hpp"
 
 using namespace igr;
 
@@ -319,6 +320,74 @@ int orc1d_run_sensitivity(GRID1D_ARGS, double gamma, double alpha, double dt, do
     if (form != 1 && form != 2) throw std::invalid_argument("Unknown elliptic_rhs (use :form1 or :form2)");
     Grid1D G = GRID1D; double* q[3] = {mu, rho, E}; double* s[3] = {smu, srho, sE};
     run_sensitivity1d(G, q, s, Sig, sSig, dt, T_end, gamma, alpha, n_iter, solver, form, s_gamma);
+  });
+}
+
+// run_forward_store (IGR_adjoints_1d/forward.jl:137-186): snaps = (n_steps + 1) * 4 * N doubles.
+int orc1d_run_forward_store(GRID1D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver,
+                            const double* mu, const double* rho, const double* E, double* snaps, long long snaps_len,
+                            int* n_steps) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid1D G = GRID1D; const double* q0[3] = {mu, rho, E};
+    std::vector<double> s;
+    *n_steps = run_forward_store1d(G, q0, dt, T_end, gamma, alpha, n_iter, solver, s);
+    if ((long long)s.size() != snaps_len) throw std::invalid_argument("snapshot buffer has the wrong size");
+    std::memcpy(snaps, s.data(), s.size() * sizeof(double));
+  });
+}
+
+// run_adjoint_conservative (IGR_adjoints_1d/adjoint_pde.jl:474-551).
+int orc1d_run_adjoint_conservative(GRID1D_ARGS, double gamma, double alpha, int n_steps, double dt, double T_end,
+                                   int n_iter, int obj, int solver, const double* prm, const double* snaps,
+                                   double* amu, double* arho, double* aE) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    Grid1D G = GRID1D; double* a[3] = {amu, arho, aE};
+    run_adjoint_conservative1d(G, snaps, n_steps, dt, T_end, gamma, alpha, n_iter, obj, solver, prm, a);
+  });
+}
+
+// compute_adjoint_rhs_conservative! (IGR_adjoints_1d/adjoint_pde.jl:410-456): Pi in-out.
+int orc1d_adjoint_rhs_conservative(GRID1D_ARGS, double gamma, double alpha, int n_iter, int solver, const double* mu,
+                                   const double* rho, const double* E, const double* Sig, double* Pi, const double* amu,
+                                   const double* arho, const double* aE, double* dmu, double* drho, double* dE) {
+  return guard([&] {
+    Grid1D G = GRID1D; const double* q[3] = {mu, rho, E}; const double* a[3] = {amu, arho, aE};
+    double* da[3] = {dmu, drho, dE};
+    Work2D<double> W; W.alloc(G.N);
+    pde1_adjoint_rhs(G, gamma, alpha, n_iter, solver, q, Sig, Pi, a, da, W);
+  });
+}
+
+// 1D duality of the local adjoint operator (alpha = 0, Sigma frozen), as orc2d_pde_duality.
+int orc1d_pde_duality(GRID1D_ARGS, double gamma, const double* q_in, const double* Sig, const double* a_in,
+                      const double* dq_in, double* lhs, double* rhs) {
+  return guard([&] {
+    typedef Dual<1> D1;
+    Grid1D G = GRID1D; const size_t N = G.N;
+    std::vector<D1> qd[3], Sd(N), kd[3];
+    for (int v = 0; v < 3; ++v) {
+      qd[v].resize(N); kd[v].resize(N);
+      for (size_t k = 0; k < N; ++k) { qd[v][k].v = q_in[v * N + k]; qd[v][k].d[0] = dq_in[v * N + k]; }
+    }
+    for (size_t k = 0; k < N; ++k) Sd[k] = D1(Sig[k]);
+    const D1* qc[3] = {qd[0].data(), qd[1].data(), qd[2].data()};
+    D1* kc[3] = {kd[0].data(), kd[1].data(), kd[2].data()};
+    hyperbolic_rhs1d(G, D1(gamma), qc, Sd.data(), kc);
+    const double* q[3] = {q_in, q_in + N, q_in + 2 * N};
+    const double* a[3] = {a_in, a_in + N, a_in + 2 * N};
+    std::vector<double> dav(3 * N);
+    double* da[3] = {dav.data(), dav.data() + N, dav.data() + 2 * N};
+    pde1_hyperbolic_rhs_local(G, gamma, q, Sig, a, da);
+    double l = 0.0, r = 0.0;
+    for (int e = 0; e < G.m.Ne; ++e)
+      for (int i = 0; i < G.np; ++i) {
+        const size_t n = G.id(i, e);
+        const double m = G.b.w[i] * G.m.J;
+        for (int v = 0; v < 3; ++v) { l += m * a[v][n] * kd[v][n].d[0]; r += m * da[v][n] * dq_in[v * N + n]; }
+      }
+    *lhs = l; *rhs = r;
   });
 }
 

@@ -330,3 +330,40 @@ def run_sensitivity_1d(G, gamma, alpha, dt, T, n_iter, solver, q0, s0, form=2, s
                                        C.c_double(s_gamma), *[_p(a) for a in q], _p(Sig), *[_p(a) for a in s],
                                        _p(sSig)))
     return q, Sig, s, sSig
+
+
+def run_forward_store_1d(G, gamma, alpha, dt, T, n_iter, solver, q0):
+    """Snapshots (n_steps + 1, 4, N): (mu, rho, E, Sigma) after each step."""
+    n = forward_store_steps(dt, T)
+    snaps = np.zeros((n + 1) * 4 * G.N)
+    ns = C.c_int(0)
+    _check(lib().orc1d_run_forward_store(*G.args(), C.c_double(gamma), C.c_double(alpha), C.c_double(dt), C.c_double(T),
+                                         C.c_int(n_iter), C.c_int(SOLVERS.get(solver, -1)), *[_p(_f(a)) for a in q0],
+                                         _p(snaps), C.c_longlong(snaps.size), C.byref(ns)))
+    return snaps.reshape(n + 1, 4, G.N), ns.value
+
+
+def run_adjoint_conservative_1d(G, snaps, n_steps, dt, T, gamma, alpha, n_iter, objective, solver, prm=None):
+    out = [np.zeros(G.N) for _ in range(3)]
+    _check(lib().orc1d_run_adjoint_conservative(*G.args(), C.c_double(gamma), C.c_double(alpha), C.c_int(n_steps),
+                                                C.c_double(dt), C.c_double(T), C.c_int(n_iter),
+                                                C.c_int(OBJECTIVES_1D.get(objective, -1)),
+                                                C.c_int(SOLVERS.get(solver, -1)), _p(_prm(prm)),
+                                                _p(_f(np.asarray(snaps).reshape(-1))), *[_p(a) for a in out]))
+    return out
+
+
+def adjoint_rhs_conservative_1d(G, gamma, alpha, n_iter, solver, q, Sig, Pi0, a):
+    Pi = _f(Pi0).copy()
+    out = [np.zeros(G.N) for _ in range(3)]
+    _check(lib().orc1d_adjoint_rhs_conservative(*G.args(), C.c_double(gamma), C.c_double(alpha), C.c_int(n_iter),
+                                                C.c_int(SOLVERS.get(solver, -1)), *[_p(_f(x)) for x in q],
+                                                _p(_f(Sig)), _p(Pi), *[_p(_f(x)) for x in a], *[_p(x) for x in out]))
+    return out, Pi
+
+
+def pde_duality_1d(G, gamma, q, Sig, a, dq):
+    l, r = C.c_double(0.0), C.c_double(0.0)
+    _check(lib().orc1d_pde_duality(*G.args(), C.c_double(gamma), _p(_f(np.concatenate(q))), _p(_f(Sig)),
+                                   _p(_f(np.concatenate(a))), _p(_f(np.concatenate(dq))), C.byref(l), C.byref(r)))
+    return l.value, r.value

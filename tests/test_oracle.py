@@ -299,3 +299,79 @@ def test_pde_adjoint_unknown_objective_raises(oracle):
     snaps, n = oracle.run_forward_store_2d(G, 1.4, 0.0, 0.01, 0.02, 1, "pcg", q)
     with pytest.raises(ValueError):
         oracle.run_adjoint_conservative_2d(G, snaps, n, 0.01, 0.02, 1.4, 0.0, 1, "entropy", "pcg")
+
+
+def _pde1_dJ_dA(oracle, ic, alpha, n_iter, T, p=2, Ne=16, CFL=0.3, A0=0.2):
+    """IGR_adjoints_1d/tests/run_adjoint_conservative_test.jl:19-137: dJ/dA
+    assembled from the conservative adjoint at t = 0 (J = sum w J rho^2, the
+    IC family's dq0/dA) and central differences of J(A), h = 1e-6."""
+    from igr_sensitivities_gb300 import igr1d
+    g, L = 1.4, 1.0
+    G = oracle.Grid1D(p, Ne, L)
+    x = G.coords()
+    dt = CFL * G.dx / ((2 * p + 1) * 2.5)
+    n = int(np.ceil(T / dt))
+    dt = T / n
+    build = igr1d.IC_BUILDERS[ic][0]
+
+    def ic_of(A):
+        mu, rho, E = np.zeros(G.N), np.zeros(G.N), np.zeros(G.N)
+        build(mu, rho, E, A, x, L, g)
+        return [mu, rho, E]
+
+    q0 = ic_of(A0)
+    snaps, ns = oracle.run_forward_store_1d(G, g, alpha, dt, T, n_iter, "pcg", q0)
+    assert ns == n and snaps.shape == (n + 1, 4, G.N)
+    am, ar, aE = oracle.run_adjoint_conservative_1d(G, snaps, ns, dt, T, g, alpha, n_iter, "l2_density", "pcg")
+    wr, wu, wp = igr1d.ic_dA_weights(ic)
+    s = np.sin(2 * np.pi * x / L)
+    rho, u = q0[1], q0[0] / q0[1]
+    drho, du, dp = wr * s, wu * s, wp * s
+    dmu = rho * du + u * drho
+    dE = dp / (g - 1) + 0.5 * (drho * u ** 2 + 2 * rho * u * du)
+    wJ = np.tile(G.w, Ne) * G.J
+    dJ = float(np.sum(wJ * (am * dmu + ar * drho + aE * dE)))
+
+    def J_of(A):
+        q, _ = oracle.run_forward_1d(G, g, alpha, dt, T, n_iter, "pcg", ic_of(A))
+        return float(np.sum(wJ * q[1] ** 2))
+
+    fd = (J_of(A0 + 1e-6) - J_of(A0 - 1e-6)) / 2e-6
+    return abs(dJ - fd) / max(abs(fd), 1e-15)
+
+
+@pytest.mark.parametrize("ic", ["acoustic_pulse", "entropy_wave", "density_pulse", "pressure_pulse", "velocity_pulse"])
+def test_pde1_adjoint_dJ_dA_vs_fd_ic_sweep(oracle, ic):
+    # run_adjoint_conservative_test.jl:233-237 (Test 3): alpha = 0, n_iter = 10, tol 1e-2 (measured <= 2e-5)
+    assert _pde1_dJ_dA(oracle, ic, 0.0, 10, 0.05) < 1e-2
+
+
+@pytest.mark.parametrize("alpha", [0.0, 0.001, 0.01, 0.05])
+def test_pde1_adjoint_dJ_dA_vs_fd_alpha_sweep(oracle, alpha):
+    # Tests 1, 2 and 4 (:226-243): n_iter = 200, tol 5e-2 (measured <= 9e-5)
+    assert _pde1_dJ_dA(oracle, "acoustic_pulse", alpha, 200, 0.05) < 5e-2
+
+
+def test_pde1_adjoint_long_time(oracle):
+    # Test 5 (:246-247): alpha = 0.01, T = 1.0, tol 0.10 (measured 0.073: the OtD gap grows with T)
+    assert _pde1_dJ_dA(oracle, "acoustic_pulse", 0.01, 200, 1.0) < 0.10
+
+
+def test_pde1_local_operator_is_the_dual_of_the_linearised_rhs(oracle):
+    """1D form of the 2D duality test: the gap converges at ~6th order
+    (3e-3 at 4 elements, 6e-10 at 64)."""
+    g = 1.4
+    gaps = []
+    for Ne in (16, 32, 64):
+        G = oracle.Grid1D(3, Ne)
+        x = G.coords()
+
+        def s(k, ph):
+            return np.sin(2 * np.pi * k * x + ph)
+
+        q = [0.3 * s(1, 0.1), 1 + 0.2 * s(1, 0.5), 2.5 + 0.3 * s(2, 0.9)]
+        lhs, rhs = oracle.pde_duality_1d(G, g, q, 0.05 * s(1, 1.1), [s(1, 0.4), s(2, 1.3), s(1, 2.0)],
+                                         [s(2, 0.2), s(1, 2.2), s(1, 0.8)])
+        gaps.append(abs(lhs - rhs) / abs(lhs))
+    assert gaps[0] > 30 * gaps[1] > 900 * gaps[2]
+    assert gaps[2] < 1e-8
