@@ -862,4 +862,150 @@ int igr1d_sensitivity_batch(igr_ctx* ctx, int p, const double* xi, const double*
   });
 }
 
+// ---- 1D continuous adjoint ------------------------------------------------------------------
+namespace {
+size_t budget1(Ctx& c, const char* name) {
+  if (c.tape_budget) return c.tape_budget;
+  size_t fr = 0, tot = 0;
+  cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+  const size_t avail = fr + c.ws.held(name);
+  return avail > ((size_t)2 << 30) ? avail - ((size_t)2 << 30) : 0;
+}
+void check_obj1(int objective, const double* obj_params) {
+  if (objective != 0 && objective != 1 && objective != 2 && objective != 4 && objective != 6)
+    throw Error(IGR_EINVAL, "Unknown objective (use :l2_density, :l2_pressure, or :kinetic_energy)");
+  if (objective == 6 && !obj_params) throw Error(IGR_EINVAL, "interval objective needs obj_params = {a, b}");
+}
+Inst1DDesc pde1_desc(int ne, double L, double gamma, double alpha, double dt, double t_end) {
+  if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+  const int n = (int)std::ceil(t_end / dt);  // IGR_adjoints_1d/forward.jl:158-159
+  Inst1DDesc d{ne, L, gamma, alpha, t_end / n, n};
+  d.h = std::min(dt, t_end);                  // IGR_adjoints_1d/adjoint_pde.jl:531
+  return d;
+}
+}  // namespace
+
+int igr1d_run_forward_store(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
+                            int n_iter, int solver, const double* mu0, const double* rho0, const double* E0,
+                            double* snapshots, long long snapshots_len, int* n_steps) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!d) throw Error(IGR_EINVAL, "null discretisation");
+    check_disc1(d->p, d->xi, d->w, d->D);
+    check_solver(solver, n_iter);
+    if (d->n_e < 1 || !(d->L > 0)) throw Error(IGR_EINVAL, "bad mesh");
+    const Inst1DDesc dsc = pde1_desc(d->n_e, d->L, gamma, alpha, dt, t_end);
+    const long long N = (long long)(d->p + 1) * d->n_e, n = dsc.n_steps;
+    if (!snapshots || !n_steps || snapshots_len != (n + 1) * 4 * N)
+      throw Error(IGR_EINVAL, "snapshots must hold (ceil(T/dt) + 1) * 4 * N doubles");
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    Plan1D P = make_plan1d(c, B, {dsc}, [&](const Inst1DDesc& x, int NN) { return pde1d_scratch_fields(x, NN, 1, 1); }, "p1");
+    double* q = c.ws.dbl("capi1:pq", 3 * N);
+    const double* in[3] = {mu0, rho0, E0};
+    for (int v = 0; v < 3; ++v) h2d(c, q + v * N, in[v], N);
+    double* S = c.ws.dbl("capi1:psnap", (size_t)(n + 1) * 4 * N);
+    long long* off = static_cast<long long*>(c.ws.get("capi1:psoff", sizeof(long long)));
+    cuda_check(cudaMemsetAsync(off, 0, sizeof(long long), c.stream), "offset");
+    Solve2DOpts o{n_iter, solver};
+    pde_adjoint1d(c, P, 1, q, nullptr, nullptr, nullptr, S, off, o, 0, nullptr, 1);
+    d2h(c, snapshots, S, (n + 1) * 4 * N);
+    sync(c);
+    *n_steps = (int)n;
+  });
+}
+
+int igr1d_run_adjoint_conservative(igr_ctx* ctx, const igr_disc1d* d, const double* snapshots, long long snapshots_len,
+                                   int n_steps, double dt, double t_end, double gamma, double alpha, int n_iter,
+                                   int objective, int solver, const double* obj_params, double* amu, double* arho,
+                                   double* aE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!d) throw Error(IGR_EINVAL, "null discretisation");
+    check_disc1(d->p, d->xi, d->w, d->D);
+    check_solver(solver, n_iter);
+    check_obj1(objective, obj_params);
+    if (d->n_e < 1 || !(d->L > 0)) throw Error(IGR_EINVAL, "bad mesh");
+    if (n_steps < 0) throw Error(IGR_EINVAL, "n_steps must be >= 0");
+    if (!(dt > 0) || !(t_end > 0)) throw Error(IGR_EINVAL, "dt and T must be positive");
+    const long long N = (long long)(d->p + 1) * d->n_e;
+    if (!snapshots || snapshots_len < (long long)(n_steps + 1) * 4 * N)
+      throw Error(IGR_EINVAL, "snapshots must hold (n_steps + 1) * 4 * N doubles");
+    Inst1DDesc dsc{d->n_e, d->L, gamma, alpha, t_end / std::max(n_steps, 1), n_steps};
+    dsc.h = std::min(dt, t_end);  // adjoint_pde.jl:531
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    Plan1D P = make_plan1d(c, B, {dsc}, [&](const Inst1DDesc& x, int NN) { return pde1d_scratch_fields(x, NN, 2, 1); }, "p1");
+    double* S = c.ws.dbl("capi1:psnap", (size_t)(n_steps + 1) * 4 * N);
+    h2d(c, S, snapshots, (long long)(n_steps + 1) * 4 * N);
+    double* out = c.ws.dbl("capi1:pout", 3 * N);
+    long long* off = static_cast<long long*>(c.ws.get("capi1:psoff", sizeof(long long)));
+    cuda_check(cudaMemsetAsync(off, 0, sizeof(long long), c.stream), "offset");
+    Solve2DOpts o{n_iter, solver};
+    pde_adjoint1d(c, P, 2, nullptr, nullptr, out, nullptr, S, off, o, objective, obj_params, 1);
+    double* outs[3] = {amu, arho, aE};
+    for (int v = 0; v < 3; ++v) d2h(c, outs[v], out + v * N, N);
+    sync(c);
+  });
+}
+
+int igr1d_adjoint_rhs_conservative(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, int n_iter, int solver,
+                                   const double* mu, const double* rho, const double* E, const double* sigma, double* pi,
+                                   const double* amu, const double* arho, const double* aE, double* damu, double* darho,
+                                   double* daE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!d) throw Error(IGR_EINVAL, "null discretisation");
+    check_disc1(d->p, d->xi, d->w, d->D);
+    check_solver(solver, n_iter);
+    if (d->n_e < 1 || !(d->L > 0)) throw Error(IGR_EINVAL, "bad mesh");
+    Inst1DDesc dsc{d->n_e, d->L, gamma, alpha, 0.0, 0};
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    Plan1D P = make_plan1d(c, B, {dsc}, [&](const Inst1DDesc& x, int NN) { return pde1d_scratch_fields(x, NN, 3, 1); }, "p1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:prhs", 11 * N);
+    const double* qin[4] = {mu, rho, E, sigma};
+    for (int v = 0; v < 4; ++v) h2d(c, buf + v * N, qin[v], N);
+    const double* ain[3] = {amu, arho, aE};
+    for (int v = 0; v < 3; ++v) h2d(c, buf + (4 + v) * N, ain[v], N);
+    double* Pi = buf + 7 * N;
+    if (alpha > 0) h2d(c, Pi, pi, N);
+    double* k = buf + 8 * N;
+    Solve2DOpts o{n_iter, solver};
+    pde_adjoint1d(c, P, 3, buf, buf + 4 * N, k, Pi, nullptr, nullptr, o, 0, nullptr, 1);
+    double* outs[3] = {damu, darho, daE};
+    for (int v = 0; v < 3; ++v) d2h(c, outs[v], k + v * N, N);
+    if (alpha > 0) d2h(c, pi, Pi, N);
+    sync(c);
+  });
+}
+
+int igr1d_adjoint_conservative_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                                     const int* n_e, const double* L, const double* gammas, const double* alphas,
+                                     const double* dts, const double* t_ends, int n_iter, int solver, int objective,
+                                     const double* obj_params, const double* q0, double* a0) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc1(p, xi, w, D);
+    check_solver(solver, n_iter);
+    check_obj1(objective, obj_params);
+    if (n_inst < 1 || !n_e || !L || !gammas || !alphas || !dts || !t_ends || !q0 || !a0)
+      throw Error(IGR_EINVAL, "bad batch arguments");
+    BasisDev B = make_basis_dev(p, xi, w, D);
+    std::vector<Inst1DDesc> insts;
+    for (int i = 0; i < n_inst; ++i) {
+      if (n_e[i] < 1 || !(L[i] > 0)) throw Error(IGR_EINVAL, "bad mesh");
+      insts.push_back(pde1_desc(n_e[i], L[i], gammas[i], alphas[i], dts[i], t_ends[i]));
+    }
+    Solve2DOpts o{n_iter, solver};
+    const int seg = pde1d_segment(insts, p + 1, budget1(c, "p1:scr"));
+    Plan1D P = make_plan1d(c, B, insts, [&](const Inst1DDesc& x, int NN) { return pde1d_scratch_fields(x, NN, 0, seg); },
+                           "p1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:pbatch", 6 * N);
+    h2d(c, buf, q0, 3 * N);
+    pde_adjoint1d(c, P, 0, buf, nullptr, buf + 3 * N, nullptr, nullptr, nullptr, o, objective, obj_params, seg);
+    d2h(c, a0, buf + 3 * N, 3 * N);
+    sync(c);
+  });
+}
+
 }  // extern "C"

@@ -8,6 +8,7 @@
 
 #include "igr1d_launch.h"
 #include "igr1d_rev_kernels.cuh"
+#include "igr1d_pde_kernels.cuh"
 #include "igr1d_sens_kernels.cuh"
 #include "igr_engine.h"
 
@@ -46,6 +47,7 @@ Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& ins
     I.idx = 1.0 / I.dx;
     I.gamma = d.gamma; I.alpha = d.alpha; I.dt = d.dt;
     I.t_end = d.t_end;
+    I.h = d.h;
     P.inst.push_back(I);
     const long long n = (long long)P.np * d.ne;
     P.inst_nodes.push_back(n);
@@ -199,6 +201,53 @@ void tangent1d(Ctx& c, const Plan1D& P, double* q, double* s, double* sig, doubl
   NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
                                [&](const Tan1DArgs& x, int n) { return launch_k1_tangent<NPV>(x, n, c.stream); },
                                "k1_tangent launch"));
+  int st = 0;
+  cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
+  cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
+  if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
+}
+
+long long pde1d_scratch_fields(const Inst1DDesc& d, int, int mode, int seg) {
+  return E1_FIELDS + P1_SNAP + (mode == 0 ? pde1_snap_fields(d.n_steps, seg) : 0);
+}
+
+// Snapshot segment of the 1D continuous adjoint: every snapshot resident when
+// the batch's scratch fits the budget, else sqrt(n)-step segments.
+int pde1d_segment(const std::vector<Inst1DDesc>& insts, int np, size_t budget) {
+  int nmax = 0;
+  for (auto& d : insts) nmax = std::max(nmax, d.n_steps);
+  if (nmax <= 1) return std::max(nmax, 1);
+  auto bytes = [&](int seg) {
+    long long t = 0;
+    for (auto& d : insts) t += pde1d_scratch_fields(d, np * d.ne, 0, seg) * (long long)np * d.ne;
+    return (size_t)t * sizeof(double);
+  };
+  if (bytes(nmax) <= budget) return nmax;
+  const int s = (int)std::ceil(std::sqrt((double)nmax));
+  if (bytes(s) > budget) throw Error(5, "device memory too small for the 1D continuous adjoint of this batch");
+  return s;
+}
+
+void pde_adjoint1d(Ctx& c, const Plan1D& P, int mode, const double* q0, const double* ain, double* a0, double* pi,
+                   double* snaps, const long long* snap_off_dev, const Solve2DOpts& o, int objective, const double* prm,
+                   int seg) {
+  double* scr = c.ws.dbl("p1:scr", (size_t)std::max<long long>(P.scratch, 1));
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
+  Pde1DArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.inst = P.d_inst; a.order = P.d_order; a.B = P.B;
+  a.q0 = q0; a.ain = ain; a.a0 = a0; a.pi = pi; a.snaps = snaps; a.snap_off = snap_off_dev;
+  a.scr = scr;
+  a.mode = mode; a.solver = o.solver; a.n_iter = o.n_iter; a.objective = objective; a.seg = std::max(seg, 1);
+  for (int k = 0; k < 4; ++k) a.prm[k] = prm ? prm[k] : 0.0;
+  a.status = c.d_status;
+  c.plan_seg = seg;
+  c.plan_groups = 1;
+  c.plan_group_size = (int)P.inst.size();
+  a.cs = cluster_size(c, P);
+  NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
+                               [&](const Pde1DArgs& x, int n) { return launch_k1_pde_adjoint<NPV>(x, n, c.stream); },
+                               "k1_pde_adjoint launch"));
   int st = 0;
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");

@@ -48,6 +48,7 @@ struct Inst1D {
   double L, dx, J, iJ, idx;  // dx = L / ne, J = dx / 2, iJ = 1/J, idx = 1/dx
   double gamma, alpha, dt;
   double t_end;  // tangent: final time of the `while t < T` stepping
+  double h;      // continuous adjoint: the backward step min(dt, T)
 };
 
 // A tile of TX x TY elements of one instance; blocks map 1:1 onto tiles.

@@ -144,6 +144,7 @@ struct Inst1DDesc {
   double L, gamma, alpha, dt;
   int n_steps;
   double t_end = 0.0;  // tangent only: final time of the `while t < T` stepping
+  double h = 0.0;      // continuous adjoint only: the backward step min(dt, T)
 };
 // A batch of 1D instances. State layout on the device: instance i's block of
 // 3 N_i doubles (mu, rho, E) starts at 3 * inst[i].off; Sigma at inst[i].off.
@@ -205,6 +206,19 @@ void pde_adjoint_ic2d(Ctx& c, const Plan2D& Pf, const Plan2D& Pa, const double* 
 // the state (q, Sigma); Pi is the warm start and returns the new Pi.
 void pde_adjoint_rhs2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const double* snap, double* Pi,
                        const double* const a[4], double* const da[4]);
+
+// 1D continuous adjoint (IGR_adjoints_1d/adjoint_pde.jl, forward.jl:137-186),
+// one persistent kernel per instance. Instance n_steps = ceil(T/dt), dt the
+// re-rounded forward step, h the backward step. mode 0: store + adjoint (q0 ->
+// a0, snapshots in scratch: all when seg >= n_steps, else checkpoints every
+// seg steps); 1: store only (q0 -> snaps); 2: adjoint only (snaps -> a0);
+// 3: one adjoint-operator evaluation (q0 = (mu, rho, E, Sigma) per instance at
+// 4 off_i, ain -> a0 = k, pi in/out).
+long long pde1d_scratch_fields(const Inst1DDesc& d, int N, int mode, int seg);
+int pde1d_segment(const std::vector<Inst1DDesc>& insts, int np, size_t budget);
+void pde_adjoint1d(Ctx& c, const Plan1D& P, int mode, const double* q0, const double* ain, double* a0, double* pi,
+                   double* snaps, const long long* snap_off_dev, const Solve2DOpts& o, int objective, const double* prm,
+                   int seg);
 
 double probe_fp64_tflops(Ctx& c);
 // y = 1 / x elementwise on stream s (no bookkeeping).

@@ -13,7 +13,9 @@ from . import DGBasis, PeriodicMesh1D, _flat, _ptr, _solver
 from ._lib import check, default_context, lib
 
 __all__ = ["DGBasis", "PeriodicMesh1D", "run_forward", "run_forward_", "forward_batch", "run_sensitivity",
-           "enzyme_adjoint_ic", "enzyme_dJ_dA", "adjoint_batch", "IC_BUILDERS", "ic_dA_weights"]
+           "enzyme_adjoint_ic", "enzyme_dJ_dA", "adjoint_batch", "IC_BUILDERS", "ic_dA_weights",
+           "Snapshots1D", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
+           "adjoint_conservative_batch"]
 
 
 class _Disc1D(C.Structure):
@@ -228,3 +230,128 @@ def enzyme_dJ_dA(A0, p, N_e, L, gamma, alpha, CFL, T, n_iter=10, ic_type="acoust
     wr, wu, wp = ic_dA_weights(ic_type)
     s = np.sin(2 * np.pi * mesh.x / L)
     return J, float(np.sum((wr * ar + wu * au + wp * ap) * s))
+
+
+# ---------------------------------------------------------------------------
+# Continuous adjoint (IGR_adjoints_1d/adjoint_pde.jl, forward.jl:137-186)
+# ---------------------------------------------------------------------------
+def _obj1(objective):
+    obj = objective.lstrip(":") if isinstance(objective, str) else objective
+    if isinstance(obj, str):
+        if obj not in _OBJ1:
+            raise ValueError("Unknown objective: %s (use :l2_density, :l2_pressure, or :kinetic_energy)" % objective)
+        obj = _OBJ1[obj]
+    return obj
+
+
+class Snapshots1D:
+    """The snapshot list of run_forward_store (forward.jl:137-186):
+    snapshots[k] = (mu, rho, E, Sigma) after step k, each (n_p, N_e) in Julia
+    order; `data` is the flat (n_steps + 1, 4, N) buffer of the C ABI."""
+
+    def __init__(self, data, shape):
+        self.data = data
+        self.shape = tuple(shape)
+
+    def __len__(self):
+        return self.data.shape[0]
+
+    def __getitem__(self, k):
+        return tuple(self.data[k, v].reshape(self.shape, order="F") for v in range(4))
+
+    @classmethod
+    def from_list(cls, snaps, shape):
+        n = int(np.prod(shape))
+        return cls(np.ascontiguousarray(np.stack([np.stack([_flat(a, n) for a in s]) for s in snaps])), shape)
+
+
+def run_forward_store(mu0, rho0, E0, dt, T, basis, mesh, gamma, alpha, n_iter=10, solver="pcg", ctx=None):
+    """run_forward_store (IGR_adjoints_1d/forward.jl:137-186): (snapshots, n_steps)."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    if not (dt > 0 and T > 0):
+        raise ValueError("dt and T must be positive")
+    steps = int(np.ceil(T / dt))
+    data = np.zeros((steps + 1, 4, n))
+    ns = C.c_int(0)
+    q = [_flat(a, n) for a in (mu0, rho0, E0)]
+    check(ctx, lib().igr1d_run_forward_store(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(gamma),
+                                             C.c_double(alpha), C.c_double(dt), C.c_double(T), C.c_int(n_iter),
+                                             C.c_int(_solver(solver)), *[_ptr(a) for a in q], _ptr(data),
+                                             C.c_longlong(data.size), C.byref(ns)))
+    return Snapshots1D(data, shape), ns.value
+
+
+def run_adjoint_conservative(snapshots, n_steps, dt, T, basis, mesh, gamma, alpha, n_iter=10, objective="l2_density",
+                             solver="pcg", obj_params=None, ctx=None):
+    """run_adjoint_conservative (IGR_adjoints_1d/adjoint_pde.jl:474-551):
+    (a_mu, a_rho, a_E) at t = 0 from the snapshots of run_forward_store."""
+    _solver(solver)  # validate before touching the device
+    obj = _obj1(objective)
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    if not isinstance(snapshots, Snapshots1D):
+        snapshots = Snapshots1D.from_list(snapshots, shape)
+    data = np.ascontiguousarray(snapshots.data, dtype=np.float64)
+    prm = np.zeros(4) if obj_params is None else np.ascontiguousarray(np.resize(np.asarray(obj_params, np.float64), 4))
+    out = [np.zeros(n) for _ in range(3)]
+    check(ctx, lib().igr1d_run_adjoint_conservative(ctx.handle, C.byref(_disc1d(basis, mesh)), _ptr(data),
+                                                    C.c_longlong(data.size), C.c_int(n_steps), C.c_double(dt),
+                                                    C.c_double(T), C.c_double(gamma), C.c_double(alpha),
+                                                    C.c_int(n_iter), C.c_int(obj), C.c_int(_solver(solver)), _ptr(prm),
+                                                    *[_ptr(a) for a in out]))
+    return tuple(np.asfortranarray(a.reshape(shape, order="F")) for a in out)
+
+
+def compute_adjoint_rhs_conservative_(damu, darho, daE, amu, arho, aE, mu, rho, E, Sigma, Pi, basis, mesh, gamma, alpha,
+                                      n_iter=10, solver="pcg", ctx=None):
+    """compute_adjoint_rhs_conservative! (IGR_adjoints_1d/adjoint_pde.jl:410-456):
+    in place; Pi is the warm start and returns the new Pi (alpha > 0)."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    q = [_flat(x, n) for x in (mu, rho, E, Sigma)]
+    a = [_flat(x, n) for x in (amu, arho, aE)]
+    P = _flat(Pi, n).copy()
+    out = [np.zeros(n) for _ in range(3)]
+    check(ctx, lib().igr1d_adjoint_rhs_conservative(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(gamma),
+                                                    C.c_double(alpha), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                                    *[_ptr(x) for x in q], _ptr(P), *[_ptr(x) for x in a],
+                                                    *[_ptr(x) for x in out]))
+    for dst, src in zip((damu, darho, daE), out):
+        dst[...] = src.reshape(shape, order="F")
+    Pi[...] = P.reshape(shape, order="F")
+
+
+def adjoint_conservative_batch(states, basis, n_e, L, gammas, alphas, dts, T, n_iter=10, solver="pcg",
+                               objective="l2_density", obj_params=None, ctx=None):
+    """run_forward_store + run_adjoint_conservative for a batch of 1D instances
+    in one launch (snapshots on the device). states: list of (mu0, rho0, E0);
+    dts and T per instance (scalars broadcast). Returns [(a_mu, a_rho, a_E)]."""
+    _solver(solver)  # validate before touching the device
+    obj = _obj1(objective)
+    ctx = ctx or default_context()
+    n_e = np.ascontiguousarray(n_e, dtype=np.int32)
+    B = n_e.size
+    sizes = basis.n_p * n_e
+    q = np.concatenate([np.concatenate([_flat(x, int(sizes[i])) for x in states[i]]) for i in range(B)])
+    a0 = np.zeros_like(q)
+    f64 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (B,)))
+    Ls, gs, als, dtv, Ts = f64(L), f64(gammas), f64(alphas), f64(dts), f64(T)
+    prm = np.zeros(4) if obj_params is None else np.ascontiguousarray(np.resize(np.asarray(obj_params, np.float64), 4))
+    check(ctx, lib().igr1d_adjoint_conservative_batch(ctx.handle, C.c_int(basis.p), _ptr(basis.xi), _ptr(basis.w),
+                                                      _ptr(basis._Dcol), C.c_int(B),
+                                                      n_e.ctypes.data_as(C.POINTER(C.c_int)), _ptr(Ls), _ptr(gs),
+                                                      _ptr(als), _ptr(dtv), _ptr(Ts), C.c_int(n_iter),
+                                                      C.c_int(_solver(solver)), C.c_int(obj), _ptr(prm), _ptr(q),
+                                                      _ptr(a0)))
+    out, o3 = [], 0
+    for i in range(B):
+        n = int(sizes[i])
+        out.append((a0[o3:o3 + n], a0[o3 + n:o3 + 2 * n], a0[o3 + 2 * n:o3 + 3 * n]))
+        o3 += 3 * n
+    return out

@@ -321,6 +321,46 @@ int igr1d_adjoint_batch(igr_ctx* ctx, int p, const double* xi, const double* w, 
                         const double* obj_params, const double* q0, double* J, double* dq0, double* dgamma,
                         double* dalpha);
 
+/* ---- 1D continuous adjoint (optimise-then-discretise) ---------------------- */
+
+/* run_forward_store (IGR_adjoints_1d/forward.jl:137-186): n_steps = ceil(T/dt),
+ * dt = T/n_steps, one more Sigma solve after every step (and at t = 0);
+ * snapshots: (n_steps + 1) x 4 x N doubles, snapshot k = (mu, rho, E, Sigma)
+ * after step k; snapshots_len must equal (ceil(T/dt) + 1) * 4 * N. */
+int igr1d_run_forward_store(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
+                            int n_iter, int solver, const double* mu0, const double* rho0, const double* E0,
+                            double* snapshots, long long snapshots_len, int* n_steps);
+
+/* run_adjoint_conservative (IGR_adjoints_1d/adjoint_pde.jl:474-551): backward
+ * SSP-RK3 of the adjoint PDE over the snapshots (step min(dt, T), one Pi solve
+ * per stage). Objectives: IGR_OBJ_L2_DENSITY, _L2_PRESSURE, _KINETIC_ENERGY,
+ * _WEIGHTED_MOMENTUM (adjoint_pde.jl:487-525) and IGR_OBJ_INTERVAL_RHO
+ * (a_rho = indicator of [a, b], obj_params = {a, b}; no reference
+ * counterpart). Output: (a_mu, a_rho, a_E) at t = 0. */
+int igr1d_run_adjoint_conservative(igr_ctx* ctx, const igr_disc1d* d, const double* snapshots, long long snapshots_len,
+                                   int n_steps, double dt, double t_end, double gamma, double alpha, int n_iter,
+                                   int objective, int solver, const double* obj_params, double* amu, double* arho,
+                                   double* aE);
+
+/* compute_adjoint_rhs_conservative! (IGR_adjoints_1d/adjoint_pde.jl:410-456):
+ * the adjoint operator at (mu, rho, E, sigma) applied to a; pi is the Pi
+ * warm start in and the solution out (alpha > 0). */
+int igr1d_adjoint_rhs_conservative(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, int n_iter, int solver,
+                                   const double* mu, const double* rho, const double* E, const double* sigma, double* pi,
+                                   const double* amu, const double* arho, const double* aE, double* damu, double* darho,
+                                   double* daE);
+
+/* Store + adjoint for a batch of 1D instances (each with its own n_e, L,
+ * gamma, alpha, dt and T) in one launch of per-instance persistent CTAs, the
+ * snapshots kept on the device (all, or sqrt(n)-step segments recomputed from
+ * checkpoints when memory is short). q0 and a0: concatenations of
+ * (mu, rho, E) per instance as in igr1d_forward_batch. No counterpart in the
+ * reference. */
+int igr1d_adjoint_conservative_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,
+                                     const int* n_e, const double* L, const double* gammas, const double* alphas,
+                                     const double* dts, const double* t_ends, int n_iter, int solver, int objective,
+                                     const double* obj_params, const double* q0, double* a0);
+
 #ifdef __cplusplus
 }
 #endif
