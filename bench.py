@@ -315,6 +315,54 @@ def secondary(args):
                                         "interval rho objective", "sample_steps": ns, "full_steps": nfull},
                     cpu_baseline={"value": 1024 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
                                   "sample": "one instance per N_e for 2 steps, scaled by counts and to 2000 steps"})
+    elif args.workload == "pde_batch1d":
+        # the batch1d instances through the continuous adjoint (store + backward PDE, one persistent CTA per
+        # instance, snapshots on the device), a bounded sample of the 2000 steps, scaled
+        basis = igr.DGBasis(3)
+        rng = W.SplitMix64(W.seed_for(4, 0xB))
+        nes = [64 * 2 ** int(rng.uniform(0, 5)) for _ in range(1024)]
+        gs = [rng.uniform(1.2, 1.8) for _ in range(1024)]
+        states, dts, als = [], [], []
+        for i, ne in enumerate(nes):
+            mesh = igr.PeriodicMesh1D(ne, 1.0, basis)
+            q0 = W.seeded_pulses_1d(mesh, gs[i], W.seed_for(4, i), n_pulses=2, width=0.02)
+            states.append(tuple(flat(a) for a in q0))
+            dts.append(W.cfl_dt_1d(mesh, 3, q0, gs[i], 0.1))
+            als.append(3.0 * mesh.dx ** 2)
+        ns, nfull = args.n_steps if args.n_steps != N_STEPS else 10, 2000
+        Ts = [ns * dt * 0.999 for dt in dts]  # ceil(T / dt) = ns
+        prm = W.seeded_interval(W.seed_for(4, 0))
+        k = 152 if args.profile_case else 1024
+        run = lambda: igr1d.adjoint_conservative_batch(states[:k], basis, nes[:k], 1.0, gs[:k], als[:k], dts[:k], Ts[:k],
+                                                       n_iter=102, solver="pcg", objective="interval_rho",
+                                                       obj_params=prm, ctx=ctx)
+        if args.profile_case:
+            run()
+            print("profile case done")
+            return
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        t = (time.perf_counter() - t0) / args.steps
+        tc = 0.0
+        for ne in (64, 128, 256, 512, 1024):
+            G = O.Grid1D(3, ne)
+            i = nes.index(ne)
+            tc0 = time.perf_counter()
+            sn, n2 = O.run_forward_store_1d(G, gs[i], als[i], dts[i], 2 * dts[i] * 0.999, 102, "pcg", list(states[i]))
+            O.run_adjoint_conservative_1d(G, sn, n2, dts[i], 2 * dts[i] * 0.999, gs[i], als[i], 102, "interval_rho", "pcg",
+                                          prm)
+            tc += (time.perf_counter() - tc0) * nes.count(ne) * nfull / 2
+        line.update(metric="1D batch of 1024 (N_e in {64..1024}, P3, PCG 102) continuous-adjoint gradients/s",
+                    value=1024 * ns / nfull / t, unit="gradients/s (2000-step equivalents)", ms_per_step=t * 1e3,
+                    gpu_launches=ctx.last_launch_count(),
+                    config={"workload": "1024 1D instances, N_e ~ U{64..1024}, gamma ~ U[1.2,1.8], PCG 102, interval rho "
+                                        "objective, run_forward_store + run_adjoint_conservative",
+                            "sample_steps": ns, "full_steps": nfull},
+                    cpu_baseline={"value": 1024 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
+                                  "sample": "one instance per N_e for 2 steps, scaled by counts and to 2000 steps"})
     elif args.workload == "pde_adjoint2d":
         # the headline's batch (32 x 128^2 P3, Chebyshev 5, 200 steps, window rho^2) through the continuous
         # adjoint: run_forward_store + run_adjoint_conservative with device-resident snapshots
@@ -390,7 +438,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
     ap.add_argument("--workload", default="adjoint2d",
-                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d")
+                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | pde_batch1d")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()
