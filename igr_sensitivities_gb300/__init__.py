@@ -24,6 +24,8 @@ __all__ = [
     "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
     "Snapshots", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
     "adjoint_conservative_ic", "adjoint_conservative_batch",
+    "init_constant_state", "init_isentropic_vortex", "build_taylor_green_ic_", "build_sedov_blast_ic_",
+    "build_oseen_pair_blast_ic_", "IC_BUILDERS", "ic_dA_weights", "l2_error", "build_ic_batch", "IC_TYPES",
 ]
 
 SOLVERS = {"pcg": 0, "jacobi": 1, "chebyshev": 2}
@@ -101,6 +103,7 @@ class CartesianMesh2D:
 
     def __init__(self, N_ex, N_ey, Lx, Ly, basis):
         self.N_ex, self.N_ey, self.Lx, self.Ly = int(N_ex), int(N_ey), float(Lx), float(Ly)
+        self.basis = basis  # node coordinates depend on it; the IC builders take (mesh, gamma) as the reference does
         self.dx, self.dy = self.Lx / self.N_ex, self.Ly / self.N_ey
         self.Jx, self.Jy = self.dx / 2.0, self.dy / 2.0
         n = basis.n_p
@@ -120,6 +123,7 @@ class PeriodicMesh1D:
 
     def __init__(self, N_e, L, basis):
         self.N_e, self.L = int(N_e), float(L)
+        self.basis = basis
         self.dx = self.L / self.N_e
         self.J = self.dx / 2.0
         e = np.arange(self.N_e)[None, :]
@@ -524,3 +528,109 @@ def adjoint_conservative_batch(q0, gammas, alphas, dts, T, basis, mesh, n_iter=1
                                                       C.c_int(_objective(objective)), _ptr(_prm(obj_params)), _ptr(q0),
                                                       _ptr(a0)))
     return a0
+
+
+# ---------------------------------------------------------------------------
+# Initial conditions (IGR_adjoints_2d/initial_conditions.jl), built on the GPU
+# ---------------------------------------------------------------------------
+IC_TYPES = {"constant": 0, "isentropic_vortex": 1, "taylor_green": 2, "sedov_blast": 3, "oseen_pair_blast": 4}
+
+
+def build_ic_batch(ic_type, basis, mesh, gammas, amps, params=None, device_array=False, ctx=None):
+    """Initial states of a batch on one mesh, built on the GPU: (n_inst, 4, N)
+    in the Julia node order (numpy, or a torch CUDA tensor with
+    device_array=True, the input adjoint_batch(device_arrays=True) takes).
+    params: the builder's keyword arguments in the order of include/igr_gb300.h
+    (None: the reference's defaults)."""
+    key = ic_type.lstrip(":") if isinstance(ic_type, str) else ic_type
+    if isinstance(key, str):
+        if key not in IC_TYPES:
+            raise ValueError("Unknown IC type: %s" % ic_type)
+        key = IC_TYPES[key]
+    ctx = ctx or default_context()
+    gammas = np.ascontiguousarray(np.atleast_1d(np.asarray(gammas, dtype=np.float64)))
+    B = gammas.size
+    amps = np.ascontiguousarray(np.broadcast_to(np.asarray(amps, dtype=np.float64), (B,)))
+    prm = None if params is None else np.ascontiguousarray(np.asarray(params, dtype=np.float64))
+    pp = None if prm is None else _ptr(prm)
+    n = mesh.x.size
+    d = _disc2d(basis, mesh)
+    if device_array:
+        import torch
+        q = torch.empty((B, 4, n), dtype=torch.float64, device="cuda")
+        check(ctx, lib().igr2d_build_ic_dev(ctx.handle, C.byref(d), C.c_int(key), C.c_int(B), _ptr(gammas), _ptr(amps),
+                                            pp, C.cast(C.c_void_p(q.data_ptr()), _D)))
+        return q
+    q = np.zeros((B, 4, n))
+    check(ctx, lib().igr2d_build_ic(ctx.handle, C.byref(d), C.c_int(key), C.c_int(B), _ptr(gammas), _ptr(amps), pp,
+                                    _ptr(q)))
+    return q
+
+
+def _build_one(ic_type, mesh, gamma, A, params, ctx):
+    q = build_ic_batch(ic_type, mesh.basis, mesh, [gamma], [A], params, ctx=ctx)[0]
+    shape = mesh.shape(mesh.basis)
+    return tuple(np.asfortranarray(q[v].reshape(shape, order="F")) for v in range(4))
+
+
+def init_constant_state(mesh, gamma, rho0=1.0, ux0=1.0, uy0=1.0, p0=1.0, ctx=None):
+    """init_constant_state (initial_conditions.jl:15-22): (mux, muy, rho, E)."""
+    return _build_one("constant", mesh, gamma, 0.0, [rho0, ux0, uy0, p0], ctx)
+
+
+def init_isentropic_vortex(mesh, gamma, beta=5.0, ux0=1.0, uy0=1.0, ctx=None):
+    """init_isentropic_vortex (initial_conditions.jl:39-67): (mux, muy, rho, E)."""
+    return _build_one("isentropic_vortex", mesh, gamma, 0.0, [beta, ux0, uy0], ctx)
+
+
+def _fill(dst, src):
+    for a, b in zip(dst, src):
+        a[...] = b
+
+
+def build_taylor_green_ic_(mux0, muy0, rho0, E0, A, mesh, gamma, ctx=None):
+    """build_taylor_green_ic! (initial_conditions.jl:105-121), in place."""
+    _fill((mux0, muy0, rho0, E0), _build_one("taylor_green", mesh, gamma, A, None, ctx))
+
+
+def build_sedov_blast_ic_(mux0, muy0, rho0, E0, A, mesh, gamma, p_bg=1.0, sigma=0.1, ctx=None):
+    """build_sedov_blast_ic! (initial_conditions.jl:136-150), in place."""
+    _fill((mux0, muy0, rho0, E0), _build_one("sedov_blast", mesh, gamma, A, [p_bg, sigma], ctx))
+
+
+def build_oseen_pair_blast_ic_(mux0, muy0, rho0, E0, A, mesh, gamma, a_core=0.05, M_star=0.5,
+                               vort_centers=((0.45, 0.60, +1), (0.45, 0.40, -1)), blast_xc=0.25, blast_yc=0.50,
+                               sigma=0.09, ctx=None):
+    """build_oseen_pair_blast_ic! (initial_conditions.jl:175-231), in place
+    (two vortices, as the reference's pair)."""
+    if len(vort_centers) != 2:
+        raise ValueError("vort_centers must hold two (xc, yc, sign) triples")
+    prm = [a_core, M_star, blast_xc, blast_yc, sigma] + [float(v) for c in vort_centers for v in c]
+    _fill((mux0, muy0, rho0, E0), _build_one("oseen_pair_blast", mesh, gamma, A, prm, ctx))
+
+
+# IC_BUILDERS and ic_dA_weights of initial_conditions.jl:240-258
+IC_BUILDERS = {
+    "taylor_green": (build_taylor_green_ic_, "ux=A sin cos, uy=-A cos sin, rho=1, p=1"),
+    "sedov_blast": (build_sedov_blast_ic_, "rho=1, u=0, p=p_bg+A exp(-r^2/sigma^2)"),
+}
+
+
+def ic_dA_weights(ic_type):
+    """(w_rho, w_ux, w_uy, w_p): which primitive variables carry d/dA."""
+    key = ic_type.lstrip(":")
+    if key == "taylor_green":
+        return (0.0, 1.0, 1.0, 0.0)
+    if key == "sedov_blast":
+        return (0.0, 0.0, 0.0, 1.0)
+    raise ValueError("Unknown IC type: %s" % ic_type)
+
+
+def l2_error(u, u_ref, basis, mesh, ctx=None):
+    """l2_error (initial_conditions.jl:74-87): the LGL-quadrature L2 norm of u - u_ref."""
+    ctx = ctx or default_context()
+    n = mesh.x.size
+    v = C.c_double(0.0)
+    check(ctx, lib().igr2d_l2_error(ctx.handle, C.byref(_disc2d(basis, mesh)), _ptr(_flat(u, n)), _ptr(_flat(u_ref, n)),
+                                    C.byref(v)))
+    return v.value

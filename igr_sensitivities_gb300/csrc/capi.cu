@@ -1008,4 +1008,85 @@ int igr1d_adjoint_conservative_batch(igr_ctx* ctx, int p, const double* xi, cons
   });
 }
 
+// ---- initial conditions -------------------------------------------------------------------
+namespace {
+Plan2D ic_plan(Ctx& c, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas, const double* amps) {
+  check_disc(d);
+  if (ic_type < 0 || ic_type > 4) throw Error(IGR_EINVAL, "Unknown IC type");
+  if (n_inst < 1 || !gammas || !amps) throw Error(IGR_EINVAL, "bad batch arguments");
+  BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+  std::vector<Inst2DDesc> insts;
+  for (int b = 0; b < n_inst; ++b) insts.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], 0.0, 0.0});
+  return make_plan2d(c, B, insts, "ic");
+}
+}  // namespace
+
+int igr2d_build_ic(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas, const double* amps,
+                   const double* params, double* q) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!q) throw Error(IGR_EINVAL, "null output");
+    Plan2D P = ic_plan(c, d, ic_type, n_inst, gammas, amps);
+    const long long N = nodes2d(d), NG = P.NG;
+    double* buf = c.ws.dbl("capi:ic", 4 * (size_t)NG);
+    double* f[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
+    build_ic2d(c, P, ic_type, amps, params, f);
+    for (int v = 0; v < 4; ++v)  // field-major [var][inst*N] -> [inst][var][N]
+      cuda_check(cudaMemcpy2DAsync(q + v * N, 4 * N * sizeof(double), f[v], N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyDeviceToHost, c.stream), "scatter ic");
+    sync(c);
+  });
+}
+
+int igr2d_build_ic_dev(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas,
+                       const double* amps, const double* params, double* q_dev) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!q_dev) throw Error(IGR_EINVAL, "null output");
+    Plan2D P = ic_plan(c, d, ic_type, n_inst, gammas, amps);
+    const long long N = nodes2d(d), NG = P.NG;
+    double* buf = c.ws.dbl("capi:ic", 4 * (size_t)NG);
+    double* f[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
+    build_ic2d(c, P, ic_type, amps, params, f);
+    for (int v = 0; v < 4; ++v)
+      cuda_check(cudaMemcpy2DAsync(q_dev + v * N, 4 * N * sizeof(double), f[v], N * sizeof(double), N * sizeof(double),
+                                   n_inst, cudaMemcpyDeviceToDevice, c.stream), "scatter ic");
+    sync(c);
+  });
+}
+
+int igr2d_l2_error(igr_ctx* ctx, const igr_disc2d* d, const double* u, const double* u_ref, double* err) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!err) throw Error(IGR_EINVAL, "null output");
+    Plan2D P = plan_single(c, d, 1.4, 0.0, 0.0, "l2e");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:l2e", 2 * (size_t)N);
+    h2d(c, buf, u, N);
+    h2d(c, buf + N, u_ref, N);
+    *err = l2_error2d(c, P, buf, buf + N);
+  });
+}
+
+int igr1d_build_ic(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst, const int* n_e,
+                   const double* L, int ic_type, const double* gammas, const double* amps, double* q) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc1(p, xi, w, D);
+    if (ic_type < 0 || ic_type > 4) throw Error(IGR_EINVAL, "Unknown IC type");
+    if (n_inst < 1 || !n_e || !L || !gammas || !amps || !q) throw Error(IGR_EINVAL, "bad batch arguments");
+    BasisDev B = make_basis_dev(p, xi, w, D);
+    std::vector<Inst1DDesc> insts;
+    for (int i = 0; i < n_inst; ++i) {
+      if (n_e[i] < 1 || !(L[i] > 0)) throw Error(IGR_EINVAL, "bad mesh");
+      insts.push_back(Inst1DDesc{n_e[i], L[i], gammas[i], 0.0, 0.0, 0});
+    }
+    Plan1D P = make_plan1d(c, B, insts, [](const Inst1DDesc&, int) { return 0LL; }, "ic1");
+    double* buf = c.ws.dbl("capi1:ic", 3 * (size_t)P.NG);
+    build_ic1d(c, P, ic_type, amps, buf);
+    d2h(c, q, buf, 3 * P.NG);
+    sync(c);
+  });
+}
+
 }  // extern "C"

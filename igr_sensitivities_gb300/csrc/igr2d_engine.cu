@@ -179,22 +179,6 @@ struct ObjArgs2D {
   long long NG;
 };
 
-__device__ __forceinline__ int find_inst(const Inst2D* inst, int ninst, long long n) {
-  int lo = 0, hi = ninst - 1;
-  while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (inst[mid].off <= n) lo = mid; else hi = mid - 1; }
-  return lo;
-}
-
-__device__ __forceinline__ void node_coords2d(const BasisDev& B, const Inst2D& I, long long local, double* c, double* x, double* y) {
-  const int nn = B.np * B.np;
-  const long long el = local / nn;
-  const int nd = (int)(local % nn);
-  const int i = nd % B.np, j = nd / B.np;
-  const int ex = (int)(el % I.nex), ey = (int)(el / I.nex);
-  *c = B.w[i] * B.w[j] * I.jx * I.jy;
-  *x = ex * I.dx + I.jx * (1.0 + B.xi[i]);
-  *y = ey * I.dy + I.jy * (1.0 + B.xi[j]);
-}
 
 __global__ void k2_obj_nodes(ObjArgs2D a) {
   const double pi = 3.14159265358979323846;

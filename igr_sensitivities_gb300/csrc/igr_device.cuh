@@ -80,6 +80,26 @@ __device__ __forceinline__ double block_sum(double v, double* s_red) {
   return r;
 }
 
+// Instance of global node n (binary search over the instances' first nodes).
+__device__ __forceinline__ int find_inst(const Inst2D* inst, int ninst, long long n) {
+  int lo = 0, hi = ninst - 1;
+  while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (inst[mid].off <= n) lo = mid; else hi = mid - 1; }
+  return lo;
+}
+
+// Quadrature weight w_i w_j Jx Jy and coordinates (mesh.jl:116-122) of the
+// instance-local node `local` in the Julia (n_p, n_p, N_ex, N_ey) order.
+__device__ __forceinline__ void node_coords2d(const BasisDev& B, const Inst2D& I, long long local, double* c, double* x, double* y) {
+  const int nn = B.np * B.np;
+  const long long el = local / nn;
+  const int nd = (int)(local % nn);
+  const int i = nd % B.np, j = nd / B.np;
+  const int ex = (int)(el % I.nex), ey = (int)(el / I.nex);
+  *c = B.w[i] * B.w[j] * I.jx * I.jy;
+  *x = ex * I.dx + I.jx * (1.0 + B.xi[i]);
+  *y = ey * I.dy + I.jy * (1.0 + B.xi[j]);
+}
+
 // Smallest power of two >= n (n <= 1024), for block_sum's scratch size.
 __host__ __device__ constexpr int pow2_at_least(int n) {
   return n <= 1 ? 1 : (n <= 2 ? 2 : (n <= 4 ? 4 : (n <= 8 ? 8 : (n <= 16 ? 16 : (n <= 32 ? 32 : (n <= 64 ? 64 :

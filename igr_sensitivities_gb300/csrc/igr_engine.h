@@ -220,6 +220,19 @@ void pde_adjoint1d(Ctx& c, const Plan1D& P, int mode, const double* q0, const do
                    double* snaps, const long long* snap_off_dev, const Solve2DOpts& o, int objective, const double* prm,
                    int seg);
 
+// Initial-condition builders (IGR_adjoints_2d/initial_conditions.jl:15-232;
+// 1D :94-204) for every instance of a plan; amps: per-instance amplitude A
+// (host); params: the builder's keyword arguments (nullptr = the reference's
+// defaults). 2D types: 0 constant, 1 isentropic vortex, 2 Taylor-Green,
+// 3 Sedov blast, 4 Oseen pair + blast; 1D: 0 acoustic, 1 entropy wave,
+// 2 density, 3 pressure, 4 velocity pulse. q: device fields (2D: 4 of NG;
+// 1D: the batch layout).
+int ic2d_param_count(int type);
+void build_ic2d(Ctx& c, const Plan2D& P, int type, const double* amps, const double* params, double* const q[4]);
+void build_ic1d(Ctx& c, const Plan1D& P, int type, const double* amps, double* q);
+// l2_error (initial_conditions.jl:74-87) over all nodes of the plan.
+double l2_error2d(Ctx& c, const Plan2D& P, const double* u, const double* r);
+
 double probe_fp64_tflops(Ctx& c);
 // y = 1 / x elementwise on stream s (no bookkeeping).
 void launch_recip(const double* x, double* y, long long n, cudaStream_t s);

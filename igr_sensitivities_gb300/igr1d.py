@@ -15,7 +15,7 @@ from ._lib import check, default_context, lib
 __all__ = ["DGBasis", "PeriodicMesh1D", "run_forward", "run_forward_", "forward_batch", "run_sensitivity",
            "enzyme_adjoint_ic", "enzyme_dJ_dA", "adjoint_batch", "IC_BUILDERS", "ic_dA_weights",
            "Snapshots1D", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
-           "adjoint_conservative_batch"]
+           "adjoint_conservative_batch", "build_ic_batch", "IC_TYPES"]
 
 
 class _Disc1D(C.Structure):
@@ -353,5 +353,36 @@ def adjoint_conservative_batch(states, basis, n_e, L, gammas, alphas, dts, T, n_
     for i in range(B):
         n = int(sizes[i])
         out.append((a0[o3:o3 + n], a0[o3 + n:o3 + 2 * n], a0[o3 + 2 * n:o3 + 3 * n]))
+        o3 += 3 * n
+    return out
+
+
+IC_TYPES = {"acoustic_pulse": 0, "entropy_wave": 1, "density_pulse": 2, "pressure_pulse": 3, "velocity_pulse": 4}
+
+
+def build_ic_batch(ic_type, basis, n_e, L, gammas, amps, ctx=None):
+    """The IC_BUILDERS of IGR_adjoints_1d/initial_conditions.jl:94-224 for a
+    batch of instances (own n_e, L, gamma, amplitude A), built on the GPU.
+    Returns [(mu0, rho0, E0)] (flat, Julia order), the input adjoint_batch and
+    adjoint_conservative_batch take."""
+    key = ic_type.lstrip(":") if isinstance(ic_type, str) else ic_type
+    if isinstance(key, str):
+        if key not in IC_TYPES:
+            raise ValueError("Unknown IC type: %s" % ic_type)
+        key = IC_TYPES[key]
+    ctx = ctx or default_context()
+    n_e = np.ascontiguousarray(np.atleast_1d(n_e), dtype=np.int32)
+    B = n_e.size
+    f64 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (B,)))
+    Ls, gs, As = f64(L), f64(gammas), f64(amps)
+    sizes = basis.n_p * n_e
+    q = np.zeros(3 * int(sizes.sum()))
+    check(ctx, lib().igr1d_build_ic(ctx.handle, C.c_int(basis.p), _ptr(basis.xi), _ptr(basis.w), _ptr(basis._Dcol),
+                                    C.c_int(B), n_e.ctypes.data_as(C.POINTER(C.c_int)), _ptr(Ls), C.c_int(key), _ptr(gs),
+                                    _ptr(As), _ptr(q)))
+    out, o3 = [], 0
+    for i in range(B):
+        n = int(sizes[i])
+        out.append((q[o3:o3 + n], q[o3 + n:o3 + 2 * n], q[o3 + 2 * n:o3 + 3 * n]))
         o3 += 3 * n
     return out

@@ -361,6 +361,42 @@ int igr1d_adjoint_conservative_batch(igr_ctx* ctx, int p, const double* xi, cons
                                      const double* dts, const double* t_ends, int n_iter, int solver, int objective,
                                      const double* obj_params, const double* q0, double* a0);
 
+/* ---- Initial conditions ------------------------------------------------------ */
+
+/* 2D builders (IGR_adjoints_2d/initial_conditions.jl). */
+typedef enum {
+  IGR_IC2D_CONSTANT = 0,          /* init_constant_state, :15; params (rho0, ux0, uy0, p0) = (1, 1, 1, 1) */
+  IGR_IC2D_ISENTROPIC_VORTEX = 1, /* init_isentropic_vortex, :39; params (beta, ux0, uy0) = (5, 1, 1) */
+  IGR_IC2D_TAYLOR_GREEN = 2,      /* build_taylor_green_ic!, :105; amplitude A, no params */
+  IGR_IC2D_SEDOV_BLAST = 3,       /* build_sedov_blast_ic!, :136; params (p_bg, sigma) = (1, 0.1) */
+  IGR_IC2D_OSEEN_PAIR_BLAST = 4   /* build_oseen_pair_blast_ic!, :175; params (a_core, M_star, blast_xc,
+                                     blast_yc, sigma, xc1, yc1, sign1, xc2, yc2, sign2) = (0.05, 0.5, 0.25,
+                                     0.5, 0.09, 0.45, 0.6, +1, 0.45, 0.4, -1) */
+} igr_ic2d;
+
+/* Builds the initial state of n_inst instances on one mesh, each with its own
+ * gamma and amplitude A (ignored by the constant state and the vortex), on the
+ * GPU: q is (n_inst, 4, N) doubles (mux, muy, rho, E per instance, Julia node
+ * order), host memory; params may be NULL (the reference's defaults). */
+int igr2d_build_ic(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas, const double* amps,
+                   const double* params, double* q);
+/* The same into device memory (q_dev: n_inst * 4 * N doubles), for batched
+ * calls such as igr2d_adjoint_batch_dev that take device inputs. */
+int igr2d_build_ic_dev(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas,
+                       const double* amps, const double* params, double* q_dev);
+/* l2_error (IGR_adjoints_2d/initial_conditions.jl:74-87): sqrt(sum w_i w_j Jx Jy (u - u_ref)^2). */
+int igr2d_l2_error(igr_ctx* ctx, const igr_disc2d* d, const double* u, const double* u_ref, double* err);
+
+/* 1D builders (IGR_adjoints_1d/initial_conditions.jl:94-204, IC_BUILDERS :218). */
+typedef enum {
+  IGR_IC1D_ACOUSTIC_PULSE = 0, IGR_IC1D_ENTROPY_WAVE = 1, IGR_IC1D_DENSITY_PULSE = 2, IGR_IC1D_PRESSURE_PULSE = 3,
+  IGR_IC1D_VELOCITY_PULSE = 4
+} igr_ic1d;
+/* n_inst instances with their own n_e, L, gamma and amplitude A; q: the
+ * concatenation of (mu, rho, E) per instance as igr1d_forward_batch takes it. */
+int igr1d_build_ic(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst, const int* n_e,
+                   const double* L, int ic_type, const double* gammas, const double* amps, double* q);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,6 +11,7 @@
 #include "igr2d_adjoint.hpp"
 #include "igr2d_pde_adjoint.hpp"
 #include "igr1d_pde_adjoint.hpp"
+#include "igr_ic.hpp"
 
 using namespace igr;
 
@@ -389,6 +390,18 @@ int orc1d_pde_duality(GRID1D_ARGS, double gamma, const double* q_in, const doubl
       }
     *lhs = l; *rhs = r;
   });
+}
+
+// IC builders (IGR_adjoints_2d/initial_conditions.jl:15-232; 1d :94-204) and l2_error.
+int orc2d_build_ic(GRID2D_ARGS, int type, double gamma, double A, const double* prm, double* mx, double* my, double* rho,
+                   double* E) {
+  return guard([&] { Grid2D G = GRID2D; double* q[4] = {mx, my, rho, E}; build_ic2d(G, type, gamma, A, prm, q); });
+}
+int orc1d_build_ic(GRID1D_ARGS, int type, double gamma, double A, double* mu, double* rho, double* E) {
+  return guard([&] { Grid1D G = GRID1D; double* q[3] = {mu, rho, E}; build_ic1d(G, type, gamma, A, q); });
+}
+int orc2d_l2_error(GRID2D_ARGS, const double* u, const double* r, double* out) {
+  return guard([&] { Grid2D G = GRID2D; *out = l2_error2d(G, u, r); });
 }
 
 }  // extern "C"

@@ -367,3 +367,26 @@ def pde_duality_1d(G, gamma, q, Sig, a, dq):
     _check(lib().orc1d_pde_duality(*G.args(), C.c_double(gamma), _p(_f(np.concatenate(q))), _p(_f(Sig)),
                                    _p(_f(np.concatenate(a))), _p(_f(np.concatenate(dq))), C.byref(l), C.byref(r)))
     return l.value, r.value
+
+
+IC2D = {"constant": 0, "isentropic_vortex": 1, "taylor_green": 2, "sedov_blast": 3, "oseen_pair_blast": 4}
+IC1D = {"acoustic_pulse": 0, "entropy_wave": 1, "density_pulse": 2, "pressure_pulse": 3, "velocity_pulse": 4}
+
+
+def build_ic_2d(G, ic, gamma, A, prm):
+    out = [G.zeros() for _ in range(4)]
+    _check(lib().orc2d_build_ic(*G.args(), C.c_int(IC2D[ic]), C.c_double(gamma), C.c_double(A),
+                                _p(_f(np.asarray(prm, dtype=np.float64))), *[_p(a) for a in out]))
+    return out
+
+
+def build_ic_1d(G, ic, gamma, A):
+    out = [np.zeros(G.N) for _ in range(3)]
+    _check(lib().orc1d_build_ic(*G.args(), C.c_int(IC1D[ic]), C.c_double(gamma), C.c_double(A), *[_p(a) for a in out]))
+    return out
+
+
+def l2_error_2d(G, u, r):
+    v = C.c_double(0.0)
+    _check(lib().orc2d_l2_error(*G.args(), _p(_f(u)), _p(_f(r)), C.byref(v)))
+    return v.value
