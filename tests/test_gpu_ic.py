@@ -123,6 +123,7 @@ def test_sedov_otd_gap_of_the_continuous_adjoint(igr):
     igr.build_sedov_blast_ic_(*q0, A0, mesh, g, sigma=sig)
     from igr_sensitivities_gb300 import workloads as W
     dt = W.cfl_dt_2d(mesh, p, q0, g, 0.4)
+    dt = T / int(np.ceil(T / dt))  # the step both the store and the backward integration use
     a = igr.adjoint_conservative_ic(*q0, dt, T, basis, mesh, g, alpha, n_iter=nit, solver="pcg",
                                     objective="kinetic_energy")
     m = np.outer(basis.w, basis.w)[:, :, None, None] * mesh.Jx * mesh.Jy
