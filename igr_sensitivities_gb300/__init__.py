@@ -26,6 +26,7 @@ __all__ = [
     "adjoint_conservative_ic", "adjoint_conservative_batch",
     "init_constant_state", "init_isentropic_vortex", "build_taylor_green_ic_", "build_sedov_blast_ic_",
     "build_oseen_pair_blast_ic_", "IC_BUILDERS", "ic_dA_weights", "l2_error", "build_ic_batch", "IC_TYPES",
+    "forward_batch",
 ]
 
 SOLVERS = {"pcg": 0, "jacobi": 1, "chebyshev": 2}
@@ -533,7 +534,8 @@ def adjoint_conservative_batch(q0, gammas, alphas, dts, T, basis, mesh, n_iter=1
 # ---------------------------------------------------------------------------
 # Initial conditions (IGR_adjoints_2d/initial_conditions.jl), built on the GPU
 # ---------------------------------------------------------------------------
-IC_TYPES = {"constant": 0, "isentropic_vortex": 1, "taylor_green": 2, "sedov_blast": 3, "oseen_pair_blast": 4}
+IC_TYPES = {"constant": 0, "isentropic_vortex": 1, "taylor_green": 2, "sedov_blast": 3, "oseen_pair_blast": 4,
+            "multi_blast": 5}
 
 
 def build_ic_batch(ic_type, basis, mesh, gammas, amps, params=None, device_array=False, ctx=None):
@@ -634,3 +636,21 @@ def l2_error(u, u_ref, basis, mesh, ctx=None):
     check(ctx, lib().igr2d_l2_error(ctx.handle, C.byref(_disc2d(basis, mesh)), _ptr(_flat(u, n)), _ptr(_flat(u_ref, n)),
                                     C.byref(v)))
     return v.value
+
+
+def forward_batch(q0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solver="pcg", final_solve=True, ctx=None):
+    """run_forward! for a batch on one mesh (fixed n_steps; pass dt = T / n_steps
+    for run_forward semantics). q0: (n_inst, 4, N). Returns (q (n_inst, 4, N),
+    Sigma (n_inst, N))."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    gammas = np.ascontiguousarray(gammas, dtype=np.float64)
+    B = gammas.size
+    f64 = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (B,)))
+    als, dtv = f64(alphas), f64(dts)
+    q = np.array(q0, dtype=np.float64, order="C", copy=True)
+    S = np.zeros((B, q.shape[2]))
+    check(ctx, lib().igr2d_forward_batch(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_int(B), _ptr(gammas), _ptr(als),
+                                         _ptr(dtv), C.c_int(n_steps), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                         C.c_int(1 if final_solve else 0), _ptr(q), _ptr(S)))
+    return q, S

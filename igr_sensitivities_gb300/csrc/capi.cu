@@ -1010,10 +1010,12 @@ int igr1d_adjoint_conservative_batch(igr_ctx* ctx, int p, const double* xi, cons
 
 // ---- initial conditions -------------------------------------------------------------------
 namespace {
-Plan2D ic_plan(Ctx& c, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas, const double* amps) {
+Plan2D ic_plan(Ctx& c, const igr_disc2d* d, int ic_type, int n_inst, const double* gammas, const double* amps,
+               const double* params) {
   check_disc(d);
-  if (ic_type < 0 || ic_type > 4) throw Error(IGR_EINVAL, "Unknown IC type");
+  if (ic_type < 0 || ic_type > 5) throw Error(IGR_EINVAL, "Unknown IC type");
   if (n_inst < 1 || !gammas || !amps) throw Error(IGR_EINVAL, "bad batch arguments");
+  if (ic_type == 5 && !params) throw Error(IGR_EINVAL, "the multi-blast IC needs params");
   BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
   std::vector<Inst2DDesc> insts;
   for (int b = 0; b < n_inst; ++b) insts.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], 0.0, 0.0});
@@ -1026,7 +1028,7 @@ int igr2d_build_ic(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_inst, c
   return guarded(ctx, [&] {
     Ctx& c = ctx->c;
     if (!q) throw Error(IGR_EINVAL, "null output");
-    Plan2D P = ic_plan(c, d, ic_type, n_inst, gammas, amps);
+    Plan2D P = ic_plan(c, d, ic_type, n_inst, gammas, amps, params);
     const long long N = nodes2d(d), NG = P.NG;
     double* buf = c.ws.dbl("capi:ic", 4 * (size_t)NG);
     double* f[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
@@ -1043,7 +1045,7 @@ int igr2d_build_ic_dev(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_ins
   return guarded(ctx, [&] {
     Ctx& c = ctx->c;
     if (!q_dev) throw Error(IGR_EINVAL, "null output");
-    Plan2D P = ic_plan(c, d, ic_type, n_inst, gammas, amps);
+    Plan2D P = ic_plan(c, d, ic_type, n_inst, gammas, amps, params);
     const long long N = nodes2d(d), NG = P.NG;
     double* buf = c.ws.dbl("capi:ic", 4 * (size_t)NG);
     double* f[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
@@ -1085,6 +1087,40 @@ int igr1d_build_ic(igr_ctx* ctx, int p, const double* xi, const double* w, const
     double* buf = c.ws.dbl("capi1:ic", 3 * (size_t)P.NG);
     build_ic1d(c, P, ic_type, amps, buf);
     d2h(c, q, buf, 3 * P.NG);
+    sync(c);
+  });
+}
+
+int igr2d_forward_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                        const double* dts, int n_steps, int n_iter, int solver, int final_solve, double* q,
+                        double* sigma) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc(d);
+    check_solver(solver, n_iter);
+    if (n_inst < 1 || !gammas || !alphas || !dts || !q || !sigma || n_steps < 0) throw Error(IGR_EINVAL, "bad batch arguments");
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    std::vector<Inst2DDesc> insts;
+    for (int b = 0; b < n_inst; ++b) insts.push_back(Inst2DDesc{d->n_ex, d->n_ey, d->lx, d->ly, gammas[b], alphas[b], dts[b]});
+    Plan2D P = make_plan2d(c, B, insts, "fwdb");
+    const long long N = nodes2d(d), NG = P.NG;
+    double* buf = c.ws.dbl("capi:fwdb", 5 * (size_t)NG);
+    double* qd[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
+    double* S = buf + 4 * NG;
+    for (int v = 0; v < 4; ++v)
+      cuda_check(cudaMemcpy2DAsync(qd[v], N * sizeof(double), q + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyHostToDevice, c.stream), "gather q");
+    cuda_check(cudaMemsetAsync(S, 0, NG * sizeof(double), c.stream), "zero Sigma");  // forward.jl:42
+    Solve2DOpts o{n_iter, solver};
+    forward2d(c, P, qd, S, n_steps, o);
+    if (final_solve) {  // forward.jl:71-73
+      const double* qc[4] = {qd[0], qd[1], qd[2], qd[3]};
+      solve_elliptic2d(c, P, qc, S, o);
+    }
+    for (int v = 0; v < 4; ++v)
+      cuda_check(cudaMemcpy2DAsync(q + v * N, 4 * N * sizeof(double), qd[v], N * sizeof(double), N * sizeof(double), n_inst,
+                                   cudaMemcpyDeviceToHost, c.stream), "scatter q");
+    d2h(c, sigma, S, NG);
     sync(c);
   });
 }

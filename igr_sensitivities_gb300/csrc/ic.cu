@@ -19,7 +19,7 @@ struct Ic2DArgs {
   const Inst2D* inst; int ninst; BasisDev B;
   int type;
   const double* amps;      // per instance
-  double prm[11];
+  double prm[15];
   const double* tables;    // Oseen enthalpy-defect tables, OSEEN_TAB per instance
   double* q[4];
   long long NG;
@@ -94,6 +94,16 @@ __global__ void k2_build_ic(Ic2DArgs a) {
         rho = pow(p_vort, 1.0 / g);
         const double r2b = (x - prm[2]) * (x - prm[2]) + (y - prm[3]) * (y - prm[3]);
         p = p_vort + A * exp(-r2b / (prm[4] * prm[4]));
+        break;
+      }
+      case 5: {  // several Gaussian blasts (the paper scripts' Sedov state); blast 1's amplitude is A
+        const int nb = (int)prm[2];
+        double pv = prm[0];
+        for (int k = 0; k < nb; ++k) {
+          const double dx = x - prm[3 + 3 * k], dy = y - prm[4 + 3 * k];
+          pv += (k == 0 ? A : prm[5 + 3 * k]) * exp(-(dx * dx + dy * dy) / (prm[1] * prm[1]));
+        }
+        p = pv;
         break;
       }
       default: break;
@@ -172,7 +182,7 @@ int grid_nodes(long long n) { return (int)std::min<long long>((n + 255) / 256, 1
 
 // Reference defaults of the builders' keyword arguments (initial_conditions.jl).
 void default_prm(int type, double* prm) {
-  std::memset(prm, 0, 11 * sizeof(double));
+  std::memset(prm, 0, 15 * sizeof(double));
   if (type == 0) { prm[0] = 1.0; prm[1] = 1.0; prm[2] = 1.0; prm[3] = 1.0; }
   if (type == 1) { prm[0] = 5.0; prm[1] = 1.0; prm[2] = 1.0; }
   if (type == 3) { prm[0] = 1.0; prm[1] = 0.1; }
@@ -190,6 +200,7 @@ int ic2d_param_count(int type) {
     case 2: return 0;
     case 3: return 2;
     case 4: return 11;
+    case 5: return 15;
     default: throw Error(1, "Unknown IC type");
   }
 }
@@ -202,6 +213,7 @@ void build_ic2d(Ctx& c, const Plan2D& P, int type, const double* amps, const dou
   a.inst = P.d_inst; a.ninst = ni; a.B = P.B; a.type = type; a.NG = P.NG;
   default_prm(type, a.prm);
   if (params) std::memcpy(a.prm, params, np_ * sizeof(double));
+  if (type == 5 && !(a.prm[2] >= 1 && a.prm[2] <= 4)) throw Error(1, "multi-blast IC needs 1..4 blasts (params[2])");
   for (int v = 0; v < 4; ++v) a.q[v] = q[v];
   double* d_amps = c.ws.dbl("ic:amps", ni);
   cuda_check(cudaMemcpyAsync(d_amps, amps, sizeof(double) * ni, cudaMemcpyHostToDevice, c.stream), "amps");

@@ -208,6 +208,17 @@ int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_
 int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const double* x_dev, const double* rho_dev,
                             double* y_dev, void* stream);
 
+/* Batched run_forward! on one mesh: n_inst instances with their own gamma,
+ * alpha and dt advance n_steps fixed SSP-RK3 steps together (the caller
+ * re-rounds: n_steps = ceil(T/dt), dt = T/n_steps reproduces run_forward!);
+ * Sigma starts at zero; final_solve != 0 adds the solve at the final state
+ * (forward.jl:71-73). q: (n_inst, 4, N) in place; sigma: (n_inst, N) out.
+ * Used for finite-difference stencils of parameter sweeps. No counterpart in
+ * the reference. */
+int igr2d_forward_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
+                        const double* dts, int n_steps, int n_iter, int solver, int final_solve, double* q,
+                        double* sigma);
+
 /* ---- 2D continuous adjoint (optimise-then-discretise) ---------------------- */
 
 /* run_forward_store (IGR_adjoints_2d/forward.jl:111-158): the forward with
@@ -369,9 +380,13 @@ typedef enum {
   IGR_IC2D_ISENTROPIC_VORTEX = 1, /* init_isentropic_vortex, :39; params (beta, ux0, uy0) = (5, 1, 1) */
   IGR_IC2D_TAYLOR_GREEN = 2,      /* build_taylor_green_ic!, :105; amplitude A, no params */
   IGR_IC2D_SEDOV_BLAST = 3,       /* build_sedov_blast_ic!, :136; params (p_bg, sigma) = (1, 0.1) */
-  IGR_IC2D_OSEEN_PAIR_BLAST = 4   /* build_oseen_pair_blast_ic!, :175; params (a_core, M_star, blast_xc,
+  IGR_IC2D_OSEEN_PAIR_BLAST = 4,  /* build_oseen_pair_blast_ic!, :175; params (a_core, M_star, blast_xc,
                                      blast_yc, sigma, xc1, yc1, sign1, xc2, yc2, sign2) = (0.05, 0.5, 0.25,
                                      0.5, 0.09, 0.45, 0.6, +1, 0.45, 0.4, -1) */
+  IGR_IC2D_MULTI_BLAST = 5        /* rho = 1, u = 0, p = p_bg + sum_k A_k exp(-r_k^2/sigma^2), the several-blast
+                                     state of 2d/paper_scripts/generate_otd_refinement_sedov_data.jl:72-86;
+                                     params (p_bg, sigma, n <= 4, x_1, y_1, A_1, ..., x_n, y_n, A_n), required;
+                                     blast 1's amplitude is the instance's A */
 } igr_ic2d;
 
 /* Builds the initial state of n_inst instances on one mesh, each with its own

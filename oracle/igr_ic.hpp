@@ -7,7 +7,8 @@
 
 namespace igr {
 
-enum IC2D { IC2_CONSTANT = 0, IC2_ISENTROPIC_VORTEX = 1, IC2_TAYLOR_GREEN = 2, IC2_SEDOV_BLAST = 3, IC2_OSEEN_PAIR_BLAST = 4 };
+enum IC2D { IC2_CONSTANT = 0, IC2_ISENTROPIC_VORTEX = 1, IC2_TAYLOR_GREEN = 2, IC2_SEDOV_BLAST = 3, IC2_OSEEN_PAIR_BLAST = 4,
+            IC2_MULTI_BLAST = 5 };
 enum IC1D { IC1_ACOUSTIC_PULSE = 0, IC1_ENTROPY_WAVE = 1, IC1_DENSITY_PULSE = 2, IC1_PRESSURE_PULSE = 3, IC1_VELOCITY_PULSE = 4 };
 
 // Enthalpy-defect table of build_oseen_pair_blast_ic! (initial_conditions.jl:
@@ -102,6 +103,19 @@ inline void ic2d_node(int type, double x, double y, double Lx, double Ly, double
       rho = std::pow(p_vort, 1.0 / g);
       const double r2b = (x - prm[2]) * (x - prm[2]) + (y - prm[3]) * (y - prm[3]);
       p = p_vort + A * std::exp(-r2b / (prm[4] * prm[4]));
+      break;
+    }
+    case IC2_MULTI_BLAST: {
+      // the paper scripts' several-blast state (2d/paper_scripts/generate_otd_refinement_sedov_data.jl:72-86):
+      // rho = 1, u = 0, p = p_bg + sum_k A_k exp(-r_k^2 / sigma^2); prm = (p_bg, sigma, n, x_1, y_1, A_1, ...),
+      // blast 1's amplitude is A (the differentiated parameter)
+      const int nb = (int)prm[2];
+      double pv = prm[0];
+      for (int k = 0; k < nb; ++k) {
+        const double r2 = (x - prm[3 + 3 * k]) * (x - prm[3 + 3 * k]) + (y - prm[4 + 3 * k]) * (y - prm[4 + 3 * k]);
+        pv += (k == 0 ? A : prm[5 + 3 * k]) * std::exp(-r2 / (prm[1] * prm[1]));
+      }
+      p = pv;
       break;
     }
     default: throw std::invalid_argument("Unknown IC type");

@@ -369,14 +369,16 @@ def pde_duality_1d(G, gamma, q, Sig, a, dq):
     return l.value, r.value
 
 
-IC2D = {"constant": 0, "isentropic_vortex": 1, "taylor_green": 2, "sedov_blast": 3, "oseen_pair_blast": 4}
+IC2D = {"constant": 0, "isentropic_vortex": 1, "taylor_green": 2, "sedov_blast": 3, "oseen_pair_blast": 4,
+        "multi_blast": 5}
 IC1D = {"acoustic_pulse": 0, "entropy_wave": 1, "density_pulse": 2, "pressure_pulse": 3, "velocity_pulse": 4}
 
 
 def build_ic_2d(G, ic, gamma, A, prm):
     out = [G.zeros() for _ in range(4)]
-    _check(lib().orc2d_build_ic(*G.args(), C.c_int(IC2D[ic]), C.c_double(gamma), C.c_double(A),
-                                _p(_f(np.asarray(prm, dtype=np.float64))), *[_p(a) for a in out]))
+    prm = np.zeros(15) + np.pad(np.asarray(prm, dtype=np.float64), (0, max(0, 15 - len(prm))))[:15]
+    _check(lib().orc2d_build_ic(*G.args(), C.c_int(IC2D[ic]), C.c_double(gamma), C.c_double(A), _p(_f(prm)),
+                                *[_p(a) for a in out]))
     return out
 
 
