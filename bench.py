@@ -363,6 +363,44 @@ def secondary(args):
                             "sample_steps": ns, "full_steps": nfull},
                     cpu_baseline={"value": 1024 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
                                   "sample": "one instance per N_e for 2 steps, scaled by counts and to 2000 steps"})
+    elif args.workload == "otd_sedov":
+        # the paper's OtD-gap refinement study on three Sedov blasts (p = 4, N_e = 12..30, T = 0.1, PCG 60,
+        # kinetic energy): per resolution a continuous adjoint and a two-instance FD forward batch, all on the GPU
+        from igr_sensitivities_gb300 import drivers
+        cfg = dict(drivers.SEDOV_THREE_BLASTS)
+        ic, A = cfg.pop("ic_type"), cfg.pop("A")
+        nes = drivers.SEDOV_N_E
+        run = lambda: drivers.otd_refinement(ic, A, nes, ctx=ctx, **cfg)
+        for _ in range(args.warmup):
+            run()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rows, rates = run()
+        t = (time.perf_counter() - t0) / args.steps
+        # CPU: the same pipeline on the oracle for 2 steps at N_e = 12, scaled by nodes and step counts
+        basis = igr.DGBasis(4)
+        G = O.Grid2D(4, 12, 12)
+        qs = [O.build_ic_2d(G, ic, GAMMA, a, cfg["params"]) for a in (A, A + cfg["eps"], A - cfg["eps"])]
+        dt12 = cfg["CFL"] * G.dx / (9 * W.max_wavespeed_2d(*qs[0], GAMMA))
+        ns = 2
+        tc0 = time.perf_counter()
+        sn, n2 = O.run_forward_store_2d(G, GAMMA, cfg["alpha"], dt12, ns * dt12 * 0.999, 60, "pcg", qs[0])
+        O.run_adjoint_conservative_2d(G, sn, n2, dt12, ns * dt12 * 0.999, GAMMA, cfg["alpha"], 60, cfg["objective"], "pcg")
+        for q in qs[1:]:
+            O.run_forward_2d(G, GAMMA, cfg["alpha"], dt12, ns * dt12 * 0.999, 60, "pcg", q)
+        per_step_node = (time.perf_counter() - tc0) / (ns * G.N)
+        tc = 0.0
+        for ne in nes:
+            steps = int(np.ceil(cfg["T"] / (dt12 * 12.0 / ne)))
+            tc += per_step_node * steps * 25 * ne * ne
+        line.update(metric="OtD refinement sweeps/hour (three Sedov blasts, P4, N_e 12..30, PCG 60, T = 0.1)",
+                    value=3600.0 / t, unit="sweeps/hour", ms_per_step=t * 1e3, gpu_launches=ctx.last_launch_count(),
+                    config={"workload": "2d/paper_scripts/generate_otd_refinement_sedov_data.jl settings: per N_e one "
+                                        "continuous adjoint (store + backward PDE) and a 2-instance central-difference "
+                                        "forward batch", "N_e": nes,
+                            "gaps": [round(r[1], 6) for r in rows], "rates": [round(r, 3) for r in rates]},
+                    cpu_baseline={"value": 3600.0 / tc, "unit": "sweeps/hour", "cores": 1, "kind": "port",
+                                  "sample": "the pipeline for 2 steps at N_e = 12, scaled by nodes and step counts"})
     elif args.workload == "pde_adjoint2d":
         # the headline's batch (32 x 128^2 P3, Chebyshev 5, 200 steps, window rho^2) through the continuous
         # adjoint: run_forward_store + run_adjoint_conservative with device-resident snapshots
@@ -438,7 +476,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
     ap.add_argument("--workload", default="adjoint2d",
-                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | pde_batch1d")
+                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | pde_batch1d | otd_sedov")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()
