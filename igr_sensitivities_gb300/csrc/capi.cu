@@ -61,6 +61,53 @@ void d2h(Ctx& c, double* dst, const double* src, long long n) {
 }
 void sync(Ctx& c) { cuda_check(cudaStreamSynchronize(c.stream), "stream sync"); }
 
+// Batched arrays cross the boundary instance-major, [inst][var][N]; on the
+// device every variable is one field over all instances, [var][inst * N].
+// The reordering is one contiguous copy of the whole block (through a device
+// staging buffer when the caller's array is in host memory) and a transpose
+// kernel: pitched host copies are avoided, since the driver may touch a whole
+// pitch past the last row of the caller's array.
+__global__ void k_interleave(const double* __restrict__ src, double* __restrict__ dst, int nv, long long N, int n_inst,
+                             int to_fields) {
+  const long long tot = (long long)nv * N * n_inst;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < tot; k += (long long)gridDim.x * blockDim.x) {
+    const long long m = k % N, bv = k / N;      // k indexes the instance-major block: (b, v, m)
+    const int v = (int)(bv % nv), b = (int)(bv / nv);
+    const long long f = ((long long)v * n_inst + b) * N + m;
+    if (to_fields) dst[f] = src[k];
+    else dst[k] = src[f];
+  }
+}
+
+void interleave(Ctx& c, const double* src, double* dst, int nv, long long N, int n_inst, int to_fields) {
+  const long long tot = (long long)nv * N * n_inst;
+  LaunchScope ls(c, KID_OTHER);
+  k_interleave<<<(int)std::min<long long>((tot + 255) / 256, 152LL * 16), 256, 0, c.stream>>>(src, dst, nv, N, n_inst, to_fields);
+}
+
+// instance-major block `src` (host, or device when src_dev) -> device fields at `fields`
+void gather_block(Ctx& c, double* fields, const double* src, int nv, long long N, int n_inst, bool src_dev) {
+  if (!src) throw Error(IGR_EINVAL, "null array");
+  const double* s = src;
+  if (!src_dev) {
+    const long long tot = (long long)nv * N * n_inst;
+    double* st = c.ws.dbl("capi:stage", (size_t)tot);
+    cuda_check(cudaMemcpyAsync(st, src, tot * sizeof(double), cudaMemcpyHostToDevice, c.stream), "H2D block");
+    s = st;
+  }
+  interleave(c, s, fields, nv, N, n_inst, 1);
+}
+
+// device fields -> instance-major block `dst` (host, or device when dst_dev)
+void scatter_block(Ctx& c, double* dst, const double* fields, int nv, long long N, int n_inst, bool dst_dev) {
+  if (!dst) throw Error(IGR_EINVAL, "null array");
+  if (dst_dev) { interleave(c, fields, dst, nv, N, n_inst, 0); return; }
+  const long long tot = (long long)nv * N * n_inst;
+  double* st = c.ws.dbl("capi:stage", (size_t)tot);
+  interleave(c, fields, st, nv, N, n_inst, 0);
+  cuda_check(cudaMemcpyAsync(dst, st, tot * sizeof(double), cudaMemcpyDeviceToHost, c.stream), "D2H block");
+}
+
 Plan2D plan_single(Ctx& c, const igr_disc2d* d, double gamma, double alpha, double dt, const char* tag) {
   check_disc(d);
   BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
@@ -312,21 +359,13 @@ int igr2d_sensitivity_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const
     for (int v = 0; v < 4; ++v) { qd[v] = buf + v * NG; sd[v] = buf + (4 + v) * NG; }
     double* S = buf + 8 * NG;
     double* V = buf + 9 * NG;
-    // [inst][var][N] <-> field-major [var][inst*N]
-    for (int v = 0; v < 4; ++v) {
-      cuda_check(cudaMemcpy2DAsync(qd[v], N * sizeof(double), q + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyHostToDevice, c.stream), "gather q");
-      cuda_check(cudaMemcpy2DAsync(sd[v], N * sizeof(double), s + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyHostToDevice, c.stream), "gather s");
-    }
+    gather_block(c, qd[0], q, 4, N, n_inst, false);
+    gather_block(c, sd[0], s, 4, N, n_inst, false);
     Solve2DOpts o{n_iter, solver};
     sensitivity2d(c, P, qd, S, sd, V, n_steps, o, s_gamma);
-    for (int v = 0; v < 4; ++v) {
-      cuda_check(cudaMemcpy2DAsync(q + v * N, 4 * N * sizeof(double), qd[v], N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyDeviceToHost, c.stream), "scatter q");
-      cuda_check(cudaMemcpy2DAsync(s + v * N, 4 * N * sizeof(double), sd[v], N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyDeviceToHost, c.stream), "scatter s");
-    }
+    scatter_block(c, q, qd[0], 4, N, n_inst, false);
+    sync(c);  // the staging buffer is reused by the next scatter
+    scatter_block(c, s, sd[0], 4, N, n_inst, false);
     d2h(c, sigma, S, NG);
     d2h(c, varsigma, V, NG);
     sync(c);
@@ -393,21 +432,13 @@ static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const do
     double* q[4];
     double* dq[4];
     for (int v = 0; v < 4; ++v) { q[v] = buf + v * NG; dq[v] = buf + (4 + v) * NG; }
-    // [inst][var][N] -> field-major [var][inst*N]
-    const cudaMemcpyKind kin = q0_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    const double* qg = q0 + (size_t)g0 * 4 * N;
-    for (int v = 0; v < 4; ++v)
-      cuda_check(cudaMemcpy2DAsync(q[v], N * sizeof(double), qg + v * N, 4 * N * sizeof(double), N * sizeof(double), gn, kin,
-                                   c.stream), "gather q0");
+    gather_block(c, q[0], q0 + (size_t)g0 * 4 * N, 4, N, gn, q0_dev);
     Solve2DOpts o{n_iter, solver};
     const double* qc[4] = {q[0], q[1], q[2], q[3]};
     adjoint2d(c, P, qc, n_steps, o, objective, obj_params, J + g0, dq, dgamma ? dgamma + g0 : nullptr,
               dalpha ? dalpha + g0 : nullptr);
-    const cudaMemcpyKind kout = dq0_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    double* dg = dq0 + (size_t)g0 * 4 * N;
-    for (int v = 0; v < 4; ++v)
-      cuda_check(cudaMemcpy2DAsync(dg + v * N, 4 * N * sizeof(double), dq[v], N * sizeof(double), N * sizeof(double), gn, kout,
-                                   c.stream), "scatter dq0");
+    scatter_block(c, dq0 + (size_t)g0 * 4 * N, dq[0], 4, N, gn, dq0_dev);
+    if (!dq0_dev) sync(c);  // the host copy has left the staging buffer before the next group reuses it
   }
   sync(c);
 }
@@ -603,15 +634,11 @@ int igr2d_adjoint_conservative_batch(igr_ctx* ctx, const igr_disc2d* d, int n_in
     double* q[4];
     double* ao[4];
     for (int v = 0; v < 4; ++v) { q[v] = buf + v * NG; ao[v] = buf + (4 + v) * NG; }
-    for (int v = 0; v < 4; ++v)  // [inst][var][N] -> field-major [var][inst*N]
-      cuda_check(cudaMemcpy2DAsync(q[v], N * sizeof(double), q0 + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyHostToDevice, c.stream), "gather q0");
+    gather_block(c, q[0], q0, 4, N, n_inst, false);
     const double* qc[4] = {q[0], q[1], q[2], q[3]};
     const Solve2DOpts o{n_iter, solver};
     pde_adjoint_ic2d(c, Pf, Pa, qc, n, o, objective, obj_params, ao);
-    for (int v = 0; v < 4; ++v)
-      cuda_check(cudaMemcpy2DAsync(a0 + v * N, 4 * N * sizeof(double), ao[v], N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyDeviceToHost, c.stream), "scatter a0");
+    scatter_block(c, a0, ao[0], 4, N, n_inst, false);
     sync(c);
   });
 }
@@ -1033,9 +1060,7 @@ int igr2d_build_ic(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_inst, c
     double* buf = c.ws.dbl("capi:ic", 4 * (size_t)NG);
     double* f[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
     build_ic2d(c, P, ic_type, amps, params, f);
-    for (int v = 0; v < 4; ++v)  // field-major [var][inst*N] -> [inst][var][N]
-      cuda_check(cudaMemcpy2DAsync(q + v * N, 4 * N * sizeof(double), f[v], N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyDeviceToHost, c.stream), "scatter ic");
+    scatter_block(c, q, f[0], 4, N, n_inst, false);
     sync(c);
   });
 }
@@ -1050,9 +1075,7 @@ int igr2d_build_ic_dev(igr_ctx* ctx, const igr_disc2d* d, int ic_type, int n_ins
     double* buf = c.ws.dbl("capi:ic", 4 * (size_t)NG);
     double* f[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
     build_ic2d(c, P, ic_type, amps, params, f);
-    for (int v = 0; v < 4; ++v)
-      cuda_check(cudaMemcpy2DAsync(q_dev + v * N, 4 * N * sizeof(double), f[v], N * sizeof(double), N * sizeof(double),
-                                   n_inst, cudaMemcpyDeviceToDevice, c.stream), "scatter ic");
+    scatter_block(c, q_dev, f[0], 4, N, n_inst, true);
     sync(c);
   });
 }
@@ -1107,9 +1130,7 @@ int igr2d_forward_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const dou
     double* buf = c.ws.dbl("capi:fwdb", 5 * (size_t)NG);
     double* qd[4] = {buf, buf + NG, buf + 2 * NG, buf + 3 * NG};
     double* S = buf + 4 * NG;
-    for (int v = 0; v < 4; ++v)
-      cuda_check(cudaMemcpy2DAsync(qd[v], N * sizeof(double), q + v * N, 4 * N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyHostToDevice, c.stream), "gather q");
+    gather_block(c, qd[0], q, 4, N, n_inst, false);
     cuda_check(cudaMemsetAsync(S, 0, NG * sizeof(double), c.stream), "zero Sigma");  // forward.jl:42
     Solve2DOpts o{n_iter, solver};
     forward2d(c, P, qd, S, n_steps, o);
@@ -1117,9 +1138,7 @@ int igr2d_forward_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const dou
       const double* qc[4] = {qd[0], qd[1], qd[2], qd[3]};
       solve_elliptic2d(c, P, qc, S, o);
     }
-    for (int v = 0; v < 4; ++v)
-      cuda_check(cudaMemcpy2DAsync(q + v * N, 4 * N * sizeof(double), qd[v], N * sizeof(double), N * sizeof(double), n_inst,
-                                   cudaMemcpyDeviceToHost, c.stream), "scatter q");
+    scatter_block(c, q, qd[0], 4, N, n_inst, false);
     d2h(c, sigma, S, NG);
     sync(c);
   });
