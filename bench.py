@@ -363,6 +363,96 @@ def secondary(args):
                             "sample_steps": ns, "full_steps": nfull},
                     cpu_baseline={"value": 1024 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
                                   "sample": "one instance per N_e for 2 steps, scaled by counts and to 2000 steps"})
+    elif args.workload == "batch2d_c5":
+        # 2D batched forward sensitivity + adjoint: 16 x 256^2 P3, gamma ~ U[1.3, 1.7], Oseen vortex pair + one
+        # Gaussian pressure pulse, PCG 60, 1000 steps; tangent dJ/dgamma vs adjoint dJ/dgamma vs central FD.
+        # Timed on a sample of the steps (the per-step cost is uniform) and extrapolated to 1000 steps.
+        B = 4 if args.profile_case else 16
+        ne5 = 64 if args.profile_case else 256
+        S = args.n_steps if args.n_steps != N_STEPS else 4
+        full, nit, h = 1000, 60, 1e-6
+        basis = igr.DGBasis(3)
+        mesh = igr.CartesianMesh2D(ne5, ne5, 1.0, 1.0, basis)
+        rng = W.SplitMix64(W.seed_for(5, 0))
+        gs = np.array([rng.uniform(1.3, 1.7) for _ in range(B)])
+        q0 = np.empty((B, 4, mesh.x.size))
+        dts = np.empty(B)
+        for b in range(B):
+            # build_oseen_pair_blast_ic! with a seeded pair centre, pulse centre, amplitude U[1, 10] and vortex Mach
+            # number U[0.25, 0.5] (circulations of order one would make the homentropic core pressure negative)
+            xc, yc, bx, by = (rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7), rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8))
+            prm = [0.05, rng.uniform(0.25, 0.5), bx, by, 0.05, xc, yc + 0.1, 1.0, xc, yc - 0.1, -1.0]
+            q0[b] = igr.build_ic_batch("oseen_pair_blast", basis, mesh, [gs[b]], [rng.uniform(1.0, 10.0)], params=prm,
+                                       ctx=ctx)[0]
+            dts[b] = W.cfl_dt_2d(mesh, 3, [q0[b, v].reshape(mesh.x.shape, order="F") for v in range(4)], gs[b], 0.1)
+        alpha = 3.0 / ne5 ** 2
+        prm_w = W.seeded_window(W.seed_for(5, 0))
+        c = np.tile(np.outer(basis.w, basis.w).reshape(-1, order="F"), ne5 * ne5) * mesh.Jx * mesh.Jy
+        x, y = mesh.x.reshape(-1, order="F"), mesh.y.reshape(-1, order="F")
+        chi = ((x >= prm_w[0]) & (x <= prm_w[0] + prm_w[2]) & (y >= prm_w[1]) & (y <= prm_w[1] + prm_w[2])).astype(float)
+
+        def parts():
+            t0 = time.perf_counter()
+            q, _, s, _ = igr.sensitivity_batch(q0, np.zeros_like(q0), gs, alpha, dts, S, basis, mesh, n_iter=nit,
+                                               solver="pcg", s_gamma=1.0, ctx=ctx)
+            t1 = time.perf_counter()
+            J, _, dg, _ = igr.adjoint_batch(q0, gs, np.full(B, alpha), dts, S, basis, mesh, n_iter=nit, solver="pcg",
+                                            objective="window_rho2", obj_params=prm_w, ctx=ctx)
+            t2 = time.perf_counter()
+            qf, _ = igr.forward_batch(np.concatenate([q0, q0]), np.concatenate([gs + h, gs - h]), alpha,
+                                      np.concatenate([dts, dts]), S, basis, mesh, n_iter=nit, solver="pcg",
+                                      final_solve=False, ctx=ctx)
+            t3 = time.perf_counter()
+            tan = np.array([np.sum(c * 2.0 * q[b, 2] * chi * s[b, 2]) for b in range(B)])
+            Jf = np.array([np.sum(c * qf[k, 2] ** 2 * chi) for k in range(2 * B)])
+            fd = (Jf[:B] - Jf[B:]) / (2 * h)
+            return (t1 - t0, t2 - t1, t3 - t2), tan, dg, fd
+
+        if args.profile_case:
+            parts()
+            print("profile case done")
+            return
+        for _ in range(args.warmup):
+            parts()
+        ts = []
+        clocks = ClockSampler(0)
+        clocks.start()
+        for _ in range(args.steps):
+            tt, tan, adj, fd = parts()
+            ts.append(tt)
+        clk = clocks.stop()
+        t_tan, t_adj, t_fd = (float(np.median([t[k] for t in ts])) for k in range(3))
+        scale = full / S
+        # at 1000 steps the adjoint's tape does not fit: it re-runs the forward once from sqrt(n) checkpoints
+        t_full = (t_tan + t_adj + t_fd) * scale + 0.5 * t_fd * scale
+        # CPU: the oracle pipeline for one 64^2 instance and one step, scaled by nodes and steps
+        G = O.Grid2D(3, 64, 64)
+        m64 = igr.CartesianMesh2D(64, 64, 1.0, 1.0, basis)
+        qc = igr.build_ic_batch("oseen_pair_blast", basis, m64, [gs[0]], [5.0], ctx=ctx)[0]
+        dtc = W.cfl_dt_2d(m64, 3, [qc[v].reshape(m64.x.shape, order="F") for v in range(4)], gs[0], 0.1)
+        tc0 = time.perf_counter()
+        O.run_sensitivity_2d(G, gs[0], 3.0 / 64 ** 2, dtc, dtc * 0.999, nit, "pcg", list(qc), [np.zeros(G.N)] * 4,
+                             s_gamma=1.0)
+        O.adjoint_2d(G, gs[0], 3.0 / 64 ** 2, 1, dtc, nit, "pcg", "window_rho2", list(qc), prm_w)
+        for gg in (gs[0] + h, gs[0] - h):
+            O.objective_run_2d(G, gg, 3.0 / 64 ** 2, 1, dtc, nit, "pcg", "window_rho2", list(qc), prm_w)
+        tcpu = (time.perf_counter() - tc0) * (B * ne5 * ne5 / 64 ** 2) * full * 1.125  # same recompute allowance
+        rel_ta = float(np.max(np.abs(tan - adj) / np.maximum(np.abs(adj), 1e-4 * np.max(np.abs(adj)))))
+        rel_af = float(np.max(np.abs(adj - fd) / np.maximum(np.abs(fd), 1e-4 * np.max(np.abs(fd)))))
+        line.update(metric="2D batched tangent + adjoint + FD dJ/dgamma sets/hour (16 x 256^2 P3, PCG 60, 1000 steps)",
+                    value=3600.0 / t_full, unit="sets/hour", ms_per_step=t_full * 1e3 / full,
+                    gpu_launches=ctx.last_launch_count(),
+                    config={"workload": "16 x 256x256 P3 Oseen vortex pair + Gaussian pulse (build_oseen_pair_blast_ic!, "
+                                        "seeded centres, amplitude U[1,10], vortex Mach U[0.25,0.5]), gamma ~ U[1.3,1.7], "
+                                        "PCG 60, window rho^2; batched tangent (s_gamma = 1), batched adjoint (dJ/dgamma), "
+                                        "32-instance FD forward batch (h = 1e-6)",
+                            "sample_steps": S, "full_steps": full,
+                            "sample_seconds": {"tangent": round(t_tan, 3), "adjoint": round(t_adj, 3), "fd": round(t_fd, 3)},
+                            "extrapolation": "sample x 1000/S, plus one forward re-run for the adjoint's checkpointed tape",
+                            "tangent_vs_adjoint_max_rel": rel_ta, "adjoint_vs_fd_max_rel": rel_af},
+                    clocks=clk,
+                    cpu_baseline={"value": 3600.0 / tcpu, "unit": "sets/hour", "cores": 1, "kind": "port",
+                                  "sample": "one 64^2 instance, one step of each part, scaled by nodes and to 1000 steps"})
     elif args.workload == "otd_sedov":
         # the paper's OtD-gap refinement study on three Sedov blasts (p = 4, N_e = 12..30, T = 0.1, PCG 60,
         # kinetic energy): per resolution a continuous adjoint and a two-instance FD forward batch, all on the GPU
@@ -476,7 +566,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
     ap.add_argument("--workload", default="adjoint2d",
-                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | pde_batch1d | otd_sedov")
+                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | pde_batch1d | otd_sedov | batch2d_c5")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()
