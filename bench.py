@@ -437,8 +437,9 @@ def secondary(args):
         for gg in (gs[0] + h, gs[0] - h):
             O.objective_run_2d(G, gg, 3.0 / 64 ** 2, 1, dtc, nit, "pcg", "window_rho2", list(qc), prm_w)
         tcpu = (time.perf_counter() - tc0) * (B * ne5 * ne5 / 64 ** 2) * full * 1.125  # same recompute allowance
-        rel_ta = float(np.max(np.abs(tan - adj) / np.maximum(np.abs(adj), 1e-4 * np.max(np.abs(adj)))))
-        rel_af = float(np.max(np.abs(adj - fd) / np.maximum(np.abs(fd), 1e-4 * np.max(np.abs(fd)))))
+        # on the batch's scale: over a short sample some instances' dJ/dgamma is tiny and FD rounding dominates it
+        rel_ta = float(np.max(np.abs(tan - adj)) / np.max(np.abs(adj)))
+        rel_af = float(np.max(np.abs(adj - fd)) / np.max(np.abs(fd)))
         line.update(metric="2D batched tangent + adjoint + FD dJ/dgamma sets/hour (16 x 256^2 P3, PCG 60, 1000 steps)",
                     value=3600.0 / t_full, unit="sets/hour", ms_per_step=t_full * 1e3 / full,
                     gpu_launches=ctx.last_launch_count(),
