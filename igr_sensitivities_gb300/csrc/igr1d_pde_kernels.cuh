@@ -293,6 +293,7 @@ struct Pde1DArgs {
   double prm[4];
   int cs;
   int* status;
+  size_t smem_bytes;  // 0: scratch in HBM
 };
 
 template <int NP>
