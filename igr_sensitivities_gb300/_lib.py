@@ -72,15 +72,6 @@ class Context:
         """1D: CTAs per instance (0 = automatic; 1, 2, 4, 8, 16)."""
         check(self, lib().igr_set_cluster_size_1d(self.handle, C.c_int(int(cs))))
 
-    def set_smem_1d(self, mode):
-        """1D forward scratch in shared memory: -1 automatic, 0 never, 1 whenever it fits."""
-        check(self, lib().igr_set_smem_1d(self.handle, C.c_int(int(mode))))
-
-    def last_smem_1d(self):
-        v = C.c_int(0)
-        check(self, lib().igr_last_smem_1d(self.handle, C.byref(v)))
-        return v.value
-
     def last_cluster_size_1d(self):
         v = C.c_int(0)
         check(self, lib().igr_last_cluster_size_1d(self.handle, C.byref(v)))

@@ -159,18 +159,6 @@ int igr_set_cluster_size_1d(igr_ctx* ctx, int cs) {
   return IGR_OK;
 }
 
-int igr_set_smem_1d(igr_ctx* ctx, int mode) {
-  if (!ctx || mode < -1 || mode > 1) return IGR_EINVAL;
-  ctx->c.smem1d = mode;
-  return IGR_OK;
-}
-
-int igr_last_smem_1d(const igr_ctx* ctx, int* out) {
-  if (!ctx || !out) return IGR_EINVAL;
-  *out = ctx->c.last_smem1d;
-  return IGR_OK;
-}
-
 int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out) {
   if (!ctx || !out) return IGR_EINVAL;
   *out = ctx->c.last_cluster1d;

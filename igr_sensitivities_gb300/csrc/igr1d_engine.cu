@@ -89,14 +89,6 @@ static int cluster_size(Ctx& c, const Plan1D& P) {
   return cs;
 }
 
-// Shared-memory scratch of the 1D forward: at most this much per CTA (GB300:
-// 227 KB usable; some is left for the kernel's static reduction buffer).
-constexpr size_t SMEM1D_MAX = 200 * 1024;
-
-// Whether the automatic choice keeps small instances' scratch in shared
-// memory (one CTA per instance) rather than spreading them over clusters.
-static bool smem_preferred(Ctx&, const Plan1D&) { return false; }
-
 // Launch with the chosen cluster size, falling back to smaller clusters when
 // the device refuses one (results are identical for every size).
 template <class Args, class F>
@@ -124,18 +116,6 @@ void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpt
   a.solver = o.solver; a.n_iter = o.n_iter; a.final_solve = final_solve ? 1 : 0;
   a.status = c.d_status;
   a.cs = cluster_size(c, P);
-  // Small instances keep their scratch (the step's work fields, 1/rho, the
-  // spare Sigma and the reduction slots) in shared memory, one CTA each.
-  long long nmax = 0;
-  for (auto n : P.inst_nodes) nmax = std::max(nmax, n);
-  const size_t sbytes = (size_t)(E1_FIELDS + F1_FIELDS) * nmax * sizeof(double);
-  const bool fits = sbytes <= SMEM1D_MAX;
-  const bool use_smem = fits && (c.smem1d == 1 || (c.smem1d < 0 && c.cluster1d <= 1 && smem_preferred(c, P)));
-  if (use_smem) {
-    a.cs = 1;
-    a.smem_bytes = sbytes;
-  }
-  c.last_smem1d = use_smem ? 1 : 0;
   NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
                                [&](const Fwd1DArgs& x, int n) { return launch_k1_forward<NPV>(x, n, c.stream); },
                                "k1_forward launch"));

@@ -64,19 +64,15 @@ struct View1 {
   }
 };
 
-// Set up the view of CTA blockIdx.x: instance order[blockIdx.x / cs]. With
-// smem != nullptr (one CTA per instance, cs == 1) the per-element work and the
-// scratch fields live in the CTA's dynamic shared memory instead of HBM: a
-// small instance's solver iterations then run at shared-memory latency.
+// Set up the view of CTA blockIdx.x: instance order[blockIdx.x / cs].
 template <int NP>
-__device__ __forceinline__ View1<NP> make_view1(const Inst1D* inst, const int* order, double* scr_base, int cs, int* idx,
-                                                double* smem = nullptr) {
+__device__ __forceinline__ View1<NP> make_view1(const Inst1D* inst, const int* order, double* scr_base, int cs, int* idx) {
   View1<NP> v;
   const int rank = blockIdx.x % cs;
   *idx = order[blockIdx.x / cs];
   v.I = inst[*idx];
   v.N = NP * v.I.ne;
-  v.ew = smem ? smem : scr_base + v.I.soff;
+  v.ew = scr_base + v.I.soff;
   v.scr = v.ew + (long long)E1_FIELDS * v.N;
   v.cs = cs;
   v.e0 = (int)((long long)v.I.ne * rank / cs);
@@ -509,7 +505,6 @@ struct Fwd1DArgs {
   int solver, n_iter, final_solve;
   int cs;             // CTAs per instance (cluster size)
   int* status;
-  size_t smem_bytes;  // > 0: scratch in dynamic shared memory (cs == 1)
 };
 
 // run_forward! (IGR_adjoints_1d/forward.jl:50-87) for one instance per CTA:
@@ -518,9 +513,8 @@ struct Fwd1DArgs {
 template <int NP>
 __global__ void __launch_bounds__(T1, 2) k1_forward(Fwd1DArgs a) {
   __shared__ double s_red[T1];
-  extern __shared__ double s_dyn[];
   int inst;
-  const View1<NP> v = make_view1<NP>(a.inst, a.order, a.scr, a.cs, &inst, a.smem_bytes ? s_dyn : nullptr);
+  const View1<NP> v = make_view1<NP>(a.inst, a.order, a.scr, a.cs, &inst);
   const BasisDev& B = a.B;
   const Inst1D& I = v.I;
   double* q[3] = {a.q + 3 * I.off, a.q + 3 * I.off + v.N, a.q + 3 * I.off + 2 * v.N};

@@ -13,11 +13,7 @@ namespace igrgpu {
 template <class Args>
 static cudaError_t launch_per_instance(void (*kernel)(Args), const Args& a, int n_inst, cudaStream_t s) {
   if (a.cs <= 1) {
-    if (a.smem_bytes > 48 * 1024) {
-      const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a.smem_bytes);
-      if (e != cudaSuccess) return e;
-    }
-    kernel<<<n_inst, T1, a.smem_bytes, s>>>(a);
+    kernel<<<n_inst, T1, 0, s>>>(a);
     return cudaGetLastError();
   }
   if (a.cs > 8) {

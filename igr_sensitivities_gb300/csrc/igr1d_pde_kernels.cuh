@@ -293,7 +293,6 @@ struct Pde1DArgs {
   double prm[4];
   int cs;
   int* status;
-  size_t smem_bytes;  // 0: scratch in HBM
 };
 
 template <int NP>

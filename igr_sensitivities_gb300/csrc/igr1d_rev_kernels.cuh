@@ -585,7 +585,6 @@ struct Adj1DArgs {
   double prm[4];
   int cs;               // CTAs per instance (cluster size)
   int* status;
-  size_t smem_bytes;    // 0: scratch in HBM
 };
 
 template <int NP>

@@ -165,7 +165,6 @@ struct Tan1DArgs {
   double s_gamma;
   int cs;         // CTAs per instance (cluster size)
   int* status;
-  size_t smem_bytes;  // 0: scratch in HBM
 };
 
 template <int NP>

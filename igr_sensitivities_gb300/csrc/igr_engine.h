@@ -73,8 +73,6 @@ struct Ctx {
   int plan_groups = 0, plan_group_size = 0, plan_seg = 0, plan_nseg = 0;
   int cluster1d = 0;            // 1D: CTAs per instance (0 = chosen per launch)
   int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
-  int smem1d = -1;              // 1D forward: scratch in shared memory (-1 auto, 0 never, 1 when it fits)
-  int last_smem1d = 0;          // 1D forward: whether the last launch kept its scratch in shared memory
   Profiler prof;
 };
 

@@ -93,12 +93,6 @@ int igr_set_tape_budget(igr_ctx* ctx, size_t bytes);
 int igr_set_cluster_size_1d(igr_ctx* ctx, int cs);
 /* CTAs per instance used by the last 1D launch on this context. */
 int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out);
-/* 1D forward: keep each instance's scratch in shared memory, one CTA per
- * instance (-1 automatic, 0 never, 1 whenever it fits). Results are bitwise
- * the same either way. No counterpart in the reference. */
-int igr_set_smem_1d(igr_ctx* ctx, int mode);
-/* Whether the last 1D forward launch used shared-memory scratch (1) or not (0). */
-int igr_last_smem_1d(const igr_ctx* ctx, int* out);
 /* Kernels launched by the last call on this context. */
 int igr_last_launch_count(const igr_ctx* ctx, long long* out);
 

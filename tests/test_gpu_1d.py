@@ -260,44 +260,3 @@ def test_cluster_size_does_not_change_results(igr, igr1d, oracle, solver):
     ref, _ = oracle.run_forward_1d(G, g, alpha, dt, 6 * dt, 7, solver, [flat(x) for x in q0])
     for x, y in zip(out[16][0][:3], ref):
         assert rel(x, y) <= RTOL_FWD
-
-
-@pytest.mark.parametrize("solver", ["pcg", "jacobi", "chebyshev"])
-def test_shared_memory_scratch_gives_the_same_forward(igr, igr1d, oracle, solver):
-    """The 1D forward with its scratch in shared memory (one CTA per instance)
-    equals the HBM-scratch runs (one CTA and a 16-CTA cluster) bitwise, single
-    and batched."""
-    from igr_sensitivities_gb300 import Context
-    g = 1.4
-    basis, mesh, G = setup1(igr, oracle, 3, 64)
-    q0 = W.seeded_pulses_1d(mesh, g, W.seed_for(1, 901), width=0.08)
-    dt = W.cfl_dt_1d(mesh, 3, q0, g, 0.1)
-    alpha = 3.0 * mesh.dx ** 2
-    ctx = Context(0)
-    out = []
-    for smem, cs in ((0, 1), (0, 16), (1, 0)):
-        ctx.set_smem_1d(smem)
-        ctx.set_cluster_size_1d(cs)
-        out.append(igr1d.run_forward(*q0, dt, 7 * dt, basis, mesh, g, alpha, n_iter=7, solver=solver, ctx=ctx))
-        assert ctx.last_smem_1d() == smem
-    for x, y, z in zip(*out):
-        assert np.array_equal(x, y) and np.array_equal(x, z)
-    # a batch of uneven instances, every one small enough
-    nes = [16, 40, 64]
-    states, dts = [], []
-    for i, ne in enumerate(nes):
-        m = igr.PeriodicMesh1D(ne, 1.0, basis)
-        q = W.seeded_pulses_1d(m, g, W.seed_for(1, 910 + i), width=0.08)
-        states.append(tuple(flat(x) for x in q))
-        dts.append(W.cfl_dt_1d(m, 3, q, g, 0.1))
-    res = []
-    for smem in (0, 1):
-        ctx.set_smem_1d(smem)
-        ctx.set_cluster_size_1d(1)
-        res.append(igr1d.forward_batch(states, basis, nes, 1.0, g, alpha, dts, 6, n_iter=7, solver=solver, ctx=ctx))
-        assert ctx.last_smem_1d() == smem
-    for ta, tb in zip(res[0], res[1]):  # (mu, rho, E, Sigma) per instance
-        for x, y in zip(ta, tb):
-            assert np.array_equal(x, y)
-    ctx.set_smem_1d(-1)
-    ctx.set_cluster_size_1d(0)
