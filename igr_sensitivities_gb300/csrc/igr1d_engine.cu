@@ -74,9 +74,13 @@ Plan1D make_plan1d(Ctx& c, const BasisDev& B, const std::vector<Inst1DDesc>& ins
 long long forward1d_scratch_fields(const Inst1DDesc&, int) { return E1_FIELDS + F1_FIELDS; }
 
 // CTAs per instance. Results do not depend on it (fixed-order reductions), so
-// it is chosen for speed: small batches spread each instance over a cluster of
-// up to 16 SMs (at least 4 elements per CTA); batches that fill the GPU use one
-// CTA per instance. A context setting overrides the choice.
+// it is chosen for speed. One CTA advances an instance at one element per
+// thread; its SM's FP64 rate bounds it (a 256-element Jacobi iteration: ~6 us).
+// Small batches of instances with at least T1 elements therefore spread each
+// over a cluster of up to 16 SMs (at least 16 elements per CTA); below T1
+// elements the cluster barrier costs more than it saves (measured on GB300:
+// N_e = 64 and 128 run 10-20% faster on one CTA), and batches that fill the
+// GPU use one CTA per instance. A context setting overrides the choice.
 static int cluster_size(Ctx& c, const Plan1D& P) {
   if (c.cluster1d > 0) return c.cluster1d;
   int sms = 0;
@@ -85,7 +89,7 @@ static int cluster_size(Ctx& c, const Plan1D& P) {
   int min_ne = 1 << 30;
   for (auto& I : P.inst) min_ne = std::min(min_ne, I.ne);
   int cs = 1;
-  while (cs < 16 && ni * cs * 2 * 2 <= sms && min_ne / (cs * 2) >= 4) cs *= 2;
+  while (cs < 16 && min_ne >= T1 && ni * cs * 2 * 2 <= sms && min_ne / (cs * 2) >= 16) cs *= 2;
   return cs;
 }
 

@@ -249,7 +249,7 @@ def test_cluster_size_does_not_change_results(igr, igr1d, oracle, solver):
         out[cs] = (f, t, a)
     ctx.set_cluster_size_1d(0)
     igr1d.run_forward(*q0, dt, 6 * dt, basis, mesh, g, alpha, n_iter=7, solver=solver, ctx=ctx)
-    assert ctx.last_cluster_size_1d() == 16  # automatic choice for one 64-element instance
+    assert ctx.last_cluster_size_1d() == 1  # automatic choice below 256 elements: one CTA
     for cs in (2, 16):
         for x, y in zip(out[1][0] + out[1][1], out[cs][0] + out[cs][1]):
             assert np.array_equal(x, y)
