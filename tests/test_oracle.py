@@ -375,3 +375,72 @@ def test_pde1_local_operator_is_the_dual_of_the_linearised_rhs(oracle):
         gaps.append(abs(lhs - rhs) / abs(lhs))
     assert gaps[0] > 30 * gaps[1] > 900 * gaps[2]
     assert gaps[2] < 1e-8
+
+
+def _acoustic_1d(G, eps, g=1.4):
+    x = G.coords()
+    s = np.sin(2 * np.pi * x / G.L)
+    rho, u, p = 1.0 + eps * s, eps * s, 1.0 + eps * s
+    return [rho * u, rho, p / (g - 1) + 0.5 * rho * u ** 2], s
+
+
+def test_dJ_dalpha_dual_vs_fd_1d(oracle):
+    """IGR_adjoints_1d/tests/run_forwarddiff_test.jl:31-91: dJ/dalpha of
+    J = int rho(T)^2 (p = 3, N_e = 8, CFL 0.3, T = 0.1, alpha = 0.01, PCG 100)
+    by forward-mode duals against central differences (h = 1e-7), rel < 1e-5;
+    the hand-written reverse's dJ/dalpha agrees with the dual."""
+    g, alpha, T = 1.4, 0.01, 0.1
+    G = oracle.Grid1D(3, 8)
+    q0, _ = _acoustic_1d(G, 0.2)
+    ws = np.max(np.abs(q0[0] / q0[1]) + np.sqrt(g * (g - 1) * (q0[2] - 0.5 * q0[0] ** 2 / q0[1]) / q0[1]))
+    dt = 0.3 * G.dx / (7 * ws)
+    n = int(np.ceil(T / dt))
+    dtr = T / n  # run_forward's re-rounded step: the fixed-step loop with it is run_forward
+    zero = [np.zeros(G.N)] * 3
+    J, dJ = oracle.objective_dual_1d(G, g, alpha, n, dtr, 100, "pcg", "l2_density", q0, zero, va=1.0)
+
+    def Jf(a):
+        q, _ = oracle.run_forward_1d(G, g, a, dt, T, 100, "pcg", q0)
+        return float(np.sum(np.tile(G.w, 8) * G.J * q[1] ** 2))
+
+    assert abs(J - Jf(alpha)) <= 1e-13 * abs(J)
+    h = 1e-7
+    fd = (Jf(alpha + h) - Jf(alpha - h)) / (2 * h)
+    assert abs(dJ - fd) / abs(fd) < 1e-5
+    _, _, _, da = oracle.adjoint_1d(G, g, alpha, n, dtr, 100, "pcg", "l2_density", q0)
+    assert abs(da - dJ) <= 1e-9 * abs(dJ)
+
+
+@pytest.mark.parametrize("form", [1, 2])
+def test_tangent_dJ_dA_vs_dual_1d(oracle, form):
+    """run_sensitivity_test.jl:240-329 (Test 5): dJ/dA from the hand-coded
+    tangent (form1 / form2 elliptic source) against forward-mode AD of the
+    forward map, rel < 1e-2 (linearise-then-discretise vs the discrete map)."""
+    g, alpha, T = 1.4, 0.01, 0.05
+    G = oracle.Grid1D(3, 8)
+    dt = 0.3 * G.dx / (7 * 2.5)
+    q0, s = _acoustic_1d(G, 0.2)
+    rho, u = q0[1], q0[0] / q0[1]
+    s0 = [s * u + rho * s, s, s / (g - 1) + 0.5 * (s * u ** 2 + 2 * rho * u * s)]
+    q, _, sv, _ = oracle.run_sensitivity_1d(G, g, alpha, dt, T, 100, "pcg", q0, s0, form=form)
+    wJ = np.tile(G.w, 8) * G.J
+    dJ_tan = float(np.sum(wJ * 2 * q[1] * sv[1]))
+    n = int(np.ceil(T / dt))
+    _, dJ_ad = oracle.objective_dual_1d(G, g, alpha, n, T / n, 100, "pcg", "l2_density", q0, s0)
+    assert abs(dJ_tan - dJ_ad) / abs(dJ_ad) < 1e-2
+
+
+def test_form1_vs_form2_1d(oracle):
+    """run_sensitivity_test.jl:335-396 (Test 6): the two tangent elliptic
+    sources share the primal exactly and agree on the tangent within 1e-2."""
+    g, alpha, T = 1.4, 0.01, 0.05
+    G = oracle.Grid1D(3, 8)
+    dt = 0.3 * G.dx / (7 * 2.5)
+    q0, s = _acoustic_1d(G, 0.2)
+    rho, u = q0[1], q0[0] / q0[1]
+    s0 = [s * u + rho * s, s, s / (g - 1) + 0.5 * (s * u ** 2 + 2 * rho * u * s)]
+    q1, S1, t1, v1 = oracle.run_sensitivity_1d(G, g, alpha, dt, T, 100, "pcg", q0, s0, form=1)
+    q2, S2, t2, v2 = oracle.run_sensitivity_1d(G, g, alpha, dt, T, 100, "pcg", q0, s0, form=2)
+    assert rel(q1[1], q2[1]) < 1e-14
+    for a, b in zip(t1 + [v1], t2 + [v2]):
+        assert rel(a, b) < 1e-2
