@@ -367,9 +367,10 @@ def secondary(args):
         # 2D batched forward sensitivity + adjoint: 16 x 256^2 P3, gamma ~ U[1.3, 1.7], Oseen vortex pair + one
         # Gaussian pressure pulse, PCG 60, 1000 steps; tangent dJ/dgamma vs adjoint dJ/dgamma vs central FD.
         # Timed on a sample of the steps (the per-step cost is uniform) and extrapolated to 1000 steps.
-        B = 4 if args.profile_case else 16
-        ne5 = 64 if args.profile_case else 256
-        S = args.n_steps if args.n_steps != N_STEPS else 4
+        # profile case (ncu): 8 x 128^2 for 2 steps, every field 16.8 MB (a launch's working set far above L2)
+        B = 8 if args.profile_case else 16
+        ne5 = 128 if args.profile_case else 256
+        S = args.n_steps if args.n_steps != N_STEPS else (2 if args.profile_case else 4)
         full, nit, h = 1000, 60, 1e-6
         basis = igr.DGBasis(3)
         mesh = igr.CartesianMesh2D(ne5, ne5, 1.0, 1.0, basis)
