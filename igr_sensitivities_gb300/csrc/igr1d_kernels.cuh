@@ -215,6 +215,31 @@ __device__ __forceinline__ void cheb_coef(const BasisDev& B, int it, double& rc,
   rc = rn;
 }
 
+// The solvers' scalar recurrences are evaluated by one thread of the CTA and
+// read by all from shared memory: an FP64 divide is a software sequence of
+// ~20 FP64 instructions on GB300, and 256 threads repeating it every iteration
+// cost as much FP64 issue as the element work of a small instance. All
+// threads of the CTA call these; every CTA of a cluster computes the same bits.
+__device__ __forceinline__ double cta_div(double x, double y) {
+  __shared__ double s_q;
+  if (threadIdx.x == 0) s_q = x / y;
+  __syncthreads();
+  const double r = s_q;
+  __syncthreads();
+  return r;
+}
+// cheb_coef on thread 0 (rc is carried by thread 0 only), coefficients to all.
+__device__ __forceinline__ void cta_cheb(const BasisDev& B, int it, double& rc, double* ca, double* cc) {
+  __shared__ double s_c[2];
+  if (threadIdx.x == 0) {
+    cheb_coef(B, it, rc, ca, cc);
+    s_c[0] = *ca; s_c[1] = *cc;
+  }
+  __syncthreads();
+  *ca = s_c[0]; *cc = s_c[1];
+  __syncthreads();
+}
+
 // Fixed-count solve A x = b on the instance (pcg_fixed! / jacobi_fixed! /
 // chebyshev_fixed!, elliptic.jl:307-430): x0 warm start, result in xout
 // (!= x0); w0..w3: scratch fields. All threads call it; ends synchronised.
@@ -257,7 +282,7 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
       });
       const double pAp = v.reduce(s_red);
       if (taped && threadIdx.x == 0) tp.scal()[n + 1 + k] = pAp;
-      const double a = rz / (pAp + 1e-30);
+      const double a = cta_div(rz, pAp + 1e-30);
       const double* xin = k == 0 ? x0 : xout;
       red = v.slot();
       for (int e = v.e0 + threadIdx.x; e < v.e1; e += blockDim.x) {
@@ -275,7 +300,7 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
       }
       const double rzn = v.reduce(s_red);
       if (taped && threadIdx.x == 0) tp.scal()[k + 1] = rzn;
-      const double beta = rzn / (rz + 1e-30);
+      const double beta = cta_div(rzn, rz + 1e-30);
       for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) p[m] = fma(beta, p[m], r[m] * cinvM[m]);
       rz = rzn;
       v.sync();
@@ -288,7 +313,7 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
   for (int k = 0; k < n; ++k) {
     double* xo = (k == n - 1) ? xout : ((k % 2 == 0) ? w0 : w1);
     double ca = 0.0, cc = 0.0;
-    if (solver == 2) cheb_coef(B, k + 1, rc, &ca, &cc);
+    if (solver == 2) cta_cheb(B, k + 1, rc, &ca, &cc);
     double* d = w2;
     d1_apply<NP>(v, B, [&](int m) { return x[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
 #pragma unroll

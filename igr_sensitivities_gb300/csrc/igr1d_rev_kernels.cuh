@@ -255,8 +255,20 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
     // u = residual adjoint r̄ (w0/w1 ping-pong), db = direction adjoint (w2, Chebyshev)
     double* U[2] = {w0, w1};
     double* db = w2;
-    // Chebyshev coefficients of iteration it (recomputed from the recurrence: scalar work)
+    // Chebyshev coefficients of iteration it: a table built by one thread when
+    // it fits, else recomputed from the recurrence
+    constexpr int CHEB_TAB = 128;
+    __shared__ double s_ct[2][CHEB_TAB];
+    const bool tab = solver == 2 && n < CHEB_TAB;
+    if (tab) {
+      if (threadIdx.x == 0) {
+        double rc = 0.0;
+        for (int j = 1; j <= n; ++j) cheb_coef(B, j, rc, &s_ct[0][j], &s_ct[1][j]);
+      }
+      __syncthreads();
+    }
     auto coef = [&](int it, double* ca, double* cc) {
+      if (tab) { *ca = s_ct[0][it]; *cc = s_ct[1][it]; return; }
       double rc = 0.0;
       for (int j = 1; j <= it; ++j) cheb_coef(B, j, rc, ca, cc);
     };
@@ -323,11 +335,18 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
   for (int m = v.m0() + threadIdx.x; m < v.m1(); m += blockDim.x) { pb[m] = 0.0; rb[m] = 0.0; }
   v.sync();
   bool first_z = true;
+  __shared__ double s_sc[3];
   for (int it = n - 1; it >= 0; --it) {
     const double rz0 = RZ[it], rz1 = RZ[it + 1], pap = PAP[it];
     const double e0 = rz0 + 1e-30, den = pap + 1e-30;
-    const double beta = rz1 / e0, al = rz0 / den;
-    const double rzb1 = rzb + betab / e0;
+    if (threadIdx.x == 0) {  // the iteration's quotients, once per CTA (see cta_div)
+      s_sc[0] = rz1 / e0;           // beta
+      s_sc[1] = rz0 / den;          // alpha
+      s_sc[2] = rzb + betab / e0;   // adjoint of rz_{it+1}
+    }
+    __syncthreads();
+    const double beta = s_sc[0], al = s_sc[1], rzb1 = s_sc[2];
+    __syncthreads();
     const double* r1 = tp.r(it + 1);
     const double* ap = tp.ap(it);
     const double* p = tp.p(it);
@@ -349,8 +368,14 @@ __device__ void d1_solve_rev(const View1<NP>& v, const BasisDev& B, int solver, 
       red[e] = pe;
     }
     const double abv = v.reduce(s_red);
-    rzb = -betab * rz1 / (e0 * e0) + abv / den;
-    const double papb = -abv * rz0 / (den * den);
+    if (threadIdx.x == 0) {
+      s_sc[0] = -betab * rz1 / (e0 * e0) + abv / den;   // adjoint of rz_it
+      s_sc[1] = -abv * rz0 / (den * den);               // adjoint of pAp_it
+    }
+    __syncthreads();
+    rzb = s_sc[0];
+    const double papb = s_sc[1];
+    __syncthreads();
     // Ap = A p: pb += alpha xb + papb Ap + A (adjoint of Ap); u = -(adjoint of Ap) = alpha rb - papb p
     const double* pn = it > 0 ? tp.p(it - 1) : nullptr;
     red = v.slot();

@@ -308,7 +308,12 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
   // PCG direction update fused into the loads (p_k is pointwise in r_k, p_{k-1})
   const bool form_p = EPI == EPI_PCG && a.pcg_p != nullptr;
   double beta = 0.0;
-  if (form_p) beta = a.rz_cur[tl.inst] / (a.rz_prev[tl.inst] + 1e-30);
+  if (form_p) {  // block-uniform: one thread divides, the block reads the quotient
+    __shared__ double s_beta;
+    if (threadIdx.x == 0) s_beta = a.rz_cur[tl.inst] / (a.rz_prev[tl.inst] + 1e-30);
+    __syncthreads();
+    beta = s_beta;
+  }
   auto ldx = [&](long long n) -> double {
     if (form_p) return fma(beta, a.pcg_p[n], a.pcg_r[n] * a.cinvM[n]);
     return a.x[n];

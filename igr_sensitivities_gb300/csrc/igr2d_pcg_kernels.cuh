@@ -14,7 +14,9 @@
 // pAp_k = p_k . A p_k for every iteration (the tape of the scalar
 // recurrence); alpha_k = rz_k / (pAp_k + 1e-30) and
 // beta_k = rz_{k+1} / (rz_k + 1e-30) are recomputed where needed, with the
-// reference's 1e-30 guards (elliptic.jl:338, 343).
+// reference's 1e-30 guards (elliptic.jl:338, 343). An FP64 divide is a
+// software sequence of ~20 FP64 instructions on GB300, so one thread of each
+// block forms these quotients and the block reads them from shared memory.
 #pragma once
 #include "igr_device.cuh"
 
@@ -46,9 +48,12 @@ struct PcgUpdateArgs {
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
   constexpr int P2 = PCG_THREADS;
   __shared__ double s_red[P2];
+  __shared__ double s_al;
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
-  const double al = a.rz[tl.inst] / (a.pap[tl.inst] + 1e-30);
+  if (threadIdx.x == 0) s_al = a.rz[tl.inst] / (a.pap[tl.inst] + 1e-30);
+  __syncthreads();
+  const double al = s_al;
   const int cnt = a.tx * a.ty * a.np * a.np;
   double part = 0.0;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
@@ -89,14 +94,19 @@ struct PcgRevArgs {
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
   constexpr int P2 = PCG_THREADS;
   __shared__ double s_red[P2];
+  __shared__ double s_sc[2];
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
   const int i = tl.inst;
-  const double rz0 = a.RZ[(long long)a.it * a.ni + i], rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
-  const double e0 = rz0 + 1e-30;
-  const double beta = rz1 / e0;
-  const double betab = a.first ? 0.0 : a.BET[i];
-  const double rzb1 = (a.first ? 0.0 : a.RZB[i]) + betab / e0;
+  if (threadIdx.x == 0) {
+    const double rz0 = a.RZ[(long long)a.it * a.ni + i], rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
+    const double e0 = rz0 + 1e-30;
+    const double betab = a.first ? 0.0 : a.BET[i];
+    s_sc[0] = rz1 / e0;                                  // beta
+    s_sc[1] = (a.first ? 0.0 : a.RZB[i]) + betab / e0;   // adjoint of rz_{it+1}
+  }
+  __syncthreads();
+  const double beta = s_sc[0], rzb1 = s_sc[1];
   const int cnt = a.tx * a.ty * a.np * a.np;
   double part = 0.0;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {

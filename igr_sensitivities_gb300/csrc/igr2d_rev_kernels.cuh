@@ -359,8 +359,11 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
   const BasisDev& B = a.B;
   const double hw = B.hw;
   double pal = 0.0, ppb = 0.0;  // PCG: alpha_it and the adjoint of pAp_it
-  if (PCG) {
-    pal = a.rz_it[tl.inst] / (a.pap_it[tl.inst] + 1e-30);
+  if (PCG) {  // one thread divides, the block reads the quotient
+    __shared__ double s_pal;
+    if (threadIdx.x == 0) s_pal = a.rz_it[tl.inst] / (a.pap_it[tl.inst] + 1e-30);
+    __syncthreads();
+    pal = s_pal;
     ppb = a.papb[tl.inst];
   }
   // u at node n, given x_k there (PCG forms it from rb and p_it)
