@@ -146,6 +146,8 @@ Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& ins
     for (int ey0 = 0; ey0 < d.ney; ey0 += ty)
       for (int ex0 = 0; ex0 < d.nex; ex0 += tx) P.tiles.push_back(Tile2D{(int)i, ex0, ey0, 0});
     I.ntiles = (int)P.tiles.size() - I.tile0;
+    for (int g = 0; g < I.ntiles; g += TILE_GROUP)
+      P.groups.push_back(TileGroup{(int)i, I.tile0 + g, std::min(TILE_GROUP, I.ntiles - g), 0});
     P.inst.push_back(I);
     const long long n = (long long)P.np * P.np * d.nex * d.ney;
     P.inst_nodes.push_back(n);
@@ -157,6 +159,9 @@ Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& ins
   P.d_tiles = static_cast<Tile2D*>(c.ws.get(tag + ":tiles", sizeof(Tile2D) * P.tiles.size()));
   cuda_check(cudaMemcpyAsync(P.d_inst, P.inst.data(), sizeof(Inst2D) * P.inst.size(), cudaMemcpyHostToDevice, c.stream), "upload inst");
   cuda_check(cudaMemcpyAsync(P.d_tiles, P.tiles.data(), sizeof(Tile2D) * P.tiles.size(), cudaMemcpyHostToDevice, c.stream), "upload tiles");
+  P.d_groups = static_cast<TileGroup*>(c.ws.get(tag + ":groups", sizeof(TileGroup) * P.groups.size()));
+  cuda_check(cudaMemcpyAsync(P.d_groups, P.groups.data(), sizeof(TileGroup) * P.groups.size(), cudaMemcpyHostToDevice,
+                             c.stream), "upload tile groups");
   return P;
 }
 
@@ -303,7 +308,8 @@ struct StageBuf {
   double *wsx = nullptr, *wsy = nullptr;  // LLF wave speeds at face nodes
   // taped solver iterates (empty when untaped). Jacobi / Chebyshev: xk = x_k,
   // rk = r_k (k < n). PCG: x0t = x_0, rk = r_0..r_n, pk = p_k, apk = A p_k,
-  // scal = per-instance rz_0..rz_n then pAp_0..pAp_{n-1}.
+  // scal = per-instance rz_0..rz_n, pAp_0..pAp_{n-1}, alpha_0..alpha_{n-1},
+  // beta_0..beta_{n-1} (pcg_scal_count).
   std::vector<double*> xk, rk;
   std::vector<double*> gxk, gyk;  // taped reference derivatives of the iterates (optional)
   std::vector<double*> pk, apk;
@@ -319,8 +325,11 @@ constexpr int STAGE_FIXED_FIELDS = 16;  // q(4) invr Sout b cm ckx cky cinvM cpx
 // reverse recomputes them.
 constexpr bool TAPE_ITERATE_DERIVATIVES = false;
 
+// Per-instance scalars of one PCG solve: rz (n + 1), pAp, alpha, beta (n each).
+static long long pcg_scal_count(int n_iter, int ni) { return (long long)(4 * n_iter + 1) * ni; }
+
 static int pcg_scal_fields(const Solve2DOpts& o, long long NG, int ni) {
-  const long long need = (long long)(2 * o.n_iter + 1) * ni;
+  const long long need = pcg_scal_count(o.n_iter, ni);
   return (int)((need + NG - 1) / NG);
 }
 
@@ -367,12 +376,14 @@ static bool all_alpha_pos(const Plan2D& P) {
   return true;
 }
 
-// Per-instance sum of per-tile partials: out[inst] (mode 0) or the PCG
-// reverse scalars (mode 1, see k2_tile_sum).
-static void tile_sum(Ctx& c, const Plan2D& P, const double* partials, double* out) {
+// Per-instance sum of per-tile partials: out[inst], and with quot the
+// quotient quot = (qnum or the sum) / ((qden or the sum) + 1e-30).
+static void tile_sum(Ctx& c, const Plan2D& P, const double* partials, double* out, const double* qnum = nullptr,
+                     const double* qden = nullptr, double* quot = nullptr) {
   TileSumArgs t;
   std::memset(&t, 0, sizeof(t));
   t.inst = P.d_inst; t.partials = partials; t.out = out; t.mode = 0;
+  t.qnum = qnum; t.qden = qden; t.quot = quot;
   LaunchScope ls(c, KID_OTHER);
   k2_tile_sum<<<(int)P.inst.size(), PCG_THREADS, 0, c.stream>>>(t);
 }
@@ -389,10 +400,12 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
   double* part = c.ws.dbl("red:part", nb);
-  double* scal = taped ? st.scal : c.ws.dbl("pcg:scal", (size_t)(2 * n + 1) * ni);
+  double* scal = taped ? st.scal : c.ws.dbl("pcg:scal", (size_t)pcg_scal_count(n, ni));
   double* apbuf = taped ? nullptr : c.ws.dbl("pcg:ap", NG);
   auto RZ = [&](int k) { return scal + (long long)k * ni; };
   auto PAP = [&](int k) { return scal + (long long)(n + 1 + k) * ni; };
+  auto AL = [&](int k) { return scal + (long long)(2 * n + 1 + k) * ni; };
+  auto BT = [&](int k) { return scal + (long long)(3 * n + 1 + k) * ni; };
   auto R = [&](int k) { return taped ? st.rk[k] : xa; };
   auto PK = [&](int k) { return taped ? st.pk[k] : ((k % 2 == 0) ? xb : dbuf); };
   auto AP = [&](int k) { return taped ? st.apk[k] : apbuf; };
@@ -420,7 +433,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
       if (k == 0) {
         a.x = PK(0);
       } else {
-        a.pcg_r = R(k); a.pcg_p = PK(k - 1); a.rz_cur = RZ(k); a.rz_prev = RZ(k - 1);
+        a.pcg_r = R(k); a.pcg_p = PK(k - 1); a.pcg_beta = BT(k - 1);
         a.p_out = PK(k);
       }
       a.ap_out = AP(k);
@@ -428,19 +441,19 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
         LaunchScope ls(c, KID_APPLY);
         NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG, a, nb, c.stream));
       }
-      tile_sum(c, P, part, PAP(k));
+      tile_sum(c, P, part, PAP(k), RZ(k), nullptr, AL(k));  // alpha_k = rz_k / (pAp_k + eps)
     }
     PcgUpdateArgs u;
-    u.tiles = P.d_tiles; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
+    u.tiles = P.d_tiles; u.groups = P.d_groups; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
     u.x_in = k == 0 ? x0 : xout; u.x_out = xout;
     u.p = PK(k); u.ap = AP(k); u.r_in = R(k); u.r_out = R(k + 1); u.cinvM = st.cinvM;
-    u.rz = RZ(k); u.pap = PAP(k);
+    u.al = AL(k);
     u.partials = part;
     {
       LaunchScope ls(c, KID_OTHER);
-      k2_pcg_update<<<nb, PCG_THREADS, 0, c.stream>>>(u);
+      k2_pcg_update<<<P.ngroups(), PCG_THREADS, 0, c.stream>>>(u);
     }
-    tile_sum(c, P, part, RZ(k + 1));
+    tile_sum(c, P, part, RZ(k + 1), nullptr, RZ(k), BT(k));  // beta_k = rz_{k+1} / (rz_k + eps)
   }
 }
 
@@ -914,7 +927,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   int tx, ty;
   tile_geometry(P, &tx, &ty);
   double* part = srev == SREV_PCG ? c.ws.dbl("red:part", P.ntiles()) : nullptr;
-  double* pscal = c.ws.dbl("adj:pcgscal", (size_t)3 * ni);  // BET, RZB, PAPB per instance
+  double* pscal = c.ws.dbl("adj:pcgscal", (size_t)4 * ni);  // BET, RZB, PAPB, RZB1 per instance
   const int nb = P.ntiles();
   const double c0s[3] = {0.0, 3.0 / 4, 1.0 / 3}, c1s[3] = {1.0, 1.0 / 4, 2.0 / 3}, c2s[3] = {1.0, 1.0 / 4, 2.0 / 3};
 
@@ -925,18 +938,20 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
     const int n = o.n_iter;
     double* PB = U[0];
     double* RB = U[1];
-    double* BET = pscal; double* RZB = pscal + ni; double* PAPB = pscal + 2 * ni;
+    double* BET = pscal; double* RZB = pscal + ni; double* PAPB = pscal + 2 * ni; double* RZB1 = pscal + 3 * ni;
     const double* RZ = sb.scal;
     const double* PAP = sb.scal + (long long)(n + 1) * ni;
+    const double* AL = sb.scal + (long long)(2 * n + 1) * ni;
+    const double* BT = sb.scal + (long long)(3 * n + 1) * ni;
     for (int it = n - 1; it >= 0; --it) {
       PcgRevArgs g;
-      g.tiles = P.d_tiles; g.inst = P.d_inst; g.np = P.np; g.tx = tx; g.ty = ty;
-      g.first = it == n - 1 ? 1 : 0; g.it = it; g.ni = ni;
+      g.tiles = P.d_tiles; g.groups = P.d_groups; g.inst = P.d_inst; g.np = P.np; g.tx = tx; g.ty = ty;
+      g.first = it == n - 1 ? 1 : 0;
       g.pb = PB; g.rb = RB; g.iMb = Mb;
       g.r1 = sb.rk[it + 1]; g.cinvM = sb.cinvM; g.ap = sb.apk[it]; g.p = sb.pk[it]; g.xb = Sb;
-      g.RZ = RZ; g.BET = BET; g.RZB = RZB;
+      g.beta = BT + (long long)it * ni; g.rzb1 = RZB1;
       g.partials = part;
-      { LaunchScope ls(c, KID_OTHER); k2_pcg_rev_update<<<nb, PCG_THREADS, 0, c.stream>>>(g); }
+      { LaunchScope ls(c, KID_OTHER); k2_pcg_rev_update<<<P.ngroups(), PCG_THREADS, 0, c.stream>>>(g); }
       {
         TileSumArgs ts;
         std::memset(&ts, 0, sizeof(ts));
@@ -956,11 +971,18 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       r.bb_op = 0;
       r.zscale = -1.0;
       r.has_next = it > 0 ? 1 : 0;
-      r.rz_it = RZ + (long long)it * ni; r.pap_it = PAP + (long long)it * ni; r.papb = PAPB;
+      r.al_it = AL + (long long)it * ni; r.papb = PAPB;
       r.xconst = Sb; r.apk = sb.apk[it]; r.p_next = it > 0 ? sb.pk[it - 1] : nullptr;
       r.partials = part;
       { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(SREV_PCG, r, nb, c.stream)); }
-      if (it > 0) tile_sum(c, P, part, BET);
+      if (it > 0) {  // betab of iteration it - 1 and rzb_it = RZB + betab / (rz_{it-1} + eps)
+        TileSumArgs ts;
+        std::memset(&ts, 0, sizeof(ts));
+        ts.inst = P.d_inst; ts.partials = part; ts.mode = 2; ts.it = it - 1; ts.ni = ni;
+        ts.RZ = RZ; ts.BET = BET; ts.RZB = RZB; ts.RZB1 = RZB1;
+        LaunchScope ls(c, KID_OTHER);
+        k2_tile_sum<<<ni, PCG_THREADS, 0, c.stream>>>(ts);
+      }
     }
     {
       PcgRevFinalArgs f;

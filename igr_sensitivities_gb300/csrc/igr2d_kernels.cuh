@@ -281,10 +281,10 @@ struct ApplyArgs2D {
   // Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347):
   //  EPI_PCG0: x = x_0; r_0 = b - A x_0 -> r_out, p_0 = M^-1 r_0 -> p_out, partial of r_0 . p_0
   //  EPI_PCG : x = p_k; with pcg_p set, p_k = M^-1 r_k + beta p_{k-1} is formed on load from
-  //            (pcg_r, pcg_p), beta = rz_cur / (rz_prev + 1e-30), and stored to p_out;
+  //            (pcg_r, pcg_p), beta = pcg_beta[inst] = rz_k / (rz_{k-1} + 1e-30), and stored to p_out;
   //            A p_k -> ap_out, partial of p_k . A p_k
   // The inner-product partial of each tile goes to partials[tile]; k2_tile_sum adds them per instance.
-  const double *pcg_r, *pcg_p, *rz_cur, *rz_prev;
+  const double *pcg_r, *pcg_p, *pcg_beta;
   double *p_out, *r_out, *ap_out;
   double* partials;
 };
@@ -307,13 +307,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
   const double hw = B.hw;
   // PCG direction update fused into the loads (p_k is pointwise in r_k, p_{k-1})
   const bool form_p = EPI == EPI_PCG && a.pcg_p != nullptr;
-  double beta = 0.0;
-  if (form_p) {  // block-uniform: one thread divides, the block reads the quotient
-    __shared__ double s_beta;
-    if (threadIdx.x == 0) s_beta = a.rz_cur[tl.inst] / (a.rz_prev[tl.inst] + 1e-30);
-    __syncthreads();
-    beta = s_beta;
-  }
+  const double beta = form_p ? a.pcg_beta[tl.inst] : 0.0;
   auto ldx = [&](long long n) -> double {
     if (form_p) return fma(beta, a.pcg_p[n], a.pcg_r[n] * a.cinvM[n]);
     return a.x[n];

@@ -11,12 +11,19 @@
 // identical from run to run and independent of the batch composition.
 //
 // Scalars live on the device, one per instance: rz_k = r_k . M^-1 r_k and
-// pAp_k = p_k . A p_k for every iteration (the tape of the scalar
-// recurrence); alpha_k = rz_k / (pAp_k + 1e-30) and
-// beta_k = rz_{k+1} / (rz_k + 1e-30) are recomputed where needed, with the
-// reference's 1e-30 guards (elliptic.jl:338, 343). An FP64 divide is a
-// software sequence of ~20 FP64 instructions on GB300, so one thread of each
-// block forms these quotients and the block reads them from shared memory.
+// pAp_k = p_k . A p_k for every iteration, with alpha_k = rz_k / (pAp_k + 1e-30)
+// and beta_k = rz_{k+1} / (rz_k + 1e-30) (the reference's 1e-30 guards,
+// elliptic.jl:338, 343): the tape of the scalar recurrence. An FP64 divide
+// is a software sequence of ~20 FP64 instructions on GB300, so the quotients
+// are formed once per instance, by k2_tile_sum as soon as their inner product
+// is complete, and the node kernels read them.
+//
+// The pointwise kernels (k2_pcg_update, k2_pcg_rev_update) run one block per
+// tile group (TILE_GROUP tiles of one instance): thread t takes node t of
+// every tile of the group, so the block reduction is paid once per group.
+// The group's partial goes to the entry of its first tile and the other
+// entries of the group get 0, so k2_tile_sum reads the same per-tile layout
+// as after the operator kernels.
 #pragma once
 #include "igr_device.cuh"
 
@@ -38,34 +45,46 @@ __device__ __forceinline__ bool tile_node(const Tile2D& tl, const Inst2D& I, int
 // Forward iteration k, after A p_k:  x_{k+1} = x_k + alpha_k p_k,
 // r_{k+1} = r_k - alpha_k A p_k, rz_{k+1} = r_{k+1} . M^-1 r_{k+1}.
 struct PcgUpdateArgs {
-  const Tile2D* tiles; const Inst2D* inst; int np, tx, ty;
+  const Tile2D* tiles; const TileGroup* groups; const Inst2D* inst; int np, tx, ty;
   const double *x_in, *p, *ap, *r_in, *cinvM;
   double *x_out, *r_out;
-  const double *rz, *pap;   // per-instance rz_k, pAp_k
+  const double* al;         // per-instance alpha_k
   double* partials;         // per-tile partials of rz_{k+1}
 };
 
+// Writes a group's partial: the group sum to its first tile, 0 to the others.
+__device__ __forceinline__ void group_partial(const TileGroup& g, double tot, double* partials) {
+  if ((int)threadIdx.x < g.count) partials[g.first + threadIdx.x] = threadIdx.x == 0 ? tot : 0.0;
+}
+
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
-  constexpr int P2 = PCG_THREADS;
+  constexpr int P2 = PCG_THREADS, G = TILE_GROUP;
   __shared__ double s_red[P2];
-  __shared__ double s_al;
-  const Tile2D tl = a.tiles[blockIdx.x];
-  const Inst2D I = a.inst[tl.inst];
-  if (threadIdx.x == 0) s_al = a.rz[tl.inst] / (a.pap[tl.inst] + 1e-30);
-  __syncthreads();
-  const double al = s_al;
+  const TileGroup g = a.groups[blockIdx.x];
+  const Inst2D I = a.inst[g.inst];
+  const double al = a.al[g.inst];
   const int cnt = a.tx * a.ty * a.np * a.np;
   double part = 0.0;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-    long long n;
-    if (!tile_node(tl, I, a.np, a.tx, idx, &n)) continue;
-    a.x_out[n] = fma(al, a.p[n], a.x_in[n]);
-    const double r = fma(-al, a.ap[n], a.r_in[n]);
-    a.r_out[n] = r;
-    part = fma(r, r * a.cinvM[n], part);
+    long long n[G];
+    bool ok[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node(a.tiles[g.first + j], I, a.np, a.tx, idx, &n[j]);
+    double p[G], ap[G], x[G], r[G], im[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+      if (ok[j]) { p[j] = a.p[n[j]]; ap[j] = a.ap[n[j]]; x[j] = a.x_in[n[j]]; r[j] = a.r_in[n[j]]; im[j] = a.cinvM[n[j]]; }
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+      if (ok[j]) {
+        a.x_out[n[j]] = fma(al, p[j], x[j]);
+        const double rn = fma(-al, ap[j], r[j]);
+        a.r_out[n[j]] = rn;
+        part = fma(rn, rn * im[j], part);
+      }
   }
   const double tot = block_sum<P2>(part, s_red);
-  if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
+  group_partial(g, tot, a.partials);
 }
 
 // ---------------------------------------------------------------------------
@@ -75,69 +94,80 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
 //   rz_{it+1} = r_{it+1} . z_{it+1}, z_{it+1} = M^-1 r_{it+1}
 //                                           -> rb += rzb_{it+1} z + M^-1 zb', iMb += zb' r
 //   ab = -(rb . A p_it) + (xb . p_it)       (reduced; stored through RZB, PAPB)
-// betab = pb . p_it arrives from the previous reverse apply (BET), or is 0 on
-// the first reverse iteration, where pb = rb = 0. The tile partials of ab go
-// to partials; k2_tile_sum (PCG-reverse mode) then sets RZB = rzb_it (its part
-// known so far) and PAPB = the adjoint of pAp_it, and k2_apply_rev<SREV_PCG>
-// finishes the iteration.
+// beta_it is read from the forward tape; rzb1 = RZB + betab / (rz_it + eps),
+// with betab = pb . p_it from the previous reverse apply, is formed by the
+// k2_tile_sum that completes betab (RZB1; 0 on the first reverse iteration,
+// where pb = rb = 0). The tile partials of ab go to partials; k2_tile_sum
+// (PCG-reverse mode) then sets RZB = rzb_it (its part known so far) and
+// PAPB = the adjoint of pAp_it, and k2_apply_rev<SREV_PCG> finishes the
+// iteration.
 // ---------------------------------------------------------------------------
 struct PcgRevArgs {
-  const Tile2D* tiles; const Inst2D* inst; int np, tx, ty;
-  int first, it, ni;
+  const Tile2D* tiles; const TileGroup* groups; const Inst2D* inst; int np, tx, ty;
+  int first;
   double *pb, *rb, *iMb;
   const double *r1, *cinvM, *ap, *p, *xb;
-  const double *RZ;                // taped scalars: RZ[k*ni+i]
-  const double *BET, *RZB;         // per-instance adjoint scalars
+  const double *beta, *rzb1;       // per-instance beta_it (tape) and rzb_{it+1}
   double* partials;
 };
 
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
-  constexpr int P2 = PCG_THREADS;
+  constexpr int P2 = PCG_THREADS, G = TILE_GROUP;
   __shared__ double s_red[P2];
-  __shared__ double s_sc[2];
-  const Tile2D tl = a.tiles[blockIdx.x];
-  const Inst2D I = a.inst[tl.inst];
-  const int i = tl.inst;
-  if (threadIdx.x == 0) {
-    const double rz0 = a.RZ[(long long)a.it * a.ni + i], rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
-    const double e0 = rz0 + 1e-30;
-    const double betab = a.first ? 0.0 : a.BET[i];
-    s_sc[0] = rz1 / e0;                                  // beta
-    s_sc[1] = (a.first ? 0.0 : a.RZB[i]) + betab / e0;   // adjoint of rz_{it+1}
-  }
-  __syncthreads();
-  const double beta = s_sc[0], rzb1 = s_sc[1];
+  const TileGroup g = a.groups[blockIdx.x];
+  const Inst2D I = a.inst[g.inst];
+  const double beta = a.beta[g.inst], rzb1 = a.first ? 0.0 : a.rzb1[g.inst];
   const int cnt = a.tx * a.ty * a.np * a.np;
   double part = 0.0;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-    long long n;
-    if (!tile_node(tl, I, a.np, a.tx, idx, &n)) continue;
-    const double pbv = a.first ? 0.0 : a.pb[n];
-    double rbv = a.first ? 0.0 : a.rb[n];
-    const double r1 = a.r1[n], im = a.cinvM[n];
-    a.pb[n] = beta * pbv;
-    const double zb = fma(rzb1, r1, pbv);
-    rbv = fma(rzb1, r1 * im, rbv);
-    rbv = fma(zb, im, rbv);
-    a.rb[n] = rbv;
-    a.iMb[n] = a.first ? zb * r1 : fma(zb, r1, a.iMb[n]);
-    part = fma(a.xb[n], a.p[n], fma(-rbv, a.ap[n], part));
+    long long n[G];
+    bool ok[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node(a.tiles[g.first + j], I, a.np, a.tx, idx, &n[j]);
+    double pbv[G], rbv[G], imb[G], r1[G], im[G], ap[G], xb[G], p[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+      if (ok[j]) {
+        pbv[j] = a.first ? 0.0 : a.pb[n[j]];
+        rbv[j] = a.first ? 0.0 : a.rb[n[j]];
+        imb[j] = a.first ? 0.0 : a.iMb[n[j]];
+        r1[j] = a.r1[n[j]]; im[j] = a.cinvM[n[j]]; ap[j] = a.ap[n[j]]; xb[j] = a.xb[n[j]]; p[j] = a.p[n[j]];
+      }
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+      if (ok[j]) {
+        a.pb[n[j]] = beta * pbv[j];
+        const double zb = fma(rzb1, r1[j], pbv[j]);
+        double rb = fma(rzb1, r1[j] * im[j], rbv[j]);
+        rb = fma(zb, im[j], rb);
+        a.rb[n[j]] = rb;
+        a.iMb[n[j]] = a.first ? zb * r1[j] : fma(zb, r1[j], imb[j]);
+        part = fma(xb[j], p[j], fma(-rb, ap[j], part));
+      }
   }
   const double tot = block_sum<P2>(part, s_red);
-  if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
+  group_partial(g, tot, a.partials);
 }
 
 // Per-instance sum of the tile partials (one block per instance, fixed
 // order: thread t adds tiles t, t + 256, ..., then a block tree).
-// mode 0: out[i] = sum. mode 1 (after k2_pcg_rev_update of iteration it):
-// ab = sum, RZB[i] = -betab rz_{it+1} / (rz_it + eps)^2 + ab / (pAp_it + eps),
-// PAPB[i] = -ab rz_it / (pAp_it + eps)^2, betab = BET[i] (0 when first).
+// mode 0: out[i] = sum; with quot set, also
+//   quot[i] = (qnum ? qnum[i] : sum) / ((qden ? qden[i] : sum) + 1e-30)
+// (alpha_k = rz_k / (pAp_k + eps) after pAp_k, beta_k = rz_{k+1} / (rz_k + eps)
+// after rz_{k+1}).
+// mode 1 (after k2_pcg_rev_update of iteration it): ab = sum,
+//   RZB[i] = -betab rz_{it+1} / (rz_it + eps)^2 + ab / (pAp_it + eps),
+//   PAPB[i] = -ab rz_it / (pAp_it + eps)^2, betab = BET[i] (0 when first).
+// mode 2 (after k2_apply_rev<SREV_PCG> of iteration it + 1, it >= 0):
+//   BET[i] = betab = sum, RZB1[i] = RZB[i] + betab / (rz_it + eps).
 struct TileSumArgs {
   const Inst2D* inst; const double* partials;
   double* out;
+  const double *qnum, *qden;
+  double* quot;
   int mode, first, it, ni;
-  const double *RZ, *PAP, *BET;
-  double *RZB, *PAPB;
+  const double *RZ, *PAP;
+  double *BET, *RZB, *PAPB, *RZB1;
 };
 
 __global__ void __launch_bounds__(PCG_THREADS) k2_tile_sum(TileSumArgs a) {
@@ -151,10 +181,17 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_tile_sum(TileSumArgs a) {
   if (threadIdx.x != 0) return;
   if (a.mode == 0) {
     a.out[i] = tot;
+    if (a.quot) a.quot[i] = (a.qnum ? a.qnum[i] : tot) / ((a.qden ? a.qden[i] : tot) + 1e-30);
     return;
   }
-  const double rz0 = a.RZ[(long long)a.it * a.ni + i], rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
+  const double rz0 = a.RZ[(long long)a.it * a.ni + i];
   const double e0 = rz0 + 1e-30;
+  if (a.mode == 2) {
+    a.BET[i] = tot;
+    a.RZB1[i] = a.RZB[i] + tot / e0;
+    return;
+  }
+  const double rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
   const double betab = a.first ? 0.0 : a.BET[i];
   const double den = a.PAP[(long long)a.it * a.ni + i] + 1e-30;
   a.RZB[i] = -betab * rz1 / (e0 * e0) + tot / den;

@@ -335,7 +335,7 @@ struct ApplyRevArgs2D {
   //   (u = rb, xk = p_it); xb = pb: pb += alpha_it xconst + pApb apk + A(adjoint of A p_it);
   //   with has_next, the tile's partial of pb . p_next (betab of the next reverse
   //   iteration) goes to partials[tile]
-  const double *rz_it, *pap_it, *papb;  // per-instance scalars
+  const double *al_it, *papb;  // per-instance alpha_it (tape) and the adjoint of pAp_it
   const double *xconst, *apk, *p_next;
   double* partials;
 };
@@ -359,11 +359,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
   const BasisDev& B = a.B;
   const double hw = B.hw;
   double pal = 0.0, ppb = 0.0;  // PCG: alpha_it and the adjoint of pAp_it
-  if (PCG) {  // one thread divides, the block reads the quotient
-    __shared__ double s_pal;
-    if (threadIdx.x == 0) s_pal = a.rz_it[tl.inst] / (a.pap_it[tl.inst] + 1e-30);
-    __syncthreads();
-    pal = s_pal;
+  if (PCG) {
+    pal = a.al_it[tl.inst];
     ppb = a.papb[tl.inst];
   }
   // u at node n, given x_k there (PCG forms it from rb and p_it)

@@ -54,6 +54,13 @@ struct Inst1D {
 // A tile of TX x TY elements of one instance; blocks map 1:1 onto tiles.
 struct Tile2D { int inst, ex0, ey0, pad; };
 
+// Up to TILE_GROUP consecutive tiles of one instance (tiles first ..
+// first + count - 1), the unit of the pointwise PCG kernels: one block per
+// group amortises the block reduction over several tiles. Groups start at
+// the instance's first tile, so group sums do not depend on the batch.
+constexpr int TILE_GROUP = 4;
+struct TileGroup { int inst, first, count, pad; };
+
 // Status word shared by the kernels and the host (device memory).
 enum : int { DEV_OK = 0, DEV_NONFINITE = 1 };
 

@@ -107,7 +107,10 @@ struct Plan2D {
   long long NG = 0;
   Inst2D* d_inst = nullptr;
   Tile2D* d_tiles = nullptr;
+  std::vector<TileGroup> groups;   // TILE_GROUP tiles per entry, per instance
+  TileGroup* d_groups = nullptr;
   int ntiles() const { return (int)tiles.size(); }
+  int ngroups() const { return (int)groups.size(); }
 };
 
 Plan2D make_plan2d(Ctx& c, const BasisDev& B, const std::vector<Inst2DDesc>& insts, const std::string& tag);
