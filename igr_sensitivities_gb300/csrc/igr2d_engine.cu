@@ -376,30 +376,56 @@ static bool all_alpha_pos(const Plan2D& P) {
   return true;
 }
 
-// Per-instance sum of per-tile partials: out[inst], and with quot the
-// quotient quot = (qnum or the sum) / ((qden or the sum) + 1e-30).
-static void tile_sum(Ctx& c, const Plan2D& P, const double* partials, double* out, const double* qnum = nullptr,
-                     const double* qden = nullptr, double* quot = nullptr) {
-  TileSumArgs t;
-  std::memset(&t, 0, sizeof(t));
-  t.inst = P.d_inst; t.partials = partials; t.out = out; t.mode = 0;
-  t.qnum = qnum; t.qden = qden; t.quot = quot;
+// The PCG inner products are completed inside their producing kernels
+// (InstSum with counters) for grids of at most this many tiles, and by a
+// separate k2_inst_sum launch above it: the fused form saves a launch per
+// product but holds every block until its partial is fenced, which costs
+// more once a kernel runs many waves (16 x 256^2 P3: 1.56 fused vs 1.63
+// separate tangent + adjoint + FD sets/hour; one 128^2 PCG-60 forward solve:
+// 3.72 vs 3.88 s). Both forms give the same bits.
+constexpr int FUSED_SUM_MAX_TILES = 4096;
+
+// Per-instance completion counters of the fused inner products, zeroed
+// before each solve (the kernels leave them at 0); null above
+// FUSED_SUM_MAX_TILES.
+static int* inst_counters(Ctx& c, const Plan2D& P) {
+  if (P.ntiles() > FUSED_SUM_MAX_TILES) return nullptr;
+  int* cnt = static_cast<int*>(c.ws.get("pcg:cnt", sizeof(int) * P.inst.size()));
+  cuda_check(cudaMemsetAsync(cnt, 0, sizeof(int) * P.inst.size(), c.stream), "zero instance counters");
+  return cnt;
+}
+
+// InstSum in mode 0: out[inst] = sum, and with quot
+// quot = (qnum or the sum) / ((qden or the sum) + 1e-30).
+static InstSum inst_sum0(int* cnt, double* out, const double* qnum = nullptr, const double* qden = nullptr,
+                         double* quot = nullptr) {
+  InstSum s;
+  std::memset(&s, 0, sizeof(s));
+  s.cnt = cnt; s.out = out; s.qnum = qnum; s.qden = qden; s.quot = quot; s.mode = 0;
+  return s;
+}
+
+// Completes an InstSum in a separate launch when its kernel did not (cnt null).
+static void inst_sum_after(Ctx& c, const Plan2D& P, const double* partials, bool grouped, const InstSum& s) {
+  if (s.cnt) return;
   LaunchScope ls(c, KID_OTHER);
-  k2_tile_sum<<<(int)P.inst.size(), PCG_THREADS, 0, c.stream>>>(t);
+  k2_inst_sum<<<(int)P.inst.size(), 32, 0, c.stream>>>(P.d_inst, partials, grouped ? 1 : 0, s);
 }
 
 static void tile_geometry(const Plan2D& P, int* tx, int* ty) { tile_shape(P.np, tx, ty); }
 
 // Fixed-count Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347) on
 // the stage's operator: x_0 = warm start, result in st.Sout. Per iteration
-// one operator kernel (A p_k and p_k . A p_k, with p_k formed on load) and one
-// pointwise kernel (x, r and r . M^-1 r). With a tape slot, r_k, p_k, A p_k
-// and the scalars are written straight into it.
+// one operator kernel (A p_k and p_k . A p_k, with p_k formed on load; its
+// last block per instance forms pAp_k and alpha_k) and one pointwise kernel
+// (x, r and r . M^-1 r; its last block forms rz_{k+1} and beta_k). With a
+// tape slot, r_k, p_k, A p_k and the scalars are written straight into it.
 static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b, const double* x0,
                       double* xout, bool taped, double* xa, double* xb, double* dbuf) {
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
   double* part = c.ws.dbl("red:part", nb);
+  int* cnt = inst_counters(c, P);
   double* scal = taped ? st.scal : c.ws.dbl("pcg:scal", (size_t)pcg_scal_count(n, ni));
   double* apbuf = taped ? nullptr : c.ws.dbl("pcg:ap", NG);
   auto RZ = [&](int k) { return scal + (long long)k * ni; };
@@ -421,11 +447,12 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
     a.x = x0;
     a.tape_x = taped ? st.x0t : nullptr;
     a.r_out = R(0); a.p_out = PK(0);
+    a.isum = inst_sum0(cnt, RZ(0));
     {
       LaunchScope ls(c, KID_APPLY);
       NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG0, a, nb, c.stream));
     }
-    tile_sum(c, P, part, RZ(0));
+    inst_sum_after(c, P, part, false, a.isum);
   }
   for (int k = 0; k < n; ++k) {
     {
@@ -437,11 +464,12 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
         a.p_out = PK(k);
       }
       a.ap_out = AP(k);
+      a.isum = inst_sum0(cnt, PAP(k), RZ(k), nullptr, AL(k));  // alpha_k = rz_k / (pAp_k + eps)
       {
         LaunchScope ls(c, KID_APPLY);
         NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG, a, nb, c.stream));
       }
-      tile_sum(c, P, part, PAP(k), RZ(k), nullptr, AL(k));  // alpha_k = rz_k / (pAp_k + eps)
+      inst_sum_after(c, P, part, false, a.isum);
     }
     PcgUpdateArgs u;
     u.tiles = P.d_tiles; u.groups = P.d_groups; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
@@ -449,11 +477,12 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
     u.p = PK(k); u.ap = AP(k); u.r_in = R(k); u.r_out = R(k + 1); u.cinvM = st.cinvM;
     u.al = AL(k);
     u.partials = part;
+    u.isum = inst_sum0(cnt, RZ(k + 1), nullptr, RZ(k), BT(k));  // beta_k = rz_{k+1} / (rz_k + eps)
     {
       LaunchScope ls(c, KID_OTHER);
       k2_pcg_update<<<P.ngroups(), PCG_THREADS, 0, c.stream>>>(u);
     }
-    tile_sum(c, P, part, RZ(k + 1), nullptr, RZ(k), BT(k));  // beta_k = rz_{k+1} / (rz_k + eps)
+    inst_sum_after(c, P, part, true, u.isum);
   }
 }
 
@@ -943,6 +972,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
     const double* PAP = sb.scal + (long long)(n + 1) * ni;
     const double* AL = sb.scal + (long long)(2 * n + 1) * ni;
     const double* BT = sb.scal + (long long)(3 * n + 1) * ni;
+    int* cnt = inst_counters(c, P);
     for (int it = n - 1; it >= 0; --it) {
       PcgRevArgs g;
       g.tiles = P.d_tiles; g.groups = P.d_groups; g.inst = P.d_inst; g.np = P.np; g.tx = tx; g.ty = ty;
@@ -951,15 +981,11 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       g.r1 = sb.rk[it + 1]; g.cinvM = sb.cinvM; g.ap = sb.apk[it]; g.p = sb.pk[it]; g.xb = Sb;
       g.beta = BT + (long long)it * ni; g.rzb1 = RZB1;
       g.partials = part;
+      std::memset(&g.isum, 0, sizeof(g.isum));  // ab, then RZB and PAPB
+      g.isum.cnt = cnt; g.isum.mode = 1; g.isum.first = g.first; g.isum.it = it; g.isum.ni = ni;
+      g.isum.RZ = RZ; g.isum.PAP = PAP; g.isum.BET = BET; g.isum.RZB = RZB; g.isum.PAPB = PAPB;
       { LaunchScope ls(c, KID_OTHER); k2_pcg_rev_update<<<P.ngroups(), PCG_THREADS, 0, c.stream>>>(g); }
-      {
-        TileSumArgs ts;
-        std::memset(&ts, 0, sizeof(ts));
-        ts.inst = P.d_inst; ts.partials = part; ts.mode = 1; ts.first = g.first; ts.it = it; ts.ni = ni;
-        ts.RZ = RZ; ts.PAP = PAP; ts.BET = BET; ts.RZB = RZB; ts.PAPB = PAPB;
-        LaunchScope ls(c, KID_OTHER);
-        k2_tile_sum<<<ni, PCG_THREADS, 0, c.stream>>>(ts);
-      }
+      inst_sum_after(c, P, part, true, g.isum);
       ApplyRevArgs2D r;
       std::memset(&r, 0, sizeof(r));
       r.tiles = P.d_tiles; r.inst = P.d_inst; r.B = P.B;
@@ -974,15 +1000,12 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       r.al_it = AL + (long long)it * ni; r.papb = PAPB;
       r.xconst = Sb; r.apk = sb.apk[it]; r.p_next = it > 0 ? sb.pk[it - 1] : nullptr;
       r.partials = part;
-      { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(SREV_PCG, r, nb, c.stream)); }
       if (it > 0) {  // betab of iteration it - 1 and rzb_it = RZB + betab / (rz_{it-1} + eps)
-        TileSumArgs ts;
-        std::memset(&ts, 0, sizeof(ts));
-        ts.inst = P.d_inst; ts.partials = part; ts.mode = 2; ts.it = it - 1; ts.ni = ni;
-        ts.RZ = RZ; ts.BET = BET; ts.RZB = RZB; ts.RZB1 = RZB1;
-        LaunchScope ls(c, KID_OTHER);
-        k2_tile_sum<<<ni, PCG_THREADS, 0, c.stream>>>(ts);
+        r.isum.cnt = cnt; r.isum.mode = 2; r.isum.it = it - 1; r.isum.ni = ni;
+        r.isum.RZ = RZ; r.isum.BET = BET; r.isum.RZB = RZB; r.isum.RZB1 = RZB1;
       }
+      { LaunchScope ls(c, KID_APPLY_REV); NP_DISPATCH(P.np, launch_k2_apply_rev<NPV>(SREV_PCG, r, nb, c.stream)); }
+      if (it > 0) inst_sum_after(c, P, part, false, r.isum);
     }
     {
       PcgRevFinalArgs f;

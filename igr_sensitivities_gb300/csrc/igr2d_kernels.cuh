@@ -283,10 +283,12 @@ struct ApplyArgs2D {
   //  EPI_PCG : x = p_k; with pcg_p set, p_k = M^-1 r_k + beta p_{k-1} is formed on load from
   //            (pcg_r, pcg_p), beta = pcg_beta[inst] = rz_k / (rz_{k-1} + 1e-30), and stored to p_out;
   //            A p_k -> ap_out, partial of p_k . A p_k
-  // The inner-product partial of each tile goes to partials[tile]; k2_tile_sum adds them per instance.
+  // The inner-product partial of each tile goes to partials[tile]; the instance's last block adds
+  // them (isum: rz_0 for EPI_PCG0; pAp_k and alpha_k for EPI_PCG).
   const double *pcg_r, *pcg_p, *pcg_beta;
   double *p_out, *r_out, *ap_out;
   double* partials;
+  InstSum isum;
 };
 
 // Partner data across one face: its value and end-node derivative of x, and its stiffness coefficient.
@@ -465,7 +467,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
   }
   if (PCG) {
     const double tot = block_sum<P2>(part, s_red);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
+    inst_sum_last_block(a.isum, tl.inst, I.ntiles, tot, a.partials, blockIdx.x, I.tile0, I.ntiles);
   }
 }
 

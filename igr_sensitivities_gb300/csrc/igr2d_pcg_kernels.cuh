@@ -3,11 +3,9 @@
 //
 // The operator applications run in k2_apply (EPI_PCG0 / EPI_PCG) and
 // k2_apply_rev (SREV_PCG); these kernels do the vector updates between them.
-// Each block covers one tile of elements (the same tile list as the operator
-// kernels), so the per-instance inner products reduce deterministically:
-// block tree sum -> one partial per tile -> k2_tile_sum adds an instance's
-// partials in tile order (a separate launch: ordering across blocks comes from
-// the kernel boundary, with no fences or atomics). The results are therefore
+// The per-instance inner products reduce deterministically: block tree sum ->
+// one partial per block -> the instance's last block to finish adds the
+// instance's partials in a fixed order (InstSum). The results are therefore
 // identical from run to run and independent of the batch composition.
 //
 // Scalars live on the device, one per instance: rz_k = r_k . M^-1 r_k and
@@ -15,15 +13,13 @@
 // and beta_k = rz_{k+1} / (rz_k + 1e-30) (the reference's 1e-30 guards,
 // elliptic.jl:338, 343): the tape of the scalar recurrence. An FP64 divide
 // is a software sequence of ~20 FP64 instructions on GB300, so the quotients
-// are formed once per instance, by k2_tile_sum as soon as their inner product
-// is complete, and the node kernels read them.
+// are formed once per instance, by the block that completes their inner
+// product (InstSum), and the node kernels read them.
 //
 // The pointwise kernels (k2_pcg_update, k2_pcg_rev_update) run one block per
 // tile group (TILE_GROUP tiles of one instance): thread t takes node t of
 // every tile of the group, so the block reduction is paid once per group.
-// The group's partial goes to the entry of its first tile and the other
-// entries of the group get 0, so k2_tile_sum reads the same per-tile layout
-// as after the operator kernels.
+// Group j of an instance writes its partial to partials[tile0 + j].
 #pragma once
 #include "igr_device.cuh"
 
@@ -49,12 +45,19 @@ struct PcgUpdateArgs {
   const double *x_in, *p, *ap, *r_in, *cinvM;
   double *x_out, *r_out;
   const double* al;         // per-instance alpha_k
-  double* partials;         // per-tile partials of rz_{k+1}
+  double* partials;         // per-group partials of rz_{k+1}
+  InstSum isum;             // rz_{k+1} and beta_k
 };
 
-// Writes a group's partial: the group sum to its first tile, 0 to the others.
-__device__ __forceinline__ void group_partial(const TileGroup& g, double tot, double* partials) {
-  if ((int)threadIdx.x < g.count) partials[g.first + threadIdx.x] = threadIdx.x == 0 ? tot : 0.0;
+// Number of tile groups of an instance.
+__host__ __device__ __forceinline__ int inst_groups(const Inst2D& I) { return (I.ntiles + TILE_GROUP - 1) / TILE_GROUP; }
+
+// Writes a group's partial (group j of the instance to partials[tile0 + j])
+// and, when fused, lets the instance's last group complete the sum.
+__device__ __forceinline__ void group_partial(const InstSum& isum, const TileGroup& g, const Inst2D& I, double tot,
+                                              double* partials) {
+  const int ng = inst_groups(I);
+  inst_sum_last_block(isum, g.inst, ng, tot, partials, I.tile0 + (g.first - I.tile0) / TILE_GROUP, I.tile0, ng);
 }
 
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
@@ -84,7 +87,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
       }
   }
   const double tot = block_sum<P2>(part, s_red);
-  group_partial(g, tot, a.partials);
+  group_partial(a.isum, g, I, tot, a.partials);
 }
 
 // ---------------------------------------------------------------------------
@@ -96,10 +99,10 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
 //   ab = -(rb . A p_it) + (xb . p_it)       (reduced; stored through RZB, PAPB)
 // beta_it is read from the forward tape; rzb1 = RZB + betab / (rz_it + eps),
 // with betab = pb . p_it from the previous reverse apply, is formed by the
-// k2_tile_sum that completes betab (RZB1; 0 on the first reverse iteration,
-// where pb = rb = 0). The tile partials of ab go to partials; k2_tile_sum
-// (PCG-reverse mode) then sets RZB = rzb_it (its part known so far) and
-// PAPB = the adjoint of pAp_it, and k2_apply_rev<SREV_PCG> finishes the
+// block that completes betab in the previous reverse apply (RZB1; 0 on the
+// first reverse iteration, where pb = rb = 0). The instance's last block
+// completes ab and sets RZB = rzb_it (its part known so far) and PAPB = the
+// adjoint of pAp_it (InstSum mode 1); k2_apply_rev<SREV_PCG> finishes the
 // iteration.
 // ---------------------------------------------------------------------------
 struct PcgRevArgs {
@@ -109,6 +112,7 @@ struct PcgRevArgs {
   const double *r1, *cinvM, *ap, *p, *xb;
   const double *beta, *rzb1;       // per-instance beta_it (tape) and rzb_{it+1}
   double* partials;
+  InstSum isum;                    // mode 1: RZB, PAPB
 };
 
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
@@ -146,56 +150,17 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
       }
   }
   const double tot = block_sum<P2>(part, s_red);
-  group_partial(g, tot, a.partials);
+  group_partial(a.isum, g, I, tot, a.partials);
 }
 
-// Per-instance sum of the tile partials (one block per instance, fixed
-// order: thread t adds tiles t, t + 256, ..., then a block tree).
-// mode 0: out[i] = sum; with quot set, also
-//   quot[i] = (qnum ? qnum[i] : sum) / ((qden ? qden[i] : sum) + 1e-30)
-// (alpha_k = rz_k / (pAp_k + eps) after pAp_k, beta_k = rz_{k+1} / (rz_k + eps)
-// after rz_{k+1}).
-// mode 1 (after k2_pcg_rev_update of iteration it): ab = sum,
-//   RZB[i] = -betab rz_{it+1} / (rz_it + eps)^2 + ab / (pAp_it + eps),
-//   PAPB[i] = -ab rz_it / (pAp_it + eps)^2, betab = BET[i] (0 when first).
-// mode 2 (after k2_apply_rev<SREV_PCG> of iteration it + 1, it >= 0):
-//   BET[i] = betab = sum, RZB1[i] = RZB[i] + betab / (rz_it + eps).
-struct TileSumArgs {
-  const Inst2D* inst; const double* partials;
-  double* out;
-  const double *qnum, *qden;
-  double* quot;
-  int mode, first, it, ni;
-  const double *RZ, *PAP;
-  double *BET, *RZB, *PAPB, *RZB1;
-};
-
-__global__ void __launch_bounds__(PCG_THREADS) k2_tile_sum(TileSumArgs a) {
-  constexpr int P2 = PCG_THREADS;
-  __shared__ double s_red[P2];
+// Per-instance sums in a separate launch (InstSum with cnt null): one warp
+// per instance over the instance's tile partials, or its group partials when
+// grouped.
+__global__ void __launch_bounds__(32) k2_inst_sum(const Inst2D* inst, const double* partials, int grouped, InstSum a) {
   const int i = blockIdx.x;
-  const Inst2D I = a.inst[i];
-  double acc = 0.0;
-  for (int k = threadIdx.x; k < I.ntiles; k += blockDim.x) acc += a.partials[I.tile0 + k];
-  const double tot = block_sum<P2>(acc, s_red);
-  if (threadIdx.x != 0) return;
-  if (a.mode == 0) {
-    a.out[i] = tot;
-    if (a.quot) a.quot[i] = (a.qnum ? a.qnum[i] : tot) / ((a.qden ? a.qden[i] : tot) + 1e-30);
-    return;
-  }
-  const double rz0 = a.RZ[(long long)a.it * a.ni + i];
-  const double e0 = rz0 + 1e-30;
-  if (a.mode == 2) {
-    a.BET[i] = tot;
-    a.RZB1[i] = a.RZB[i] + tot / e0;
-    return;
-  }
-  const double rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
-  const double betab = a.first ? 0.0 : a.BET[i];
-  const double den = a.PAP[(long long)a.it * a.ni + i] + 1e-30;
-  a.RZB[i] = -betab * rz1 / (e0 * e0) + tot / den;
-  a.PAPB[i] = -tot * rz0 / (den * den);
+  const Inst2D I = inst[i];
+  const double s = warp_sum_partials(partials + I.tile0, grouped ? inst_groups(I) : I.ntiles);
+  if (threadIdx.x == 0) inst_sum_finish(a, i, s);
 }
 
 // Reverse of the PCG start (p_0 = z_0, rz_0 = r_0 . z_0, z_0 = M^-1 r_0):

@@ -334,10 +334,11 @@ struct ApplyRevArgs2D {
   //   u = -(adjoint of A p_it) = alpha_it rb - pApb p_it, formed on load from
   //   (u = rb, xk = p_it); xb = pb: pb += alpha_it xconst + pApb apk + A(adjoint of A p_it);
   //   with has_next, the tile's partial of pb . p_next (betab of the next reverse
-  //   iteration) goes to partials[tile]
+  //   iteration) goes to partials[tile] and the instance's last block completes it (isum, mode 2)
   const double *al_it, *papb;  // per-instance alpha_it (tape) and the adjoint of pAp_it
   const double *xconst, *apk, *p_next;
   double* partials;
+  InstSum isum;
 };
 
 // Partner data across one face for the reverse apply: values and end-node
@@ -553,7 +554,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
   }
   if (PCG && a.has_next) {
     const double tot = block_sum<P2>(part, s_red);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = tot;
+    inst_sum_last_block(a.isum, tl.inst, I.ntiles, tot, a.partials, blockIdx.x, I.tile0, I.ntiles);
   }
 }
 

@@ -87,6 +87,97 @@ __device__ __forceinline__ double block_sum(double v, double* s_red) {
   return r;
 }
 
+// Per-instance inner products of the PCG solve and of its reverse. Every
+// block of an instance writes one partial; the instance's sum is the
+// canonical warp sum of its partials (warp_sum_partials), formed either by
+// the instance's last block inside the producing kernel (cnt set: the block
+// fences its partial and counts itself in cnt[inst]; the block that brings
+// the count to the instance's number of blocks sums and resets the counter,
+// and no block waits for another) or by k2_inst_sum in a separate launch
+// (cnt null). Both give the same bits, which do not depend on which block
+// finishes last nor on the batch. The fence holds each block's SM slot until
+// its partial is visible, which costs more than the extra launch once a
+// kernel runs many waves of blocks, so the host fuses only small grids.
+//
+// What is done with the sum s of instance i (one thread):
+//   mode 0: out[i] = s and, with quot set,
+//           quot[i] = (qnum ? qnum[i] : s) / ((qden ? qden[i] : s) + 1e-30)
+//           (alpha_k = rz_k / (pAp_k + eps), beta_k = rz_{k+1} / (rz_k + eps));
+//   mode 1 (reverse iteration it, ab = s): RZB[i] = -betab rz_{it+1} / (rz_it + eps)^2
+//           + ab / (pAp_it + eps), PAPB[i] = -ab rz_it / (pAp_it + eps)^2,
+//           betab = BET[i] (0 when first);
+//   mode 2 (betab = s of reverse iteration it): BET[i] = s,
+//           RZB1[i] = RZB[i] + s / (rz_it + eps).
+// The 1e-30 guards are the reference's (elliptic.jl:338, 343).
+struct InstSum {
+  int* cnt;          // per-instance completion counters, 0 between launches
+  double* out;
+  const double *qnum, *qden;
+  double* quot;
+  int mode, first, it, ni;
+  const double *RZ, *PAP;
+  double *BET, *RZB, *PAPB, *RZB1;
+};
+
+__device__ __forceinline__ void inst_sum_finish(const InstSum& a, int i, double s) {
+  if (a.mode == 0) {
+    a.out[i] = s;
+    if (a.quot) a.quot[i] = (a.qnum ? a.qnum[i] : s) / ((a.qden ? a.qden[i] : s) + 1e-30);
+    return;
+  }
+  const double rz0 = a.RZ[(long long)a.it * a.ni + i];
+  const double e0 = rz0 + 1e-30;
+  if (a.mode == 2) {
+    a.BET[i] = s;
+    a.RZB1[i] = a.RZB[i] + s / e0;
+    return;
+  }
+  const double rz1 = a.RZ[(long long)(a.it + 1) * a.ni + i];
+  const double betab = a.first ? 0.0 : a.BET[i];
+  const double den = a.PAP[(long long)a.it * a.ni + i] + 1e-30;
+  a.RZB[i] = -betab * rz1 / (e0 * e0) + s / den;
+  a.PAPB[i] = -s * rz0 / (den * den);
+}
+
+// The canonical sum of count partials, by one warp: lane l adds partials
+// l, l + 32, ... in order, then a fixed shuffle tree; lane 0 holds the sum.
+__device__ __forceinline__ double warp_sum_partials(const double* p, int count) {
+  const int l = threadIdx.x & 31;
+  double acc = 0.0;
+#pragma unroll 16
+  for (int k = l; k < count; k += 32) acc += __ldcg(p + k);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
+// Called by every thread (blockDim >= 32) with the block's partial v, known
+// to thread 0, which stores it to partials[slot]. With a.cnt set, the last of
+// the instance's `nblocks` blocks then sums partials[first .. first + count)
+// and applies inst_sum_finish. Only the partial is fenced: everything else
+// the block writes is read by later launches.
+__device__ __forceinline__ void inst_sum_last_block(const InstSum& a, int inst, int nblocks, double v, double* partials,
+                                                    int slot, int first, int count) {
+  __shared__ int s_last;
+  if (!a.cnt) {
+    if (threadIdx.x == 0) partials[slot] = v;
+    return;
+  }
+  if (threadIdx.x == 0) {
+    partials[slot] = v;
+    __threadfence();
+    s_last = atomicAdd(a.cnt + inst, 1) == nblocks - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x >= 32) return;
+  __threadfence();
+  const double s = warp_sum_partials(partials + first, count);
+  if (threadIdx.x == 0) {
+    inst_sum_finish(a, inst, s);
+    a.cnt[inst] = 0;
+  }
+}
+
 // Instance of global node n (binary search over the instances' first nodes).
 __device__ __forceinline__ int find_inst(const Inst2D* inst, int ninst, long long n) {
   int lo = 0, hi = ninst - 1;

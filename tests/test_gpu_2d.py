@@ -292,3 +292,28 @@ def test_adjoint_batch_of_uneven_meshes_equals_single_calls(igr, oracle):
     assert abs(J[1] - Jr) <= 1e-12 * abs(Jr)
     num = np.sqrt(sum(np.sum((dq[1][v] - dqr[v]) ** 2) for v in range(4)))
     assert num <= RTOL_GRAD * np.sqrt(sum(np.sum(b ** 2) for b in dqr))
+
+
+def test_pcg_sums_fused_and_separate_agree_bitwise(igr, oracle):
+    """The PCG inner products are completed inside their kernels for small
+    grids and by a separate launch for large ones; both give the same bits.
+    A 64^2 instance alone (256 tiles: fused) and inside a batch with a
+    256 x 260 instance (4416 tiles: separate) has bitwise equal gradients."""
+    basis = igr.DGBasis(3)
+    meshes = [igr.CartesianMesh2D(64, 64, 1.0, 1.0, basis), igr.CartesianMesh2D(256, 260, 1.0, 1.0, basis)]
+    gams, states, dts, als = [1.4, 1.5], [], [], []
+    for i, m in enumerate(meshes):
+        q = W.seeded_pulses_2d(m, gams[i], W.seed_for(3, 60 + i), width=0.12)
+        states.append(tuple(flat(a) for a in q))
+        dts.append(W.cfl_dt_2d(m, 3, q, gams[i], 0.1))
+        als.append(3.0 * min(m.dx, m.dy) ** 2)
+    prm = (0.1, 0.1, 0.5)
+    J, dq, dg, da = igr.adjoint_batch_meshes(states, basis, meshes, gams, als, dts, 2, n_iter=4, solver="pcg",
+                                             objective="window_rho2", obj_params=prm)
+    m = meshes[0]
+    one = igr.enzyme_adjoint_ic(*[a.reshape(m.shape(basis), order="F") for a in states[0]], 2, dts[0], basis, m,
+                                gams[0], als[0], n_iter=4, solver="pcg", objective="window_rho2", obj_params=prm,
+                                with_params=True)
+    assert one[0] == J[0] and one[5] == dg[0] and one[6] == da[0]
+    for v in range(4):
+        assert np.array_equal(flat(one[1 + v]), dq[0][v])
