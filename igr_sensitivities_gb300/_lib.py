@@ -72,6 +72,10 @@ class Context:
         """1D: CTAs per instance (0 = automatic; 1, 2, 4, 8, 16)."""
         check(self, lib().igr_set_cluster_size_1d(self.handle, C.c_int(int(cs))))
 
+    def set_graphs(self, on):
+        """2D forward solves: replay repeated RK steps as CUDA graphs (default on)."""
+        check(self, lib().igr_set_graphs(self.handle, C.c_int(1 if on else 0)))
+
     def last_cluster_size_1d(self):
         v = C.c_int(0)
         check(self, lib().igr_last_cluster_size_1d(self.handle, C.byref(v)))

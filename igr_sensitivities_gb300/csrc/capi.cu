@@ -159,6 +159,12 @@ int igr_set_cluster_size_1d(igr_ctx* ctx, int cs) {
   return IGR_OK;
 }
 
+int igr_set_graphs(igr_ctx* ctx, int on) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.use_graphs = on != 0;
+  return IGR_OK;
+}
+
 int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out) {
   if (!ctx || !out) return IGR_EINVAL;
   *out = ctx->c.last_cluster1d;

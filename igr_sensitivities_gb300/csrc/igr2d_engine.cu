@@ -591,6 +591,42 @@ static void check_alpha_uniform(const Plan2D& P) {
   if (any_alpha_pos(P) && !all_alpha_pos(P)) throw Error(1, "a batch must have alpha > 0 for all instances or for none");
 }
 
+// A piece of stream work replayed as a CUDA graph: captured on its first
+// run, launched as one graph afterwards. The work must use the same buffers
+// and launch arguments every time and allocate nothing (run it once eagerly
+// first so that the workspace holds every buffer it names).
+struct StreamGraph {
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;  // kernel launches per replay
+  StreamGraph() = default;
+  StreamGraph(const StreamGraph&) = delete;
+  StreamGraph& operator=(const StreamGraph&) = delete;
+  ~StreamGraph() { if (exec) cudaGraphExecDestroy(exec); }
+  template <class F>
+  void run(Ctx& c, F&& work) {
+    if (!exec) {
+      cuda_check(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), "begin graph capture");
+      const long long l0 = c.launches;
+      cudaGraph_t g = nullptr;
+      try {
+        work();
+      } catch (...) {
+        cudaStreamEndCapture(c.stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      launches = c.launches - l0;
+      c.launches = l0;
+      cuda_check(cudaStreamEndCapture(c.stream, &g), "end graph capture");
+      const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      cuda_check(e, "graph instantiate");
+    }
+    cuda_check(cudaGraphLaunch(exec, c.stream), "graph launch");
+    c.launches += launches;
+  }
+};
+
 void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_steps, const Solve2DOpts& o) {
   check_alpha_uniform(P);
   const long long NG = P.NG;
@@ -605,15 +641,21 @@ void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_s
   recip(c, q[2], st[0].invr, NG);
   cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
   if (!apos) cuda_check(cudaMemsetAsync(Sig, 0, NG * sizeof(double), c.stream), "zero Sigma");
-  // Sigma ping-pong: the stage-3 output of step s is the warm start of step s+1.
-  double* sig_cur = Sig;
+  // Sigma ping-pong: the stage-3 output of step s is the warm start of step
+  // s+1, copied back to Sig, so every step runs the same launches on the same
+  // buffers. From the second step on the step is replayed as a CUDA graph
+  // (one graph launch instead of 3 (2 n_iter + 3) kernel launches for PCG):
+  // the single-instance solves are bound by launch gaps, not by the kernels.
+  for (int k = 0; k < 3; ++k) st[k].Sout = !apos ? Sig : ((k % 2 == 0) ? c.ws.dbl("fwd:sA", NG) : c.ws.dbl("fwd:sB", NG));
+  auto step = [&]() {
+    step_forward(c, P, o, st, Sig, q, st[0].invr, xa, xb, db);
+    if (apos) cuda_check(cudaMemcpyAsync(Sig, st[2].Sout, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Sigma copy");
+  };
+  StreamGraph graph;
+  const bool use_graph = c.use_graphs && !c.prof.on;
   for (int s = 0; s < n_steps; ++s) {
-    for (int k = 0; k < 3; ++k) st[k].Sout = !apos ? Sig : ((k % 2 == 0) ? c.ws.dbl("fwd:sA", NG) : c.ws.dbl("fwd:sB", NG));
-    step_forward(c, P, o, st, sig_cur, q, st[0].invr, xa, xb, db);
-    if (apos) {
-      cuda_check(cudaMemcpyAsync(Sig, st[2].Sout, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Sigma copy");
-      sig_cur = Sig;
-    }
+    if (use_graph && s > 0) graph.run(c, step);
+    else step();
   }
   check_status(c);
 }

@@ -73,6 +73,7 @@ struct Ctx {
   int plan_groups = 0, plan_group_size = 0, plan_seg = 0, plan_nseg = 0;
   int cluster1d = 0;            // 1D: CTAs per instance (0 = chosen per launch)
   int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
+  bool use_graphs = true;       // replay repeated forward steps as CUDA graphs
   Profiler prof;
 };
 

@@ -317,3 +317,28 @@ def test_pcg_sums_fused_and_separate_agree_bitwise(igr, oracle):
     assert one[0] == J[0] and one[5] == dg[0] and one[6] == da[0]
     for v in range(4):
         assert np.array_equal(flat(one[1 + v]), dq[0][v])
+
+
+@pytest.mark.parametrize("solver", ["pcg", "chebyshev"])
+def test_forward_graph_replay_equals_eager_launches(igr, oracle, solver):
+    """From the second step on the forward replays each RK step as a CUDA
+    graph; launching every kernel from the host gives bitwise the same state
+    and Sigma, and the launch count is the same."""
+    from igr_sensitivities_gb300._lib import default_context
+    g = 1.4
+    basis, mesh, _ = setup(igr, oracle, 3, 8, 8)
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 1), width=0.1)
+    dt = W.cfl_dt_2d(mesh, 3, q0, g, 0.1)
+    ctx = default_context()
+    outs, counts = [], []
+    try:
+        for on in (False, True):
+            ctx.set_graphs(on)
+            outs.append(igr.run_forward(*q0, dt, 6 * dt * 0.999, basis, mesh, g, 3.0 * (1 / 8) ** 2, n_iter=7,
+                                        solver=solver))
+            counts.append(ctx.last_launch_count())
+    finally:
+        ctx.set_graphs(True)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(flat(a), flat(b))
+    assert counts[0] == counts[1] > 0
