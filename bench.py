@@ -552,6 +552,31 @@ def secondary(args):
                     clocks=clk,
                     cpu_baseline={"value": 1.0 / tc, "unit": "gradients/s", "cores": 1, "kind": "port",
                                   "sample": "1 instance, %d of %d steps, single thread, scaled" % (ns, nst)})
+    elif args.workload == "batch_sweep":
+        # the headline workload at several batch sizes (B = 1 is the plain path): gradients/s per B
+        sizes = [1, 8, 32, 64]
+        by_batch = {}
+        clk = ClockSampler(0)
+        clk.start()
+        for B in sizes:
+            basis, mesh, q0h, gam, alp, dts, prm = make_batch(igr, W, B)
+            q0d = torch.from_numpy(q0h).to(torch.device("cuda", 0))
+            run = lambda: igr.adjoint_batch(q0d, gam, alp, dts, N_STEPS, basis, mesh, n_iter=N_ITER, solver=SOLVER,
+                                            objective=OBJ, obj_params=prm, ctx=ctx, device_arrays=True)
+            run()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            run()
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+            pg = ctx.last_adjoint_plan()
+            by_batch[B] = {"gradients_per_s": B / t, "s_per_call": t, "tape_plan": pg}
+            del q0d
+        clk_v = clk.stop()
+        line.update(metric=METRIC + " (batch sweep)", value=by_batch[32]["gradients_per_s"], unit="gradients/s",
+                    ms_per_step=by_batch[32]["s_per_call"] * 1e3, gpu_launches=ctx.last_launch_count(),
+                    config=dict(config_dict(32), batch_sizes=sizes), by_batch=by_batch, clocks=clk_v,
+                    batched_over_plain={B: by_batch[B]["gradients_per_s"] / by_batch[1]["gradients_per_s"] for B in sizes})
     else:
         raise SystemExit("unknown workload " + args.workload)
     print(json.dumps(line))
@@ -568,7 +593,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--n-steps", type=int, default=N_STEPS, help="RK steps per gradient (200 = the workload)")
     ap.add_argument("--workload", default="adjoint2d",
-                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | pde_batch1d | otd_sedov | batch2d_c5")
+                    help="adjoint2d (the headline) | adjoint2d_64 | forward2d_pcg | forward1d | batch1d | pde_adjoint2d | "
+                         "pde_batch1d | otd_sedov | batch2d_c5 | batch_sweep")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: batch 2, 4 steps, one call, no timing output")
     args = ap.parse_args()

@@ -36,6 +36,7 @@ def lib():
             _lib.igr_ctx_destroy.argtypes = [C.c_void_p]
             _lib.igr_set_tape_budget.argtypes = [C.c_void_p, C.c_size_t]
             _lib.igr_last_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+            _lib.igr_set_autotune.argtypes = [C.c_void_p, C.c_int, C.c_char_p]
         return _lib
 
 
@@ -75,6 +76,18 @@ class Context:
     def set_graphs(self, on):
         """2D forward solves: replay repeated RK steps as CUDA graphs (default on)."""
         check(self, lib().igr_set_graphs(self.handle, C.c_int(1 if on else 0)))
+
+    def set_autotune(self, on, cache_path=None):
+        """Measure result-invariant launch choices (1D CTAs per instance, 2D fused
+        or separate PCG inner products) on the first call of each batch shape and
+        keep the fastest; cache_path keeps them in a file across processes."""
+        path = None if cache_path is None else os.fsencode(cache_path)
+        check(self, lib().igr_set_autotune(self.handle, C.c_int(1 if on else 0), path))
+
+    def autotune_count(self):
+        n = C.c_int(0)
+        check(self, lib().igr_autotune_count(self.handle, C.byref(n)))
+        return n.value
 
     def last_cluster_size_1d(self):
         v = C.c_int(0)

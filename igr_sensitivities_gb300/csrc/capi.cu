@@ -165,6 +165,20 @@ int igr_set_graphs(igr_ctx* ctx, int on) {
   return IGR_OK;
 }
 
+int igr_set_autotune(igr_ctx* ctx, int on, const char* cache_path) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.tune.on = on != 0;
+  ctx->c.tune.path = cache_path ? cache_path : "";
+  ctx->c.tune.load();  // a missing or unreadable file is an empty cache
+  return IGR_OK;
+}
+
+int igr_autotune_count(const igr_ctx* ctx, int* n) {
+  if (!ctx || !n) return IGR_EINVAL;
+  *n = (int)ctx->c.tune.table.size();
+  return IGR_OK;
+}
+
 int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out) {
   if (!ctx || !out) return IGR_EINVAL;
   *out = ctx->c.last_cluster1d;

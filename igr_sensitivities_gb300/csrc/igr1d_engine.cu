@@ -1,6 +1,7 @@
 // 1D host engine: batch plans and drivers of the per-instance persistent
 // kernels (igr1d_kernels.cuh).
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <functional>
@@ -80,9 +81,9 @@ long long forward1d_scratch_fields(const Inst1DDesc&, int) { return E1_FIELDS + 
 // over a cluster of up to 16 SMs (at least 16 elements per CTA); below T1
 // elements the cluster barrier costs more than it saves (measured on GB300:
 // N_e = 64 and 128 run 10-20% faster on one CTA), and batches that fill the
-// GPU use one CTA per instance. A context setting overrides the choice.
-static int cluster_size(Ctx& c, const Plan1D& P) {
-  if (c.cluster1d > 0) return c.cluster1d;
+// GPU use one CTA per instance. A context setting overrides the choice, and
+// autotuning replaces it with a measurement (cluster_size).
+static int cluster_heuristic(Ctx& c, const Plan1D& P) {
   int sms = 0;
   cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device), "attr");
   const long long ni = (long long)P.inst.size();
@@ -110,6 +111,99 @@ static void launch_1d(Ctx& c, Args& a, int n_inst, F launch, const char* what) {
   }
 }
 
+// CTAs per instance for this launch: the context setting, else (with
+// autotuning on and the state q at hand) the fastest candidate measured for
+// this batch shape, else cluster_heuristic. The measurement advances a copy
+// of q by up to 3 steps of the forward kernel for every candidate (powers of
+// two up to 16 that keep at least 16 elements per CTA), after one untimed
+// run, timed with CUDA events; results do not depend on the choice.
+static int cluster_size(Ctx& c, const Plan1D& P, const Solve2DOpts& o, const double* q) {
+  if (c.cluster1d > 0) return c.cluster1d;
+  const int h = cluster_heuristic(c, P);
+  if (!c.tune.on || !q || P.inst.empty()) return h;
+  int ne_min = 1 << 30, ne_max = 0;
+  long long ne_sum = 0;
+  for (auto& I : P.inst) {
+    ne_min = std::min(ne_min, I.ne); ne_max = std::max(ne_max, I.ne); ne_sum += I.ne;
+    if (!(I.dt > 0)) return h;
+  }
+  char key[160];
+  std::snprintf(key, sizeof(key), "1d.cluster np=%d inst=%d ne_min=%d ne_max=%d ne_sum=%lld solver=%d iters=%d", P.np,
+                (int)P.inst.size(), ne_min, ne_max, ne_sum, o.solver, o.n_iter);
+  int v = 0;
+  if (c.tune.get(key, &v)) return v;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cuda_check(cudaStreamIsCapturing(c.stream, &cap), "stream capture status");
+  if (cap != cudaStreamCaptureStatusNone) return h;
+
+  std::vector<Inst1DDesc> d(P.inst.size());
+  for (size_t i = 0; i < P.inst.size(); ++i) {
+    const Inst1D& I = P.inst[i];
+    d[i].ne = I.ne; d[i].L = I.L; d[i].gamma = I.gamma; d[i].alpha = I.alpha; d[i].dt = I.dt;
+    d[i].n_steps = std::min(std::max(I.n_steps, 1), 3);
+  }
+  const long long nodes_saved = c.cur_nodes, launches_saved = c.launches;
+  const int last_saved = c.last_cluster1d;
+  Plan1D Q;
+  double *qq = nullptr, *sg = nullptr, *scr = nullptr;
+  int* status = nullptr;
+  try {  // no room for the probe's copies: keep the heuristic's choice, untuned
+    Q = make_plan1d(c, P.B, d, forward1d_scratch_fields, "tune1");
+    qq = c.ws.dbl("tune1:q", (size_t)3 * Q.NG);
+    sg = c.ws.dbl("tune1:sig", (size_t)Q.NG);
+    scr = c.ws.dbl("tune1:scr", (size_t)std::max<long long>(Q.scratch, 1));
+    status = static_cast<int*>(c.ws.get("tune1:status", sizeof(int)));
+  } catch (const Error&) {
+    (void)cudaGetLastError();
+    c.cur_nodes = nodes_saved;
+    c.ws.release("tune1:q"); c.ws.release("tune1:sig"); c.ws.release("tune1:scr");
+    return h;
+  }
+  c.cur_nodes = nodes_saved;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cuda_check(cudaEventCreate(&e0), "tune event");
+  cuda_check(cudaEventCreate(&e1), "tune event");
+  int best = h;
+  float best_ms = 0.f;
+  try {
+    std::vector<int> cand{h};
+    for (int cs = 1; cs <= 16; cs *= 2)
+      if (cs != h && ne_min / cs >= 16) cand.push_back(cs);
+    for (size_t k = 0; k <= cand.size(); ++k) {  // k = 0: untimed run with the heuristic's choice
+      const int cs = cand[k == 0 ? 0 : k - 1];
+      cuda_check(cudaMemcpyAsync(qq, q, sizeof(double) * 3 * Q.NG, cudaMemcpyDeviceToDevice, c.stream), "tune copy");
+      cuda_check(cudaMemsetAsync(sg, 0, sizeof(double) * Q.NG, c.stream), "tune sigma");
+      Fwd1DArgs a;
+      std::memset(&a, 0, sizeof(a));
+      a.inst = Q.d_inst; a.order = Q.d_order; a.B = Q.B;
+      a.q = qq; a.sig = sg; a.scr = scr;
+      a.solver = o.solver; a.n_iter = o.n_iter; a.final_solve = 0;
+      a.status = status;
+      a.cs = cs;
+      cuda_check(cudaEventRecord(e0, c.stream), "tune event record");
+      NP1_DISPATCH(Q.np, launch_1d(c, a, (int)Q.inst.size(),
+                                   [&](const Fwd1DArgs& x, int n) { return launch_k1_forward<NPV>(x, n, c.stream); },
+                                   "k1_forward launch (autotune)"));
+      cuda_check(cudaEventRecord(e1, c.stream), "tune event record");
+      cuda_check(cudaEventSynchronize(e1), "tune event sync");
+      float ms = 0.f;
+      cuda_check(cudaEventElapsedTime(&ms, e0, e1), "tune event time");
+      if (k > 0 && a.cs == cs && (k == 1 || ms < best_ms)) { best = cs; best_ms = ms; }
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c.ws.release("tune1:q"); c.ws.release("tune1:sig"); c.ws.release("tune1:scr");  // frees after the stream drains
+  c.launches = launches_saved;
+  c.last_cluster1d = last_saved;
+  c.tune.put(key, best);
+  return best;
+}
+
 void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpts& o, bool final_solve) {
   double* scr = c.ws.dbl("f1:scr", (size_t)std::max<long long>(P.scratch, 1));
   cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
@@ -119,7 +213,7 @@ void forward1d(Ctx& c, const Plan1D& P, double* q, double* sig, const Solve2DOpt
   a.q = q; a.sig = sig; a.scr = scr;
   a.solver = o.solver; a.n_iter = o.n_iter; a.final_solve = final_solve ? 1 : 0;
   a.status = c.d_status;
-  a.cs = cluster_size(c, P);
+  a.cs = cluster_size(c, P, o, q);
   NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
                                [&](const Fwd1DArgs& x, int n) { return launch_k1_forward<NPV>(x, n, c.stream); },
                                "k1_forward launch"));
@@ -167,7 +261,7 @@ void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Sol
   c.plan_seg = seg;
   c.plan_groups = 1;
   c.plan_group_size = ni;
-  a.cs = cluster_size(c, P);
+  a.cs = cluster_size(c, P, o, q0);
   NP1_DISPATCH(P.np, launch_1d(c, a, ni,
                                [&](const Adj1DArgs& x, int n) { return launch_k1_adjoint<NPV>(x, n, c.stream); },
                                "k1_adjoint launch"));
@@ -201,7 +295,7 @@ void tangent1d(Ctx& c, const Plan1D& P, double* q, double* s, double* sig, doubl
   a.q = q; a.s = s; a.sig = sig; a.vs = vs; a.scr = scr;
   a.solver = o.solver; a.n_iter = o.n_iter; a.form = form; a.s_gamma = s_gamma;
   a.status = c.d_status;
-  a.cs = cluster_size(c, P);
+  a.cs = cluster_size(c, P, o, q);
   NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
                                [&](const Tan1DArgs& x, int n) { return launch_k1_tangent<NPV>(x, n, c.stream); },
                                "k1_tangent launch"));
@@ -248,7 +342,7 @@ void pde_adjoint1d(Ctx& c, const Plan1D& P, int mode, const double* q0, const do
   c.plan_seg = seg;
   c.plan_groups = 1;
   c.plan_group_size = (int)P.inst.size();
-  a.cs = cluster_size(c, P);
+  a.cs = cluster_size(c, P, o, mode <= 1 ? q0 : nullptr);
   NP1_DISPATCH(P.np, launch_1d(c, a, (int)P.inst.size(),
                                [&](const Pde1DArgs& x, int n) { return launch_k1_pde_adjoint<NPV>(x, n, c.stream); },
                                "k1_pde_adjoint launch"));

@@ -1,6 +1,7 @@
 // 2D host engine: plans, forward / adjoint drivers and the small pointwise and
 // reduction kernels that do not depend on the polynomial degree.
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 
@@ -30,6 +31,12 @@ void* Workspace::get(const std::string& name, size_t bytes) {
     b.n = bytes;
   }
   return b.p;
+}
+void Workspace::release(const std::string& name) {
+  auto it = bufs_.find(name);
+  if (it == bufs_.end()) return;
+  if (it->second.p) cudaFree(it->second.p);
+  bufs_.erase(it);
 }
 void Workspace::release_all() {
   for (auto& kv : bufs_) if (kv.second.p) cudaFree(kv.second.p);
@@ -386,13 +393,73 @@ static bool all_alpha_pos(const Plan2D& P) {
 constexpr int FUSED_SUM_MAX_TILES = 4096;
 
 // Per-instance completion counters of the fused inner products, zeroed
-// before each solve (the kernels leave them at 0); null above
-// FUSED_SUM_MAX_TILES.
+// before each solve (the kernels leave them at 0).
 static int* inst_counters(Ctx& c, const Plan2D& P) {
-  if (P.ntiles() > FUSED_SUM_MAX_TILES) return nullptr;
   int* cnt = static_cast<int*>(c.ws.get("pcg:cnt", sizeof(int) * P.inst.size()));
   cuda_check(cudaMemsetAsync(cnt, 0, sizeof(int) * P.inst.size(), c.stream), "zero instance counters");
   return cnt;
+}
+
+// Whether a solve on this plan completes its inner products inside the
+// kernels. Without autotuning: grids of at most FUSED_SUM_MAX_TILES tiles.
+// With it, the first solve of a new shape runs fused and the second
+// separate, each timed with CUDA events (both give the same bits), and the
+// faster is remembered. No trial runs while the stream is being captured.
+struct SumChoice {
+  bool fused = false, trial = false;
+  std::string key;
+};
+static SumChoice sum_choice(Ctx& c, const Plan2D& P, bool allow_trial) {
+  SumChoice ch;
+  ch.fused = P.ntiles() <= FUSED_SUM_MAX_TILES;
+  if (!c.tune.on) return ch;
+  char key[96];
+  std::snprintf(key, sizeof(key), "2d.pcg_sums np=%d tiles=%d inst=%d", P.np, P.ntiles(), (int)P.inst.size());
+  int v = 0;
+  if (c.tune.get(key, &v)) {
+    ch.fused = v != 0;
+    return ch;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cuda_check(cudaStreamIsCapturing(c.stream, &cap), "stream capture status");
+  if (!allow_trial || cap != cudaStreamCaptureStatusNone) return ch;
+  ch.trial = true;
+  ch.key = key;
+  ch.fused = c.tune.trial_ms.count(ch.key) == 0;
+  return ch;
+}
+
+// Times one trial solve (CUDA events on the engine's stream).
+struct TrialTimer {
+  Ctx& c;
+  cudaEvent_t a = nullptr, b = nullptr;
+  explicit TrialTimer(Ctx& cc, bool on) : c(cc) {
+    if (!on) return;
+    cuda_check(cudaEventCreate(&a), "trial event");
+    cuda_check(cudaEventCreate(&b), "trial event");
+    cuda_check(cudaEventRecord(a, c.stream), "trial event record");
+  }
+  ~TrialTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  double stop() {
+    float ms = 0.f;
+    cuda_check(cudaEventRecord(b, c.stream), "trial event record");
+    cuda_check(cudaEventSynchronize(b), "trial event sync");
+    cuda_check(cudaEventElapsedTime(&ms, a, b), "trial event time");
+    return ms;
+  }
+};
+
+static void sum_trial_done(Ctx& c, const SumChoice& ch, double ms) {
+  if (ch.fused) {
+    c.tune.trial_ms[ch.key] = ms;
+    return;
+  }
+  const double fused_ms = c.tune.trial_ms[ch.key];
+  c.tune.trial_ms.erase(ch.key);
+  c.tune.put(ch.key, fused_ms <= ms ? 1 : 0);
 }
 
 // InstSum in mode 0: out[inst] = sum, and with quot
@@ -425,7 +492,9 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
   double* part = c.ws.dbl("red:part", nb);
-  int* cnt = inst_counters(c, P);
+  const SumChoice ch = sum_choice(c, P, true);
+  int* cnt = ch.fused ? inst_counters(c, P) : nullptr;
+  TrialTimer timer(c, ch.trial);
   double* scal = taped ? st.scal : c.ws.dbl("pcg:scal", (size_t)pcg_scal_count(n, ni));
   double* apbuf = taped ? nullptr : c.ws.dbl("pcg:ap", NG);
   auto RZ = [&](int k) { return scal + (long long)k * ni; };
@@ -484,6 +553,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
     }
     inst_sum_after(c, P, part, true, u.isum);
   }
+  if (ch.trial) sum_trial_done(c, ch, timer.stop());
 }
 
 // Operator coefficients, IGR source b and diag(A) of one stage (the setup
@@ -1014,7 +1084,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
     const double* PAP = sb.scal + (long long)(n + 1) * ni;
     const double* AL = sb.scal + (long long)(2 * n + 1) * ni;
     const double* BT = sb.scal + (long long)(3 * n + 1) * ni;
-    int* cnt = inst_counters(c, P);
+    int* cnt = sum_choice(c, P, false).fused ? inst_counters(c, P) : nullptr;
     for (int it = n - 1; it >= 0; --it) {
       PcgRevArgs g;
       g.tiles = P.d_tiles; g.groups = P.d_groups; g.inst = P.d_inst; g.np = P.np; g.tx = tx; g.ty = ty;

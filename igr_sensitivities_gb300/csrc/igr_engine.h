@@ -30,6 +30,7 @@ class Workspace {
   void* get(const std::string& name, size_t bytes);
   double* dbl(const std::string& name, size_t n) { return static_cast<double*>(get(name, n * sizeof(double))); }
   void release_all();
+  void release(const std::string& name);  // frees one buffer (cudaFree: waits for the device)
   size_t bytes() const;
   size_t held(const std::string& name) const;  // current capacity of one named buffer (0 if absent)
 
@@ -59,6 +60,23 @@ struct Profiler {
   ~Profiler();
 };
 
+// Launch choices that do not change results, measured on this device and
+// remembered per problem shape: the 1D CTAs per instance and whether the 2D
+// PCG inner products complete inside their kernels. Every candidate gives
+// bitwise the same results, so tuning never changes an answer. With a cache
+// path the table is read when tuning is switched on and written after every
+// new entry (text: one "key<TAB>value" line per entry).
+struct Autotune {
+  bool on = false;
+  std::string path;
+  std::map<std::string, int> table;
+  std::map<std::string, double> trial_ms;  // 2D sums: time of the fused trial, per key
+  void load();
+  void save() const;
+  bool get(const std::string& key, int* v) const;
+  void put(const std::string& key, int v);
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -74,6 +92,7 @@ struct Ctx {
   int cluster1d = 0;            // 1D: CTAs per instance (0 = chosen per launch)
   int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
   bool use_graphs = true;       // replay repeated forward steps as CUDA graphs
+  Autotune tune;
   Profiler prof;
 };
 

@@ -95,6 +95,16 @@ int igr_set_cluster_size_1d(igr_ctx* ctx, int cs);
  * (1, default) or launch every kernel from the host (0). Results are bitwise
  * the same. No reference counterpart. */
 int igr_set_graphs(igr_ctx* ctx, int on);
+/* Autotuning of launch choices that leave results bitwise unchanged: the 1D
+ * CTAs per instance (when not forced by igr_set_cluster_size_1d) and whether
+ * the 2D PCG inner products complete inside their kernels. on = 1 measures
+ * the candidates on the first call of each batch shape (CUDA events) and
+ * keeps the fastest; cache_path (NULL or "" = memory only) is read now and
+ * rewritten after every new entry, so later processes skip the measurement.
+ * No reference counterpart. */
+int igr_set_autotune(igr_ctx* ctx, int on, const char* cache_path);
+/* Entries in the context's autotune table. */
+int igr_autotune_count(const igr_ctx* ctx, int* n);
 /* CTAs per instance used by the last 1D launch on this context. */
 int igr_last_cluster_size_1d(const igr_ctx* ctx, int* out);
 /* Kernels launched by the last call on this context. */
