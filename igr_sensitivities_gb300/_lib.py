@@ -74,7 +74,7 @@ class Context:
         check(self, lib().igr_set_cluster_size_1d(self.handle, C.c_int(int(cs))))
 
     def set_graphs(self, on):
-        """2D forward solves: replay repeated RK steps as CUDA graphs (default on)."""
+        """2D forward and tangent solves: replay repeated RK steps as CUDA graphs (default on)."""
         check(self, lib().igr_set_graphs(self.handle, C.c_int(1 if on else 0)))
 
     def set_autotune(self, on, cache_path=None):

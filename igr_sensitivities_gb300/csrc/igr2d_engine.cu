@@ -770,7 +770,7 @@ void sensitivity2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, dou
   // Sigma and varsigma chains: warm start in *_cur, solution into the other buffer
   double* sig_cur = Sig; double* sig_nxt = sigAlt;
   double* vs_cur = vs; double* vs_nxt = vsAlt;
-  for (int step = 0; step < n_steps; ++step) {
+  auto step_body = [&]() {
     for (int k = 0; k < 3; ++k) {
       if (apos) {
         st[k].Sout = sig_nxt;
@@ -793,6 +793,33 @@ void sensitivity2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, dou
       h.status = c.d_status;
       LaunchScope ls(c, KID_TAN);
       NP_DISPATCH(P.np, launch_k2_sens_hyp_rk<NPV>(h, P.ntiles(), c.stream));
+    }
+  };
+  // The host-side effect of one step on the Sigma / varsigma chains.
+  auto step_pointers = [&]() {
+    for (int k = 0; k < 3; ++k) {
+      if (apos) {
+        st[k].Sout = sig_nxt;
+        std::swap(sig_cur, sig_nxt);
+        std::swap(vs_cur, vs_nxt);
+      } else {
+        st[k].Sout = sig_cur;
+      }
+    }
+  };
+  // Three swaps per step: the buffers repeat every second step, so steps of
+  // one parity replay one CUDA graph (captured at steps 2 and 3, after the
+  // first steps have allocated every buffer).
+  StreamGraph graphs[2];
+  const bool use_graph = c.use_graphs && !c.prof.on;
+  for (int step = 0; step < n_steps; ++step) {
+    StreamGraph& g = graphs[step % 2];
+    if (!use_graph || step < 2) {
+      step_body();
+    } else {
+      const bool replay = g.exec != nullptr;
+      g.run(c, step_body);  // runs step_body only while capturing
+      if (replay) step_pointers();
     }
   }
   if (apos) {  // sensitivity.jl:404-409: Sigma and varsigma at the final state

@@ -91,7 +91,7 @@ int igr_set_tape_budget(igr_ctx* ctx, size_t bytes);
  * to 16 SMs); 1, 2, 4, 8 or 16 force it. Results do not depend on it.
  * No reference counterpart. */
 int igr_set_cluster_size_1d(igr_ctx* ctx, int cs);
-/* 2D forward solves: replay the repeated RK steps as one CUDA graph per step
+/* 2D forward and tangent solves: replay the repeated RK steps as CUDA graphs
  * (1, default) or launch every kernel from the host (0). Results are bitwise
  * the same. No reference counterpart. */
 int igr_set_graphs(igr_ctx* ctx, int on);

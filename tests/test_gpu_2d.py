@@ -342,3 +342,27 @@ def test_forward_graph_replay_equals_eager_launches(igr, oracle, solver):
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(flat(a), flat(b))
     assert counts[0] == counts[1] > 0
+
+
+def test_tangent_graph_replay_equals_eager_launches(igr, oracle):
+    """run_sensitivity replays steps of each parity as a CUDA graph from the
+    third step on; eager launches give bitwise the same ten fields."""
+    from igr_sensitivities_gb300._lib import default_context
+    g = 1.4
+    basis, mesh, _ = setup(igr, oracle, 3, 8, 8)
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 2), width=0.1)
+    rng = np.random.default_rng(11)
+    s0 = [np.asfortranarray(0.1 * rng.standard_normal(mesh.x.shape)) for _ in range(4)]
+    dt = W.cfl_dt_2d(mesh, 3, q0, g, 0.1)
+    ctx = default_context()
+    outs = []
+    try:
+        for on in (False, True):
+            ctx.set_graphs(on)
+            outs.append(igr.run_sensitivity(*q0, *s0, dt, 7 * dt * 0.999, basis, mesh, g, 3.0 * (1 / 8) ** 2, n_iter=6,
+                                            solver="pcg"))
+    finally:
+        ctx.set_graphs(True)
+    assert len(outs[0]) == 10
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(flat(a), flat(b))
