@@ -46,7 +46,12 @@ bool Autotune::get(const std::string& key, int* v) const {
 
 void Autotune::put(const std::string& key, int v) {
   table[key] = v;
-  save();
+  try {
+    save();
+  } catch (const Error&) {
+    // the cache file became unwritable after igr_set_autotune checked it:
+    // keep the entry in memory and let the solve finish
+  }
 }
 
 }  // namespace igrgpu

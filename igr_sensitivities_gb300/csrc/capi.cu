@@ -167,9 +167,17 @@ int igr_set_graphs(igr_ctx* ctx, int on) {
 
 int igr_set_autotune(igr_ctx* ctx, int on, const char* cache_path) {
   if (!ctx) return IGR_EINVAL;
+  ctx->c.err.clear();
   ctx->c.tune.on = on != 0;
   ctx->c.tune.path = cache_path ? cache_path : "";
-  ctx->c.tune.load();  // a missing or unreadable file is an empty cache
+  ctx->c.tune.load();  // a missing file is an empty cache
+  try {
+    ctx->c.tune.save();  // the path must be writable: fail here, not inside a solve
+  } catch (const Error& e) {
+    ctx->c.err = e.what();
+    ctx->c.tune.path.clear();
+    return e.code;
+  }
   return IGR_OK;
 }
 

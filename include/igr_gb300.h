@@ -100,7 +100,8 @@ int igr_set_graphs(igr_ctx* ctx, int on);
  * the 2D PCG inner products complete inside their kernels. on = 1 measures
  * the candidates on the first call of each batch shape (CUDA events) and
  * keeps the fastest; cache_path (NULL or "" = memory only) is read now and
- * rewritten after every new entry, so later processes skip the measurement.
+ * rewritten after every new entry, so later processes skip the measurement;
+ * IGR_EINVAL if it cannot be written (tuning then stays in memory).
  * No reference counterpart. */
 int igr_set_autotune(igr_ctx* ctx, int on, const char* cache_path);
 /* Entries in the context's autotune table. */

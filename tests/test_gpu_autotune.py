@@ -74,3 +74,13 @@ def test_2d_tuned_pcg_sums_keep_results(igr, oracle, solver, tmp_path):
         for a, b in zip(plain, res):
             assert np.array_equal(flat(a), flat(b))
     ctx.set_autotune(False)
+
+
+def test_unwritable_cache_path_is_rejected_up_front(igr, tmp_path):
+    from igr_sensitivities_gb300 import Context
+    from igr_sensitivities_gb300._lib import IGRError
+    ctx = Context(0)
+    with pytest.raises(IGRError) as ei:
+        ctx.set_autotune(True, str(tmp_path / "no_such_dir" / "tune.txt"))
+    assert "IGR_EINVAL" in str(ei.value) and "autotune cache" in str(ei.value)
+    assert ctx.autotune_count() == 0
