@@ -151,11 +151,13 @@ __device__ void d1_setup(const View1<NP>& v, const BasisDev& B, const double* mu
 //   F = hw (ck_L d_L + ck_R d_R) + cp (x_L - x_R),  hw = -1/(2 w_0)
 //   y_L-side += F, y_R-side -= F, symmetry term into the stiffness transpose.
 // ldx(n) supplies x at node n; epi(e, x[], y[]) consumes the element's result.
-// Does not synchronise (the epilogue decides what it writes).
+// Does not synchronise (the epilogue decides what it writes). d1_apply picks
+// one thread per element (d1_apply_elems) or one lane per node
+// (d1_apply_nodes); both give the same bits.
 // ---------------------------------------------------------------------------
 template <int NP, class LDX, class EPI>
-__device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm, const double* ck,
-                                         const double* cpR, EPI epi) {
+__device__ __forceinline__ void d1_apply_elems(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm,
+                                               const double* ck, const double* cpR, EPI epi) {
   constexpr int L = NP - 1;
   const int ne = v.I.ne;
   const double hw = B.hw;
@@ -186,6 +188,106 @@ __device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, 
       y[k] = dot_col<NP>(B, k, sx, fma(cm[base + k], x[k], (k == 0) ? -Fl : ((k == L) ? Fr : 0.0)));
     epi(e, x, y);
   }
+}
+
+// Lanes per element in d1_apply_nodes: NP rounded up to a power of two.
+template <int NP>
+__host__ __device__ constexpr int group1() { return NP <= 2 ? 2 : (NP <= 4 ? 4 : 8); }
+
+// d1_apply with one lane per node, for CTAs holding at most T1 / (2 group1)
+// elements (a small instance spread over a cluster). GB300's FP64 unit
+// issues one warp instruction per ~64 cycles per SM sub-partition whatever
+// the number of active lanes (measured with a DFMA micro-probe: 64.1 cycles
+// per warp instruction for 1 to 32 active lanes), so one thread per element
+// left 3/4 of the lanes of every FP64 instruction idle there. A group of
+// group1<NP>() lanes takes one element and lane i its node i: every lane
+// forms the derivative at its node, the lanes of nodes 0 and L the left and
+// right face terms (interior lanes run the same instructions on the right
+// face and discard them), each lane its stiffness-transpose input; the group
+// exchanges those by shuffles, lane i forms y_i, and the group's first lane
+// runs the element epilogue. Every output is the expression of
+// d1_apply_elems evaluated in the same order, so the results are bitwise
+// equal; operands are chosen by register selects so that the warp runs one
+// instruction stream.
+template <int NP, class LDX, class EPI>
+__device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm,
+                                               const double* ck, const double* cpR, EPI epi) {
+  constexpr int L = NP - 1, G = group1<NP>();
+  const int ne = v.I.ne;
+  const double hw = B.hw;
+  const int li = threadIdx.x % G;
+  const int ii = li < NP ? li : L;  // lanes past the element's nodes shadow node L (results unused)
+  const bool interior = ii > 0 && ii < L;
+  const bool left = ii == 0;        // the face this lane evaluates: left of node 0, else right of node L
+  const bool face = !interior;
+  double Dr[NP], Dc[NP];            // D[ii][k] and D[k][ii]
+#pragma unroll
+  for (int k = 0; k < NP; ++k) { Dr[k] = B.D[0][k]; Dc[k] = B.D[k][0]; }
+#pragma unroll
+  for (int r = 1; r < NP; ++r)
+    if (ii == r) {
+#pragma unroll
+      for (int k = 0; k < NP; ++k) { Dr[k] = B.D[r][k]; Dc[k] = B.D[k][r]; }
+    }
+  for (int eb = v.e0; eb < v.e1; eb += T1 / G) {
+    if (eb + (int)(threadIdx.x & ~31u) / G >= v.e1) continue;  // a warp without elements (warp-uniform)
+    const int e = eb + threadIdx.x / G;
+    const bool live = e < v.e1;
+    const int ec = live ? e : v.e0;  // groups past the range shadow a live element; they store nothing
+    const int base = ec * NP;
+    double x[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) x[k] = ldx(base + k);
+    double xo = x[0];
+#pragma unroll
+    for (int r = 1; r < NP; ++r) xo = (ii == r) ? x[r] : xo;
+    // derivative at the lane's node: dot_row<NP>(B, ii, x)
+    double g = Dr[0] * x[0];
+#pragma unroll
+    for (int k = 1; k < NP; ++k) {
+      const double t = fma(Dr[k], x[k], g);
+      g = (interior && k == ii) ? g : t;
+    }
+    // the lane's face (d1_apply_elems: Fl for node 0, Fr for node L)
+    const int eL = wrap_left(ec, ne), eR = wrap_right(ec, ne);
+    const int pe = left ? eL : eR;
+    double xp[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) xp[k] = ldx(pe * NP + k);
+    const double gp = dot_end<NP>(B, left, xp);
+    const double kco = ck[base + ii];
+    const double ckp = ck[left ? eL * NP + L : eR * NP];
+    const double cpf = cpR[left ? eL : ec];
+    const double jmp = (left ? xp[L] : x[L]) - (left ? x[0] : xp[0]);
+    const double inner = fma(left ? ckp : kco, left ? gp : g, (left ? kco : ckp) * (left ? g : gp));
+    const double F = fma(cpf, jmp, hw * inner);
+    const double sxi = kco * (face ? fma(hw, jmp, g) : g);
+    double sx[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) sx[k] = __shfl_sync(0xffffffffu, sxi, k, G);
+    // y at the lane's node: dot_col<NP>(B, ii, sx, fma(cm, x_ii, -Fl | Fr | 0))
+    double y = fma(cm[base + ii], xo, left ? -F : (ii == L ? F : 0.0));
+#pragma unroll
+    for (int r = 0; r < NP; ++r) {
+      const double t = fma(Dc[r], sx[r], y);
+      y = (interior && r == ii) ? y : t;
+    }
+    double yv[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) yv[k] = __shfl_sync(0xffffffffu, y, k, G);
+    if (live && li == 0) epi(e, x, yv);
+  }
+}
+
+template <int NP, class LDX, class EPI>
+__device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm, const double* ck,
+                                         const double* cpR, EPI epi) {
+  // node form for CTAs filling at most half their threads with nodes: there the
+  // element form leaves lanes idle; a CTA of a batch with more elements is
+  // already bound by FP64 throughput, where both forms issue the same number
+  // of warp instructions and the element form needs no shuffles
+  if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2) d1_apply_nodes<NP>(v, B, ldx, cm, ck, cpR, epi);
+  else d1_apply_elems<NP>(v, B, ldx, cm, ck, cpR, epi);
 }
 
 // ---------------------------------------------------------------------------

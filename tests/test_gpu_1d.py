@@ -260,3 +260,27 @@ def test_cluster_size_does_not_change_results(igr, igr1d, oracle, solver):
     ref, _ = oracle.run_forward_1d(G, g, alpha, dt, 6 * dt, 7, solver, [flat(x) for x in q0])
     for x, y in zip(out[16][0][:3], ref):
         assert rel(x, y) <= RTOL_FWD
+
+
+@pytest.mark.parametrize("solver", ["jacobi", "pcg"])
+def test_node_and_element_apply_agree_bitwise(igr, igr1d, oracle, solver):
+    """CTAs with at most 32 elements (P3) apply the operator one lane per
+    node, larger ones one thread per element; the forms give the same bits.
+    N_e = 96 on one or two CTAs runs the element form, on four the node form."""
+    from igr_sensitivities_gb300 import Context
+    g = 1.4
+    basis, mesh, G = setup1(igr, oracle, 3, 96)
+    q0 = W.seeded_pulses_1d(mesh, g, W.seed_for(1, 901), width=0.08)
+    dt = W.cfl_dt_1d(mesh, 3, q0, g, 0.1)
+    alpha = 3.0 * mesh.dx ** 2
+    ctx = Context(0)
+    out = {}
+    for cs in (1, 2, 4):
+        ctx.set_cluster_size_1d(cs)
+        out[cs] = igr1d.run_forward(*q0, dt, 5 * dt, basis, mesh, g, alpha, n_iter=9, solver=solver, ctx=ctx)
+    for cs in (2, 4):
+        for x, y in zip(out[1], out[cs]):
+            assert np.array_equal(x, y)
+    ref, _ = oracle.run_forward_1d(G, g, alpha, dt, 5 * dt, 9, solver, [flat(x) for x in q0])
+    for x, y in zip(out[4][:3], ref):
+        assert rel(x, y) <= RTOL_FWD
