@@ -128,8 +128,8 @@ __device__ void d1_setup(const View1<NP>& v, const BasisDev& B, const double* mu
       ck[base + i] = kk[i];
     }
     const double irLL = ir[eL * NP + L], irR0 = ir[eR * NP];
-    const double cpr = al * eta * I.idx * ((irR0 > r[L]) ? irR0 : r[L]);
-    const double cpl = al * eta * I.idx * ((r[0] > irLL) ? r[0] : irLL);
+    const double cpr = al * eta * I.idx * max_nonneg(irR0, r[L]);
+    const double cpl = al * eta * I.idx * max_nonneg(r[0], irLL);
     cpR[e] = cpr;
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
@@ -477,7 +477,7 @@ __device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* c
       const double pir = ir[m];
       const Node1 o = node1(g, pq[0], pq[2], S[m], pir);
       const double wl = ws1(g, nL, ir[base + L]), wr = ws1(g, o, pir);
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double fs = 0.5 * fma(lam, qq[c][L] - pq[c], f[c][L] + o.f[c]);
@@ -491,7 +491,7 @@ __device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* c
       const double pir = ir[m];
       const Node1 o = node1(g, pq[0], pq[2], S[m], pir);
       const double wl = ws1(g, o, pir), wr = ws1(g, n0, ir[base]);
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double fs = 0.5 * fma(lam, pq[c] - qq[c][0], o.f[c] + f[c][0]);
@@ -514,7 +514,7 @@ __device__ void d1_hyp_rk(const View1<NP>& v, const BasisDev& B, const double* c
         for (int c = 0; c < 3; ++c) qo[c][m] = out[c];
         iro[m] = 1.0 / out[1];
       }
-      bad |= !(out[1] > 0.0) || !isfinite(out[0]) || !isfinite(out[1]) || !isfinite(out[2]);
+      bad |= not_positive_finite(out[1]) || nonfinite_bits(out[0]) || nonfinite_bits(out[2]);
     }
   }
   if (bad) flag_nonfinite(status);

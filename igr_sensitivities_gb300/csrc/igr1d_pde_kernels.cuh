@@ -177,7 +177,7 @@ __device__ void d1_pde_rk(const View1<NP>& v, const BasisDev& B, const double* s
       double pf[3];
       pde1_flux(g, sq[0][m], sq[2][m], sq[3][m], irS[m], pa, pf);
       const double wl = ws[base + L], wr = ws[m];
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double fs = 0.5 * fma(-lam, aa[c][L] - pa[c], f[c][L] + pf[c]);
@@ -191,7 +191,7 @@ __device__ void d1_pde_rk(const View1<NP>& v, const BasisDev& B, const double* s
       double pf[3];
       pde1_flux(g, sq[0][m], sq[2][m], sq[3][m], irS[m], pa, pf);
       const double wl = ws[m], wr = ws[base];
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double fs = 0.5 * fma(-lam, pa[c] - aa[c][0], pf[c] + f[c][0]);

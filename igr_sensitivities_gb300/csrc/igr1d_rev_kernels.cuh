@@ -95,7 +95,7 @@ __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* 
       const Node1 nl = node1(g, q[0][o], q[2][o], S[o], ir[o]);
       const Node1 nr = node1(g, q[0][m], q[2][m], S[m], ir[m]);
       const double wl = ws1(g, nl, ir[o]), wr = ws1(g, nr, ir[m]);
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
       double lamb = 0.0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -103,7 +103,7 @@ __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* 
         qb[c][L] = fma(0.5 * lam, fsb[c], qb[c][L]);
         lamb = fma(0.5 * fsb[c], jq[c], lamb);
       }
-      if (!(wr > wl)) {
+      if (!gt_nonneg(wr, wl)) {
         double t[3] = {0.0, 0.0, 0.0};
         ws1_rev(g, q[0][o], ir[o], q[2][o], lamb, t, gb);
 #pragma unroll
@@ -122,7 +122,7 @@ __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* 
       const Node1 nl = node1(g, q[0][m], q[2][m], S[m], ir[m]);
       const Node1 nr = node1(g, q[0][o], q[2][o], S[o], ir[o]);
       const double wl = ws1(g, nl, ir[m]), wr = ws1(g, nr, ir[o]);
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
       double lamb = 0.0;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -130,7 +130,7 @@ __device__ void d1_hyp_rev(const View1<NP>& v, const BasisDev& B, const double* 
         qb[c][0] = fma(-0.5 * lam, fsb[c], qb[c][0]);
         lamb = fma(0.5 * fsb[c], jq[c], lamb);
       }
-      if (wr > wl) {
+      if (gt_nonneg(wr, wl)) {
         double t[3] = {0.0, 0.0, 0.0};
         ws1_rev(g, q[0][o], ir[o], q[2][o], lamb, t, gb);
 #pragma unroll
@@ -222,15 +222,15 @@ __device__ __forceinline__ void d1_apply_rev(const View1<NP>& v, const BasisDev&
       const double ju = u[L] - ur[0], jw = w[L] - wr[0];
       const double cL = fma(gw[L], ju, gu[L] * jw), cR = fma(gwr, ju, gur * jw);
       z[L] += -al * iJ * 0.5 * cL;
-      if (!(iR > iL)) z[L] += al * eta * I.idx * jw * ju;
-      abl += -iJ * 0.5 * fma(iL, cL, iR * cR) + eta * ((iR > iL) ? iR : iL) * I.idx * jw * ju;
+      if (!gt_nonneg(iR, iL)) z[L] += al * eta * I.idx * jw * ju;
+      abl += -iJ * 0.5 * fma(iL, cL, iR * cR) + eta * max_nonneg(iR, iL) * I.idx * jw * ju;
     }
     {  // left face (eL | e)
       const double iL = ir[eL * NP + L], iR = ir[base];
       const double ju = ul[L] - u[0], jw = wl[L] - w[0];
       const double cR = fma(gw[0], ju, gu[0] * jw);
       z[0] += -al * iJ * 0.5 * cR;
-      if (iR > iL) z[0] += al * eta * I.idx * jw * ju;
+      if (gt_nonneg(iR, iL)) z[0] += al * eta * I.idx * jw * ju;
     }
 #pragma unroll
     for (int i = 0; i < NP; ++i) Zinv[base + i] = z_first ? zscale * z[i] : fma(zscale, z[i], Zinv[base + i]);
@@ -465,7 +465,7 @@ __device__ void d1_setup_rev(const View1<NP>& v, const BasisDev& B, const StageT
       const double mR = Mb(eR * NP);
       const double sigb = (mb[L] + mR) * al;
       if (!(iR > iL)) invb[L] = fma(sigb, eta * I.idx, invb[L]);
-      const double sig = eta * ((iR > iL) ? iR : iL) * I.idx;
+      const double sig = eta * max_nonneg(iR, iL) * I.idx;
       ab += mb[L] * (-iJ * B.D[L][L] * iL + sig) + mR * (iJ * B.D[0][0] * iR + sig);
     }
     {  // left face

@@ -60,7 +60,7 @@ __device__ void d1_sens_hyp_rk(const View1<NP>& v, const BasisDev& B, double sg,
       double fp[3];
       flux(m, fp);
       const double wl = wsp(base + L), wr = wsp(m);
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double fs = 0.5 * fma(lam, ss[c][L] - s[c][m], f[c][L] + fp[c]);
@@ -72,7 +72,7 @@ __device__ void d1_sens_hyp_rk(const View1<NP>& v, const BasisDev& B, double sg,
       double fp[3];
       flux(m, fp);
       const double wl = wsp(m), wr = wsp(base);
-      const double lam = (wr > wl) ? wr : wl;
+      const double lam = max_nonneg(wr, wl);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const double fs = 0.5 * fma(lam, s[c][m] - ss[c][0], fp[c] + f[c][0]);
@@ -87,7 +87,7 @@ __device__ void d1_sens_hyp_rk(const View1<NP>& v, const BasisDev& B, double sg,
         double val = fma(c2dt, k[c][i], c1 * ss[c][i]);
         if (c0 != 0.0) val = fma(c0, sn[c][m], val);
         so[c][m] = val;
-        bad |= !isfinite(val);
+        bad |= nonfinite_bits(val);
       }
     }
   }

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
     double px = 0.0, py = 0.0;
     if (t == 0 || t == L) {
       const double wf = B.w[l] * I.jy;
-      const double sig = eta * fmax(t == L ? cir[l] : irx[l], t == L ? irx[l] : cir[l]) * I.idx;
+      const double sig = eta * max_nonneg(t == L ? cir[l] : irx[l], t == L ? irx[l] : cir[l]) * I.idx;
       px = I.alpha * sig * wf;
       // x-face self terms: right side of its left face (t == 0) / left side of its right face (t == L)
       M += fma((t == L ? -I.alpha * invJx * B.D[L][L] : I.alpha * invJx * B.D[0][0]) * wf, cir[l], px);
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
     if (l == 0 || l == L) {
       const double wf = B.w[t] * I.jx;
       const double ip = iry[l == 0 ? 0 : 1];
-      const double sig = eta * fmax(l == L ? cir[l] : ip, l == L ? ip : cir[l]) * I.idy;
+      const double sig = eta * max_nonneg(l == L ? cir[l] : ip, l == L ? ip : cir[l]) * I.idy;
       py = I.alpha * sig * wf;
       M += fma((l == L ? -I.alpha * invJy * B.D[L][L] : I.alpha * invJy * B.D[0][0]) * wf, cir[l], py);
     }
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
       const FaceState& of = s_xf[e][t][s];
       const FaceState& Ls = s == 0 ? pf : of;
       const FaceState& Rs = s == 0 ? of : pf;
-      const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
+      const double lam = max_nonneg(Rs.ws, Ls.ws);
       const int io = s == 0 ? 0 : L;
       const double cf = s == 0 ? invJx * B.iw0 : -invJx * B.iwL;
 #pragma unroll
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
     const FaceState& of = s_yf[e][t][s];
     const FaceState& Ls = s == 0 ? pf : of;
     const FaceState& Rs = s == 0 ? of : pf;
-    const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
+    const double lam = max_nonneg(Rs.ws, Ls.ws);
     const int lo = s == 0 ? 0 : L;
     const double cf = s == 0 ? invJy * B.iw0 : -invJy * B.iwL;
 #pragma unroll
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rk(HypArgs2D a) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) if (a.qo[c]) a.qo[c][n] = qo[c];
     if (a.invro) a.invro[n] = 1.0 / qo[2];
-    bad |= !(qo[2] > 0.0) || !isfinite(qo[0]) || !isfinite(qo[1]) || !isfinite(qo[3]) || !isfinite(qo[2]);
+    bad |= not_positive_finite(qo[2]) || nonfinite_bits(qo[0]) || nonfinite_bits(qo[1]) || nonfinite_bits(qo[3]);
   }
   if (bad) flag_nonfinite(a.status);
 }

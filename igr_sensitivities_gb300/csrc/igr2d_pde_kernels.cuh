@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_rk(PdeRkArgs2D a) {
       const AdjFace& of = s_xf[e][t][s];
       const AdjFace& Ls = s == 0 ? pf : of;
       const AdjFace& Rs = s == 0 ? of : pf;
-      const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
+      const double lam = max_nonneg(Rs.ws, Ls.ws);
       const int io = s == 0 ? 0 : L;
       const double cf = s == 0 ? -invJx * B.iw0 : invJx * B.iwL;
 #pragma unroll
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_pde_rk(PdeRkArgs2D a) {
     const AdjFace of = own_y(s);
     const AdjFace& Ls = s == 0 ? pf : of;
     const AdjFace& Rs = s == 0 ? of : pf;
-    const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
+    const double lam = max_nonneg(Rs.ws, Ls.ws);
     const int lo = s == 0 ? 0 : L;
     const double cf = s == 0 ? -invJy * B.iw0 : invJy * B.iwL;
 #pragma unroll

@@ -159,8 +159,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_hyp_rev(HypRevArgs2D a) {
     const double cfo = s == 0 ? invJ * B.iw0 : -invJ * B.iwL;
     const double cfp = s == 0 ? -invJ * B.iwL : invJ * B.iw0;
     const double wsL = s == 0 ? pws : ows, wsR = s == 0 ? ows : pws;
-    const double lam = (wsR > wsL) ? wsR : wsL;
-    const bool own_wins = (s == 0) ? (wsR > wsL) : !(wsR > wsL);
+    const double lam = max_nonneg(wsR, wsL);
+    const bool own_wins = (s == 0) ? gt_nonneg(wsR, wsL) : !gt_nonneg(wsR, wsL);
     double lamb = 0.0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -446,13 +446,13 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
     const double pl_ = a.cpx[vr.base + t * NP];
     const double Fl = fma(pl_, jul, hw * fma(pl.k, pl.du, kxr[0] * gxu[0]));
     zr[0] = fma(hw * kxr[0], fma(gxv[0], jul, gxu[0] * jvl), zr[0]);
-    if (irl0 > pl.ir) zr[0] = fma(pl_ * jvl, jul, zr[0]);  // R wins only when strictly larger
+    if (gt_nonneg(irl0, pl.ir)) zr[0] = fma(pl_ * jvl, jul, zr[0]);  // R wins only when strictly larger
     // right face (own L side, node L)
     const double jur = ur[L] - prt.u, jvr = vr_[L] - prt.v;
     const double pr_ = a.cpx[vr.base + t * NP + L];
     const double Fr = fma(pr_, jur, hw * fma(kxr[L], gxu[L], prt.k * prt.du));
     zr[L] = fma(hw * kxr[L], fma(gxv[L], jur, gxu[L] * jvr), zr[L]);
-    if (!(prt.ir > irlL)) zr[L] = fma(pr_ * jvr, jur, zr[L]);
+    if (!gt_nonneg(prt.ir, irlL)) zr[L] = fma(pr_ * jvr, jur, zr[L]);
     double sx[NP];
 #pragma unroll
     for (int i = 1; i < L; ++i) sx[i] = kxr[i] * gxu[i];
@@ -511,12 +511,12 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
     const double pbot = a.cpy[vc.base + t];
     const double Fb = fma(pbot, jub, hw * fma(qb.k, qb.du, kyc[0] * gyu[0]));
     zc[0] = fma(hw * kyc[0], fma(gyv[0], jub, gyu[0] * jvb), zc[0]);
-    if (ic0 > qb.ir) zc[0] = fma(pbot * jvb, jub, zc[0]);
+    if (gt_nonneg(ic0, qb.ir)) zc[0] = fma(pbot * jvb, jub, zc[0]);
     const double jut = uc[L] - qt.u, jvt = vc_[L] - qt.v;
     const double ptop = a.cpy[vc.base + L * NP + t];
     const double Ft = fma(ptop, jut, hw * fma(kyc[L], gyu[L], qt.k * qt.du));
     zc[L] = fma(hw * kyc[L], fma(gyv[L], jut, gyu[L] * jvt), zc[L]);
-    if (!(qt.ir > icL)) zc[L] = fma(ptop * jvt, jut, zc[L]);
+    if (!gt_nonneg(qt.ir, icL)) zc[L] = fma(ptop * jvt, jut, zc[L]);
     double sy[NP];
 #pragma unroll
     for (int l = 1; l < L; ++l) sy[l] = kyc[l] * gyu[l];
@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
         const double wf = B.w[l] * I.jy;
         ib[l] = fma(cMb[l] * cself, wf, ib[l]);
         const double iL = t == L ? cir[l] : pir, iR = t == L ? pir : cir[l];
-        const bool own_wins = (t == L) ? !(iR > iL) : (iR > iL);
+        const bool own_wins = (t == L) ? !gt_nonneg(iR, iL) : gt_nonneg(iR, iL);
         if (own_wins) ib[l] = fma((cMb[l] + pMb) * alpha * wf, eta * I.idx, ib[l]);
       }
     }
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
       const double wf = B.w[t] * I.jx;
       ib[l] = fma(cMb[l] * (l == L ? -alpha * invJy * B.D[L][L] : alpha * invJy * B.D[0][0]), wf, ib[l]);
       const double iL = l == L ? cir[l] : pir, iR = l == L ? pir : cir[l];
-      const bool own_wins = (l == L) ? !(iR > iL) : (iR > iL);
+      const bool own_wins = (l == L) ? !gt_nonneg(iR, iL) : gt_nonneg(iR, iL);
       if (own_wins) ib[l] = fma((cMb[l] + pMb) * alpha * wf, eta * I.idy, ib[l]);
     }
   }

@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_sens_hyp_rk(SensHypArgs2D
       const SensFace& of = s_xf[e][t][s];
       const SensFace& Ls = s == 0 ? pf : of;
       const SensFace& Rs = s == 0 ? of : pf;
-      const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
+      const double lam = max_nonneg(Rs.ws, Ls.ws);
       const int io = s == 0 ? 0 : L;
       const double cf = s == 0 ? invJx * B.iw0 : -invJx * B.iwL;
 #pragma unroll
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_sens_hyp_rk(SensHypArgs2D
     const SensFace& of = s_yf[e][t][s];
     const SensFace& Ls = s == 0 ? pf : of;
     const SensFace& Rs = s == 0 ? of : pf;
-    const double lam = (Rs.ws > Ls.ws) ? Rs.ws : Ls.ws;
+    const double lam = max_nonneg(Rs.ws, Ls.ws);
     const int lo = s == 0 ? 0 : L;
     const double cf = s == 0 ? invJy * B.iw0 : -invJy * B.iwL;
 #pragma unroll
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_sens_hyp_rk(SensHypArgs2D
       double val = fma(c2dt, kc[c][l], a.c1 * s_s[c][e][l * NP + t]);
       if (a.c0 != 0.0) val = fma(a.c0, a.sn[c][n], val);
       so[c] = val;
-      bad |= !isfinite(val);
+      bad |= nonfinite_bits(val);
     }
 #pragma unroll
     for (int c = 0; c < 4; ++c) if (a.so[c]) a.so[c][n] = so[c];

@@ -68,6 +68,25 @@ __device__ __forceinline__ void flag_nonfinite(int* status) {
   if (status) atomicOr(status, DEV_NONFINITE);
 }
 
+// Comparisons on bit patterns. GB300 issues a double compare (DSETP), fmax and
+// isfinite through the FP64 unit at ~94 cycles per warp instruction per SM
+// sub-partition (measured with a micro-probe; a DFMA takes ~64), while the
+// same decisions on the IEEE 754 encodings run on the integer pipe at a few
+// cycles. For doubles >= +0 (wave speeds, inverse densities, penalties) the
+// encodings, read as signed 64-bit integers, order exactly like the numbers,
+// so these give the same decisions and the same results as the double forms.
+__device__ __forceinline__ bool gt_nonneg(double a, double b) {
+  return __double_as_longlong(a) > __double_as_longlong(b);
+}
+// (a > b) ? a : b for a, b >= +0
+__device__ __forceinline__ double max_nonneg(double a, double b) { return gt_nonneg(a, b) ? a : b; }
+// x is +-inf or NaN (all exponent bits set)
+__device__ __forceinline__ bool nonfinite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) == 0x7ff00000; }
+// !(x > 0) || !isfinite(x)
+__device__ __forceinline__ bool not_positive_finite(double x) {
+  return __double_as_longlong(x) <= 0 || nonfinite_bits(x);
+}
+
 // Deterministic sum over the threads of a block (fixed tree order). P2 is a
 // power of two >= blockDim.x; every thread must call it; s_red holds P2
 // doubles. Returns the sum to every thread.
