@@ -209,7 +209,10 @@ __host__ __device__ constexpr int group1() { return NP <= 2 ? 2 : (NP <= 4 ? 4 :
 // d1_apply_elems evaluated in the same order, so the results are bitwise
 // equal; operands are chosen by register selects so that the warp runs one
 // instruction stream.
-template <int NP, class LDX, class EPI>
+// NODE_EPI: epi(m, x_m, y_m) is a per-node epilogue that every node lane runs
+// for its own node; otherwise the group's first lane runs the element
+// epilogue epi(e, x[], y[]).
+template <int NP, bool NODE_EPI, class LDX, class EPI>
 __device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm,
                                                const double* ck, const double* cpR, EPI epi) {
   constexpr int L = NP - 1, G = group1<NP>();
@@ -272,10 +275,14 @@ __device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDe
       const double t = fma(Dc[r], sx[r], y);
       y = (interior && r == ii) ? y : t;
     }
-    double yv[NP];
+    if constexpr (NODE_EPI) {
+      if (live && li < NP) epi(base + li, xo, y);
+    } else {
+      double yv[NP];
 #pragma unroll
-    for (int k = 0; k < NP; ++k) yv[k] = __shfl_sync(0xffffffffu, y, k, G);
-    if (live && li == 0) epi(e, x, yv);
+      for (int k = 0; k < NP; ++k) yv[k] = __shfl_sync(0xffffffffu, y, k, G);
+      if (live && li == 0) epi(e, x, yv);
+    }
   }
 }
 
@@ -286,8 +293,23 @@ __device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, 
   // element form leaves lanes idle; a CTA of a batch with more elements is
   // already bound by FP64 throughput, where both forms issue the same number
   // of warp instructions and the element form needs no shuffles
-  if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2) d1_apply_nodes<NP>(v, B, ldx, cm, ck, cpR, epi);
+  if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2) d1_apply_nodes<NP, false>(v, B, ldx, cm, ck, cpR, epi);
   else d1_apply_elems<NP>(v, B, ldx, cm, ck, cpR, epi);
+}
+
+// d1_apply with a per-node epilogue nepi(m, x_m, y_m) (no per-element
+// coupling): in the node form each node lane runs it for its node.
+template <int NP, class LDX, class NEPI>
+__device__ __forceinline__ void d1_apply_pointwise(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm,
+                                                   const double* ck, const double* cpR, NEPI nepi) {
+  if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2) {
+    d1_apply_nodes<NP, true>(v, B, ldx, cm, ck, cpR, nepi);
+  } else {
+    d1_apply_elems<NP>(v, B, ldx, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
+#pragma unroll
+      for (int i = 0; i < NP; ++i) nepi(e * NP + i, xx[i], y[i]);
+    });
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -417,20 +439,16 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
     double ca = 0.0, cc = 0.0;
     if (solver == 2) cta_cheb(B, k + 1, rc, &ca, &cc);
     double* d = w2;
-    d1_apply<NP>(v, B, [&](int m) { return x[m]; }, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
-#pragma unroll
-      for (int i = 0; i < NP; ++i) {
-        const int m = e * NP + i;
-        const double rr = b[m] - y[i];
-        if (taped) { tp.x(k)[m] = xx[i]; tp.r(k)[m] = rr; }
-        if (solver == 2) {
-          const double z = rr * cinvM[m];
-          const double dn = k == 0 ? cc * z : fma(ca, d[m], cc * z);
-          d[m] = dn;
-          xo[m] = xx[i] + dn;
-        } else {
-          xo[m] = fma((2.0 / 3.0) * rr, cinvM[m], xx[i]);
-        }
+    d1_apply_pointwise<NP>(v, B, [&](int m) { return x[m]; }, cm, ck, cpR, [&](int m, double xm, double ym) {
+      const double rr = b[m] - ym;
+      if (taped) { tp.x(k)[m] = xm; tp.r(k)[m] = rr; }
+      if (solver == 2) {
+        const double z = rr * cinvM[m];
+        const double dn = k == 0 ? cc * z : fma(ca, d[m], cc * z);
+        d[m] = dn;
+        xo[m] = xm + dn;
+      } else {
+        xo[m] = fma((2.0 / 3.0) * rr, cinvM[m], xm);
       }
     });
     v.sync();
