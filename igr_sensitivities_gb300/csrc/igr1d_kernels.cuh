@@ -211,10 +211,11 @@ __host__ __device__ constexpr int group1() { return NP <= 2 ? 2 : (NP <= 4 ? 4 :
 // instruction stream.
 // NODE_EPI: epi(m, x_m, y_m) is a per-node epilogue that every node lane runs
 // for its own node; otherwise the group's first lane runs the element
-// epilogue epi(e, x[], y[]).
-template <int NP, bool NODE_EPI, class LDX, class EPI>
-__device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm,
-                                               const double* ck, const double* cpR, EPI epi) {
+// epilogue epi(e, x[], y[]). The coefficients are read through accessors
+// cmf(m), ckf(m) (node m) and cpf(e) (element e).
+template <int NP, bool NODE_EPI, class LDX, class CMF, class CKF, class CPF, class EPI>
+__device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDev& B, LDX ldx, CMF cmf, CKF ckf,
+                                               CPF cpf_, EPI epi) {
   constexpr int L = NP - 1, G = group1<NP>();
   const int ne = v.I.ne;
   const double hw = B.hw;
@@ -258,9 +259,9 @@ __device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDe
 #pragma unroll
     for (int k = 0; k < NP; ++k) xp[k] = ldx(pe * NP + k);
     const double gp = dot_end<NP>(B, left, xp);
-    const double kco = ck[base + ii];
-    const double ckp = ck[left ? eL * NP + L : eR * NP];
-    const double cpf = cpR[left ? eL : ec];
+    const double kco = ckf(base + ii);
+    const double ckp = ckf(left ? eL * NP + L : eR * NP);
+    const double cpf = cpf_(left ? eL : ec);
     const double jmp = (left ? xp[L] : x[L]) - (left ? x[0] : xp[0]);
     const double inner = fma(left ? ckp : kco, left ? gp : g, (left ? kco : ckp) * (left ? g : gp));
     const double F = fma(cpf, jmp, hw * inner);
@@ -269,7 +270,7 @@ __device__ __forceinline__ void d1_apply_nodes(const View1<NP>& v, const BasisDe
 #pragma unroll
     for (int k = 0; k < NP; ++k) sx[k] = __shfl_sync(0xffffffffu, sxi, k, G);
     // y at the lane's node: dot_col<NP>(B, ii, sx, fma(cm, x_ii, -Fl | Fr | 0))
-    double y = fma(cm[base + ii], xo, left ? -F : (ii == L ? F : 0.0));
+    double y = fma(cmf(base + ii), xo, left ? -F : (ii == L ? F : 0.0));
 #pragma unroll
     for (int r = 0; r < NP; ++r) {
       const double t = fma(Dc[r], sx[r], y);
@@ -293,7 +294,9 @@ __device__ __forceinline__ void d1_apply(const View1<NP>& v, const BasisDev& B, 
   // element form leaves lanes idle; a CTA of a batch with more elements is
   // already bound by FP64 throughput, where both forms issue the same number
   // of warp instructions and the element form needs no shuffles
-  if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2) d1_apply_nodes<NP, false>(v, B, ldx, cm, ck, cpR, epi);
+  if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2)
+    d1_apply_nodes<NP, false>(v, B, ldx, [&](int m) { return cm[m]; }, [&](int m) { return ck[m]; },
+                              [&](int e) { return cpR[e]; }, epi);
   else d1_apply_elems<NP>(v, B, ldx, cm, ck, cpR, epi);
 }
 
@@ -303,7 +306,8 @@ template <int NP, class LDX, class NEPI>
 __device__ __forceinline__ void d1_apply_pointwise(const View1<NP>& v, const BasisDev& B, LDX ldx, const double* cm,
                                                    const double* ck, const double* cpR, NEPI nepi) {
   if ((v.e1 - v.e0) * group1<NP>() <= T1 / 2) {
-    d1_apply_nodes<NP, true>(v, B, ldx, cm, ck, cpR, nepi);
+    d1_apply_nodes<NP, true>(v, B, ldx, [&](int m) { return cm[m]; }, [&](int m) { return ck[m]; },
+                             [&](int e) { return cpR[e]; }, nepi);
   } else {
     d1_apply_elems<NP>(v, B, ldx, cm, ck, cpR, [&](int e, const double* xx, const double* y) {
 #pragma unroll
@@ -362,6 +366,84 @@ __device__ __forceinline__ void cta_cheb(const BasisDev& B, int it, double& rc, 
   __syncthreads();
   *ca = s_c[0]; *cc = s_c[1];
   __syncthreads();
+}
+
+// Jacobi / Chebyshev for an instance whose CTAs hold at most T1 / (2 group1)
+// elements each (a small instance, usually spread over a cluster), in node
+// form with the iterate, its coefficients, b and 1/M in shared memory. The
+// two halo elements are read from the neighbouring CTAs' shared memory (the
+// cluster's distributed shared memory), so after each cluster barrier an
+// iteration waits for a DSMEM load instead of an L2 round trip, and touches
+// global memory only for the tape and the result. The arithmetic is
+// d1_solve's, so the results are bitwise equal. The choice depends only on
+// the instance (N_e, CTAs per instance), so all CTAs of a cluster agree.
+template <int NP>
+__device__ __forceinline__ bool d1_local_ok(const View1<NP>& v) {
+  const int per = (v.I.ne + v.cs - 1) / v.cs;
+  return v.I.ne >= v.cs && per * group1<NP>() <= T1 / 2;
+}
+
+template <int NP>
+__device__ void d1_solve_local(const View1<NP>& v, const BasisDev& B, int solver, int n, const double* b, const double* x0,
+                               double* xout, const double* cm, const double* ck, const double* cpR, const double* cinvM,
+                               const SolveTape1& tp) {
+  constexpr int L = NP - 1, MAXE = T1 / 2 / group1<NP>(), MAXN = MAXE * NP;
+  __shared__ double s_x[2][MAXN], s_d[MAXN], s_cm[MAXN], s_ck[MAXN], s_b[MAXN], s_im[MAXN], s_cp[MAXE], s_h[3];
+  const int ne = v.I.ne, cs = v.cs, m0 = v.m0(), nl = (v.e1 - v.e0) * NP;
+  const bool taped = tp.base != nullptr;
+  for (int j = threadIdx.x; j < nl; j += blockDim.x) {
+    const int m = m0 + j;
+    s_x[0][j] = x0[m]; s_cm[j] = cm[m]; s_ck[j] = ck[m]; s_b[j] = b[m]; s_im[j] = cinvM[m];
+  }
+  for (int j = threadIdx.x; j < v.e1 - v.e0; j += blockDim.x) s_cp[j] = cpR[v.e0 + j];
+  const int eLh = wrap_left(v.e0, ne), eRh = v.e1 == ne ? 0 : v.e1;  // the halo elements
+  if (threadIdx.x == 0) { s_h[0] = ck[eLh * NP + L]; s_h[1] = ck[eRh * NP]; s_h[2] = cpR[eLh]; }
+  // neighbouring ranks (eLh is the last element of rank rank_l, eRh the first of rank rank_r)
+  const int rank = blockIdx.x % cs, rank_l = (rank + cs - 1) % cs, rank_r = (rank + 1) % cs;
+  const int nl_left = (int)((long long)ne * (rank_l + 1) / cs - (long long)ne * rank_l / cs) * NP;
+  v.sync();
+  auto cmf = [&](int m) { return s_cm[m - m0]; };
+  auto ckf = [&](int m) {
+    const int j = m - m0;
+    return (j >= 0 && j < nl) ? s_ck[j] : (m == eLh * NP + L ? s_h[0] : s_h[1]);
+  };
+  auto cpf = [&](int e) { return (e >= v.e0 && e < v.e1) ? s_cp[e - v.e0] : s_h[2]; };
+  double rc = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double ca = 0.0, cc = 0.0;
+    if (solver == 2) cta_cheb(B, k + 1, rc, &ca, &cc);
+    double* xs = s_x[k & 1];
+    double* xd = s_x[(k + 1) & 1];
+    const double* xl = xs;
+    const double* xr = xs;
+    if (cs > 1) {
+      cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+      xl = cl.map_shared_rank(xs, rank_l);
+      xr = cl.map_shared_rank(xs, rank_r);
+    }
+    auto ldx = [&](int m) -> double {
+      const int j = m - m0;
+      if (j >= 0 && j < nl) return xs[j];
+      return (m / NP == eLh) ? xl[nl_left - NP + m % NP] : xr[m % NP];
+    };
+    d1_apply_nodes<NP, true>(v, B, ldx, cmf, ckf, cpf, [&](int m, double xm, double ym) {
+      const int j = m - m0;
+      const double rr = s_b[j] - ym;
+      if (taped) { tp.x(k)[m] = xm; tp.r(k)[m] = rr; }
+      double xn;
+      if (solver == 2) {
+        const double z = rr * s_im[j];
+        const double dn = k == 0 ? cc * z : fma(ca, s_d[j], cc * z);
+        s_d[j] = dn;
+        xn = xm + dn;
+      } else {
+        xn = fma((2.0 / 3.0) * rr, s_im[j], xm);
+      }
+      xd[j] = xn;
+      if (k == n - 1) xout[m] = xn;
+    });
+    v.sync();
+  }
 }
 
 // Fixed-count solve A x = b on the instance (pcg_fixed! / jacobi_fixed! /
@@ -432,6 +514,10 @@ __device__ void d1_solve(const View1<NP>& v, const BasisDev& B, int solver, int 
     return;
   }
   // ---- Jacobi / Chebyshev: one apply per iteration, x ping-pong in w0/w1, d in w2
+  if (d1_local_ok(v)) {
+    d1_solve_local<NP>(v, B, solver, n, b, x0, xout, cm, ck, cpR, cinvM, tp);
+    return;
+  }
   double rc = 0.0;
   const double* x = x0;
   for (int k = 0; k < n; ++k) {
