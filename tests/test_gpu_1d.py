@@ -284,3 +284,28 @@ def test_node_and_element_apply_agree_bitwise(igr, igr1d, oracle, solver):
     ref, _ = oracle.run_forward_1d(G, g, alpha, dt, 5 * dt, 9, solver, [flat(x) for x in q0])
     for x, y in zip(out[4][:3], ref):
         assert rel(x, y) <= RTOL_FWD
+
+
+@pytest.mark.parametrize("ne,cs", [(16, 16), (3, 2), (2, 2), (5, 4)])
+@pytest.mark.parametrize("solver", ["jacobi", "chebyshev"])
+def test_local_solve_edge_splits(igr, igr1d, oracle, ne, cs, solver):
+    """Small instances keep the Jacobi / Chebyshev iterate in shared memory and
+    read the halo from the neighbouring CTAs: one element per CTA, uneven
+    splits and two CTAs that are each other's left and right neighbour give
+    bitwise the one-CTA results, and match the oracle."""
+    from igr_sensitivities_gb300 import Context
+    g = 1.4
+    basis, mesh, G = setup1(igr, oracle, 3, ne)
+    q0 = W.seeded_pulses_1d(mesh, g, W.seed_for(1, 910 + ne), width=0.2)
+    dt = W.cfl_dt_1d(mesh, 3, q0, g, 0.1)
+    alpha = 3.0 * mesh.dx ** 2
+    ctx = Context(0)
+    out = {}
+    for c in (1, cs):
+        ctx.set_cluster_size_1d(c)
+        out[c] = igr1d.run_forward(*q0, dt, 4 * dt, basis, mesh, g, alpha, n_iter=6, solver=solver, ctx=ctx)
+    for x, y in zip(out[1], out[cs]):
+        assert np.array_equal(x, y)
+    ref, _ = oracle.run_forward_1d(G, g, alpha, dt, 4 * dt, 6, solver, [flat(x) for x in q0])
+    for x, y in zip(out[cs][:3], ref):
+        assert rel(x, y) <= RTOL_FWD
