@@ -479,8 +479,6 @@ static void inst_sum_after(Ctx& c, const Plan2D& P, const double* partials, bool
   k2_inst_sum<<<(int)P.inst.size(), 32, 0, c.stream>>>(P.d_inst, partials, grouped ? 1 : 0, s);
 }
 
-static void tile_geometry(const Plan2D& P, int* tx, int* ty) { tile_shape(P.np, tx, ty); }
-
 // Fixed-count Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347) on
 // the stage's operator: x_0 = warm start, result in st.Sout. Per iteration
 // one operator kernel (A p_k and p_k . A p_k, with p_k formed on load; its
@@ -504,8 +502,6 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
   auto R = [&](int k) { return taped ? st.rk[k] : xa; };
   auto PK = [&](int k) { return taped ? st.pk[k] : ((k % 2 == 0) ? xb : dbuf); };
   auto AP = [&](int k) { return taped ? st.apk[k] : apbuf; };
-  int tx, ty;
-  tile_geometry(P, &tx, &ty);
   ApplyArgs2D base;
   std::memset(&base, 0, sizeof(base));
   base.tiles = P.d_tiles; base.inst = P.d_inst; base.B = P.B;
@@ -541,7 +537,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
       inst_sum_after(c, P, part, false, a.isum);
     }
     PcgUpdateArgs u;
-    u.tiles = P.d_tiles; u.groups = P.d_groups; u.inst = P.d_inst; u.np = P.np; u.tx = tx; u.ty = ty;
+    u.tiles = P.d_tiles; u.groups = P.d_groups; u.inst = P.d_inst;
     u.x_in = k == 0 ? x0 : xout; u.x_out = xout;
     u.p = PK(k); u.ap = AP(k); u.r_in = R(k); u.r_out = R(k + 1); u.cinvM = st.cinvM;
     u.al = AL(k);
@@ -549,7 +545,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
     u.isum = inst_sum0(cnt, RZ(k + 1), nullptr, RZ(k), BT(k));  // beta_k = rz_{k+1} / (rz_k + eps)
     {
       LaunchScope ls(c, KID_OTHER);
-      k2_pcg_update<<<P.ngroups(), PCG_THREADS, 0, c.stream>>>(u);
+      NP_DISPATCH(P.np, launch_k2_pcg_update<NPV>(u, P.ngroups(), c.stream));
     }
     inst_sum_after(c, P, part, true, u.isum);
   }
@@ -1092,8 +1088,6 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   std::vector<double> ca, cc;
   cheb_coeffs(P.B, o.n_iter, ca, cc);
   const int srev = !apos ? SREV_NONE : (o.solver == SOLVER_CHEBYSHEV ? SREV_CHEB : (o.solver == SOLVER_JACOBI ? SREV_JACOBI : SREV_PCG));
-  int tx, ty;
-  tile_geometry(P, &tx, &ty);
   double* part = srev == SREV_PCG ? c.ws.dbl("red:part", P.ntiles()) : nullptr;
   double* pscal = c.ws.dbl("adj:pcgscal", (size_t)4 * ni);  // BET, RZB, PAPB, RZB1 per instance
   const int nb = P.ntiles();
@@ -1114,7 +1108,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
     int* cnt = sum_choice(c, P, false).fused ? inst_counters(c, P) : nullptr;
     for (int it = n - 1; it >= 0; --it) {
       PcgRevArgs g;
-      g.tiles = P.d_tiles; g.groups = P.d_groups; g.inst = P.d_inst; g.np = P.np; g.tx = tx; g.ty = ty;
+      g.tiles = P.d_tiles; g.groups = P.d_groups; g.inst = P.d_inst;
       g.first = it == n - 1 ? 1 : 0;
       g.pb = PB; g.rb = RB; g.iMb = Mb;
       g.r1 = sb.rk[it + 1]; g.cinvM = sb.cinvM; g.ap = sb.apk[it]; g.p = sb.pk[it]; g.xb = Sb;
@@ -1123,7 +1117,7 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       std::memset(&g.isum, 0, sizeof(g.isum));  // ab, then RZB and PAPB
       g.isum.cnt = cnt; g.isum.mode = 1; g.isum.first = g.first; g.isum.it = it; g.isum.ni = ni;
       g.isum.RZ = RZ; g.isum.PAP = PAP; g.isum.BET = BET; g.isum.RZB = RZB; g.isum.PAPB = PAPB;
-      { LaunchScope ls(c, KID_OTHER); k2_pcg_rev_update<<<P.ngroups(), PCG_THREADS, 0, c.stream>>>(g); }
+      { LaunchScope ls(c, KID_OTHER); NP_DISPATCH(P.np, launch_k2_pcg_rev_update<NPV>(g, P.ngroups(), c.stream)); }
       inst_sum_after(c, P, part, true, g.isum);
       ApplyRevArgs2D r;
       std::memset(&r, 0, sizeof(r));
@@ -1148,10 +1142,10 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
     }
     {
       PcgRevFinalArgs f;
-      f.tiles = P.d_tiles; f.inst = P.d_inst; f.np = P.np; f.tx = tx; f.ty = ty;
+      f.tiles = P.d_tiles; f.inst = P.d_inst;
       f.pb = PB; f.r0 = sb.rk[0]; f.cinvM = sb.cinvM; f.RZB = RZB; f.rb = RB; f.iMb = Mb;
       LaunchScope ls(c, KID_OTHER);
-      k2_pcg_rev_final<<<nb, PCG_THREADS, 0, c.stream>>>(f);
+      NP_DISPATCH(P.np, launch_k2_pcg_rev_final<NPV>(f, nb, c.stream));
     }
     // r_0 = b - A x_0
     ApplyRevArgs2D r;

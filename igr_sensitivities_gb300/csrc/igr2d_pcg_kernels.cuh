@@ -21,6 +21,7 @@
 // every tile of the group, so the block reduction is paid once per group.
 // Group j of an instance writes its partial to partials[tile0 + j].
 #pragma once
+#include "igr2d_kernels.cuh"  // Tiling2D
 #include "igr_device.cuh"
 
 namespace igrgpu {
@@ -28,9 +29,12 @@ namespace igrgpu {
 constexpr int PCG_THREADS = 256;
 
 // Node n of element-local index idx within the tile; false if the element is
-// outside the mesh (ragged last tile).
-__device__ __forceinline__ bool tile_node(const Tile2D& tl, const Inst2D& I, int np, int tx, int idx, long long* n) {
-  const int nn = np * np;
+// outside the mesh (ragged last tile). The tile shape is the operator
+// kernels' (Tiling2D<NP>), a compile-time constant, so the index arithmetic
+// needs no run-time integer division.
+template <int NP>
+__device__ __forceinline__ bool tile_node(const Tile2D& tl, const Inst2D& I, int idx, long long* n) {
+  constexpr int nn = NP * NP, tx = Tiling2D<NP>::TX;
   const int e = idx / nn, nd = idx - e * nn;
   const int ex = tl.ex0 + e % tx, ey = tl.ey0 + e / tx;
   if (ex >= I.nex || ey >= I.ney) return false;
@@ -41,7 +45,7 @@ __device__ __forceinline__ bool tile_node(const Tile2D& tl, const Inst2D& I, int
 // Forward iteration k, after A p_k:  x_{k+1} = x_k + alpha_k p_k,
 // r_{k+1} = r_k - alpha_k A p_k, rz_{k+1} = r_{k+1} . M^-1 r_{k+1}.
 struct PcgUpdateArgs {
-  const Tile2D* tiles; const TileGroup* groups; const Inst2D* inst; int np, tx, ty;
+  const Tile2D* tiles; const TileGroup* groups; const Inst2D* inst;
   const double *x_in, *p, *ap, *r_in, *cinvM;
   double *x_out, *r_out;
   const double* al;         // per-instance alpha_k
@@ -60,19 +64,20 @@ __device__ __forceinline__ void group_partial(const InstSum& isum, const TileGro
   inst_sum_last_block(isum, g.inst, ng, tot, partials, I.tile0 + (g.first - I.tile0) / TILE_GROUP, I.tile0, ng);
 }
 
+template <int NP>
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
   constexpr int P2 = PCG_THREADS, G = TILE_GROUP;
   __shared__ double s_red[P2];
   const TileGroup g = a.groups[blockIdx.x];
   const Inst2D I = a.inst[g.inst];
   const double al = a.al[g.inst];
-  const int cnt = a.tx * a.ty * a.np * a.np;
+  constexpr int cnt = Tiling2D<NP>::TE * NP * NP;
   double part = 0.0;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
     long long n[G];
     bool ok[G];
 #pragma unroll
-    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node(a.tiles[g.first + j], I, a.np, a.tx, idx, &n[j]);
+    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node<NP>(a.tiles[g.first + j], I, idx, &n[j]);
     double p[G], ap[G], x[G], r[G], im[G];
 #pragma unroll
     for (int j = 0; j < G; ++j)
@@ -106,7 +111,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
 // iteration.
 // ---------------------------------------------------------------------------
 struct PcgRevArgs {
-  const Tile2D* tiles; const TileGroup* groups; const Inst2D* inst; int np, tx, ty;
+  const Tile2D* tiles; const TileGroup* groups; const Inst2D* inst;
   int first;
   double *pb, *rb, *iMb;
   const double *r1, *cinvM, *ap, *p, *xb;
@@ -115,19 +120,20 @@ struct PcgRevArgs {
   InstSum isum;                    // mode 1: RZB, PAPB
 };
 
+template <int NP>
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
   constexpr int P2 = PCG_THREADS, G = TILE_GROUP;
   __shared__ double s_red[P2];
   const TileGroup g = a.groups[blockIdx.x];
   const Inst2D I = a.inst[g.inst];
   const double beta = a.beta[g.inst], rzb1 = a.first ? 0.0 : a.rzb1[g.inst];
-  const int cnt = a.tx * a.ty * a.np * a.np;
+  constexpr int cnt = Tiling2D<NP>::TE * NP * NP;
   double part = 0.0;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
     long long n[G];
     bool ok[G];
 #pragma unroll
-    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node(a.tiles[g.first + j], I, a.np, a.tx, idx, &n[j]);
+    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node<NP>(a.tiles[g.first + j], I, idx, &n[j]);
     double pbv[G], rbv[G], imb[G], r1[G], im[G], ap[G], xb[G], p[G];
 #pragma unroll
     for (int j = 0; j < G; ++j)
@@ -153,6 +159,15 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_update(PcgRevArgs a) {
   group_partial(a.isum, g, I, tot, a.partials);
 }
 
+template <int NP>
+void launch_k2_pcg_update(const PcgUpdateArgs& a, int nblocks, cudaStream_t s) {
+  k2_pcg_update<NP><<<nblocks, PCG_THREADS, 0, s>>>(a);
+}
+template <int NP>
+void launch_k2_pcg_rev_update(const PcgRevArgs& a, int nblocks, cudaStream_t s) {
+  k2_pcg_rev_update<NP><<<nblocks, PCG_THREADS, 0, s>>>(a);
+}
+
 // Per-instance sums in a separate launch (InstSum with cnt null): one warp
 // per instance over the instance's tile partials, or its group partials when
 // grouped.
@@ -167,24 +182,30 @@ __global__ void __launch_bounds__(32) k2_inst_sum(const Inst2D* inst, const doub
 //   rb += rzb_0 z_0 + M^-1 (pb + rzb_0 r_0),  iMb += (pb + rzb_0 r_0) r_0.
 // rb then holds the adjoint of r_0 = b - A x_0 for the final reverse apply.
 struct PcgRevFinalArgs {
-  const Tile2D* tiles; const Inst2D* inst; int np, tx, ty;
+  const Tile2D* tiles; const Inst2D* inst;
   const double *pb, *r0, *cinvM, *RZB;
   double *rb, *iMb;
 };
 
+template <int NP>
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_rev_final(PcgRevFinalArgs a) {
   const Tile2D tl = a.tiles[blockIdx.x];
   const Inst2D I = a.inst[tl.inst];
   const double rzb0 = a.RZB[tl.inst];
-  const int cnt = a.tx * a.ty * a.np * a.np;
+  constexpr int cnt = Tiling2D<NP>::TE * NP * NP;
   for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
     long long n;
-    if (!tile_node(tl, I, a.np, a.tx, idx, &n)) continue;
+    if (!tile_node<NP>(tl, I, idx, &n)) continue;
     const double r0 = a.r0[n], im = a.cinvM[n];
     const double z0b = fma(rzb0, r0, a.pb[n]);
     a.rb[n] = a.rb[n] + fma(rzb0, r0 * im, z0b * im);
     a.iMb[n] = fma(z0b, r0, a.iMb[n]);
   }
+}
+
+template <int NP>
+void launch_k2_pcg_rev_final(const PcgRevFinalArgs& a, int nblocks, cudaStream_t s) {
+  k2_pcg_rev_final<NP><<<nblocks, PCG_THREADS, 0, s>>>(a);
 }
 
 }  // namespace igrgpu
