@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -86,8 +87,7 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
-            else "/tmp/igr_clocks_bench.csv"
+        self.path = os.path.join(tempfile.gettempdir(), "igr_clocks_bench_%d.csv" % os.getpid())
 
     def start(self):
         try:
