@@ -366,3 +366,28 @@ def test_tangent_graph_replay_equals_eager_launches(igr, oracle):
     assert len(outs[0]) == 10
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(flat(a), flat(b))
+
+
+@pytest.mark.parametrize("p,nex,ney", [(1, 6, 5), (2, 5, 4), (4, 5, 3)])
+def test_pcg_forward_and_adjoint_other_degrees(igr, oracle, p, nex, ney):
+    """PCG (its pointwise kernels are compiled per degree) for p = 1, 2, 4 on
+    ragged tile grids: forward state and gradient against the oracle."""
+    g = 1.4
+    basis, mesh, G = setup(igr, oracle, p, nex, ney)
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(8, p), width=0.15)
+    dt = 0.4 * W.cfl_dt_2d(mesh, p, q0, g, 0.1)
+    alpha = 0.02
+    out = igr.run_forward(*q0, dt, 4 * dt * 0.999, basis, mesh, g, alpha, n_iter=7, solver="pcg")
+    ref, Sr = oracle.run_forward_2d(G, g, alpha, dt, 4 * dt * 0.999, 7, "pcg", [flat(a) for a in q0])
+    for a, b in zip(out[:4], ref):
+        assert rel(a, b) <= RTOL_FWD
+    assert rel(out[4], Sr) <= RTOL_FWD
+    res = igr.enzyme_adjoint_ic(*q0, 4, dt, basis, mesh, g, alpha, n_iter=7, solver="pcg", objective="l2_density",
+                                with_params=True)
+    Jr, dqr, dgr, dar = oracle.adjoint_2d(G, g, alpha, 4, dt, 7, "pcg", "l2_density", [flat(a) for a in q0])
+    assert abs(res[0] - Jr) <= 1e-12 * abs(Jr)
+    num = np.sqrt(sum(np.sum((flat(a) - b) ** 2) for a, b in zip(res[1:5], dqr)))
+    den = np.sqrt(sum(np.sum(b ** 2) for b in dqr))
+    assert num <= RTOL_GRAD * den
+    assert abs(res[5] - dgr) <= RTOL_GRAD * abs(dgr)
+    assert abs(res[6] - dar) <= RTOL_GRAD * abs(dar)
