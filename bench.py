@@ -46,6 +46,10 @@ BYTES_PER_NODE = {0: 8 * 11, 1: 8 * 13, 2: 8 * 17, 3: 8 * 35, 4: 8 * 23, 5: 8 * 
 # 8-instance case whose fields exceed L2 (profiles/adjoint2d_kernels_128.md);
 # scaled by the launch's node count for `roofline.traffic`.
 TRAFFIC_PER_NODE = {0: 61.9, 1: 91.8, 2: 123.7, 3: 208.1, 4: 143.8, 5: 141.0}
+# FP64 instructions per node (DFMA + DADD + DMUL thread instructions of the same
+# captures): the issue-rate view of the FP64 roof, whose peak is half the DFMA
+# probe's flop rate (one DFMA = 2 flops).
+INST_PER_NODE = {0: 59.0, 1: 30.0, 2: 107.0, 3: 155.1, 4: 52.5, 5: 90.3}
 FAMILY = {0: "k2_setup", 1: "k2_apply", 2: "k2_hyp_rk", 3: "k2_hyp_rev", 4: "k2_apply_rev", 5: "k2_setup_rev"}
 
 
@@ -717,6 +721,7 @@ def main():
     flops = FLOPS_PER_NODE[dom] * nodes
     achieved = flops / (ms_launch * 1e-3) / 1e12
     hbm = BYTES_PER_NODE[dom] * nodes / (ms_launch * 1e-3) / 1e9
+    issue = INST_PER_NODE[dom] * nodes / (ms_launch * 1e-3) / 1e12
     all_flops = sum(FLOPS_PER_NODE[k] * fam[k][2] for k in FAMILY)
     all_ms = sum(fam[k][0] for k in FAMILY)
     try:
@@ -732,6 +737,10 @@ def main():
                 "ms_per_launch": ms_launch, "flops_per_launch": flops, "nodes_per_launch": nodes,
                 "all_kernels_fp64_tflops": all_flops / (all_ms * 1e-3) / 1e12 if all_ms else None,
                 "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak, "peak_source": hbm_src},
+                "fp64_issue": {"achieved": issue, "peak": peak.value / 2, "unit": "T FP64 instructions/s",
+                               "frac": issue / (peak.value / 2) if peak.value else None,
+                               "note": "DFMA, DADD and DMUL each take one FP64 issue slot; a third of these kernels' "
+                                       "FP64 instructions are DADD/DMUL (1 flop), so the flop fraction is lower"},
                 "time_share": {k: v / tot for k, v in share.items()},
                 "profiled_step_ms": t_prof * 1e3, "kernel_ms_in_profiled_step": sum(v[0] for v in fam.values())}
     cfg = config_dict(B)
