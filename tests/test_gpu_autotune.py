@@ -84,3 +84,39 @@ def test_unwritable_cache_path_is_rejected_up_front(igr, tmp_path):
         ctx.set_autotune(True, str(tmp_path / "no_such_dir" / "tune.txt"))
     assert "IGR_EINVAL" in str(ei.value) and "autotune cache" in str(ei.value)
     assert ctx.autotune_count() == 0
+
+
+def test_1d_tuned_adjoint_and_continuous_adjoint_keep_results(igr):
+    """The 1D CTA count is also measured inside the discrete and continuous
+    adjoint calls (the probe advances a copy of q0); their results do not
+    change."""
+    from igr_sensitivities_gb300 import Context, igr1d
+    basis = igr.DGBasis(3)
+    nes, g = [48, 160], 1.4
+    states = []
+    for i, ne in enumerate(nes):
+        mesh = igr.PeriodicMesh1D(ne, 1.0, basis)
+        q0 = W.seeded_pulses_1d(mesh, g, W.seed_for(4, 80 + i), width=0.08)
+        states.append(tuple(flat(a) for a in q0))
+    mesh = igr.PeriodicMesh1D(nes[1], 1.0, basis)
+    dt = W.cfl_dt_1d(mesh, 3, [a.reshape(4, nes[1], order="F") for a in states[1]], g, 0.1)
+    alpha = 3.0 / nes[1] ** 2
+    run = lambda ctx: igr1d.adjoint_batch(states, basis, nes, 1.0, g, alpha, dt, 6, n_iter=6, solver="pcg",
+                                          objective="l2_pressure", ctx=ctx)
+    run_c = lambda ctx: igr1d.adjoint_conservative_batch(states, basis, nes, 1.0, g, alpha, dt, 6 * dt, n_iter=6,
+                                                         objective="l2_pressure", ctx=ctx)
+    plain, plain_c = run(Context(0)), run_c(Context(0))
+    ctx = Context(0)
+    ctx.set_autotune(True)
+    tuned, tuned_c = run(ctx), run_c(ctx)
+    assert ctx.autotune_count() >= 1
+    def same(a, b):
+        if isinstance(a, (list, tuple)):
+            assert len(a) == len(b)
+            for x, y in zip(a, b):
+                same(x, y)
+        else:
+            assert np.array_equal(np.asarray(a), np.asarray(b))
+
+    same(plain, tuned)
+    same(plain_c, tuned_c)
