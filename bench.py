@@ -131,7 +131,9 @@ class ClockSampler:
 
 def cpu_baseline(B_cpu, n_steps_sample, threads):
     """The CPU oracle (C++ restatement of the reference) on a bounded sample:
-    B_cpu instances for n_steps_sample steps, OpenMP over instances."""
+    B_cpu instances for n_steps_sample steps, OpenMP over instances. Returns
+    (gradients/s scaled to full gradients, seconds, the sample's inputs and the
+    oracle's (J, dq0, dgamma, dalpha))."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as O
     from igr_sensitivities_gb300 import workloads as W
@@ -139,10 +141,30 @@ def cpu_baseline(B_cpu, n_steps_sample, threads):
     basis, mesh, q0, gam, alp, dts, prm = make_batch(igr, W, B_cpu)
     G = O.Grid2D(P, NE, NE)
     t0 = time.perf_counter()
-    O.adjoint_batch_2d(G, gam, alp, n_steps_sample, float(dts[0]), N_ITER, SOLVER, OBJ, q0, prm, n_threads=threads)
+    ref = O.adjoint_batch_2d(G, gam, alp, n_steps_sample, float(dts[0]), N_ITER, SOLVER, OBJ, q0, prm,
+                             n_threads=threads)
     t = time.perf_counter() - t0
+    sample = (basis, mesh, q0, gam, alp, float(dts[0]), prm)
     # per-step cost is uniform: a full 200-step gradient costs 200/n_steps_sample times the sample
-    return B_cpu / (t * N_STEPS / n_steps_sample), t
+    return B_cpu / (t * N_STEPS / n_steps_sample), t, sample, ref
+
+
+def parity_vs_oracle(igr, ctx, sample, ref, n_steps_sample):
+    """The GPU batch on the CPU baseline's sample (same instances, step size and
+    steps) against the oracle's result: relative errors of J, the gradient
+    w.r.t. q0 (L2 over each instance's four fields; max over instances and over
+    the whole batch), dJ/dgamma and dJ/dalpha."""
+    basis, mesh, q0, gam, alp, dt, prm = sample
+    B = q0.shape[0]
+    J, dq, dg, da = igr.adjoint_batch(q0, gam, alp, np.full(B, dt), n_steps_sample, basis, mesh, n_iter=N_ITER,
+                                      solver=SOLVER, objective=OBJ, obj_params=prm, ctx=ctx)
+    Jr, dqr, dgr, dar = ref
+    r = lambda a, b: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+    per = [float(np.linalg.norm(dq[b] - dqr[b]) / np.linalg.norm(dqr[b])) for b in range(B)]
+    return {"rel_l2_grad": float(np.linalg.norm(dq - dqr) / np.linalg.norm(dqr)), "rel_l2_grad_max_instance": max(per),
+            "rel_J": r(J, Jr), "rel_dgamma": r(dg, dgr), "rel_dalpha": r(da, dar), "tolerance_grad": 1e-9,
+            "config": "%d instances of the workload (128x128 P3, Chebyshev 5, window rho^2), %d steps of dt = %.6e, "
+                      "GPU batch vs the CPU oracle" % (B, n_steps_sample, dt)}
 
 
 def reference_arm(args):
@@ -156,7 +178,7 @@ def reference_arm(args):
     for _ in range(args.warmup):
         cpu_baseline(B_cpu, n_sample, threads)
     for _ in range(args.steps):
-        v, t = cpu_baseline(B_cpu, n_sample, threads)
+        v, t, _, _ = cpu_baseline(B_cpu, n_sample, threads)
         vals.append((v, t))
     value = statistics.median(v for v, _ in vals)
     ms = statistics.median(t for _, t in vals) * 1e3
@@ -757,10 +779,11 @@ def main():
     if not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
         n_sample = 5
-        v, tcpu = cpu_baseline(threads, n_sample, threads)
+        v, tcpu, sample, ref = cpu_baseline(threads, n_sample, threads)
         line["cpu_baseline"] = {"value": v, "unit": "gradients/s", "cores": threads, "kind": "port",
                                 "sample": "%d instances x %d of %d steps (OpenMP over instances, %.1f s), scaled to full "
                                           "gradients" % (threads, n_sample, N_STEPS, tcpu)}
+        line["parity"] = parity_vs_oracle(igr, ctx, sample, ref, n_sample)
     print(json.dumps(line))
 
 

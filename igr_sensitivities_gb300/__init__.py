@@ -21,7 +21,8 @@ from ._lib import Context, check, default_context, lib
 __all__ = [
     "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
     "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch_meshes", "adjoint_batch", "objective_value",
-    "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "SOLVERS", "OBJECTIVES",
+    "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "compute_igr_euler_rhs_", "compute_igr_rhs_",
+    "compute_sip_diagonal", "SIPOperator", "sip_operator", "cg_solve_", "cg_fixed_", "SOLVERS", "OBJECTIVES",
     "Snapshots", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
     "adjoint_conservative_ic", "adjoint_conservative_batch",
     "init_constant_state", "init_isentropic_vortex", "build_taylor_green_ic_", "build_sedov_blast_ic_",
@@ -282,7 +283,7 @@ def sensitivity_batch(q0, s0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=
 
 def enzyme_adjoint_ic(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",
                       objective="l2_density", obj_params=None, with_params=False, ctx=None):
-    """enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:428-454).
+    """enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:270-296).
 
     Returns (J, dmux0, dmuy0, drho0, dE0), the objective and its gradient with
     respect to the initial conservative state after `n_steps` SSP-RK3 steps of
@@ -345,7 +346,7 @@ def adjoint_batch(q0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solv
 def objective_value(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",
                     objective="l2_density", obj_params=None, ctx=None):
     """The primal objective of enzyme_adjoint_ic (the inlined RK3 loop of
-    IGR_adjoints_2d/enzyme_adjoint.jl:206-235 and its objective tail)."""
+    IGR_adjoints_2d/enzyme_adjoint.jl:56-71 and its objective tail, :72-81)."""
     _solver(solver)  # validate before touching the device
     _objective(objective)
     ctx = ctx or default_context()
@@ -395,6 +396,116 @@ def solve_elliptic_(Sigma, mux, muy, rho, E, basis, mesh, alpha, n_iter=10, solv
     check(ctx, lib().igr2d_solve_elliptic(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(alpha), C.c_int(n_iter),
                                           C.c_int(_solver(solver)), *[_ptr(a) for a in q], _ptr(S)))
     Sigma[...] = S.reshape(shape, order="F")
+
+
+def compute_igr_euler_rhs_(dmux, dmuy, drho, dE, mux, muy, rho, E, Sigma, basis, mesh, gamma, alpha, n_iter=10,
+                           solver="pcg", ctx=None):
+    """compute_igr_euler_rhs! (IGR_adjoints_2d/forward.jl:15-31): the Sigma solve
+    (Sigma is the warm start and the result) when alpha > 0, else Sigma = 0;
+    then the hyperbolic DG RHS at (q, Sigma) into (dmux, dmuy, drho, dE)."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n) for a in (mux, muy, rho, E)]
+    S = _flat(Sigma, n).copy()
+    out = [np.zeros(n) for _ in range(4)]
+    check(ctx, lib().igr2d_igr_euler_rhs(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(gamma),
+                                         C.c_double(alpha), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                         *[_ptr(a) for a in q], _ptr(S), *[_ptr(a) for a in out]))
+    for dst, src in zip((dmux, dmuy, drho, dE), out):
+        dst[...] = src.reshape(shape, order="F")
+    Sigma[...] = S.reshape(shape, order="F")
+
+
+def compute_igr_rhs_(b, mux, muy, rho, E, basis, mesh, alpha, ctx=None):
+    """compute_igr_rhs! (IGR_adjoints_2d/elliptic.jl:159-197): the IGR source b."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    q = [_flat(a, n) for a in (mux, muy, rho, E)]
+    out = np.zeros(n)
+    check(ctx, lib().igr2d_igr_rhs(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(alpha),
+                                   *[_ptr(a) for a in q], _ptr(out)))
+    b[...] = out.reshape(shape, order="F")
+
+
+def compute_sip_diagonal(rho, basis, mesh, alpha, ctx=None):
+    """compute_sip_diagonal (IGR_adjoints_2d/elliptic.jl:205-264): diag(A) as a new array."""
+    ctx = ctx or default_context()
+    shape = mesh.shape(basis)
+    n = int(np.prod(shape))
+    out = np.zeros(n)
+    check(ctx, lib().igr2d_sip_diagonal(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_double(alpha),
+                                        _ptr(_flat(rho, n)), _ptr(out)))
+    return np.asfortranarray(out.reshape(shape, order="F"))
+
+
+class SIPOperator:
+    """The operator the reference's tests hand to cg_solve! / cg_fixed!:
+    `apply_A!(y, x) = apply_sip!(y, x, rho, basis, mesh, alpha)`
+    (IGR_adjoints_2d/tests/run_euler_test.jl:64). Calling it applies A once
+    (apply_sip_); cg_solve_ / cg_fixed_ recognise it and run the whole CG
+    iteration on the GPU. `dim` is 2 (CartesianMesh2D) or 1 (PeriodicMesh1D)."""
+
+    def __init__(self, rho, basis, mesh, alpha, ctx=None):
+        self.rho, self.basis, self.mesh, self.alpha, self.ctx = rho, basis, mesh, float(alpha), ctx
+        self.dim = 1 if hasattr(mesh, "N_e") else 2
+
+    def __call__(self, y, x):
+        if self.dim == 2:
+            apply_sip_(y, x, self.rho, self.basis, self.mesh, self.alpha, self.ctx)
+        else:
+            from . import igr1d
+            igr1d.apply_sip_(y, x, self.rho, self.basis, self.mesh, self.alpha, self.ctx)
+
+
+def sip_operator(rho, basis, mesh, alpha, ctx=None):
+    """apply_A! for cg_solve_ / cg_fixed_: y <- A(rho, alpha) x (2D or 1D mesh)."""
+    return SIPOperator(rho, basis, mesh, alpha, ctx)
+
+
+def _cg(x, apply_A, b, tol, maxiter, fixed):
+    if not isinstance(apply_A, SIPOperator):
+        raise TypeError("the GPU CG applies the SIP operator: pass apply_A = sip_operator(rho, basis, mesh, alpha)")
+    op = apply_A
+    ctx = op.ctx or default_context()
+    n = x.size
+    xf = _flat(x, n).copy()
+    rho, bb = _flat(op.rho, n), _flat(b, n)
+    it = C.c_int(0)
+    if op.dim == 2:
+        d = C.byref(_disc2d(op.basis, op.mesh))
+        if fixed:
+            check(ctx, lib().igr2d_cg_fixed(ctx.handle, d, C.c_double(op.alpha), _ptr(rho), _ptr(bb), _ptr(xf),
+                                            C.c_int(maxiter)))
+        else:
+            check(ctx, lib().igr2d_cg_solve(ctx.handle, d, C.c_double(op.alpha), _ptr(rho), _ptr(bb), _ptr(xf),
+                                            C.c_double(tol), C.c_int(maxiter), C.byref(it)))
+    else:
+        from .igr1d import _disc1d
+        d = C.byref(_disc1d(op.basis, op.mesh))
+        if fixed:
+            check(ctx, lib().igr1d_cg_fixed(ctx.handle, d, C.c_double(op.alpha), _ptr(rho), _ptr(bb), _ptr(xf),
+                                            C.c_int(maxiter)))
+        else:
+            check(ctx, lib().igr1d_cg_solve(ctx.handle, d, C.c_double(op.alpha), _ptr(rho), _ptr(bb), _ptr(xf),
+                                            C.c_double(tol), C.c_int(maxiter), C.byref(it)))
+    x[...] = xf.reshape(x.shape, order="F")
+    return int(maxiter) if fixed else it.value
+
+
+def cg_solve_(x, apply_A, b, tol, maxiter):
+    """cg_solve! (IGR_adjoints_2d/elliptic.jl:278-297; 1D :163-199): CG with the
+    exit sqrt(r.r) < tol tested before each iteration; x is the initial guess
+    and the solution. Returns the reference's iteration count."""
+    return _cg(x, apply_A, b, float(tol), int(maxiter), False)
+
+
+def cg_fixed_(x, apply_A, b, n_iter):
+    """cg_fixed! (IGR_adjoints_2d/elliptic.jl:304-320; 1D :265-292): n_iter CG
+    iterations with the 1e-30 guards. Returns n_iter."""
+    return _cg(x, apply_A, b, 0.0, int(n_iter), True)
 
 
 # ---------------------------------------------------------------------------

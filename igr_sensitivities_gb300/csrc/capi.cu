@@ -430,17 +430,25 @@ static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const do
   const long long N = nodes2d(d);
   // Instances per group: as many as fit with a full tape (no recompute);
   // a single instance that does not fit runs with segment checkpointing.
+  // Without a budget: the free device memory less a reserve, with ~110
+  // working fields per instance beside the tape; with one (igr_set_tape_budget):
+  // the full tapes and checkpoints of the group within the budget.
   int G = n_inst;
-  if (c.tape_budget == 0) {
-    size_t fr = 0, tot = 0;
-    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
-    const size_t avail = fr + c.ws.bytes();  // workspace buffers are reused or regrown
-    const size_t reserve = (size_t)4 << 30;
+  {
     const bool apos = alphas[0] > 0;
     const size_t F = (size_t)stage_fields2d(Solve2DOpts{n_iter, solver}, apos, N, 1);
-    // full tape (3 stages x F fields per step) + checkpoints + ~110 working fields per instance
-    const size_t per_inst = ((size_t)3 * F * std::max(n_steps, 1) + 6 + 110) * N * sizeof(double);
-    const size_t fit = avail > reserve ? (size_t)((avail - reserve) * 0.92) / per_inst : 0;
+    const size_t tape_inst = ((size_t)3 * F * std::max(n_steps, 1) + 6) * N * sizeof(double);
+    size_t fit = 0;
+    if (c.tape_budget == 0) {
+      size_t fr = 0, tot = 0;
+      cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+      const size_t avail = fr + c.ws.bytes();  // workspace buffers are reused or regrown
+      const size_t reserve = (size_t)4 << 30;
+      const size_t per_inst = tape_inst + (size_t)110 * N * sizeof(double);
+      fit = avail > reserve ? (size_t)((avail - reserve) * 0.92) / per_inst : 0;
+    } else {
+      fit = c.tape_budget / tape_inst;
+    }
     G = (int)std::max<size_t>(1, std::min<size_t>((size_t)n_inst, fit));
   }
   // balanced groups: sizes differ by at most one (workspace sized for the largest)
@@ -746,10 +754,95 @@ int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_
     h2d(c, buf + 4 * N, sigma, N);
     const double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
     Solve2DOpts o{n_iter, solver};
-    solve_elliptic2d(c, P, q, buf + 4 * N, o);
+    solve_elliptic2d(c, P, q, buf + 4 * N, o, true);  // elliptic.jl:413-427 solves for any alpha
     d2h(c, sigma, buf + 4 * N, N);
     sync(c);
   });
+}
+
+int igr2d_igr_euler_rhs(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_iter, int solver,
+                        const double* mux, const double* muy, const double* rho, const double* E, double* sigma,
+                        double* dmux, double* dmuy, double* drho, double* dE) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_solver(solver, n_iter);
+    Plan2D P = plan_single(c, d, gamma, alpha, 0.0, "eul");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:eul", 9 * N);
+    const double* in[4] = {mux, muy, rho, E};
+    for (int v = 0; v < 4; ++v) h2d(c, buf + v * N, in[v], N);
+    double* S = buf + 4 * N;
+    if (alpha > 0) h2d(c, S, sigma, N);  // warm start; alpha <= 0 sets Sigma = 0 (forward.jl:26-27)
+    const double* q[4] = {buf, buf + N, buf + 2 * N, buf + 3 * N};
+    double* k[4] = {buf + 5 * N, buf + 6 * N, buf + 7 * N, buf + 8 * N};
+    Solve2DOpts o{n_iter, solver};
+    igr_euler_rhs2d(c, P, q, S, k, o);
+    double* out[4] = {dmux, dmuy, drho, dE};
+    for (int v = 0; v < 4; ++v) d2h(c, out[v], k[v], N);
+    d2h(c, sigma, S, N);
+    sync(c);
+  });
+}
+
+int igr2d_igr_rhs(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* mux, const double* muy,
+                  const double* rho, const double* E, double* b) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    (void)E;  // the reference's argument list; R(q) does not depend on E
+    Plan2D P = plan_single(c, d, 1.4, alpha, 0.0, "igrb");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:igrb", 4 * N);
+    const double* in[3] = {mux, muy, rho};
+    for (int v = 0; v < 3; ++v) h2d(c, buf + v * N, in[v], N);
+    const double* q[4] = {buf, buf + N, buf + 2 * N, nullptr};
+    igr_rhs_diag2d(c, P, q, buf + 3 * N, nullptr);
+    d2h(c, b, buf + 3 * N, N);
+    sync(c);
+  });
+}
+
+int igr2d_sip_diagonal(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, double* M) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    Plan2D P = plan_single(c, d, 1.4, alpha, 0.0, "sipd");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:sipd", 2 * N);
+    h2d(c, buf, rho, N);
+    const double* q[4] = {nullptr, nullptr, buf, nullptr};
+    igr_rhs_diag2d(c, P, q, nullptr, buf + N);
+    d2h(c, M, buf + N, N);
+    sync(c);
+  });
+}
+
+namespace {
+int cg2d_call(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, const double* b, double* x,
+              double tol, int maxiter, bool fixed, int* iters) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (maxiter < 0) throw Error(IGR_EINVAL, fixed ? "n_iter must be >= 0" : "maxiter must be >= 0");
+    Plan2D P = plan_single(c, d, 1.4, alpha, 0.0, "cg");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi:cg", 3 * N);
+    h2d(c, buf, rho, N);
+    h2d(c, buf + N, b, N);
+    h2d(c, buf + 2 * N, x, N);
+    const int it = cg2d(c, P, buf, buf + N, buf + 2 * N, tol, maxiter, fixed);
+    d2h(c, x, buf + 2 * N, N);
+    sync(c);
+    if (iters) *iters = it;
+  });
+}
+}  // namespace
+
+int igr2d_cg_solve(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, const double* b, double* x,
+                   double tol, int maxiter, int* iters) {
+  return cg2d_call(ctx, d, alpha, rho, b, x, tol, maxiter, false, iters);
+}
+
+int igr2d_cg_fixed(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, const double* b, double* x,
+                   int n_iter) {
+  return cg2d_call(ctx, d, alpha, rho, b, x, 0.0, n_iter, true, nullptr);
 }
 
 }  // extern "C"
@@ -788,6 +881,120 @@ int igr1d_run_forward(igr_ctx* ctx, const igr_disc1d* d, double gamma, double al
     d2h(c, sigma, buf + 3 * N, N);
     sync(c);
   });
+}
+
+namespace {
+// One 1D operator evaluation on one instance through k1_ops. in: host fields
+// copied to the device slots the operation reads (q = (mu, rho, E), x, rho,
+// b, sigma); outputs copied back as the operation writes them.
+struct Op1Io {
+  const double *mu = nullptr, *rho = nullptr, *E = nullptr, *x = nullptr, *b = nullptr;
+  double* sigma = nullptr;  // in/out when set
+  const double* sigma_in = nullptr;  // read only
+  double* out[3] = {nullptr, nullptr, nullptr};
+  double* diag = nullptr;
+  double* x_out = nullptr;
+};
+int op1d_call(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, int op, int n_iter, int solver,
+              const Op1Io& io, double tol, int maxiter, bool fixed, int* iters, bool args_ok) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    if (!args_ok) throw Error(IGR_EINVAL, "null array");
+    if (!d) throw Error(IGR_EINVAL, "null discretisation");
+    check_disc1(d->p, d->xi, d->w, d->D);
+    if (op == OP1_SOLVE || op == OP1_EULER_RHS) check_solver(solver, n_iter);
+    if (op == OP1_CG && maxiter < 0) throw Error(IGR_EINVAL, fixed ? "n_iter must be >= 0" : "maxiter must be >= 0");
+    if (d->n_e < 1 || !(d->L > 0)) throw Error(IGR_EINVAL, "bad mesh");
+    BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
+    Plan1D P = make_plan1d(c, B, {Inst1DDesc{d->n_e, d->L, gamma, alpha, 0.0, 0}}, ops1d_scratch_fields, "o1");
+    const long long N = P.NG;
+    double* buf = c.ws.dbl("capi1:ops", 12 * N);
+    double* q = buf;             // mu, rho, E
+    double* xs = buf + 3 * N;    // x
+    double* rs = buf + 4 * N;    // rho (operator)
+    double* bs = buf + 5 * N;    // b
+    double* ss = buf + 6 * N;    // Sigma
+    double* os = buf + 7 * N;    // outputs (3 fields)
+    double* ds = buf + 10 * N;   // diag(A)
+    if (io.mu) h2d(c, q, io.mu, N);
+    if (io.rho) { h2d(c, q + N, io.rho, N); h2d(c, rs, io.rho, N); }
+    if (io.E) h2d(c, q + 2 * N, io.E, N);
+    if (io.x) h2d(c, xs, io.x, N);
+    if (io.b) h2d(c, bs, io.b, N);
+    if (io.sigma) h2d(c, ss, io.sigma, N);
+    if (io.sigma_in) h2d(c, ss, io.sigma_in, N);
+    Solve2DOpts o{n_iter, solver};
+    const int it = ops1d(c, P, op, o, q, rs, bs, xs, ss, os, io.diag ? ds : nullptr, tol, maxiter, fixed);
+    for (int v = 0; v < 3; ++v)
+      if (io.out[v]) d2h(c, io.out[v], os + v * N, N);
+    if (io.diag) d2h(c, io.diag, ds, N);
+    if (io.sigma) d2h(c, io.sigma, ss, N);
+    if (io.x_out) d2h(c, io.x_out, xs, N);
+    sync(c);
+    if (iters) *iters = it;
+  });
+}
+}  // namespace
+
+int igr1d_apply_sip(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* x, const double* rho, double* y) {
+  Op1Io io;
+  io.x = x; io.rho = rho; io.out[0] = y;
+  return op1d_call(ctx, d, 1.4, alpha, OP1_APPLY_SIP, 1, 0, io, 0.0, 0, false, nullptr, x && rho && y);
+}
+
+int igr1d_igr_rhs(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* mu, const double* rho, const double* E,
+                  double* b) {
+  (void)E;  // the reference's argument list; the source does not depend on E
+  Op1Io io;
+  io.mu = mu; io.rho = rho; io.out[0] = b;
+  return op1d_call(ctx, d, 1.4, alpha, OP1_IGR_RHS, 1, 0, io, 0.0, 0, false, nullptr, mu && rho && b);
+}
+
+int igr1d_sip_diagonal(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* rho, double* M) {
+  Op1Io io;
+  io.mu = rho; io.rho = rho; io.diag = M;  // the source formed on the way is discarded
+  return op1d_call(ctx, d, 1.4, alpha, OP1_IGR_RHS, 1, 0, io, 0.0, 0, false, nullptr, rho && M);
+}
+
+int igr1d_solve_elliptic(igr_ctx* ctx, const igr_disc1d* d, double alpha, int n_iter, int solver, const double* mu,
+                         const double* rho, const double* E, double* sigma) {
+  Op1Io io;
+  io.mu = mu; io.rho = rho; io.E = E; io.sigma = sigma;
+  return op1d_call(ctx, d, 1.4, alpha, OP1_SOLVE, n_iter, solver, io, 0.0, 0, false, nullptr, mu && rho && E && sigma);
+}
+
+int igr1d_hyperbolic_rhs(igr_ctx* ctx, const igr_disc1d* d, double gamma, const double* mu, const double* rho,
+                         const double* E, const double* sigma, double* dmu, double* drho, double* dE) {
+  Op1Io io;
+  io.mu = mu; io.rho = rho; io.E = E;
+  io.out[0] = dmu; io.out[1] = drho; io.out[2] = dE;
+  io.sigma_in = sigma;
+  return op1d_call(ctx, d, gamma, 0.0, OP1_HYP_RHS, 1, 0, io, 0.0, 0, false, nullptr,
+                   mu && rho && E && sigma && dmu && drho && dE);
+}
+
+int igr1d_igr_euler_rhs(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, int n_iter, int solver,
+                        const double* mu, const double* rho, const double* E, double* sigma, double* dmu, double* drho,
+                        double* dE) {
+  Op1Io io;
+  io.mu = mu; io.rho = rho; io.E = E; io.sigma = sigma;
+  io.out[0] = dmu; io.out[1] = drho; io.out[2] = dE;
+  return op1d_call(ctx, d, gamma, alpha, OP1_EULER_RHS, n_iter, solver, io, 0.0, 0, false, nullptr,
+                   mu && rho && E && sigma && dmu && drho && dE);
+}
+
+int igr1d_cg_solve(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* rho, const double* b, double* x,
+                   double tol, int maxiter, int* iters) {
+  Op1Io io;
+  io.rho = rho; io.b = b; io.x = x; io.x_out = x;
+  return op1d_call(ctx, d, 1.4, alpha, OP1_CG, 1, 0, io, tol, maxiter, false, iters, rho && b && x);
+}
+
+int igr1d_cg_fixed(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* rho, const double* b, double* x,
+                   int n_iter) {
+  Op1Io io;
+  io.rho = rho; io.b = b; io.x = x; io.x_out = x;
+  return op1d_call(ctx, d, 1.4, alpha, OP1_CG, 1, 0, io, 0.0, n_iter, true, nullptr, rho && b && x);
 }
 
 int igr1d_forward_batch(igr_ctx* ctx, int p, const double* xi, const double* w, const double* D, int n_inst,

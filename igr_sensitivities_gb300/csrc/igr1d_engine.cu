@@ -8,6 +8,7 @@
 #include <numeric>
 
 #include "igr1d_launch.h"
+#include "igr1d_ops_kernels.cuh"
 #include "igr1d_rev_kernels.cuh"
 #include "igr1d_pde_kernels.cuh"
 #include "igr1d_sens_kernels.cuh"
@@ -350,6 +351,30 @@ void pde_adjoint1d(Ctx& c, const Plan1D& P, int mode, const double* q0, const do
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
   if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
+}
+
+long long ops1d_scratch_fields(const Inst1DDesc&, int) { return E1_FIELDS + O1_FIELDS; }
+
+int ops1d(Ctx& c, const Plan1D& P, int op, const Solve2DOpts& o, const double* q, const double* rho, const double* b,
+          double* x, double* sig, double* out, double* diag, double tol, int maxiter, bool fixed) {
+  const int ni = (int)P.inst.size();
+  double* scr = c.ws.dbl("o1:scr", (size_t)std::max<long long>(P.scratch, 1));
+  int* iters = static_cast<int*>(c.ws.get("o1:iters", sizeof(int) * ni));
+  Ops1DArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.inst = P.d_inst; a.order = P.d_order; a.B = P.B;
+  a.q = q; a.rho = rho; a.b = b; a.x = x; a.sig = sig; a.out = out; a.diag = diag; a.iters = iters;
+  a.scr = scr;
+  a.op = op; a.solver = o.solver; a.n_iter = o.n_iter;
+  a.tol = tol; a.maxiter = maxiter; a.fixed = fixed ? 1 : 0;
+  a.status = c.d_status;
+  a.cs = cluster_size(c, P, o, nullptr);
+  NP1_DISPATCH(P.np, launch_1d(c, a, ni, [&](const Ops1DArgs& v, int n) { return launch_k1_ops<NPV>(v, n, c.stream); },
+                               "k1_ops launch"));
+  int it = 0;
+  if (op == OP1_CG) cuda_check(cudaMemcpyAsync(&it, iters, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "iterations");
+  cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
+  return it;
 }
 
 }  // namespace igrgpu

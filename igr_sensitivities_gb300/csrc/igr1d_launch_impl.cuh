@@ -3,6 +3,7 @@
 #pragma once
 #include "igr1d_launch.h"
 #include "igr1d_rev_kernels.cuh"
+#include "igr1d_ops_kernels.cuh"
 #include "igr1d_pde_kernels.cuh"
 #include "igr1d_sens_kernels.cuh"
 
@@ -49,10 +50,15 @@ template <int NP> cudaError_t launch_k1_pde_adjoint(const Pde1DArgs& a, int n_in
   return launch_per_instance<Pde1DArgs>(k1_pde_adjoint<NP>, a, n_inst, s);
 }
 
+template <int NP> cudaError_t launch_k1_ops(const Ops1DArgs& a, int n_inst, cudaStream_t s) {
+  return launch_per_instance<Ops1DArgs>(k1_ops<NP>, a, n_inst, s);
+}
+
 #define IGR1D_INSTANTIATE(NP)                                                          \
   template cudaError_t launch_k1_forward<NP>(const Fwd1DArgs&, int, cudaStream_t);    \
   template cudaError_t launch_k1_adjoint<NP>(const Adj1DArgs&, int, cudaStream_t);    \
   template cudaError_t launch_k1_tangent<NP>(const Tan1DArgs&, int, cudaStream_t);    \
-  template cudaError_t launch_k1_pde_adjoint<NP>(const Pde1DArgs&, int, cudaStream_t);
+  template cudaError_t launch_k1_pde_adjoint<NP>(const Pde1DArgs&, int, cudaStream_t); \
+  template cudaError_t launch_k1_ops<NP>(const Ops1DArgs&, int, cudaStream_t);
 
 }  // namespace igrgpu

@@ -179,7 +179,7 @@ __global__ void k_recip(const double* __restrict__ x, double* __restrict__ y, lo
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) y[i] = 1.0 / x[i];
 }
 
-// Per-node objective integrands (enzyme_adjoint.jl:230-385 and the nodal
+// Per-node objective integrands (IGR_adjoints_2d/enzyme_adjoint.jl:72-229 and the nodal
 // window extension). j1 = integrand, j2 = mass integrand (kinetic energy only).
 struct ObjArgs2D {
   const Inst2D* inst; int ninst; BasisDev B;
@@ -463,12 +463,13 @@ static void sum_trial_done(Ctx& c, const SumChoice& ch, double ms) {
 }
 
 // InstSum in mode 0: out[inst] = sum, and with quot
-// quot = (qnum or the sum) / ((qden or the sum) + 1e-30).
+// quot = (qnum or the sum) / ((qden or the sum) + eps), eps = 1e-30 (the
+// fixed-count solvers' guard) unless given.
 static InstSum inst_sum0(int* cnt, double* out, const double* qnum = nullptr, const double* qden = nullptr,
-                         double* quot = nullptr) {
+                         double* quot = nullptr, double eps = 1e-30) {
   InstSum s;
   std::memset(&s, 0, sizeof(s));
-  s.cnt = cnt; s.out = out; s.qnum = qnum; s.qden = qden; s.quot = quot; s.mode = 0;
+  s.cnt = cnt; s.out = out; s.qnum = qnum; s.qden = qden; s.quot = quot; s.mode = 0; s.eps = eps;
   return s;
 }
 
@@ -554,12 +555,15 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
 
 // Operator coefficients, IGR source b and diag(A) of one stage (the setup
 // part of solve_elliptic!, elliptic.jl:413-416).
-static void stage_setup(Ctx& c, const Plan2D& P, StageBuf& st) {
+// always: also for instances with alpha <= 0 (the stand-alone solve_elliptic!
+// has no alpha test; the RK stages skip the solve there, forward.jl:24-28).
+static void stage_setup(Ctx& c, const Plan2D& P, StageBuf& st, bool always = false) {
   SetupArgs2D sa;
   std::memset(&sa, 0, sizeof(sa));
   sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
   sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
   sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = st.cM;
+  sa.always = always ? 1 : 0;
   LaunchScope ls(c, KID_SETUP);
   NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, P.ntiles(), c.stream));
 }
@@ -832,10 +836,10 @@ void sensitivity2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, dou
   check_status(c);
 }
 
-void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o) {
+void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o, bool always) {
   const long long NG = P.NG;
-  if (!any_alpha_pos(P)) return;
-  check_alpha_uniform(P);
+  if (!always && !any_alpha_pos(P)) return;
+  if (!always) check_alpha_uniform(P);
   double* scratch = c.ws.dbl("sol:stage", (size_t)NG * STAGE_FIXED_FIELDS);
   StageBuf st = stage_from(scratch, NG, o, true, false, (int)P.inst.size());
   for (int v = 0; v < 4; ++v) st.q[v] = const_cast<double*>(q[v]);
@@ -843,7 +847,9 @@ void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double*
   double* x0 = c.ws.dbl("sol:x0", NG);
   cuda_check(cudaMemcpyAsync(x0, Sig, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "x0 copy");
   st.Sout = Sig;
-  stage_solve(c, P, o, st, x0, c.ws.dbl("sol:xa", NG), c.ws.dbl("sol:xb", NG), c.ws.dbl("sol:d", NG));
+  stage_setup(c, P, st, always);
+  stage_solve_b(c, P, o, st, st.b, x0, st.Sout, false, c.ws.dbl("sol:xa", NG), c.ws.dbl("sol:xb", NG),
+                c.ws.dbl("sol:d", NG));
   cuda_check(cudaStreamSynchronize(c.stream), "sync");
 }
 
@@ -862,22 +868,29 @@ void hyperbolic_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], const d
   cuda_check(cudaStreamSynchronize(c.stream), "sync");
 }
 
+// Operator coefficients of A(rho, alpha) into the stage buffer st (for any
+// alpha), its IGR source from (mx, my, rho) when mx is given (else st.b is not
+// written) and diag(A) into st.cM when set.
+static void operator_setup(Ctx& c, const Plan2D& P, StageBuf& st, const double* rho, const double* mx, const double* my) {
+  recip(c, rho, st.invr, P.NG);
+  SetupArgs2D sa;
+  std::memset(&sa, 0, sizeof(sa));
+  sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
+  sa.mx = mx; sa.my = my; sa.invr = st.invr;
+  sa.b = mx ? st.b : nullptr;
+  sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = st.cM;
+  sa.always = 1;
+  LaunchScope ls(c, KID_SETUP);
+  NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, P.ntiles(), c.stream));
+}
+
 void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, double* y) {
   const long long NG = P.NG;
   double* scratch = c.ws.dbl("sip:stage", (size_t)NG * STAGE_FIXED_FIELDS);
   Solve2DOpts o;
   StageBuf st = stage_from(scratch, NG, o, true, false, (int)P.inst.size());
-  double* zeros = c.ws.dbl("sip:zero", NG);
-  cuda_check(cudaMemsetAsync(zeros, 0, NG * sizeof(double), c.stream), "zero");
-  st.q[0] = zeros; st.q[1] = zeros; st.q[2] = const_cast<double*>(rho); st.q[3] = zeros;
-  recip(c, rho, st.invr, NG);
-  SetupArgs2D sa;
-  std::memset(&sa, 0, sizeof(sa));
-  sa.tiles = P.d_tiles; sa.inst = P.d_inst; sa.B = P.B;
-  sa.mx = st.q[0]; sa.my = st.q[1]; sa.invr = st.invr;
-  sa.b = st.b; sa.cm = st.cm; sa.ckx = st.ckx; sa.cky = st.cky; sa.cinvM = st.cinvM; sa.cpx = st.cpx; sa.cpy = st.cpy; sa.cM = nullptr;
-  sa.always = 1;
-  { LaunchScope ls(c, KID_SETUP); NP_DISPATCH(P.np, launch_k2_setup<NPV>(sa, P.ntiles(), c.stream)); }
+  st.cM = nullptr;
+  operator_setup(c, P, st, rho, nullptr, nullptr);
   ApplyArgs2D a;
   std::memset(&a, 0, sizeof(a));
   a.tiles = P.d_tiles; a.inst = P.d_inst; a.B = P.B;
@@ -885,6 +898,117 @@ void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, do
   a.y_out = y;
   { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_RESID, a, P.ntiles(), c.stream)); }
   cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void igr_rhs_diag2d(Ctx& c, const Plan2D& P, const double* const q[4], double* b, double* M) {
+  const long long NG = P.NG;
+  Solve2DOpts o;
+  StageBuf st = stage_from(c.ws.dbl("sip:stage", (size_t)NG * STAGE_FIXED_FIELDS), NG, o, true, false, (int)P.inst.size());
+  if (b) st.b = b;
+  st.cM = M;
+  operator_setup(c, P, st, q[2], b ? q[0] : nullptr, q[1]);
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void igr_euler_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, double* const k[4],
+                     const Solve2DOpts& o) {
+  check_alpha_uniform(P);
+  if (any_alpha_pos(P)) solve_elliptic2d(c, P, q, Sig, o);
+  else cuda_check(cudaMemsetAsync(Sig, 0, P.NG * sizeof(double), c.stream), "zero Sigma");  // forward.jl:26-27
+  hyperbolic_rhs2d(c, P, q, Sig, k);
+}
+
+// Conjugate gradients on A(rho, alpha) x = b with M = I: the PCG kernels
+// (k2_apply<EPI_PCG0 / EPI_PCG>, k2_pcg_update) with a field of ones as
+// M^-1, so p_0 = r_0, rz = r . r and p_{k+1} = r_{k+1} + beta_k p_k
+// (cg_fixed!, elliptic.jl:304-320, with its 1e-30 guards). Without `fixed`
+// (cg_solve!, :278-297) the guards are 0 and the loop stops before iteration
+// `it` (1-based) at the first it with sqrt(rz_{it-1}) < tol, returning it and
+// x_{it-1}; else it returns maxiter and x_maxiter. The test reads rz back
+// after every CG_CHUNK - 1 iterations, whose iterates x_k sit in a ring of
+// CG_CHUNK fields, so the stop costs no extra work beyond the chunk.
+constexpr int CG_CHUNK = 32;
+int cg2d(Ctx& c, const Plan2D& P, const double* rho, const double* b, double* x, double tol, int maxiter, bool fixed) {
+  if (P.inst.size() != 1) throw Error(1, "the CG solve takes one instance");
+  if (maxiter < 0) throw Error(1, "maxiter must be >= 0");
+  const long long NG = P.NG;
+  const int nb = P.ntiles(), n = maxiter;
+  Solve2DOpts o;
+  StageBuf st = stage_from(c.ws.dbl("cg:stage", (size_t)NG * STAGE_FIXED_FIELDS), NG, o, true, false, 1);
+  st.cM = nullptr;
+  operator_setup(c, P, st, rho, nullptr, nullptr);
+  double* ones = c.ws.dbl("cg:ones", NG);
+  { LaunchScope ls(c, KID_OTHER); k_fill<<<grid_for(NG), 256, 0, c.stream>>>(ones, 1.0, NG); }
+  double* r = c.ws.dbl("cg:r", NG);
+  double* pv[2] = {c.ws.dbl("cg:pA", NG), c.ws.dbl("cg:pB", NG)};
+  double* ap = c.ws.dbl("cg:ap", NG);
+  const int K = fixed ? 1 : CG_CHUNK;
+  double* ring = fixed ? x : c.ws.dbl("cg:xring", (size_t)NG * K);
+  double* part = c.ws.dbl("red:part", nb);
+  double* scal = c.ws.dbl("cg:scal", (size_t)pcg_scal_count(n, 1));
+  auto RZ = [&](int k) { return scal + k; };
+  auto PAP = [&](int k) { return scal + (n + 1) + k; };
+  auto AL = [&](int k) { return scal + (2 * n + 1) + k; };
+  auto BT = [&](int k) { return scal + (3 * n + 1) + k; };
+  auto XK = [&](int k) { return (fixed || k == 0) ? x : ring + (long long)((k - 1) % K) * NG; };  // x_k
+  const double eps = fixed ? 1e-30 : 0.0;
+  int* cnt = sum_choice(c, P, false).fused ? inst_counters(c, P) : nullptr;
+  ApplyArgs2D base;
+  std::memset(&base, 0, sizeof(base));
+  base.tiles = P.d_tiles; base.inst = P.d_inst; base.B = P.B;
+  base.cm = st.cm; base.ckx = st.ckx; base.cky = st.cky; base.cpx = st.cpx; base.cpy = st.cpy; base.b = b; base.cinvM = ones;
+  base.partials = part;
+  {  // r_0 = b - A x_0, p_0 = r_0, rz_0 = r_0 . r_0
+    ApplyArgs2D a = base;
+    a.x = x; a.r_out = r; a.p_out = pv[0];
+    a.isum = inst_sum0(cnt, RZ(0));
+    { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG0, a, nb, c.stream)); }
+    inst_sum_after(c, P, part, false, a.isum);
+  }
+  auto iteration = [&](int k) {
+    ApplyArgs2D a = base;
+    if (k == 0) {
+      a.x = pv[0];
+    } else {
+      a.pcg_r = r; a.pcg_p = pv[(k - 1) % 2]; a.pcg_beta = BT(k - 1);
+      a.p_out = pv[k % 2];
+    }
+    a.ap_out = ap;
+    a.isum = inst_sum0(cnt, PAP(k), RZ(k), nullptr, AL(k), eps);
+    { LaunchScope ls(c, KID_APPLY); NP_DISPATCH(P.np, launch_k2_apply<NPV>(EPI_PCG, a, nb, c.stream)); }
+    inst_sum_after(c, P, part, false, a.isum);
+    PcgUpdateArgs u;
+    u.tiles = P.d_tiles; u.groups = P.d_groups; u.inst = P.d_inst;
+    u.x_in = XK(k); u.x_out = XK(k + 1);
+    u.p = pv[k % 2]; u.ap = ap; u.r_in = r; u.r_out = r; u.cinvM = ones;
+    u.al = AL(k);
+    u.partials = part;
+    u.isum = inst_sum0(cnt, RZ(k + 1), nullptr, RZ(k), BT(k), eps);
+    { LaunchScope ls(c, KID_OTHER); NP_DISPATCH(P.np, launch_k2_pcg_update<NPV>(u, P.ngroups(), c.stream)); }
+    inst_sum_after(c, P, part, true, u.isum);
+  };
+  int iters = n;
+  if (fixed) {
+    for (int k = 0; k < n; ++k) iteration(k);
+  } else {
+    std::vector<double> rz(K);
+    int k0 = 0, stop = -1;
+    while (stop < 0 && k0 < n) {
+      const int k1 = std::min(n, k0 + K - 1);  // iterations k0 .. k1-1 keep x_k0 .. x_k1 in the ring
+      for (int k = k0; k < k1; ++k) iteration(k);
+      cuda_check(cudaMemcpyAsync(rz.data(), RZ(k0), sizeof(double) * (k1 - k0), cudaMemcpyDeviceToHost, c.stream),
+                 "rz readback");
+      cuda_check(cudaStreamSynchronize(c.stream), "sync");
+      for (int k = k0; k < k1 && stop < 0; ++k)
+        if (std::sqrt(rz[k - k0]) < tol) stop = k;
+      k0 = k1;
+    }
+    const int kx = stop >= 0 ? stop : n;
+    iters = stop >= 0 ? stop + 1 : n;
+    if (kx > 0) cuda_check(cudaMemcpyAsync(x, XK(kx), NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "x copy");
+  }
+  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+  return iters;
 }
 
 // ------------------------------------------------------------------------------------------

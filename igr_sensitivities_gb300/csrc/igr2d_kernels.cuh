@@ -139,7 +139,8 @@ __device__ __forceinline__ int first_side(int pos_across, int extent) { return p
 struct SetupArgs2D {
   const Tile2D* tiles; const Inst2D* inst; BasisDev B;
   const double *mx, *my, *invr;
-  double *b, *cm, *ckx, *cky, *cinvM, *cpx, *cpy;
+  double *b;  // IGR source (null: not formed; mx, my are then not read)
+  double *cm, *ckx, *cky, *cinvM, *cpx, *cpy;
   double *cM;  // diag(A) itself (optional; the reverse needs it for d/d alpha)
   int always;  // compute the coefficients even when alpha <= 0 (operator application on its own)
 };
@@ -172,15 +173,20 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
     for (int i = 0; i < NP; ++i) {
       const long long n = vr.base + t * NP + i;
       ir[i] = a.invr[n];
-      ux[i] = a.mx[n] * ir[i];
-      uy[i] = a.my[n] * ir[i];
-      s_ux[e][t * NP + i] = ux[i]; s_uy[e][t * NP + i] = uy[i]; s_ir[e][t * NP + i] = ir[i];
+      s_ir[e][t * NP + i] = ir[i];
+      if (a.b) {
+        ux[i] = a.mx[n] * ir[i];
+        uy[i] = a.my[n] * ir[i];
+        s_ux[e][t * NP + i] = ux[i]; s_uy[e][t * NP + i] = uy[i];
+      }
     }
     const double cxs = I.alpha * B.w[t] * I.jy * invJx;
 #pragma unroll
     for (int i = 0; i < NP; ++i) {
-      s_uxx[e][t * NP + i] = dot_row<NP>(B, i, ux) * invJx;
-      s_uyx[e][t * NP + i] = dot_row<NP>(B, i, uy) * invJx;
+      if (a.b) {
+        s_uxx[e][t * NP + i] = dot_row<NP>(B, i, ux) * invJx;
+        s_uyx[e][t * NP + i] = dot_row<NP>(B, i, uy) * invJx;
+      }
       double m = B.W2[0][i] * ir[0];
 #pragma unroll
       for (int k = 1; k < NP; ++k) m = fma(B.W2[k][i], ir[k], m);
@@ -194,7 +200,10 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
   const int t = vc.t, e = vc.e;
   double cux[NP], cuy[NP], cir[NP];
 #pragma unroll
-  for (int l = 0; l < NP; ++l) { cux[l] = s_ux[e][l * NP + t]; cuy[l] = s_uy[e][l * NP + t]; cir[l] = s_ir[e][l * NP + t]; }
+  for (int l = 0; l < NP; ++l) {
+    cir[l] = s_ir[e][l * NP + t];
+    if (a.b) { cux[l] = s_ux[e][l * NP + t]; cuy[l] = s_uy[e][l * NP + t]; }
+  }
   const double cys = I.alpha * B.w[t] * I.jx * invJy;
   const double eta = (double)(NP * NP);
   // partner 1/rho across the x faces of column t (only t == 0 or t == L) and the y faces (l == 0, l == L)
@@ -217,15 +226,17 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup(SetupArgs2D a) {
 #pragma unroll
   for (int l = 0; l < NP; ++l) {
     const long long n = vc.base + l * NP + t;
-    const double uxy = dot_row<NP>(B, l, cux) * invJy;
-    const double uyy = dot_row<NP>(B, l, cuy) * invJy;
-    const double uxx = s_uxx[e][l * NP + t], uyx = s_uyx[e][l * NP + t];
-    const double s = uxx + uyy;
-    double R = fma(s, s, uxx * uxx);
-    R = fma(2.0 * uxy, uyx, R);
-    R = fma(uyy, uyy, R);
     const int nd = l * NP + t;
-    a.b[n] = s_c[0][nd] * (I.alpha * R);
+    if (a.b) {
+      const double uxy = dot_row<NP>(B, l, cux) * invJy;
+      const double uyy = dot_row<NP>(B, l, cuy) * invJy;
+      const double uxx = s_uxx[e][l * NP + t], uyx = s_uyx[e][l * NP + t];
+      const double s = uxx + uyy;
+      double R = fma(s, s, uxx * uxx);
+      R = fma(2.0 * uxy, uyx, R);
+      R = fma(uyy, uyy, R);
+      a.b[n] = s_c[0][nd] * (I.alpha * R);
+    }
     double my_ = B.W2[0][l] * cir[0];
 #pragma unroll
     for (int k = 1; k < NP; ++k) my_ = fma(B.W2[k][l], cir[k], my_);

@@ -61,6 +61,16 @@ struct Tile2D { int inst, ex0, ey0, pad; };
 constexpr int TILE_GROUP = 4;
 struct TileGroup { int inst, first, count, pad; };
 
+// Operator-level calls of the 1D package, one evaluation per instance (k1_ops).
+enum : int {
+  OP1_APPLY_SIP = 0,  // apply_sip!, elliptic.jl:32-116: y = A(rho, alpha) x
+  OP1_IGR_RHS = 1,    // compute_igr_rhs!, elliptic.jl:126-154, and compute_sip_diagonal, :206-253
+  OP1_SOLVE = 2,      // solve_elliptic!, elliptic.jl:451-467 (Sigma warm start in, solution out)
+  OP1_HYP_RHS = 3,    // compute_hyperbolic_rhs!, hyperbolic.jl:23-83
+  OP1_EULER_RHS = 4,  // compute_igr_euler_rhs!, forward.jl:24-33
+  OP1_CG = 5          // cg_solve! / cg_fixed!, elliptic.jl:163-199 / 265-292, with apply_A! = apply_sip!
+};
+
 // Status word shared by the kernels and the host (device memory).
 enum : int { DEV_OK = 0, DEV_NONFINITE = 1 };
 
@@ -120,8 +130,9 @@ __device__ __forceinline__ double block_sum(double v, double* s_red) {
 //
 // What is done with the sum s of instance i (one thread):
 //   mode 0: out[i] = s and, with quot set,
-//           quot[i] = (qnum ? qnum[i] : s) / ((qden ? qden[i] : s) + 1e-30)
+//           quot[i] = (qnum ? qnum[i] : s) / ((qden ? qden[i] : s) + eps)
 //           (alpha_k = rz_k / (pAp_k + eps), beta_k = rz_{k+1} / (rz_k + eps));
+//           eps = 1e-30 in the fixed-count solvers, 0 in cg_solve! (elliptic.jl:292);
 //   mode 1 (reverse iteration it, ab = s): RZB[i] = -betab rz_{it+1} / (rz_it + eps)^2
 //           + ab / (pAp_it + eps), PAPB[i] = -ab rz_it / (pAp_it + eps)^2,
 //           betab = BET[i] (0 when first);
@@ -134,6 +145,7 @@ struct InstSum {
   const double *qnum, *qden;
   double* quot;
   int mode, first, it, ni;
+  double eps;        // mode 0 quotient guard
   const double *RZ, *PAP;
   double *BET, *RZB, *PAPB, *RZB1;
 };
@@ -141,7 +153,7 @@ struct InstSum {
 __device__ __forceinline__ void inst_sum_finish(const InstSum& a, int i, double s) {
   if (a.mode == 0) {
     a.out[i] = s;
-    if (a.quot) a.quot[i] = (a.qnum ? a.qnum[i] : s) / ((a.qden ? a.qden[i] : s) + 1e-30);
+    if (a.quot) a.quot[i] = (a.qnum ? a.qnum[i] : s) / ((a.qden ? a.qden[i] : s) + a.eps);
     return;
   }
   const double rz0 = a.RZ[(long long)a.it * a.ni + i];

@@ -149,8 +149,24 @@ void forward2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, int n_s
 // returned for the final state. s_gamma adds the direct dP/dgamma source.
 void sensitivity2d(Ctx& c, const Plan2D& P, double* const q[4], double* Sig, double* const s[4], double* vs, int n_steps,
                    const Solve2DOpts& o, double s_gamma);
-// One elliptic solve (solve_elliptic!, elliptic.jl:413-427) with Sigma as warm start.
-void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o);
+// One elliptic solve (solve_elliptic!, elliptic.jl:413-427) with Sigma as warm
+// start. Instances with alpha <= 0 are skipped (Sigma unchanged), as the RK
+// stages and the final solve of run_forward! do, unless `always` (the
+// stand-alone solve_elliptic!, which has no alpha test).
+void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, const Solve2DOpts& o,
+                      bool always = false);
+// compute_igr_rhs! (elliptic.jl:159-197) into b and compute_sip_diagonal
+// (elliptic.jl:205-264) into M; either may be null.
+void igr_rhs_diag2d(Ctx& c, const Plan2D& P, const double* const q[4], double* b, double* M);
+// compute_igr_euler_rhs! (forward.jl:22-31): the Sigma solve (warm start in
+// Sig, result out) when alpha > 0, else Sigma = 0; then the DG RHS into k.
+void igr_euler_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], double* Sig, double* const k[4],
+                     const Solve2DOpts& o);
+// cg_fixed! (fixed, maxiter = n_iter) or cg_solve! (tolerance tol) on
+// A(rho, alpha) x = b for one instance, x the initial guess in and the
+// solution out (elliptic.jl:278-320 with apply_A! = apply_sip!). Returns the
+// iteration count the reference returns.
+int cg2d(Ctx& c, const Plan2D& P, const double* rho, const double* b, double* x, double tol, int maxiter, bool fixed);
 // One hyperbolic RHS evaluation (compute_hyperbolic_rhs!, hyperbolic.jl:27).
 void hyperbolic_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], const double* Sig, double* const k[4]);
 // y = A x (apply_sip!, elliptic.jl:30).
@@ -203,6 +219,15 @@ long long adjoint1d_scratch_fields(const Inst1DDesc& d, int N, const Solve2DOpts
 // conservative variables): J, dq0 (same layout as q0), dgamma, dalpha.
 void adjoint1d(Ctx& c, const Plan1D& P, const double* q0, double* dq0, const Solve2DOpts& o, int objective,
                const double* prm, int seg, double* J, double* dgamma, double* dalpha);
+
+// One operator evaluation per instance of a 1D batch (k1_ops, one CTA or
+// cluster per instance): op is one of OP1_APPLY_SIP, OP1_IGR_RHS, OP1_SOLVE,
+// OP1_HYP_RHS, OP1_EULER_RHS, OP1_CG (igr1d_ops_kernels.cuh, which lists the
+// fields each reads and writes). For OP1_CG returns the first instance's
+// iteration count (cg_solve! / cg_fixed!); otherwise 0.
+long long ops1d_scratch_fields(const Inst1DDesc& d, int N);
+int ops1d(Ctx& c, const Plan1D& P, int op, const Solve2DOpts& o, const double* q, const double* rho, const double* b,
+          double* x, double* sig, double* out, double* diag, double tol, int maxiter, bool fixed);
 
 // ---- continuous adjoint (IGR_adjoints_2d/adjoint_pde.jl, forward.jl:111-158) ----
 // Snapshot k of the forward store: 5 fields of NG doubles (mux, muy, rho, E,

@@ -6,44 +6,28 @@ directional derivative dJ/dA of an initial-condition amplitude two ways,
   adjoint  <a, dq0/dA>_M   (continuous PDE adjoint at t = 0, M the nodal mass)
   FD       (J(A + eps) - J(A - eps)) / (2 eps)   (central difference of run_forward)
 
-and their relative difference, the OtD gap. Everything stays on the GPU: the
+and their relative difference, the OtD gap. The arithmetic runs on the GPU: the
 three initial states (A, A + eps, A - eps) are built in one launch, the store +
-adjoint runs with device-resident snapshots, and both FD forwards advance as
-one batch.
+adjoint runs with device-resident snapshots, both FD forwards advance as one
+batch and the objectives are evaluated by the engine; the host forms the
+inner product <a, dq0/dA>_M and the difference quotient from the returned
+arrays.
 """
 import numpy as np
 
-from . import (CartesianMesh2D, DGBasis, adjoint_conservative_batch, build_ic_batch, default_context, forward_batch)
+from . import (CartesianMesh2D, DGBasis, adjoint_conservative_batch, build_ic_batch, default_context, forward_batch,
+               objective_value)
 from .workloads import max_wavespeed_2d
 
-KE_WINDOW = (0.55, 0.50, 0.15)  # IGR_adjoints_2d/enzyme_adjoint.jl:26
 
-
-def objective_at(q, objective, basis, mesh, gamma, obj_params=None):
-    """J of a state q (4, N) by nodal quadrature (the objective tails of
-    IGR_adjoints_2d/enzyme_adjoint.jl and window_rho2)."""
-    mx, my, rho, E = (np.asarray(a).reshape(mesh.x.shape, order="F") for a in q)
-    m = np.outer(basis.w, basis.w)[:, :, None, None] * mesh.Jx * mesh.Jy
-    x, y = mesh.x, mesh.y
-    key = objective.lstrip(":")
-    if key == "kinetic_energy":
-        return float(np.sum(m * (mx ** 2 + my ** 2) / (2 * rho)) / np.sum(m * rho))
-    if key == "windowed_kinetic_energy":
-        xc, yc, s = KE_WINDOW
-        w = np.exp(-((x - xc) ** 2 + (y - yc) ** 2) / s ** 2)
-        return float(np.sum(m * w * (mx ** 2 + my ** 2) / (2 * rho)))
-    if key == "l2_density":
-        return float(np.sum(m * rho ** 2))
-    if key == "l2_pressure":
-        P = (gamma - 1) * (E - (mx ** 2 + my ** 2) / (2 * rho))
-        return float(np.sum(m * P ** 2))
-    if key == "weighted_momentum":
-        return float(np.sum(m * mx * np.sin(2 * np.pi * x / mesh.Lx) * np.sin(2 * np.pi * y / mesh.Ly)))
-    if key == "window_rho2":
-        a, b, s = obj_params
-        chi = (x >= a) & (x <= a + s) & (y >= b) & (y <= b + s)
-        return float(np.sum(m * rho ** 2 * chi))
-    raise ValueError("Unknown objective: %s" % objective)
+def objective_at(q, objective, basis, mesh, gamma, obj_params=None, ctx=None):
+    """J of a state q (4, N) by the engine's nodal quadrature on the GPU (the
+    objective tails of IGR_adjoints_2d/enzyme_adjoint.jl:72-229, and
+    window_rho2): igr2d_objective with zero steps."""
+    shape = mesh.x.shape
+    st = [np.asarray(a).reshape(shape, order="F") for a in q]
+    return objective_value(*st, 0, 0.0, basis, mesh, gamma, 0.0, n_iter=1, solver="pcg", objective=objective,
+                           obj_params=obj_params, ctx=ctx)
 
 
 def otd_gap(ic_type, A, N_e, p=4, L=1.0, gamma=1.4, T=0.10, CFL=0.4, alpha=3.0 * (1.0 / 20) ** 2, n_iter=60,
@@ -64,8 +48,8 @@ def otd_gap(ic_type, A, N_e, p=4, L=1.0, gamma=1.4, T=0.10, CFL=0.4, alpha=3.0 *
     adj = float(np.sum(m * np.sum(a * dq, axis=0)))
     qT, _ = forward_batch(q3[1:], [gamma] * 2, [alpha] * 2, [T / n_fwd] * 2, n_fwd, basis, mesh, n_iter=n_iter,
                           solver=solver, final_solve=False, ctx=ctx)
-    fd = (objective_at(qT[0], objective, basis, mesh, gamma, obj_params) -
-          objective_at(qT[1], objective, basis, mesh, gamma, obj_params)) / (2 * eps)
+    fd = (objective_at(qT[0], objective, basis, mesh, gamma, obj_params, ctx) -
+          objective_at(qT[1], objective, basis, mesh, gamma, obj_params, ctx)) / (2 * eps)
     return L / N_e, abs(adj - fd) / max(abs(fd), 1e-30), adj, fd
 
 

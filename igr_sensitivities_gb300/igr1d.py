@@ -15,7 +15,8 @@ from ._lib import check, default_context, lib
 __all__ = ["DGBasis", "PeriodicMesh1D", "run_forward", "run_forward_", "forward_batch", "run_sensitivity",
            "enzyme_adjoint_ic", "enzyme_dJ_dA", "adjoint_batch", "IC_BUILDERS", "ic_dA_weights",
            "Snapshots1D", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
-           "adjoint_conservative_batch", "build_ic_batch", "IC_TYPES"]
+           "adjoint_conservative_batch", "build_ic_batch", "IC_TYPES", "apply_sip_", "compute_igr_rhs_",
+           "compute_sip_diagonal", "solve_elliptic_", "compute_hyperbolic_rhs_", "compute_igr_euler_rhs_"]
 
 
 class _Disc1D(C.Structure):
@@ -88,6 +89,84 @@ def forward_batch(states, basis, n_e, L, gammas, alphas, dts, n_steps, n_iter=10
         o3 += 3 * n
         o1 += n
     return out
+
+
+# ----------------------------------------------------------------------------- operator-level calls
+def apply_sip_(y, x, rho, basis, mesh, alpha, ctx=None):
+    """apply_sip! (IGR_adjoints_1d/elliptic.jl:32-116): y = A(rho, alpha) x."""
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    out = np.zeros(n)
+    check(ctx, lib().igr1d_apply_sip(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(alpha), _ptr(_flat(x, n)),
+                                     _ptr(_flat(rho, n)), _ptr(out)))
+    y[...] = out.reshape(shape, order="F")
+
+
+def compute_igr_rhs_(b, mu, rho, E, basis, mesh, alpha, ctx=None):
+    """compute_igr_rhs! (IGR_adjoints_1d/elliptic.jl:126-154): b = w_i J 2 alpha (d_x u)^2."""
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    out = np.zeros(n)
+    check(ctx, lib().igr1d_igr_rhs(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(alpha),
+                                   *[_ptr(_flat(a, n)) for a in (mu, rho, E)], _ptr(out)))
+    b[...] = out.reshape(shape, order="F")
+
+
+def compute_sip_diagonal(rho, basis, mesh, alpha, ctx=None):
+    """compute_sip_diagonal (IGR_adjoints_1d/elliptic.jl:206-253): diag(A) as a new array."""
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    out = np.zeros(n)
+    check(ctx, lib().igr1d_sip_diagonal(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(alpha),
+                                        _ptr(_flat(rho, n)), _ptr(out)))
+    return np.asfortranarray(out.reshape(shape, order="F"))
+
+
+def solve_elliptic_(Sigma, mu, rho, E, basis, mesh, alpha, n_iter=10, solver="pcg", ctx=None):
+    """solve_elliptic! (IGR_adjoints_1d/elliptic.jl:446-467); Sigma is the warm start and the result."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    S = _flat(Sigma, n).copy()
+    check(ctx, lib().igr1d_solve_elliptic(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(alpha), C.c_int(n_iter),
+                                          C.c_int(_solver(solver)), *[_ptr(_flat(a, n)) for a in (mu, rho, E)],
+                                          _ptr(S)))
+    Sigma[...] = S.reshape(shape, order="F")
+
+
+def compute_hyperbolic_rhs_(dmu, drho, dE, mu, rho, E, Sigma, basis, mesh, gamma, ctx=None):
+    """compute_hyperbolic_rhs! (IGR_adjoints_1d/hyperbolic.jl:23-83)."""
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    out = [np.zeros(n) for _ in range(3)]
+    check(ctx, lib().igr1d_hyperbolic_rhs(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(gamma),
+                                          *[_ptr(_flat(a, n)) for a in (mu, rho, E, Sigma)], *[_ptr(a) for a in out]))
+    for dst, src in zip((dmu, drho, dE), out):
+        dst[...] = src.reshape(shape, order="F")
+
+
+def compute_igr_euler_rhs_(dmu, drho, dE, mu, rho, E, Sigma, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",
+                           ctx=None):
+    """compute_igr_euler_rhs! (IGR_adjoints_1d/forward.jl:17-33): the Sigma solve
+    (warm start in Sigma, result out) when alpha > 0, else Sigma = 0; then the
+    hyperbolic RHS at (q, Sigma)."""
+    _solver(solver)  # validate before touching the device
+    ctx = ctx or default_context()
+    shape = _shape(basis, mesh)
+    n = int(np.prod(shape))
+    S = _flat(Sigma, n).copy()
+    out = [np.zeros(n) for _ in range(3)]
+    check(ctx, lib().igr1d_igr_euler_rhs(ctx.handle, C.byref(_disc1d(basis, mesh)), C.c_double(gamma),
+                                         C.c_double(alpha), C.c_int(n_iter), C.c_int(_solver(solver)),
+                                         *[_ptr(_flat(a, n)) for a in (mu, rho, E)], _ptr(S), *[_ptr(a) for a in out]))
+    for dst, src in zip((dmu, drho, dE), out):
+        dst[...] = src.reshape(shape, order="F")
+    Sigma[...] = S.reshape(shape, order="F")
 
 
 # ----------------------------------------------------------------------------- initial conditions

@@ -4,8 +4,7 @@
  *
  * Every entry point is a drop-in for one function of the reference's Julia
  * module API (IGRAdjoints2D / IGRAdjoints1D); the file:line of the function
- * it replaces is given beside it. A Julia `ccall` binding for each is shown in
- * INTEGRATION.md.
+ * it replaces is given beside it.
  *
  * Conventions
  *  - Arrays are caller-owned host arrays of double in the reference's Julia
@@ -44,14 +43,14 @@ typedef enum {
 
 typedef struct igr_ctx igr_ctx;
 
-/* Objectives of enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:398-412)
+/* Objectives of enzyme_adjoint_ic (enzyme_objective_fn, IGR_adjoints_2d/enzyme_adjoint.jl:240-254)
  * plus nodal-window extensions. */
 typedef enum {
-  IGR_OBJ_L2_DENSITY = 0,          /* :l2_density, enzyme_adjoint.jl:206 */
-  IGR_OBJ_L2_PRESSURE = 1,         /* :l2_pressure, enzyme_adjoint.jl:242 */
-  IGR_OBJ_KINETIC_ENERGY = 2,      /* :kinetic_energy, enzyme_adjoint.jl:279 */
-  IGR_OBJ_WINDOWED_KE = 3,         /* :windowed_kinetic_energy, enzyme_adjoint.jl:318 */
-  IGR_OBJ_WEIGHTED_MOMENTUM = 4,   /* :weighted_momentum, enzyme_adjoint.jl:357 */
+  IGR_OBJ_L2_DENSITY = 0,          /* :l2_density, enzyme_adjoint.jl:48-82 */
+  IGR_OBJ_L2_PRESSURE = 1,         /* :l2_pressure, enzyme_adjoint.jl:84-119 */
+  IGR_OBJ_KINETIC_ENERGY = 2,      /* :kinetic_energy, enzyme_adjoint.jl:121-156 */
+  IGR_OBJ_WINDOWED_KE = 3,         /* :windowed_kinetic_energy, enzyme_adjoint.jl:160-195 */
+  IGR_OBJ_WEIGHTED_MOMENTUM = 4,   /* :weighted_momentum, enzyme_adjoint.jl:199-229 */
   IGR_OBJ_WINDOW_RHO2 = 5,         /* sum w_i w_j Jx Jy rho^2 over nodes inside the square
                                       [x0, x0+s] x [y0, y0+s]; obj_params = {x0, y0, s} */
   IGR_OBJ_INTERVAL_RHO = 6         /* 1D: sum w_i J rho over nodes in [a, b]; obj_params = {a, b} */
@@ -84,7 +83,9 @@ int igr_ctx_create(int device, igr_ctx** out);
 int igr_ctx_destroy(igr_ctx* ctx);
 const char* igr_last_error(const igr_ctx* ctx);
 /* Device bytes the adjoint may use for its tape; 0 (default) = most of the
- * free memory. A smaller budget turns on segment checkpointing. */
+ * free memory. A batch runs as groups of instances whose full tapes fit the
+ * budget together; an instance whose tape alone exceeds it runs by itself
+ * with segment checkpointing. */
 int igr_set_tape_budget(igr_ctx* ctx, size_t bytes);
 /* 1D: CTAs that advance one instance (a thread-block cluster when > 1):
  * 0 (default) = chosen per launch (small batches spread each instance over up
@@ -159,7 +160,7 @@ int igr2d_sensitivity_batch(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const
                             const double* dts, int n_steps, int n_iter, int solver, double s_gamma, double* q,
                             double* s, double* sigma, double* varsigma);
 
-/* enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:428-454): J and
+/* enzyme_adjoint_ic (IGR_adjoints_2d/enzyme_adjoint.jl:270-296): J and
  * dJ/dq0 of the objective after n_steps SSP-RK3 steps of size dt (no dt
  * re-rounding, Sigma warm start from zero). dgamma/dalpha (may be NULL) are
  * dJ/dgamma and dJ/dalpha, which the reference does not compute. */
@@ -205,9 +206,41 @@ int igr2d_hyperbolic_rhs(igr_ctx* ctx, const igr_disc2d* d, double gamma, const 
                          double* drho, double* dE);
 
 /* solve_elliptic! (IGR_adjoints_2d/elliptic.jl:413-427): sigma is the warm
- * start on entry and the solution on exit. */
+ * start on entry and the solution on exit (for any alpha, as the reference's
+ * solve has no alpha test). */
 int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_iter, int solver,
                          const double* mux, const double* muy, const double* rho, const double* E, double* sigma);
+
+/* compute_igr_euler_rhs! (IGR_adjoints_2d/forward.jl:15-31, both methods):
+ * the full IGR Euler operator. When alpha > 0, sigma is the warm start of one
+ * solve_elliptic! and holds its result on return; otherwise sigma is set to
+ * zero. Then (dmux, dmuy, drho, dE) = compute_hyperbolic_rhs! at
+ * (mux, muy, rho, E, sigma). */
+int igr2d_igr_euler_rhs(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, int n_iter, int solver,
+                        const double* mux, const double* muy, const double* rho, const double* E, double* sigma,
+                        double* dmux, double* dmuy, double* drho, double* dE);
+
+/* compute_igr_rhs! (IGR_adjoints_2d/elliptic.jl:159-197): the IGR source b
+ * = w_i w_j Jx Jy alpha [(u_x + v_y)^2 + u_x^2 + 2 u_y v_x + v_y^2]. E is part
+ * of the reference's argument list and is not read. */
+int igr2d_igr_rhs(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* mux, const double* muy,
+                  const double* rho, const double* E, double* b);
+
+/* compute_sip_diagonal (IGR_adjoints_2d/elliptic.jl:205-264): M = diag(A). */
+int igr2d_sip_diagonal(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, double* M);
+
+/* cg_solve! (IGR_adjoints_2d/elliptic.jl:278-297) with apply_A! = apply_sip!
+ * at (rho, alpha), as the reference's manufactured-solution test calls it
+ * (tests/run_euler_test.jl:64-65): unpreconditioned CG from the initial guess
+ * x (solution on return) that stops before iteration `it` (1-based) at the
+ * first it with sqrt(r.r) < tol; *iters = that it, or maxiter. */
+int igr2d_cg_solve(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, const double* b, double* x,
+                   double tol, int maxiter, int* iters);
+
+/* cg_fixed! (IGR_adjoints_2d/elliptic.jl:304-320) with apply_A! = apply_sip!:
+ * n_iter CG iterations with the reference's 1e-30 guards, x in place. */
+int igr2d_cg_fixed(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double* rho, const double* b, double* x,
+                   int n_iter);
 
 /* y = A(rho, alpha) x like igr2d_apply_sip, for callers that cannot let this
  * library allocate device memory: hosts whose GPU memory belongs to another
@@ -217,9 +250,13 @@ int igr2d_solve_elliptic(igr_ctx* ctx, const igr_disc2d* d, double alpha, int n_
  * pointers; stream may be NULL (default stream); the call returns after the
  * result is complete. It allocates nothing: its scratch is a fixed device
  * array of about 4.8 MB, so it accepts at most 65,536 nodes
- * ((p+1)^2 n_ex n_ey) and returns IGR_EINVAL above that. All calls share that
- * array, so calls that overlap on the GPU race. The first call on each device
- * looks up the array's address; make it before any stream capture. */
+ * ((p+1)^2 n_ex n_ey, any mesh shape) and returns IGR_EINVAL above that. All
+ * calls share that array, so calls that overlap on the GPU race. With CUDA's
+ * lazy module loading the first call on each device loads the library's
+ * kernels there, which reserves the array then: make that first call during
+ * set-up. The first call on each device (and the first after the device's
+ * context was reset) looks up the array's address; make it before any stream
+ * capture. */
 int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const double* x_dev, const double* rho_dev,
                             double* y_dev, void* stream);
 
@@ -296,6 +333,42 @@ int igr2d_adjoint_rhs_conservative(igr_ctx* ctx, const igr_disc2d* d, double gam
  * State ordering (mu, rho, E) as IGR_adjoints_1d/euler.jl:23. */
 int igr1d_run_forward(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, double dt, double t_end,
                       int n_iter, int solver, double* mu, double* rho, double* E, double* sigma);
+
+/* apply_sip! (IGR_adjoints_1d/elliptic.jl:32-116): y = A(rho, alpha) x. */
+int igr1d_apply_sip(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* x, const double* rho, double* y);
+
+/* compute_igr_rhs! (IGR_adjoints_1d/elliptic.jl:126-154): b = w_i J 2 alpha
+ * (d_x u)^2. E is part of the reference's argument list and is not read. */
+int igr1d_igr_rhs(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* mu, const double* rho,
+                  const double* E, double* b);
+
+/* compute_sip_diagonal (IGR_adjoints_1d/elliptic.jl:206-253): M = diag(A). */
+int igr1d_sip_diagonal(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* rho, double* M);
+
+/* solve_elliptic! (IGR_adjoints_1d/elliptic.jl:446-467): sigma is the warm
+ * start on entry and the solution on exit. */
+int igr1d_solve_elliptic(igr_ctx* ctx, const igr_disc1d* d, double alpha, int n_iter, int solver, const double* mu,
+                         const double* rho, const double* E, double* sigma);
+
+/* compute_hyperbolic_rhs! (IGR_adjoints_1d/hyperbolic.jl:23-83). */
+int igr1d_hyperbolic_rhs(igr_ctx* ctx, const igr_disc1d* d, double gamma, const double* mu, const double* rho,
+                         const double* E, const double* sigma, double* dmu, double* drho, double* dE);
+
+/* compute_igr_euler_rhs! (IGR_adjoints_1d/forward.jl:17-33, both methods):
+ * sigma is the warm start and result of one solve when alpha > 0, else set to
+ * zero; then (dmu, drho, dE) = compute_hyperbolic_rhs! at (mu, rho, E, sigma). */
+int igr1d_igr_euler_rhs(igr_ctx* ctx, const igr_disc1d* d, double gamma, double alpha, int n_iter, int solver,
+                        const double* mu, const double* rho, const double* E, double* sigma, double* dmu, double* drho,
+                        double* dE);
+
+/* cg_solve! (IGR_adjoints_1d/elliptic.jl:163-199) with apply_A! = apply_sip!
+ * at (rho, alpha) (tests/run_euler_test.jl:160-161); as igr2d_cg_solve. */
+int igr1d_cg_solve(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* rho, const double* b, double* x,
+                   double tol, int maxiter, int* iters);
+
+/* cg_fixed! (IGR_adjoints_1d/elliptic.jl:265-292) with apply_A! = apply_sip!. */
+int igr1d_cg_fixed(igr_ctx* ctx, const igr_disc1d* d, double alpha, const double* rho, const double* b, double* x,
+                   int n_iter);
 
 /* Batched 1D forward: n_inst instances sharing the basis (p, xi, w, D), each
  * with its own n_e, L, gamma, alpha, dt and step count, advanced in one

@@ -401,7 +401,7 @@ void run_forward(const Grid2D& G, T* const q[4], T* Sig, double dt, double T_end
 }
 
 // ---------------------------------------------------------------------------
-// Objectives (enzyme_adjoint.jl:206-387) plus the nodal-window extensions.
+// Objectives (enzyme_adjoint.jl:48-229) plus the nodal-window extensions.
 // ---------------------------------------------------------------------------
 enum Objective2D {
   OBJ_L2_DENSITY = 0, OBJ_L2_PRESSURE = 1, OBJ_KINETIC_ENERGY = 2, OBJ_WINDOWED_KE = 3,
@@ -454,7 +454,7 @@ T objective2d(const Grid2D& G, int obj, const T* const q[4], const T& g, const d
   return J;
 }
 
-// Inlined SSP-RK3 objective loop of enzyme_adjoint.jl:206-235 (no dt re-rounding,
+// Inlined SSP-RK3 objective loop of enzyme_adjoint.jl:56-71 (no dt re-rounding,
 // Sigma warm start from zero). Leaves the final state in q.
 template <class T>
 T objective_run(const Grid2D& G, int obj, T* const q[4], int n_steps, double dt, const T& g, const T& alpha, int n_iter, int solver, const double* prm) {

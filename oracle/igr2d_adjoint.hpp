@@ -1,7 +1,7 @@
 // ORACLE — test infrastructure only (see igr_common.hpp for the parity status).
 // Hand-written discrete adjoint (reverse mode) of the 2D IGR-Euler map that
 // IGR_adjoints_2d/enzyme_adjoint.jl:270-296 differentiates with Enzyme:
-// J(q_T) after n_steps inlined SSP-RK3 steps (enzyme_adjoint.jl:206-235), with
+// J(q_T) after n_steps inlined SSP-RK3 steps (enzyme_adjoint.jl:56-71), with
 // the gradient taken w.r.t. the initial conservative state q0 and, as an
 // extension the reference lacks, w.r.t. gamma and alpha.
 //

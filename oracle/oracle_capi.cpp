@@ -270,6 +270,41 @@ int orc1d_apply_sip(GRID1D_ARGS, double alpha, const double* x, const double* rh
   return guard([&] { Grid1D G = GRID1D; apply_sip1d(G, y, x, rho, alpha); });
 }
 
+int orc1d_igr_rhs(GRID1D_ARGS, double alpha, const double* mu, const double* rho, double* b) {
+  return guard([&] { Grid1D G = GRID1D; igr_rhs1d(G, b, mu, rho, alpha); });
+}
+
+int orc1d_sip_diagonal(GRID1D_ARGS, double alpha, const double* rho, double* M) {
+  return guard([&] { Grid1D G = GRID1D; sip_diagonal1d(G, M, rho, alpha); });
+}
+
+int orc1d_solve_elliptic(GRID1D_ARGS, double alpha, int n_iter, int solver, const double* mu, const double* rho,
+                         const double* E, double* Sig) {
+  return guard([&] {
+    Grid1D G = GRID1D; const double* q[3] = {mu, rho, E};
+    Work2D<double> W; W.alloc(G.N); solve_elliptic1d(G, Sig, q, alpha, n_iter, solver, W);
+  });
+}
+
+int orc1d_igr_euler_rhs(GRID1D_ARGS, double gamma, double alpha, int n_iter, int solver, const double* mu,
+                        const double* rho, const double* E, double* Sig, double* dmu, double* drho, double* dE) {
+  return guard([&] {
+    Grid1D G = GRID1D; const double* q[3] = {mu, rho, E};
+    Work2D<double> W; W.alloc(G.N); igr_euler_rhs1d(G, q, Sig, gamma, alpha, n_iter, solver, W);
+    double* out[3] = {dmu, drho, dE};
+    for (int v = 0; v < 3; ++v) std::memcpy(out[v], W.dq[v].data(), G.N * sizeof(double));
+  });
+}
+
+// cg_solve! (tol exit) or cg_fixed! (fixed=1) on A x = b with A = SIP(rho, alpha), IGR_adjoints_1d/elliptic.jl:163-292.
+int orc1d_cg(GRID1D_ARGS, double alpha, const double* rho, const double* b, double* x, double tol, int maxiter, int fixed,
+             int* iters) {
+  return guard([&] {
+    Grid1D G = GRID1D; Work2D<double> W; W.alloc(G.N);
+    *iters = cg_solve(G, x, b, rho, alpha, tol, maxiter, fixed != 0, W);
+  });
+}
+
 int orc1d_run_forward(GRID1D_ARGS, double gamma, double alpha, double dt, double T_end, int n_iter, int solver,
                       double* mu, double* rho, double* E, double* Sig) {
   return guard([&] {

@@ -283,6 +283,42 @@ def apply_sip_1d(G, alpha, x, rho):
     return y
 
 
+def igr_rhs_1d(G, alpha, mu, rho):
+    b = np.zeros(G.N)
+    _check(lib().orc1d_igr_rhs(*G.args(), C.c_double(alpha), _p(_f(mu)), _p(_f(rho)), _p(b)))
+    return b
+
+
+def sip_diagonal_1d(G, alpha, rho):
+    M = np.zeros(G.N)
+    _check(lib().orc1d_sip_diagonal(*G.args(), C.c_double(alpha), _p(_f(rho)), _p(M)))
+    return M
+
+
+def solve_elliptic_1d(G, alpha, n_iter, solver, q, Sig0):
+    Sig = _f(Sig0).copy()
+    _check(lib().orc1d_solve_elliptic(*G.args(), C.c_double(alpha), C.c_int(n_iter), C.c_int(SOLVERS.get(solver, -1)),
+                                      *[_p(_f(a)) for a in q], _p(Sig)))
+    return Sig
+
+
+def igr_euler_rhs_1d(G, gamma, alpha, n_iter, solver, q, Sig0):
+    Sig = _f(Sig0).copy()
+    out = [np.zeros(G.N) for _ in range(3)]
+    _check(lib().orc1d_igr_euler_rhs(*G.args(), C.c_double(gamma), C.c_double(alpha), C.c_int(n_iter),
+                                     C.c_int(SOLVERS.get(solver, -1)), *[_p(_f(a)) for a in q], _p(Sig),
+                                     *[_p(a) for a in out]))
+    return out, Sig
+
+
+def cg_1d(G, alpha, rho, b, x0, tol=1e-13, maxiter=1000, fixed=False):
+    x = _f(x0).copy()
+    it = C.c_int(0)
+    _check(lib().orc1d_cg(*G.args(), C.c_double(alpha), _p(_f(rho)), _p(_f(b)), _p(x), C.c_double(tol),
+                          C.c_int(maxiter), C.c_int(int(fixed)), C.byref(it)))
+    return x, it.value
+
+
 def run_forward_1d(G, gamma, alpha, dt, T, n_iter, solver, q0):
     q = [_f(a).copy() for a in q0]
     Sig = np.zeros(G.N)

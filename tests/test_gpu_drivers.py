@@ -14,8 +14,6 @@ PRM3 = [1.0, 0.09, 3, 0.30, 0.34, 6.0, 0.70, 0.40, 5.0, 0.52, 0.74, 5.5, 0, 0, 0
 
 
 def oracle_gap(igr, oracle, ic, A, Ne, p, T, alpha, nit, objective, eps, prm, g=1.4, CFL=0.4):
-    basis = igr.DGBasis(p)
-    mesh = igr.CartesianMesh2D(Ne, Ne, 1.0, 1.0, basis)
     G = oracle.Grid2D(p, Ne, Ne)
     qs = [oracle.build_ic_2d(G, ic, g, a, prm) for a in (A, A + eps, A - eps)]
     dt = CFL * min(G.dx, G.dy) / ((2 * p + 1) * max_wavespeed_2d(*qs[0], g))
@@ -27,7 +25,7 @@ def oracle_gap(igr, oracle, ic, A, Ne, p, T, alpha, nit, objective, eps, prm, g=
     J = []
     for q in qs[1:]:
         qT, _ = oracle.run_forward_2d(G, g, alpha, dt, T, nit, "pcg", q)
-        J.append(drivers.objective_at(qT, objective, basis, mesh, g))
+        J.append(oracle.objective_run_2d(G, g, alpha, 0, dt, nit, "pcg", objective, qT))  # J(q_T) on the CPU
     fd = (J[0] - J[1]) / (2 * eps)
     return adj, fd
 

@@ -45,6 +45,22 @@ def test_apply_sip_noalloc_matches_regular_entry_point_twice(igr):
         assert np.linalg.norm(y - ref) <= 1e-13 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("p,nex,ney", [(1, 1, 16384), (1, 16384, 1), (4, 20, 16), (2, 3, 500)])
+def test_apply_sip_noalloc_any_mesh_under_the_node_limit(igr, p, nex, ney):
+    # the node count is the only limit: P1 one element wide (4,096 tiles, 65,536 nodes) and other degrees
+    basis = igr.DGBasis(p)
+    mesh = igr.CartesianMesh2D(nex, ney, 1.0, 1.0, basis)
+    rng = np.random.default_rng(p + nex)
+    x = rng.standard_normal(mesh.x.shape)
+    rho = 0.5 + 1.5 * rng.random(mesh.x.shape)
+    rc, y = _call(igr, basis, mesh, 4e-3, x, rho)
+    assert rc == 0
+    ref = np.zeros(mesh.x.shape, order="F")
+    igr.apply_sip_(ref, x, rho, basis, mesh, 4e-3)
+    ref = ref.reshape(-1, order="F")
+    assert np.linalg.norm(y - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
 def test_apply_sip_noalloc_rejects_oversize(igr):
     basis = igr.DGBasis(3)
     mesh = igr.CartesianMesh2D(65, 64, 1.0, 1.0, basis)  # 66,560 nodes > 65,536
