@@ -253,10 +253,34 @@ void sip_diagonal(const Grid2D& G, T* M, const T* rho, const T& alpha) {
   }
 }
 
+// Summation order of dotv: 0 = sequential (the default), 1 = reversed, 2 =
+// pairwise (a binary tree over halves). The tests switch orders to measure how
+// far a result moves under a change of inner-product summation order alone,
+// the size of the difference between two correct implementations (the GPU
+// sums in a fixed tree order).
+inline int& dot_order() { static int o = 0; return o; }
+
+template <class T> inline T dot_pairwise(const T* a, const T* b, size_t n) {
+  if (n <= 8) {
+    T s(0.0);
+    for (size_t k = 0; k < n; ++k) s = s + a[k] * b[k];
+    return s;
+  }
+  const size_t h = n / 2;
+  return dot_pairwise(a, b, h) + dot_pairwise(a + h, b + h, n - h);
+}
+
 template <class T> inline T dotv(const T* a, const T* b, size_t n) {
   // LinearAlgebra.dot on Vector{Float64} is a BLAS ddot in the reference; the
   // summation order there is implementation-defined, here it is sequential.
-  T s(0.0); for (size_t k = 0; k < n; ++k) s = s + a[k] * b[k]; return s;
+  if (dot_order() == 2) return dot_pairwise(a, b, n);
+  T s(0.0);
+  if (dot_order() == 1) {
+    for (size_t k = n; k-- > 0;) s = s + a[k] * b[k];
+  } else {
+    for (size_t k = 0; k < n; ++k) s = s + a[k] * b[k];
+  }
+  return s;
 }
 
 // Workspace for the solvers and the RK loop.

@@ -35,6 +35,13 @@ extern "C" {
 
 const char* orc_last_error() { return g_err.c_str(); }
 
+// Inner-product summation order of the solvers: 0 sequential (default), 1 reversed, 2 pairwise.
+int orc_set_dot_order(int order) {
+  if (order < 0 || order > 2) return 1;
+  dot_order() = order;
+  return 0;
+}
+
 int orc_basis(int p, double* xi, double* w, double* Dcol) {
   return guard([&] {
     Basis b = make_basis(p);

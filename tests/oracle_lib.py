@@ -51,6 +51,13 @@ def _check(rc):
         raise (ValueError if rc == 1 else RuntimeError)(msg)
 
 
+def set_dot_order(order):
+    """Summation order of the oracle's solver inner products: 0 sequential (the
+    default), 1 reversed, 2 pairwise (to measure a result's sensitivity to that
+    order)."""
+    _check(lib().orc_set_dot_order(C.c_int(order)))
+
+
 def basis(p):
     n = p + 1
     xi = np.zeros(n)

@@ -25,7 +25,7 @@ def oracle_gap(igr, oracle, ic, A, Ne, p, T, alpha, nit, objective, eps, prm, g=
     J = []
     for q in qs[1:]:
         qT, _ = oracle.run_forward_2d(G, g, alpha, dt, T, nit, "pcg", q)
-        J.append(oracle.objective_run_2d(G, g, alpha, 0, dt, nit, "pcg", objective, qT))  # J(q_T) on the CPU
+        J.append(oracle.objective_run_2d(G, g, alpha, 0, dt, nit, "pcg", objective, qT)[0])  # J(q_T) on the CPU
     fd = (J[0] - J[1]) / (2 * eps)
     return adj, fd
 

@@ -12,8 +12,13 @@ step count the oracle finishes in seconds (OpenMP over instances):
       separate-launch inner products), 2 steps
   2D 128^2 P3 forward, PCG 60, 3 of 500 steps
   1D N_e = 256 P3 forward, Jacobi 50, the whole T = 0.1
-Tolerances (relative L2): forward state and Sigma 1e-11, gradients 1e-9,
-J 1e-11, dJ/dgamma and dJ/dalpha 1e-9.
+Tolerances (relative L2): forward state and Sigma 1e-11 (Sigma of the PCG-60
+forward: 3x the oracle's own change under a one-ulp input perturbation,
+which is larger), gradients 1e-9,
+J 1e-11, dJ/dgamma and dJ/dalpha 1e-9 (of the value, or of J / parameter
+where the value is at the rounding level of J: a window away from the
+pulses barely feels gamma or alpha within a few steps; a pressure objective
+checks a large dJ/dgamma).
 """
 import os
 import sys
@@ -47,13 +52,22 @@ def batch_128(igr, B, first=0):
     return basis, mesh, q0, gam, alp, np.full(B, dt), prm
 
 
-def check_gradients(out, ref):
+def check_params(J, dg, da, Jr, dgr, dar, gamma, alpha):
+    # dJ/dgamma, dJ/dalpha: relative error 1e-9, or, where the window objective is insensitive to the parameter
+    # over a few steps (the value sits at the rounding level of J's sum), 1e-9 on the scale of J / parameter
+    for d, dr, par in ((dg, dgr, gamma), (da, dar, alpha)):
+        d, dr, par, Jr_ = np.ravel(d), np.ravel(dr), np.ravel(par) * np.ones(np.size(dr)), np.ravel(Jr)
+        for k in range(dr.size):
+            assert abs(d[k] - dr[k]) <= RTOL_GRAD * max(abs(dr[k]), abs(Jr_[k]) / par[k]), (k, d[k], dr[k])
+
+
+def check_gradients(out, ref, gam, alp):
     J, dq, dg, da = out
     Jr, dqr, dgr, dar = ref
     assert rel(J, Jr) <= RTOL_J
     for b in range(len(J)):
         assert rel(dq[b], dqr[b]) <= RTOL_GRAD, b
-    assert rel(dg, dgr) <= RTOL_GRAD and rel(da, dar) <= RTOL_GRAD
+    check_params(J, dg, da, Jr, dgr, dar, gam, alp)
 
 
 def test_adjoint_64_chebyshev_matches_oracle(igr, oracle):
@@ -71,7 +85,24 @@ def test_adjoint_64_chebyshev_matches_oracle(igr, oracle):
     Jr, dqr, dgr, dar = oracle.adjoint_2d(G, g, alpha, nst, dt, 5, "chebyshev", "window_rho2", [flat(a) for a in q0], prm)
     assert rel(out[0], Jr) <= RTOL_J
     assert rel(np.concatenate([flat(a) for a in out[1:5]]), np.concatenate(dqr)) <= RTOL_GRAD
-    assert rel(out[5], dgr) <= RTOL_GRAD and rel(out[6], dar) <= RTOL_GRAD
+    check_params(out[0], out[5], out[6], Jr, dgr, dar, g, alpha)
+
+
+def test_adjoint_64_l2_pressure_gamma_gradient_matches_oracle(igr, oracle):
+    # the same mesh and solver with J = integral of P^2, which depends on gamma directly: dJ/dgamma is large
+    g, p, ne, nst = 1.4, 3, 64, 10
+    basis = igr.DGBasis(p)
+    mesh = igr.CartesianMesh2D(ne, ne, 1.0, 1.0, basis)
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(3, 1), n_pulses=3, width=0.03)
+    dt = W.cfl_dt_2d(mesh, p, q0, g, 0.1)
+    alpha = 3.0 / ne ** 2
+    out = igr.enzyme_adjoint_ic(*q0, nst, dt, basis, mesh, g, alpha, n_iter=5, solver="chebyshev",
+                                objective="l2_pressure", with_params=True)
+    G = oracle.Grid2D(p, ne, ne)
+    Jr, dqr, dgr, dar = oracle.adjoint_2d(G, g, alpha, nst, dt, 5, "chebyshev", "l2_pressure", [flat(a) for a in q0])
+    assert abs(dgr) * g > 0.1 * abs(Jr)
+    assert rel(out[0], Jr) <= RTOL_J and rel(out[5], dgr) <= RTOL_GRAD
+    assert rel(np.concatenate([flat(a) for a in out[1:5]]), np.concatenate(dqr)) <= RTOL_GRAD
 
 
 def test_adjoint_batch_128_two_groups_matches_oracle(igr, oracle):
@@ -90,7 +121,7 @@ def test_adjoint_batch_128_two_groups_matches_oracle(igr, oracle):
     G = oracle.Grid2D(3, 128, 128)
     ref = oracle.adjoint_batch_2d(G, gam, alp, nst, float(dts[0]), 5, "chebyshev", "window_rho2", q0, prm,
                                   n_threads=THREADS)
-    check_gradients(out, ref)
+    check_gradients(out, ref, gam, alp)
 
 
 def test_adjoint_batch_128_pcg_separate_sums_matches_oracle(igr, oracle):
@@ -105,7 +136,7 @@ def test_adjoint_batch_128_pcg_separate_sums_matches_oracle(igr, oracle):
     G = oracle.Grid2D(3, 128, 128)
     ref = oracle.adjoint_batch_2d(G, gam, alp, nst, float(dts[0]), 10, "pcg", "window_rho2", q0, prm,
                                   n_threads=THREADS)
-    check_gradients(out, ref)
+    check_gradients(out, ref, gam, alp)
 
 
 def test_forward_128_pcg60_matches_oracle(igr, oracle):
@@ -118,10 +149,17 @@ def test_forward_128_pcg60_matches_oracle(igr, oracle):
     alpha, T = 3.0 / ne ** 2, 3 * dt * 0.999
     out = igr.run_forward(*q0, dt, T, basis, mesh, g, alpha, n_iter=60, solver="pcg")
     G = oracle.Grid2D(p, ne, ne)
-    qr, Sr = oracle.run_forward_2d(G, g, alpha, dt, T, 60, "pcg", [flat(a) for a in q0])
+    f0 = [flat(a) for a in q0]
+    qr, Sr = oracle.run_forward_2d(G, g, alpha, dt, T, 60, "pcg", f0)
     for a, b in zip(out[:4], qr):
         assert rel(flat(a), b) <= RTOL_FWD
-    assert rel(flat(out[4]), Sr) <= RTOL_FWD
+    # Sigma of this state is sensitive to rounding: the oracle's own Sigma moves by ~4e-10 (relative L2) when
+    # rho0 and E0 move by one ulp (state: ~5e-14), more than the GPU differs from it. Its bound is that spread.
+    rng = np.random.default_rng(0)
+    fp = [np.nextafter(a, a + rng.choice([-1.0, 1.0], size=a.size)) if v >= 2 else a for v, a in enumerate(f0)]
+    _, Sp = oracle.run_forward_2d(G, g, alpha, dt, T, 60, "pcg", fp)
+    spread = rel(Sp, Sr)
+    assert rel(flat(out[4]), Sr) <= max(RTOL_FWD, 3.0 * spread), spread
 
 
 def test_forward_1d_256_jacobi50_full_matches_oracle(igr, oracle):

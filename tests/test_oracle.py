@@ -444,3 +444,23 @@ def test_form1_vs_form2_1d(oracle):
     assert rel(q1[1], q2[1]) < 1e-14
     for a, b in zip(t1 + [v1], t2 + [v2]):
         assert rel(a, b) < 1e-2
+
+
+def test_solver_summation_order_moves_results_at_rounding_level(oracle):
+    """The solver inner products' summation order (sequential, reversed,
+    pairwise: the GPU sums in a fixed tree order) moves a short PCG forward by
+    rounding only; the differences bound what the parity tests can demand."""
+    g, p, ne = 1.4, 3, 6
+    G = oracle.Grid2D(p, ne, ne)
+    x, y = G.coords()
+    rho = 1.0 + 0.2 * np.exp(-((x - 0.4) ** 2 + (y - 0.6) ** 2) / 0.02)
+    q0 = [0.1 * np.sin(2 * np.pi * y), 0.1 * np.cos(2 * np.pi * x), rho, 1.0 / (g - 1) + 0.01 / rho]
+    ref = oracle.run_forward_2d(G, g, 3.0 / ne ** 2, 2e-3, 6e-3, 20, "pcg", q0)
+    try:
+        for order in (1, 2):
+            oracle.set_dot_order(order)
+            q, S = oracle.run_forward_2d(G, g, 3.0 / ne ** 2, 2e-3, 6e-3, 20, "pcg", q0)
+            assert max(rel(a, b) for a, b in zip(q, ref[0])) < 1e-13
+            assert 0 < rel(S, ref[1]) < 1e-10
+    finally:
+        oracle.set_dot_order(0)
