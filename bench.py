@@ -69,9 +69,25 @@ def max_over_ranks(t, dist=None, device=None):
     return float(tt.item())
 
 
-def make_batch(igr, W, B, first=0):
+def gather_by_seed(dist, seeds, *arrays):
+    """Every rank's per-instance results in the order of the instance seeds
+    (identity on one rank): (seeds, arrays), each array concatenated along its
+    first axis over all ranks' instances."""
+    if dist is None:
+        return list(seeds), [np.asarray(a) for a in arrays]
+    parts = [None] * dist.get_world_size()
+    dist.all_gather_object(parts, (list(seeds), [np.asarray(a) for a in arrays]))
+    allseeds = [s for p in parts for s in p[0]]
+    order = np.argsort(allseeds, kind="stable")
+    cat = [np.concatenate([p[1][k] for p in parts])[order] for k in range(len(arrays))]
+    return [allseeds[i] for i in order], cat
+
+
+def make_batch(igr, W, B, first=0, ne=NE):
+    """Instances first .. first + B - 1 of the workload (one seed each) and the
+    job's objective window (the same for every instance, whichever rank runs it)."""
     basis = igr.DGBasis(P)
-    mesh = igr.CartesianMesh2D(NE, NE, 1.0, 1.0, basis)
+    mesh = igr.CartesianMesh2D(ne, ne, 1.0, 1.0, basis)
     q0 = np.empty((B, 4, mesh.x.size))
     dts = np.empty(B)
     for b in range(B):
@@ -79,8 +95,8 @@ def make_batch(igr, W, B, first=0):
         for v in range(4):
             q0[b, v] = np.asarray(q[v]).reshape(-1, order="F")
         dts[b] = W.cfl_dt_2d(mesh, P, q, GAMMA, 0.1)
-    alpha = 3.0 * (1.0 / NE) ** 2
-    return basis, mesh, q0, np.full(B, GAMMA), np.full(B, alpha), dts, W.seeded_window(W.seed_for(3, first))
+    alpha = 3.0 * (1.0 / ne) ** 2
+    return basis, mesh, q0, np.full(B, GAMMA), np.full(B, alpha), dts, W.seeded_window(W.seed_for(3, 0))
 
 
 class ClockSampler:
@@ -695,7 +711,7 @@ def main():
     lib.igr_profile_enable(ctx.handle, 1)
     barrier()
     tp0 = time.perf_counter()
-    run_dev()
+    Jl = run_dev()[0]  # the instances' J, gathered below in seed order (outside the timed region)
     barrier()
     t_prof = time.perf_counter() - tp0
     lib.igr_profile_enable(ctx.handle, 0)
@@ -711,6 +727,7 @@ def main():
         fam[k] = (ms.value, cnt.value, nn.value)
     tmax = max_over_ranks(t, dist, dev)
     value = B * world * args.steps / tmax
+    seeds_all, (J_all,) = gather_by_seed(dist, instance_seeds(rank, B), Jl)
 
     # end to end: host buffers through the C ABI
     barrier()
@@ -775,6 +792,8 @@ def main():
     cfg = config_dict(B)
     cfg["n_steps"] = n_steps
     cfg["tape_plan"] = tape_plan
+    cfg["instances_total"] = len(seeds_all)
+    cfg["J_sum_over_instances"] = float(np.sum(J_all))
     line = {"metric": METRIC, "value": value, "unit": "gradients/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tmax / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian pressure pulses)",
