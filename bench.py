@@ -51,6 +51,13 @@ TRAFFIC_PER_NODE = {0: 61.9, 1: 91.8, 2: 123.7, 3: 208.1, 4: 143.8, 5: 141.0}
 # probe's flop rate (one DFMA = 2 flops).
 INST_PER_NODE = {0: 59.0, 1: 30.0, 2: 107.0, 3: 155.1, 4: 52.5, 5: 90.3}
 FAMILY = {0: "k2_setup", 1: "k2_apply", 2: "k2_hyp_rk", 3: "k2_hyp_rev", 4: "k2_apply_rev", 5: "k2_setup_rev"}
+# Algorithmic FP64 operations per node: the reference's arithmetic as restated in the oracle, counted with an
+# operation-counting scalar (+ - * / sqrt |x| max = 1 each, a multiply-add = 2), and its reverse by the
+# operation-by-operation adjoint rule Enzyme applies to the same code (tests/test_opcount.py pins these).
+# P3, Chebyshev 5: per launch of each family (the five operator launches of a stage share the solver's cost)
+# and per node and RK step of a whole gradient (forward 2892 + reverse 6970.5).
+ALG_OPS_PER_NODE = {0: 131.0, 1: (105.0 + 5 * 112.0) / 5, 2: 168.0, 3: 406.5, 4: (247.0 + 5 * 264.0) / 5, 5: 350.0}
+ALG_OPS_PER_NODE_STEP = 2892.0 + 6970.5
 
 
 def instance_seeds(rank, B):
@@ -759,6 +766,8 @@ def main():
         return
     peak = C.c_double(0)
     lib.igr_probe_fp64_peak(ctx.handle, C.byref(peak))
+    tpeak = C.c_double(0)
+    lib.igr_probe_fp64_tensor_peak(ctx.handle, C.byref(tpeak))
     share = {FAMILY[k]: fam[k][0] for k in FAMILY}
     tot = sum(v[0] for v in fam.values()) or 1.0
     dom = max(FAMILY, key=lambda k: fam[k][0])
@@ -768,6 +777,9 @@ def main():
     achieved = flops / (ms_launch * 1e-3) / 1e12
     hbm = BYTES_PER_NODE[dom] * nodes / (ms_launch * 1e-3) / 1e9
     issue = INST_PER_NODE[dom] * nodes / (ms_launch * 1e-3) / 1e12
+    alg_dom = ALG_OPS_PER_NODE[dom] * nodes / (ms_launch * 1e-3) / 1e12
+    # whole gradient: forward + reverse operations of every RK step, over the profiled step's device time
+    alg_all = ALG_OPS_PER_NODE_STEP * mesh.x.size * B * n_steps / (sum(v[0] for v in fam.values()) * 1e-3) / 1e12
     all_flops = sum(FLOPS_PER_NODE[k] * fam[k][2] for k in FAMILY)
     all_ms = sum(fam[k][0] for k in FAMILY)
     try:
@@ -780,6 +792,7 @@ def main():
                 "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
                 "traffic_note": "DRAM bytes per launch (ncu, 8-instance case scaled by nodes)",
                 "peak_source": "measured live (DFMA-chain probe in libigr_gb300.so)",
+                "fp64_tensor_probe_tflops": tpeak.value,
                 "ms_per_launch": ms_launch, "flops_per_launch": flops, "nodes_per_launch": nodes,
                 "all_kernels_fp64_tflops": all_flops / (all_ms * 1e-3) / 1e12 if all_ms else None,
                 "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak, "peak_source": hbm_src},
@@ -787,6 +800,13 @@ def main():
                                "frac": issue / (peak.value / 2) if peak.value else None,
                                "note": "DFMA, DADD and DMUL each take one FP64 issue slot; a third of these kernels' "
                                        "FP64 instructions are DADD/DMUL (1 flop), so the flop fraction is lower"},
+                "fp64_algorithmic": {
+                    "achieved": alg_dom, "peak": peak.value, "unit": "TFLOP/s", "frac": alg_dom / peak.value if peak.value else None,
+                    "whole_gradient_achieved": alg_all, "whole_gradient_frac": alg_all / peak.value if peak.value else None,
+                    "ops_per_node_per_launch": ALG_OPS_PER_NODE[dom], "ops_per_node_step": ALG_OPS_PER_NODE_STEP,
+                    "note": "the reference's arithmetic (operation-counted restatement, reverse by the adjoint rule) per "
+                            "second: above 1 where the kernels need fewer operations than the reference's expressions "
+                            "(per-stage coefficients, skipped zero terms, folded face terms)"},
                 "time_share": {k: v / tot for k, v in share.items()},
                 "profiled_step_ms": t_prof * 1e3, "kernel_ms_in_profiled_step": sum(v[0] for v in fam.values())}
     cfg = config_dict(B)

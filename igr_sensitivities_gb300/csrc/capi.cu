@@ -243,6 +243,13 @@ int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops) {
   });
 }
 
+int igr_probe_fp64_tensor_peak(igr_ctx* ctx, double* tflops) {
+  return guarded(ctx, [&] {
+    if (!tflops) throw Error(IGR_EINVAL, "null output");
+    *tflops = probe_dmma_tflops(ctx->c);
+  });
+}
+
 int igr2d_run_forward(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alpha, double dt, double t_end,
                       int n_iter, int solver, double* mux, double* muy, double* rho, double* E, double* sigma) {
   return guarded(ctx, [&] {

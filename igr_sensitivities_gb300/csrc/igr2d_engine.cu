@@ -1387,6 +1387,27 @@ __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
   if (s == 1234.5) out[threadIdx.x] = s;  // never true; keeps the chains live
 }
 
+// FP64 tensor-core (DMMA) throughput probe: eight independent accumulator
+// chains per warp of mma.sync.m8n8k4 f64 (one warp instruction = 8 x 8 x 4
+// multiply-adds = 512 flops), the question being whether the 4 x 4 line
+// contractions would issue faster on the FP64 tensor path than as DFMAs.
+__global__ void k_dmma_probe(double* out, int iters, double a, double b) {
+  double c[8][2];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { c[k][0] = threadIdx.x * 1e-3 + k; c[k][1] = c[k][0] + 0.5; }
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(c[k][0]), "+d"(c[k][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1];
+  if (s == 1234.5) out[threadIdx.x] = s;  // never true; keeps the chains live
+}
+
 // ------------------------------------------------------------------------------------------
 // Continuous adjoint: run_forward_store (forward.jl:111-158) and
 // run_adjoint_conservative (adjoint_pde.jl:527-611)
@@ -1749,6 +1770,32 @@ double probe_fp64_tflops(Ctx& c) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return 2.0 * 8.0 * iters * (double)grid * tpb / (best * 1e-3) / 1e12;
+}
+
+double probe_dmma_tflops(Ctx& c) {
+  int sms = 0;
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device), "attr");
+  double* d = c.ws.dbl("probe", 1024);
+  const int grid = sms * 4, tpb = 256, iters = 2048;
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "event");
+  cuda_check(cudaEventCreate(&e1), "event");
+  k_dmma_probe<<<grid, tpb, 0, c.stream>>>(d, 32, 1e-3, 1e-3);
+  cuda_check(cudaGetLastError(), "dmma probe launch");
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0, c.stream);
+    k_dmma_probe<<<grid, tpb, 0, c.stream>>>(d, iters, 1e-3, 1e-3);
+    cudaEventRecord(e1, c.stream);
+    cuda_check(cudaEventSynchronize(e1), "probe sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double warps = (double)grid * tpb / 32.0;
+  return 512.0 * 8.0 * iters * warps / (best * 1e-3) / 1e12;
 }
 
 }  // namespace igrgpu

@@ -282,6 +282,8 @@ void build_ic1d(Ctx& c, const Plan1D& P, int type, const double* amps, double* q
 double l2_error2d(Ctx& c, const Plan2D& P, const double* u, const double* r);
 
 double probe_fp64_tflops(Ctx& c);
+// FP64 tensor-core (mma.sync m8n8k4 f64) throughput in TFLOP/s.
+double probe_dmma_tflops(Ctx& c);
 // y = 1 / x elementwise on stream s (no bookkeeping).
 void launch_recip(const double* x, double* y, long long n, cudaStream_t s);
 

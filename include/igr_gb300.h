@@ -130,6 +130,10 @@ int igr_last_adjoint_plan(const igr_ctx* ctx, int* groups, int* group_size, int*
 /* Measured FP64 FMA throughput of the device in TFLOP/s (the roofline
  * denominator of this FP64-bound path; no reference counterpart). */
 int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops);
+/* Measured FP64 tensor-core throughput (mma.sync m8n8k4 f64, 512 flops per
+ * warp instruction) in TFLOP/s, beside the FMA figure above (no reference
+ * counterpart). */
+int igr_probe_fp64_tensor_peak(igr_ctx* ctx, double* tflops);
 
 /* ---- 2D ------------------------------------------------------------------- */
 

@@ -12,6 +12,7 @@
 #include "igr2d_pde_adjoint.hpp"
 #include "igr1d_pde_adjoint.hpp"
 #include "igr_ic.hpp"
+#include "opcount.hpp"
 
 using namespace igr;
 
@@ -40,6 +41,68 @@ int orc_set_dot_order(int order) {
   if (order < 0 || order > 2) return 1;
   dot_order() = order;
   return 0;
+}
+
+// Algorithmic FP64 operations per node of the restated 2D arithmetic (opcount.hpp), on
+// a smooth state of the given grid: out[2k] forward and out[2k+1] reverse-mode
+// counts of family k = 0 stage setup (compute_igr_rhs! + compute_sip_diagonal),
+// 1 one apply_sip!, 2 one iteration of the solver (its marginal cost), 3 the
+// solver's fixed part (n_iter = 1 minus one iteration), 4 the hyperbolic RHS
+// plus the RK stage combination (per stage), 5 one SSP-RK3 step with its
+// three solves of n_iter iterations, 6 objective window rho^2 (J at T).
+int orc2d_opcount(GRID2D_ARGS, int solver, int n_iter, double* out) {
+  return guard([&] {
+    if (solver < 0 || solver > 2) throw std::invalid_argument("Unknown solver");
+    if (n_iter < 2) throw std::invalid_argument("n_iter must be >= 2");
+    Grid2D G = GRID2D;
+    const size_t N = G.N;
+    std::vector<Ops> qv[4], S(N), b(N), M(N), x(N), y(N);
+    for (int v = 0; v < 4; ++v) qv[v].resize(N);
+    for (int ey = 0; ey < G.m.Ney; ++ey) for (int ex = 0; ex < G.m.Nex; ++ex)
+      for (int j = 0; j < G.np; ++j) for (int i = 0; i < G.np; ++i) {
+        const size_t n = G.id(i, j, ex, ey);
+        const double X = node_x(G.b, G.m, i, ex), Y = node_y(G.b, G.m, j, ey);
+        const double r = 1.0 + 0.2 * std::sin(6.283185307179586 * X) * std::cos(6.283185307179586 * Y);
+        const double u = 0.1 * std::sin(6.283185307179586 * Y), w = 0.1 * std::cos(6.283185307179586 * X);
+        qv[0][n] = r * u; qv[1][n] = r * w; qv[2][n] = r; qv[3][n] = 2.5 + 0.5 * r * (u * u + w * w);
+        S[n] = 1e-3 * std::sin(6.283185307179586 * (X + Y)); x[n] = S[n].v;
+      }
+    const Ops g(1.4), alpha(3.0 / ((double)G.m.Nex * G.m.Nex));
+    Work2D<Ops> W; W.alloc(N);
+    auto measure = [&](auto&& f) {
+      op_tally() = OpTally();
+      f();
+      const OpTally t = op_tally();
+      return std::pair<double, double>((double)t.fwd / N, (double)t.rev / N);
+    };
+    auto solve = [&](int n) {
+      std::vector<Ops> xx = x;
+      if (solver == SOLVER_PCG) pcg_fixed(G, xx.data(), b.data(), M.data(), n, qv[2].data(), alpha, W);
+      else if (solver == SOLVER_JACOBI) jacobi_fixed(G, xx.data(), b.data(), M.data(), n, qv[2].data(), alpha, 2.0 / 3.0, W);
+      else chebyshev_fixed(G, xx.data(), b.data(), M.data(), n, qv[2].data(), alpha, W);
+    };
+    const auto setup = measure([&] {
+      igr_rhs(G, b.data(), qv[0].data(), qv[1].data(), qv[2].data(), alpha);
+      sip_diagonal(G, M.data(), qv[2].data(), alpha);
+    });
+    const auto apply = measure([&] { apply_sip(G, y.data(), x.data(), qv[2].data(), alpha); });
+    const auto s1 = measure([&] { solve(1); });
+    const auto s2 = measure([&] { solve(2); });
+    std::vector<Ops> q0[4] = {qv[0], qv[1], qv[2], qv[3]};
+    Ops* qs[4] = {q0[0].data(), q0[1].data(), q0[2].data(), q0[3].data()};
+    std::vector<Ops> Sig = S;
+    const auto step = measure([&] { rk3_step(G, qs, Sig.data(), g, alpha, 1e-4, n_iter, solver, W); });
+    const Ops* qc[4] = {qv[0].data(), qv[1].data(), qv[2].data(), qv[3].data()};
+    const double prm[4] = {0.2, 0.2, 0.5, 0.0};
+    const auto obj = measure([&] { (void)objective2d(G, OBJ_WINDOW_RHO2, qc, g, prm); });
+    const double it_f = s2.first - s1.first, it_r = s2.second - s1.second;
+    const double sol_f = s1.first + (n_iter - 1) * it_f, sol_r = s1.second + (n_iter - 1) * it_r;
+    const double vals[14] = {setup.first, setup.second, apply.first, apply.second, it_f, it_r, s1.first - it_f,
+                             s1.second - it_r, (step.first - 3 * (setup.first + sol_f)) / 3,
+                             (step.second - 3 * (setup.second + sol_r)) / 3, step.first, step.second, obj.first,
+                             obj.second};
+    for (int k = 0; k < 14; ++k) out[k] = vals[k];
+  });
 }
 
 int orc_basis(int p, double* xi, double* w, double* Dcol) {

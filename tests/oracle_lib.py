@@ -51,6 +51,17 @@ def _check(rc):
         raise (ValueError if rc == 1 else RuntimeError)(msg)
 
 
+OPCOUNT_FAMILIES = ("setup", "apply", "iteration", "solver_init", "hyperbolic_rk", "step", "objective")
+
+
+def opcount_2d(G, solver, n_iter):
+    """Algorithmic FP64 operations per node of the restated arithmetic
+    (oracle/opcount.hpp): {family: (forward, reverse)}."""
+    out = np.zeros(14)
+    _check(lib().orc2d_opcount(*G.args(), C.c_int(SOLVERS.get(solver, -1)), C.c_int(n_iter), _p(out)))
+    return {k: (out[2 * i], out[2 * i + 1]) for i, k in enumerate(OPCOUNT_FAMILIES)}
+
+
 def set_dot_order(order):
     """Summation order of the oracle's solver inner products: 0 sequential (the
     default), 1 reversed, 2 pairwise (to measure a result's sensitivity to that
