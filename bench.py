@@ -480,8 +480,12 @@ def secondary(args):
         clk = clocks.stop()
         t_tan, t_adj, t_fd = (float(np.median([t[k] for t in ts])) for k in range(3))
         scale = full / S
-        # at 1000 steps the adjoint's tape does not fit: it re-runs the forward once from sqrt(n) checkpoints
-        t_full = (t_tan + t_adj + t_fd) * scale + 0.5 * t_fd * scale
+        # at 1000 steps the adjoint's tape does not fit: the revolve schedule re-runs forward steps from its
+        # checkpoints (the FD batch is two forwards of all instances, so half of it is one forward)
+        rerun = igr.adjoint_plan(B, full, basis, mesh, alpha, n_iter=nit, solver="pcg", ctx=ctx)
+        groups = -(-B // rerun["instances_per_group"])
+        extra = (rerun["step_evaluations"] - full) / full * groups * rerun["instances_per_group"] / B
+        t_full = (t_tan + t_adj + t_fd) * scale + 0.5 * t_fd * scale * extra
         # CPU: the oracle pipeline for one 64^2 instance and one step, scaled by nodes and steps
         G = O.Grid2D(3, 64, 64)
         m64 = igr.CartesianMesh2D(64, 64, 1.0, 1.0, basis)
@@ -495,6 +499,7 @@ def secondary(args):
             O.objective_run_2d(G, gg, 3.0 / 64 ** 2, 1, dtc, nit, "pcg", "window_rho2", list(qc), prm_w)
         tcpu = (time.perf_counter() - tc0) * (B * ne5 * ne5 / 64 ** 2) * full * 1.125  # same recompute allowance
         # on the batch's scale: over a short sample some instances' dJ/dgamma is tiny and FD rounding dominates it
+        plan = rerun  # the adjoint's memory plan for the whole 1000 steps (revolve schedule of one instance group)
         rel_ta = float(np.max(np.abs(tan - adj)) / np.max(np.abs(adj)))
         rel_af = float(np.max(np.abs(adj - fd)) / np.max(np.abs(fd)))
         line.update(metric="2D batched tangent + adjoint + FD dJ/dgamma sets/hour (16 x 256^2 P3, PCG 60, 1000 steps)",
@@ -506,7 +511,9 @@ def secondary(args):
                                         "32-instance FD forward batch (h = 1e-6)",
                             "sample_steps": S, "full_steps": full,
                             "sample_seconds": {"tangent": round(t_tan, 3), "adjoint": round(t_adj, 3), "fd": round(t_fd, 3)},
-                            "extrapolation": "sample x 1000/S, plus one forward re-run for the adjoint's checkpointed tape",
+                            "extrapolation": "sample x 1000/S, plus the forward re-runs of the adjoint's checkpoint "
+                                             "schedule (adjoint_plan: step_evaluations / 1000 - 1)",
+                            "adjoint_plan_1000_steps": plan,
                             "tangent_vs_adjoint_max_rel": rel_ta, "adjoint_vs_fd_max_rel": rel_af},
                     clocks=clk,
                     cpu_baseline={"value": 3600.0 / tcpu, "unit": "sets/hour", "cores": 1, "kind": "port",

@@ -20,7 +20,8 @@ from ._lib import Context, check, default_context, lib
 
 __all__ = [
     "DGBasis", "CartesianMesh2D", "PeriodicMesh1D", "Context", "default_context",
-    "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch_meshes", "adjoint_batch", "objective_value",
+    "run_forward", "run_forward_", "run_sensitivity", "sensitivity_batch", "enzyme_adjoint_ic", "adjoint_batch_meshes",
+    "adjoint_batch", "adjoint_plan", "objective_value",
     "apply_sip_", "compute_hyperbolic_rhs_", "solve_elliptic_", "compute_igr_euler_rhs_", "compute_igr_rhs_",
     "compute_sip_diagonal", "SIPOperator", "sip_operator", "cg_solve_", "cg_fixed_", "SOLVERS", "OBJECTIVES",
     "Snapshots", "run_forward_store", "run_adjoint_conservative", "compute_adjoint_rhs_conservative_",
@@ -341,6 +342,19 @@ def adjoint_batch(q0, gammas, alphas, dts, n_steps, basis, mesh, n_iter=10, solv
                                          C.c_int(_objective(objective)), _ptr(prm), _ptr(q0), _ptr(J), _ptr(dq), _ptr(dg),
                                          _ptr(da)))
     return J, dq, dg, da
+
+
+def adjoint_plan(n_inst, n_steps, basis, mesh, alpha, n_iter=10, solver="pcg", ctx=None):
+    """The memory plan adjoint_batch would use, without running it:
+    {"instances_per_group", "tape_steps", "snapshots", "step_evaluations"} (the
+    revolve checkpoint schedule of one group; step_evaluations == n_steps means
+    the whole tape fits and nothing is recomputed)."""
+    ctx = ctx or default_context()
+    g, w, s, e = C.c_int(0), C.c_int(0), C.c_int(0), C.c_longlong(0)
+    check(ctx, lib().igr2d_adjoint_plan(ctx.handle, C.byref(_disc2d(basis, mesh)), C.c_int(n_inst), C.c_int(n_steps),
+                                        C.c_int(n_iter), C.c_int(_solver(solver)), C.c_double(alpha), C.byref(g),
+                                        C.byref(w), C.byref(s), C.byref(e)))
+    return {"instances_per_group": g.value, "tape_steps": w.value, "snapshots": s.value, "step_evaluations": e.value}
 
 
 def objective_value(mux0, muy0, rho0, E0, n_steps, dt, basis, mesh, gamma, alpha, n_iter=10, solver="pcg",

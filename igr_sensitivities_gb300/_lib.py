@@ -101,6 +101,13 @@ class Context:
         check(self, lib().igr_last_adjoint_plan(self.handle, *[C.byref(x) for x in v]))
         return dict(zip(("groups", "instances_per_group", "steps_per_segment", "segments"), (x.value for x in v)))
 
+    def last_checkpoint_schedule(self):
+        """2D discrete adjoint: RK steps taped at once, checkpoint slots beyond
+        the initial state and RK step evaluations of its revolve schedule."""
+        w, s, e = C.c_int(0), C.c_int(0), C.c_longlong(0)
+        check(self, lib().igr_last_checkpoint_schedule(self.handle, C.byref(w), C.byref(s), C.byref(e)))
+        return {"tape_steps": w.value, "snapshots": s.value, "step_evaluations": e.value}
+
 
 _default = None
 

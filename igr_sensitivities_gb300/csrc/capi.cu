@@ -236,6 +236,14 @@ int igr_last_adjoint_plan(const igr_ctx* ctx, int* groups, int* group_size, int*
   return IGR_OK;
 }
 
+int igr_last_checkpoint_schedule(const igr_ctx* ctx, int* tape_steps, int* snapshots, long long* step_evaluations) {
+  if (!ctx || !tape_steps || !snapshots || !step_evaluations) return IGR_EINVAL;
+  *tape_steps = ctx->c.plan_seg;
+  *snapshots = ctx->c.plan_snapshots;
+  *step_evaluations = ctx->c.plan_step_evals;
+  return IGR_OK;
+}
+
 int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops) {
   return guarded(ctx, [&] {
     if (!tflops) throw Error(IGR_EINVAL, "null output");
@@ -426,6 +434,50 @@ int igr2d_objective(igr_ctx* ctx, const igr_disc2d* d, double gamma, double alph
   });
 }
 
+// Instances per group of a batched 2D adjoint on one mesh of N nodes: as many
+// as fit with a full tape (no recompute); a single instance that does not fit
+// runs with a revolve checkpoint schedule. Without a budget: the free device
+// memory less a reserve, with ~110 working fields per instance beside the tape;
+// with one (igr_set_tape_budget): the full tapes and checkpoints of the group
+// within the budget.
+static int adjoint_group_size(Ctx& c, long long N, int n_inst, int n_steps, int n_iter, int solver, bool apos) {
+  const size_t F = (size_t)stage_fields2d(Solve2DOpts{n_iter, solver}, apos, N, 1);
+  const size_t tape_inst = ((size_t)3 * F * std::max(n_steps, 1) + 6) * N * sizeof(double);
+  size_t fit = 0;
+  if (c.tape_budget == 0) {
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    const size_t avail = fr + c.ws.bytes();  // workspace buffers are reused or regrown
+    const size_t reserve = (size_t)4 << 30;
+    const size_t per_inst = tape_inst + (size_t)110 * N * sizeof(double);
+    fit = avail > reserve ? (size_t)((avail - reserve) * 0.92) / per_inst : 0;
+  } else {
+    fit = c.tape_budget / tape_inst;
+  }
+  return (int)std::max<size_t>(1, std::min<size_t>((size_t)n_inst, fit));
+}
+
+int igr2d_adjoint_plan(igr_ctx* ctx, const igr_disc2d* d, int n_inst, int n_steps, int n_iter, int solver, double alpha,
+                       int* group_size, int* tape_steps, int* snapshots, long long* step_evaluations) {
+  return guarded(ctx, [&] {
+    Ctx& c = ctx->c;
+    check_disc(d);
+    check_solver(solver, n_iter);
+    if (n_inst < 1 || n_steps < 0 || !group_size || !tape_steps || !snapshots || !step_evaluations)
+      throw Error(IGR_EINVAL, "bad arguments");
+    const long long N = nodes2d(d);
+    const int G = adjoint_group_size(c, N, n_inst, n_steps, n_iter, solver, alpha > 0);
+    const long long NG = N * G;
+    const int F = stage_fields2d(Solve2DOpts{n_iter, solver}, alpha > 0, NG, G);
+    const RevolvePlan rp = adjoint_checkpoints2d(c, NG, F, n_steps);
+    if (rp.w < 1) throw Error(IGR_ENOMEM, "device memory too small for one taped step and one checkpoint");
+    *group_size = G;
+    *tape_steps = rp.w;
+    *snapshots = rp.slots;
+    *step_evaluations = rp.evals;
+  });
+}
+
 static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const double* gammas, const double* alphas,
                                const double* dts, int n_steps, int n_iter, int solver, int objective,
                                const double* obj_params, const double* q0, bool q0_dev, double* J, double* dq0,
@@ -435,29 +487,7 @@ static void adjoint_batch_impl(Ctx& c, const igr_disc2d* d, int n_inst, const do
   if (n_inst < 1 || !gammas || !alphas || !dts || !J) throw Error(IGR_EINVAL, "bad batch arguments");
   BasisDev B = make_basis_dev(d->p, d->xi, d->w, d->D);
   const long long N = nodes2d(d);
-  // Instances per group: as many as fit with a full tape (no recompute);
-  // a single instance that does not fit runs with segment checkpointing.
-  // Without a budget: the free device memory less a reserve, with ~110
-  // working fields per instance beside the tape; with one (igr_set_tape_budget):
-  // the full tapes and checkpoints of the group within the budget.
-  int G = n_inst;
-  {
-    const bool apos = alphas[0] > 0;
-    const size_t F = (size_t)stage_fields2d(Solve2DOpts{n_iter, solver}, apos, N, 1);
-    const size_t tape_inst = ((size_t)3 * F * std::max(n_steps, 1) + 6) * N * sizeof(double);
-    size_t fit = 0;
-    if (c.tape_budget == 0) {
-      size_t fr = 0, tot = 0;
-      cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
-      const size_t avail = fr + c.ws.bytes();  // workspace buffers are reused or regrown
-      const size_t reserve = (size_t)4 << 30;
-      const size_t per_inst = tape_inst + (size_t)110 * N * sizeof(double);
-      fit = avail > reserve ? (size_t)((avail - reserve) * 0.92) / per_inst : 0;
-    } else {
-      fit = c.tape_budget / tape_inst;
-    }
-    G = (int)std::max<size_t>(1, std::min<size_t>((size_t)n_inst, fit));
-  }
+  int G = adjoint_group_size(c, N, n_inst, n_steps, n_iter, solver, alphas[0] > 0);
   // balanced groups: sizes differ by at most one (workspace sized for the largest)
   const int ngroups = (n_inst + G - 1) / G;
   std::vector<int> gstart(ngroups + 1, 0);

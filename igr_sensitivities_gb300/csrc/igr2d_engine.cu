@@ -1073,6 +1073,86 @@ void objective2d(Ctx& c, const Plan2D& P, double* const q[4], int n_steps, const
   objective_value(c, P, qc, objective, prm, J, c.ws.dbl("obj:s1", P.inst.size()), c.ws.dbl("obj:s2", P.inst.size()));
 }
 
+// Binomial checkpointing (revolve) over super-steps. cost(n, s) = the fewest
+// forward super-step evaluations that reverse n super-steps when the first
+// one's state sits in a slot and s more slots are free: the last super-step is
+// taped and reversed first, and
+//   cost(1, s) = 1,   cost(n, 0) = n (n + 1) / 2   (every super-step re-run from the first state),
+//   cost(n, s) = min over 0 < m < n of  m + cost(n - m, s - 1) + cost(m, s)
+// (advance m super-steps, store the state, reverse the right part with one
+// slot fewer, then the left part with the slot back). Tabulated once for up to
+// REVOLVE_MAX super-steps, with the minimising m of each entry.
+constexpr int REVOLVE_MAX = 512;
+struct RevolveTable {
+  std::vector<long long> cost;  // [n][s], s < n
+  std::vector<int> split;
+  long long at(int n, int s) const { return cost[(size_t)n * (REVOLVE_MAX + 1) + std::min(s, n - 1)]; }
+};
+static const RevolveTable& revolve_table() {
+  static const RevolveTable t = [] {
+    RevolveTable r;
+    const size_t W = REVOLVE_MAX + 1;
+    r.cost.assign(W * W, 0);
+    r.split.assign(W * W, 1);
+    for (int n = 1; n <= REVOLVE_MAX; ++n)
+      for (int s = 0; s < n; ++s) {
+        long long best;
+        int bm = 1;
+        if (n == 1) best = 1;
+        else if (s == 0) best = (long long)n * (n + 1) / 2;
+        else {
+          best = -1;
+          for (int m = 1; m < n; ++m) {
+            const long long v = m + r.cost[(size_t)(n - m) * W + std::min(s - 1, n - m - 1)] + r.cost[(size_t)m * W + std::min(s, m - 1)];
+            if (best < 0 || v < best) { best = v; bm = m; }
+          }
+        }
+        r.cost[(size_t)n * W + s] = best;
+        r.split[(size_t)n * W + s] = bm;
+      }
+    return r;
+  }();
+  return t;
+}
+// Where the schedule stores its next checkpoint within a range of n super-steps
+// with `free` slots (1 <= result < n).
+static int revolve_split(int n, int free) {
+  return revolve_table().split[(size_t)n * (REVOLVE_MAX + 1) + std::min(free, n - 1)];
+}
+
+// Tape window w (RK steps per super-step) and checkpoint slots for n steps
+// within `budget` bytes (w taped steps + the first state + `slots` states),
+// minimising the forward step evaluations; w = 0 when nothing fits.
+static RevolvePlan plan_revolve(int n, size_t step_bytes, size_t ckpt_bytes, size_t budget) {
+  const RevolveTable& t = revolve_table();
+  RevolvePlan best;
+  for (int w = n; w >= 1; --w) {
+    const int ns = (n + w - 1) / w;
+    if (ns > REVOLVE_MAX) break;
+    if ((size_t)w * step_bytes + ckpt_bytes > budget) continue;
+    const long long avail = (long long)((budget - (size_t)w * step_bytes) / ckpt_bytes) - 1;
+    const int slots = (int)std::min<long long>(avail, ns - 1);
+    const long long evals = t.at(ns, slots) * w;
+    if (best.w == 0 || evals < best.evals) { best.w = w; best.slots = slots; best.evals = evals; }
+  }
+  return best;
+}
+
+RevolvePlan adjoint_checkpoints2d(Ctx& c, long long NG, int F, int n_steps) {
+  const size_t step_bytes = (size_t)3 * F * NG * sizeof(double);
+  const size_t ckpt_bytes = (size_t)6 * NG * sizeof(double);
+  size_t budget = c.tape_budget;
+  if (budget == 0) {
+    // free memory plus what the tape and checkpoint buffers already hold (they are reused)
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    const size_t avail = fr + c.ws.held("adj:tape") + c.ws.held("adj:ckpt");
+    const size_t reserve = (size_t)1 << 30;
+    budget = avail > reserve ? avail - reserve : 0;
+  }
+  return plan_revolve(std::max(n_steps, 1), step_bytes, ckpt_bytes, budget);
+}
+
 void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, const Solve2DOpts& o, int objective,
                const double* prm, double* J, double* const dq0[4], double* dgamma, double* dalpha) {
   check_objective(objective);
@@ -1100,31 +1180,22 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   double* anode = c.ws.dbl("adj:anode", NG);
   c.ws.dbl("obj:j1", NG);
   c.ws.dbl("obj:j2", NG);
-  // ---- memory plan: the longest segment (steps taped at once) that fits
-  // next to the checkpoints (q, 1/rho, Sigma at every segment start).
-  const size_t step_bytes = (size_t)3 * F * NG * sizeof(double);
-  const size_t ckpt_bytes = (size_t)6 * NG * sizeof(double);
-  size_t budget = c.tape_budget;
-  if (budget == 0) {
-    // free memory plus what the tape and checkpoint buffers already hold (they are reused)
-    size_t fr = 0, tot = 0;
-    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
-    const size_t avail = fr + c.ws.held("adj:tape") + c.ws.held("adj:ckpt");
-    const size_t reserve = (size_t)1 << 30;
-    budget = avail > reserve ? avail - reserve : 0;
-  }
+  // ---- memory plan: a binomial (revolve) checkpoint schedule over super-steps
+  // of w RK steps. The tape holds one super-step (w taped steps); checkpoint
+  // slots hold (q, 1/rho, Sigma) at super-step boundaries, slot 0 the initial
+  // state. Among the tape windows that fit the budget with their slots, the one
+  // with the fewest forward step evaluations is taken (the full tape, w = n,
+  // when it fits: no recomputation).
   const int nsteps_eff = std::max(n_steps, 1);
-  int seg = 0;
-  for (int sg = nsteps_eff; sg >= 1; --sg) {
-    const size_t nseg = (size_t)((nsteps_eff + sg - 1) / sg);
-    if ((size_t)sg * step_bytes + nseg * ckpt_bytes <= budget) { seg = sg; break; }
-  }
-  if (seg < 1) throw Error(5, "device memory too small for one taped step of this batch");
-  const int n_seg = (nsteps_eff + seg - 1) / seg;
-  c.plan_seg = seg;
-  c.plan_nseg = n_seg;
-  double* ckpt = c.ws.dbl("adj:ckpt", (size_t)n_seg * 6 * NG);
-  double* tape = c.ws.dbl("adj:tape", (size_t)seg * 3 * F * NG);
+  const RevolvePlan rp = adjoint_checkpoints2d(c, NG, F, nsteps_eff);
+  if (rp.w < 1) throw Error(5, "device memory too small for one taped step and one checkpoint of this batch");
+  const int w = rp.w, n_super = (nsteps_eff + w - 1) / w;
+  c.plan_seg = w;
+  c.plan_nseg = n_super;
+  c.plan_snapshots = rp.slots;
+  c.plan_step_evals = 0;
+  double* ckpt = c.ws.dbl("adj:ckpt", (size_t)(rp.slots + 1) * 6 * NG);
+  double* tape = c.ws.dbl("adj:tape", (size_t)w * 3 * F * NG);
   auto slot = [&](int local_step, int stage) {
     return stage_from(tape + ((long long)local_step * 3 + stage) * F * NG, NG, o, apos, true, ni);
   };
@@ -1153,42 +1224,59 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
       else { for (int v = 0; v < 4; ++v) qo[v] = qendp[v]; iro = qend + 4 * NG; }
       step_forward(c, P, o, st, sg, qo, iro, xa, xb, dbuf);
       sg = st[2].Sout;
+      ++c.plan_step_evals;
     }
     return sg;
   };
-
-  // ---- forward: untaped segments with checkpoints, last segment taped
-  for (int k = 0; k < n_seg; ++k) {
-    const int s0 = k * seg, s1 = std::min(n_steps, (k + 1) * seg);
+  auto copy_nd = [&](double* dst, const double* src, const char* what) {
+    cuda_check(cudaMemcpyAsync(dst, src, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), what);
+  };
+  // checkpoint slot k <-> the untaped state (q, 1/rho and the carried Sigma)
+  auto save_slot = [&](int k) {
     double* ck = ckpt + (long long)k * 6 * NG;
-    for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(ck + v * NG, ust[0].q[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "ckpt");
-    cuda_check(cudaMemcpyAsync(ck + 4 * NG, ust[0].invr, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "ckpt");
-    cuda_check(cudaMemcpyAsync(ck + 5 * NG, sig_cur, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "ckpt");
-    if (k == n_seg - 1) {
-      if (s1 > s0) {
-        StageBuf first = slot(0, 0);
-        for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(first.q[v], ust[0].q[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "seg in");
-        cuda_check(cudaMemcpyAsync(first.invr, ust[0].invr, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "seg in");
-        taped_range(s0, s1, sig_cur);
-      } else {
-        for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(qendp[v], ust[0].q[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "q end");
+    for (int v = 0; v < 4; ++v) copy_nd(ck + v * NG, ust[0].q[v], "ckpt");
+    copy_nd(ck + 4 * NG, ust[0].invr, "ckpt");
+    copy_nd(ck + 5 * NG, sig_cur, "ckpt");
+  };
+  auto restore_slot = [&](int k) {
+    const double* ck = ckpt + (long long)k * 6 * NG;
+    for (int v = 0; v < 4; ++v) copy_nd(ust[0].q[v], ck + v * NG, "restore");
+    copy_nd(ust[0].invr, ck + 4 * NG, "restore");
+    copy_nd(sig0, ck + 5 * NG, "restore");
+    sig_cur = sig0;
+  };
+  auto super_begin = [&](int k) { return k * w; };
+  auto super_end = [&](int k) { return std::min(n_steps, (k + 1) * w); };
+  // untaped steps of super-steps [k0, k1) from the untaped state
+  auto advance = [&](int k0, int k1) {
+    for (int s = super_begin(k0); s < super_begin(k1); ++s) {
+      if (apos) for (int kk = 0; kk < 3; ++kk) ust[kk].Sout = (kk % 2 == 0) ? sigA : sigB;
+      step_forward(c, P, o, ust, sig_cur, ust[0].q, ust[0].invr, xa, xb, dbuf);
+      if (apos) {  // carried Sigma lives in sig0 (its zero start is only read by step 0)
+        copy_nd(sig0, ust[2].Sout, "Sigma carry");
+        sig_cur = sig0;
       }
-    } else {
-      for (int s = s0; s < s1; ++s) {
-        if (apos) for (int kk = 0; kk < 3; ++kk) ust[kk].Sout = (kk % 2 == 0) ? sigA : sigB;
-        step_forward(c, P, o, ust, sig_cur, ust[0].q, ust[0].invr, xa, xb, dbuf);
-        if (apos) {  // carried Sigma lives in sig0 (its zero start is only read by step 0)
-          cuda_check(cudaMemcpyAsync(sig0, ust[2].Sout, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Sigma carry");
-          sig_cur = sig0;
-        }
-      }
+      ++c.plan_step_evals;
     }
-  }
-  // ---- objective and its gradient at the final state
+  };
+  // tape super-step k from the untaped state (its output state goes to qend)
+  auto tape_super = [&](int k) {
+    const int s0 = super_begin(k), s1 = super_end(k);
+    if (s1 <= s0) {  // no steps at all: the final state is the initial one
+      for (int v = 0; v < 4; ++v) copy_nd(qendp[v], ust[0].q[v], "q end");
+      return;
+    }
+    StageBuf first = slot(0, 0);
+    for (int v = 0; v < 4; ++v) copy_nd(first.q[v], ust[0].q[v], "seg in");
+    copy_nd(first.invr, ust[0].invr, "seg in");
+    taped_range(s0, s1, sig_cur);
+  };
+  save_slot(0);
+
+  // ---- objective and its gradient at the final state (once the last super-step has run)
   const double* qf[4] = {qendp[0], qendp[1], qendp[2], qendp[3]};
   double* s1d = c.ws.dbl("adj:s1", ni);
   double* s2d = c.ws.dbl("adj:s2", ni);
-  objective_value(c, P, qf, objective, prm, J, s1d, s2d);
   // reverse buffers
   double* QB[4]; double* QN[4]; double* Q2b[4]; double* Q1b[4];
   for (int v = 0; v < 4; ++v) { QB[v] = rb + v * NG; QN[v] = rb + (4 + v) * NG; Q2b[v] = rb + (8 + v) * NG; Q1b[v] = rb + (12 + v) * NG; }
@@ -1199,14 +1287,15 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
   double* Mb = rb + 21 * NG;
   double* Zm = rb + 22 * NG;
   double* Zs = rb + 23 * NG;
-  {
+  auto objective_and_seed = [&]() {
+    objective_value(c, P, qf, objective, prm, J, s1d, s2d);
     ObjArgs2D a = obj_args(P, qf, objective, prm);
     a.s1 = s1d; a.s2 = s2d;
     for (int v = 0; v < 4; ++v) a.qb[v] = QB[v];
     a.gb = gnode;   // initialises the per-node gamma accumulator
     LaunchScope ls(c, KID_OTHER);
     k2_obj_grad<<<grid_for(NG), 256, 0, c.stream>>>(a);
-  }
+  };
   cuda_check(cudaMemsetAsync(Sb, 0, NG * sizeof(double), c.stream), "zero Sb");
   cuda_check(cudaMemsetAsync(anode, 0, NG * sizeof(double), c.stream), "zero anode");
   std::vector<double> ca, cc;
@@ -1351,19 +1440,30 @@ void adjoint2d(Ctx& c, const Plan2D& P, const double* const q0[4], int n_steps, 
     for (int v = 0; v < 4; ++v) std::swap(QB[v], QN[v]);
   };
 
-  for (int k = n_seg - 1; k >= 0; --k) {
-    const int s0 = k * seg, s1 = std::min(n_steps, (k + 1) * seg);
-    if (s1 <= s0) continue;
-    if (k != n_seg - 1) {
-      // recompute the segment from its checkpoint, taped
-      const double* ck = ckpt + (long long)k * 6 * NG;
-      StageBuf first = slot(0, 0);
-      for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(first.q[v], ck + v * NG, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "restore");
-      cuda_check(cudaMemcpyAsync(first.invr, ck + 4 * NG, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "restore");
-      taped_range(s0, s1, ck + 5 * NG);
+  // ---- the schedule: revolve(a, b, k, free) reverses super-steps [a, b) from
+  // the state of super-step a held in slot k, with `free` slots above k. The
+  // first super-step reversed is the last one, whose taped run also yields the
+  // final state for the objective.
+  bool seeded = false;
+  auto leaf = [&](int a) {
+    tape_super(a);
+    if (!seeded) { objective_and_seed(); seeded = true; }
+    for (int st = super_end(a) - 1; st >= super_begin(a); --st) reverse_step(st - super_begin(a));
+  };
+  std::function<void(int, int, int, int)> revolve = [&](int a, int b, int k, int free) {
+    if (b - a == 1) { restore_slot(k); leaf(a); return; }
+    if (free == 0) {  // no slot left: every super-step is re-run from slot k
+      for (int j = b - 1; j >= a; --j) { restore_slot(k); advance(a, j); leaf(j); }
+      return;
     }
-    for (int s = s1 - 1; s >= s0; --s) reverse_step(s - s0);
-  }
+    const int m = a + revolve_split(b - a, free);
+    restore_slot(k);
+    advance(a, m);
+    save_slot(k + 1);
+    revolve(m, b, k + 1, free - 1);
+    revolve(a, m, k, free);
+  };
+  revolve(0, n_super, 0, rp.slots);
   for (int v = 0; v < 4; ++v) cuda_check(cudaMemcpyAsync(dq0[v], QB[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "dq0");
   // per-instance parameter gradients
   double* gsum = c.ws.dbl("adj:gsum", ni);

@@ -89,6 +89,10 @@ struct Ctx {
   // memory plan of the last adjoint call: instance groups, instances per group,
   // steps taped per segment and segments per group (1 = no forward recompute)
   int plan_groups = 0, plan_group_size = 0, plan_seg = 0, plan_nseg = 0;
+  // 2D discrete adjoint: checkpoint slots of its revolve schedule (beyond the
+  // first state) and RK step evaluations of the last group (taped and untaped)
+  int plan_snapshots = 0;
+  long long plan_step_evals = 0;
   int cluster1d = 0;            // 1D: CTAs per instance (0 = chosen per launch)
   int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
   bool use_graphs = true;       // replay repeated forward steps as CUDA graphs
@@ -171,6 +175,12 @@ int cg2d(Ctx& c, const Plan2D& P, const double* rho, const double* b, double* x,
 void hyperbolic_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], const double* Sig, double* const k[4]);
 // y = A x (apply_sip!, elliptic.jl:30).
 void apply_sip2d(Ctx& c, const Plan2D& P, const double* x, const double* rho, double* y);
+
+// Checkpoint schedule of a 2D adjoint over NG nodes with F taped fields per
+// stage: RK steps taped at once (w), checkpoint slots beyond the initial state
+// and forward step evaluations (w = 0: not even one taped step fits).
+struct RevolvePlan { int w = 0, slots = 0; long long evals = 0; };
+RevolvePlan adjoint_checkpoints2d(Ctx& c, long long NG, int F, int n_steps);
 
 // Gradient of the objective after n_steps fixed steps (enzyme_adjoint_ic,
 // enzyme_adjoint.jl:270): J[inst], dq0 (4 fields), dgamma[inst], dalpha[inst].

@@ -127,6 +127,14 @@ int igr_profile_nodes(igr_ctx* ctx, int kernel_family, double* nodes);
  * other, instances per group, RK steps taped per segment and segments per
  * group (segments > 1 means the forward is recomputed from checkpoints). */
 int igr_last_adjoint_plan(const igr_ctx* ctx, int* groups, int* group_size, int* segment_steps, int* segments);
+/* Checkpoint schedule of the last 2D discrete adjoint (its last instance
+ * group): RK steps taped at once, checkpoint slots beyond the initial state,
+ * and the RK step evaluations of the forward sweeps (n_steps when the whole
+ * tape fits; more when states are recomputed from checkpoints). The schedule
+ * is binomial (revolve) over super-steps of tape_steps steps: with s slots and
+ * r re-runs it reverses up to C(s + r, s) super-steps. No reference
+ * counterpart (the reference's Enzyme call keeps the whole trajectory). */
+int igr_last_checkpoint_schedule(const igr_ctx* ctx, int* tape_steps, int* snapshots, long long* step_evaluations);
 /* Measured FP64 FMA throughput of the device in TFLOP/s (the roofline
  * denominator of this FP64-bound path; no reference counterpart). */
 int igr_probe_fp64_peak(igr_ctx* ctx, double* tflops);
@@ -190,6 +198,14 @@ int igr2d_adjoint_batch_meshes(igr_ctx* ctx, int p, const double* xi, const doub
                                const double* gammas, const double* alphas, const double* dts, int n_steps, int n_iter,
                                int solver, int objective, const double* obj_params, const double* q0, double* J,
                                double* dq0, double* dgamma, double* dalpha);
+/* The memory plan igr2d_adjoint_batch would use for n_inst instances of d
+ * with this step count and solver, without running it: instances per group,
+ * RK steps taped at once, checkpoint slots beyond the initial state and the
+ * forward step evaluations of its revolve schedule (per group, an upper bound
+ * when tape_steps does not divide n_steps; n_steps means no recomputation).
+ * Reads the free device memory or the tape budget. No reference counterpart. */
+int igr2d_adjoint_plan(igr_ctx* ctx, const igr_disc2d* d, int n_inst, int n_steps, int n_iter, int solver, double alpha,
+                       int* group_size, int* tape_steps, int* snapshots, long long* step_evaluations);
 /* Same with q0 and dq0 in device memory (J, dgamma, dalpha stay host arrays). */
 int igr2d_adjoint_batch_dev(igr_ctx* ctx, const igr_disc2d* d, int n_inst, const double* gammas,
                             const double* alphas, const double* dts, int n_steps, int n_iter, int solver,

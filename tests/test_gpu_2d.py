@@ -182,8 +182,9 @@ def test_adjoint_degrees_and_ics(igr, oracle, p, ic, alpha, nex):
 
 @pytest.mark.parametrize("solver", ["chebyshev", "pcg"])
 def test_checkpointed_adjoint_equals_full_tape(igr, oracle, solver):
-    """A tape budget of a few steps forces segment checkpointing + recompute;
-    the gradient must be bitwise the one of the full tape."""
+    """A tape budget of a few steps forces checkpointing + recompute (a revolve
+    schedule over super-steps of several taped steps); the gradient must be
+    bitwise the one of the full tape."""
     g = 1.4
     basis, mesh, _ = setup(igr, oracle, 3, 5, 4)
     alpha = 3.0 * (1 / 5) ** 2
@@ -204,6 +205,53 @@ def test_checkpointed_adjoint_equals_full_tape(igr, oracle, solver):
     for a, b in zip(full[1:5], seg[1:5]):
         assert np.array_equal(a, b)
     assert full[5] == seg[5] and full[6] == seg[6]
+
+
+def revolve_evaluations(n, slots):
+    """Fewest forward evaluations of a binomial (revolve) reversal of n steps
+    with `slots` checkpoint slots beyond the first state (taped runs counted)."""
+    cost = {}
+    for k in range(1, n + 1):
+        for s in range(0, k):
+            if k == 1:
+                cost[(k, s)] = 1
+            elif s == 0:
+                cost[(k, s)] = k * (k + 1) // 2
+            else:
+                cost[(k, s)] = min(m + cost[(k - m, min(s - 1, k - m - 1))] + cost[(m, min(s, m - 1))]
+                                   for m in range(1, k))
+    return cost[(n, min(slots, n - 1))]
+
+
+@pytest.mark.parametrize("solver,slots", [("chebyshev", 2), ("pcg", 1), ("chebyshev", 0)])
+def test_revolve_adjoint_equals_full_tape(igr, oracle, solver, slots):
+    """Binomial checkpointing: room for one taped step and 1 + slots stored
+    states; 13 steps are reversed with recomputation from the stored states,
+    bitwise equal to the full tape, with the optimal revolve evaluation count."""
+    g, nst = 1.4, 13
+    basis, mesh, _ = setup(igr, oracle, 3, 4, 5)
+    alpha = 3.0 * (1 / 5) ** 2
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(3, 5), width=0.12)
+    dt = W.cfl_dt_2d(mesh, 3, q0, g, 0.1)
+    ctx = igr.Context(0)
+    full = igr.enzyme_adjoint_ic(*q0, nst, dt, basis, mesh, g, alpha, n_iter=5, solver=solver, objective="l2_density",
+                                 with_params=True, ctx=ctx)
+    assert ctx.last_checkpoint_schedule() == {"tape_steps": nst, "snapshots": 0, "step_evaluations": nst}
+    n = mesh.x.size
+    F = 16 + (1 + 6 + 2 * 5 + 1 if solver == "pcg" else 2 * 5)  # fields of one taped stage at n_iter = 5
+    ctx.set_tape_budget(3 * F * n * 8 + (1 + slots) * 6 * n * 8)
+    rev = igr.enzyme_adjoint_ic(*q0, nst, dt, basis, mesh, g, alpha, n_iter=5, solver=solver, objective="l2_density",
+                                with_params=True, ctx=ctx)
+    sched = ctx.last_checkpoint_schedule()
+    assert sched["tape_steps"] == 1 and sched["snapshots"] == slots
+    assert sched["step_evaluations"] == revolve_evaluations(nst, slots) > nst
+    plan = igr.adjoint_plan(1, nst, basis, mesh, alpha, n_iter=5, solver=solver, ctx=ctx)  # the same, without running
+    assert plan == {"instances_per_group": 1, "tape_steps": 1, "snapshots": slots,
+                    "step_evaluations": sched["step_evaluations"]}
+    assert full[0] == rev[0]
+    for a, b in zip(full[1:5], rev[1:5]):
+        assert np.array_equal(a, b)
+    assert full[5] == rev[5] and full[6] == rev[6]
 
 
 @pytest.mark.parametrize("solver", ["chebyshev", "pcg"])
