@@ -77,6 +77,11 @@ class Context:
         """2D forward and tangent solves: replay repeated RK steps as CUDA graphs (default on)."""
         check(self, lib().igr_set_graphs(self.handle, C.c_int(1 if on else 0)))
 
+    def set_pcg_persistent(self, on):
+        """2D untaped PCG solves of one wave of tiles: one persistent launch per
+        solve (default on) or two kernels per iteration; bitwise the same."""
+        check(self, lib().igr_set_pcg_persistent(self.handle, C.c_int(1 if on else 0)))
+
     def set_autotune(self, on, cache_path=None):
         """Measure result-invariant launch choices (1D CTAs per instance, 2D fused
         or separate PCG inner products) on the first call of each batch shape and

@@ -165,6 +165,12 @@ int igr_set_graphs(igr_ctx* ctx, int on) {
   return IGR_OK;
 }
 
+int igr_set_pcg_persistent(igr_ctx* ctx, int on) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.pcg_persistent = on != 0;
+  return IGR_OK;
+}
+
 int igr_set_autotune(igr_ctx* ctx, int on, const char* cache_path) {
   if (!ctx) return IGR_EINVAL;
   ctx->c.err.clear();

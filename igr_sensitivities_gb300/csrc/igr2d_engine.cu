@@ -8,6 +8,7 @@
 #include "igr2d_kernels.cuh"
 #include "igr2d_launch.h"
 #include "igr2d_pcg_kernels.cuh"
+#include "igr2d_pcg_persist.cuh"
 #include "igr2d_pde_kernels.cuh"
 #include "igr2d_rev_kernels.cuh"
 #include "igr2d_sens_kernels.cuh"
@@ -486,8 +487,59 @@ static void inst_sum_after(Ctx& c, const Plan2D& P, const double* partials, bool
 // last block per instance forms pAp_k and alpha_k) and one pointwise kernel
 // (x, r and r . M^-1 r; its last block forms rz_{k+1} and beta_k). With a
 // tape slot, r_k, p_k, A p_k and the scalars are written straight into it.
+// CTAs of the persistent PCG kernel that the device holds at once.
+static int pcg_persist_capacity(Ctx& c, int np) {
+  int per_sm = 0, sms = 0;
+  NP_DISPATCH(np, per_sm = pcg_persist_blocks_per_sm<NPV>());
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device), "attr");
+  return per_sm * sms;
+}
+
+// The untaped solve runs as one persistent launch (k2_pcg_persist, bitwise the
+// two-kernel result) when the plan's tiles fit one wave of resident CTAs (one
+// tile per CTA) and it has at most PCG_PERSIST_MAX_INST instances: there the
+// two-kernel form pays two launches and two short kernels' latency per
+// iteration. Larger plans keep the two-kernel form, whose waves of tiles
+// hide those costs.
+static bool pcg_persistent(Ctx& c, const Plan2D& P, bool taped) {
+  if (taped || !c.pcg_persistent || (int)P.inst.size() > PCG_PERSIST_MAX_INST) return false;
+  const int cap = pcg_persist_capacity(c, P.np);
+  return cap >= 1 && P.ntiles() <= cap;
+}
+
+static void pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b,
+                                 const double* x0, double* xout, double* xa, double* xb, double* dbuf) {
+  const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
+  PcgPersistArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.op.tiles = P.d_tiles; a.op.inst = P.d_inst; a.op.B = P.B;
+  a.op.cm = st.cm; a.op.ckx = st.ckx; a.op.cky = st.cky; a.op.cpx = st.cpx; a.op.cpy = st.cpy; a.op.b = b;
+  a.op.cinvM = st.cinvM;
+  a.op.partials = c.ws.dbl("pcgp:part", nb);
+  a.ntiles = nb; a.ninst = ni; a.n_iter = n;
+  a.x0 = x0; a.xout = xout; a.r = xa; a.p[0] = xb; a.p[1] = dbuf; a.ap = c.ws.dbl("pcg:ap", P.NG);
+  a.upart = c.ws.dbl("pcgp:upart", nb);
+  a.scal = c.ws.dbl("pcg:scal", (size_t)pcg_scal_count(n, ni));
+  a.beta_cta = c.ws.dbl("pcgp:beta", (size_t)nb * ni);
+  a.eps = 1e-30;
+  const int nw = bar_words(nb);
+  unsigned* bar = static_cast<unsigned*>(c.ws.get("pcgp:bar", nw * sizeof(unsigned)));
+  cuda_check(cudaMemsetAsync(bar, 0, nw * sizeof(unsigned), c.stream), "barrier reset");
+  a.bar.words = bar; a.bar.status = c.d_status;
+  cudaError_t e = cudaSuccess;
+  {
+    LaunchScope ls(c, KID_APPLY);
+    NP_DISPATCH(P.np, e = launch_k2_pcg_persist<NPV>(a, nb, c.stream));
+  }
+  cuda_check(e, "persistent PCG launch");
+}
+
 static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b, const double* x0,
                       double* xout, bool taped, double* xa, double* xb, double* dbuf) {
+  if (pcg_persistent(c, P, taped)) {
+    pcg_solve_persistent(c, P, o, st, b, x0, xout, xa, xb, dbuf);
+    return;
+  }
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
   double* part = c.ws.dbl("red:part", nb);
@@ -548,7 +600,7 @@ static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& s
       LaunchScope ls(c, KID_OTHER);
       NP_DISPATCH(P.np, launch_k2_pcg_update<NPV>(u, P.ngroups(), c.stream));
     }
-    inst_sum_after(c, P, part, true, u.isum);
+    inst_sum_after(c, P, part, false, u.isum);
   }
   if (ch.trial) sum_trial_done(c, ch, timer.stop());
 }
@@ -654,6 +706,7 @@ static void check_status(Ctx& c) {
   int st = 0;
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
+  if (st & DEV_TIMEOUT) throw Error(6, "a grid barrier of the persistent PCG solve gave up waiting");
   if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
 }
 
@@ -847,10 +900,11 @@ void solve_elliptic2d(Ctx& c, const Plan2D& P, const double* const q[4], double*
   double* x0 = c.ws.dbl("sol:x0", NG);
   cuda_check(cudaMemcpyAsync(x0, Sig, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "x0 copy");
   st.Sout = Sig;
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
   stage_setup(c, P, st, always);
   stage_solve_b(c, P, o, st, st.b, x0, st.Sout, false, c.ws.dbl("sol:xa", NG), c.ws.dbl("sol:xb", NG),
                 c.ws.dbl("sol:d", NG));
-  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+  check_status(c);
 }
 
 void hyperbolic_rhs2d(Ctx& c, const Plan2D& P, const double* const q[4], const double* Sig, double* const k[4]) {
@@ -985,7 +1039,7 @@ int cg2d(Ctx& c, const Plan2D& P, const double* rho, const double* b, double* x,
     u.partials = part;
     u.isum = inst_sum0(cnt, RZ(k + 1), nullptr, RZ(k), BT(k), eps);
     { LaunchScope ls(c, KID_OTHER); NP_DISPATCH(P.np, launch_k2_pcg_update<NPV>(u, P.ngroups(), c.stream)); }
-    inst_sum_after(c, P, part, true, u.isum);
+    inst_sum_after(c, P, part, false, u.isum);
   };
   int iters = n;
   if (fixed) {
@@ -1573,7 +1627,9 @@ void forward_store_init2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const d
   for (int v = 0; v < 4; ++v) st.q[v] = snap0 + v * NG;
   recip(c, st.q[2], st.invr, NG);
   st.Sout = Sig;
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
   stage_solve(c, P, o, st, zero, c.ws.dbl("fst:xa", NG), c.ws.dbl("fst:xb", NG), c.ws.dbl("fst:d", NG));
+  check_status(c);
 }
 
 void forward_store_range2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const SnapSlot& slot, int k0, int k1) {
@@ -1760,13 +1816,14 @@ void pde_adjoint2d(Ctx& c, const Plan2D& P, int n_steps, const Solve2DOpts& o, i
   pde_checks(P, o, objective, n_steps);
   const long long NG = P.NG;
   PdeWork w = pde_work(c, P, o);
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
   pde_terminal(c, P, w, slot(n_steps), objective, prm);
   cuda_check(cudaMemsetAsync(w.Pi[0], 0, NG * sizeof(double), c.stream), "zero Pi");
   w.cur = 0;
   pde_steps(c, P, o, w, slot, n_steps, 0);
   for (int v = 0; v < 4; ++v)
     cuda_check(cudaMemcpyAsync(a_out[v], w.a[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "adjoint out");
-  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+  check_status(c);
 }
 
 void pde_adjoint_ic2d(Ctx& c, const Plan2D& Pf, const Plan2D& Pa, const double* const q0[4], int n_steps,
@@ -1810,6 +1867,7 @@ void pde_adjoint_ic2d(Ctx& c, const Plan2D& Pf, const Plan2D& Pa, const double* 
   forward_store_range2d(c, Pf, o, pass1, 0, n);
   pde_checks(Pa, o, objective, n);
   PdeWork w = pde_work(c, Pa, o);
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
   pde_terminal(c, Pa, w, pass1(n), objective, prm);
   cuda_check(cudaMemsetAsync(w.Pi[0], 0, NG * sizeof(double), c.stream), "zero Pi");
   w.cur = 0;
@@ -1821,7 +1879,7 @@ void pde_adjoint_ic2d(Ctx& c, const Plan2D& Pf, const Plan2D& Pa, const double* 
   }
   for (int v = 0; v < 4; ++v)
     cuda_check(cudaMemcpyAsync(a_out[v], w.a[v], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "adjoint out");
-  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+  check_status(c);
 }
 
 void pde_adjoint_rhs2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const double* snap, double* Pi,
@@ -1831,6 +1889,7 @@ void pde_adjoint_rhs2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const doub
   const long long NG = P.NG;
   const bool apos = any_alpha_pos(P);
   PdeWork w = pde_work(c, P, o);
+  cuda_check(cudaMemsetAsync(c.d_status, 0, sizeof(int), c.stream), "status reset");
   pde_prep(c, P, w, snap, apos);
   if (apos) {
     cuda_check(cudaMemcpyAsync(w.Pi[0], Pi, NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Pi in");
@@ -1845,7 +1904,7 @@ void pde_adjoint_rhs2d(Ctx& c, const Plan2D& P, const Solve2DOpts& o, const doub
     NP_DISPATCH(P.np, launch_k2_pde_rk<NPV>(r, P.ntiles(), c.stream));
   }
   if (apos) cuda_check(cudaMemcpyAsync(Pi, w.Pi[w.cur], NG * sizeof(double), cudaMemcpyDeviceToDevice, c.stream), "Pi out");
-  cuda_check(cudaStreamSynchronize(c.stream), "sync");
+  check_status(c);
 }
 
 double probe_fp64_tflops(Ctx& c) {

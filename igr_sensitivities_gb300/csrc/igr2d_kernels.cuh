@@ -305,16 +305,28 @@ struct ApplyArgs2D {
 // Partner data across one face: its value and end-node derivative of x, and its stiffness coefficient.
 struct Partner1 { double x, d, k; };
 
+// Shared memory of one tile's operator application: the tile's x, the x-phase
+// result and the end-node derivatives of every line.
+template <int NP>
+struct ApplySmem {
+  double x[Tiling2D<NP>::TE][Tiling2D<NP>::NN], yx[Tiling2D<NP>::TE][Tiling2D<NP>::NN];
+  double gxf[Tiling2D<NP>::TE][NP][2], gyf[Tiling2D<NP>::TE][NP][2];
+};
+
+// y = A x on tile tl (of instance I) with the EPI epilogue, by the CTA's
+// Tiling2D<NP>::NT threads (all of which call it; it synchronises the CTA
+// twice). Returns this thread's PCG inner-product partial (EPI_PCG0 / EPI_PCG;
+// 0 otherwise). k2_apply runs it on tile blockIdx.x; the persistent PCG kernel
+// on every tile of its CTA.
 template <int NP, int EPI>
-__global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
+__device__ __forceinline__ double apply_tile(const ApplyArgs2D& a, const Tile2D tl, const Inst2D& I, ApplySmem<NP>& sm) {
   using TL = Tiling2D<NP>;
-  constexpr int TE = TL::TE, NN = TL::NN, L = TL::L, TX = TL::TX, TY = TL::TY;
+  constexpr int L = TL::L, TX = TL::TX, TY = TL::TY;
   constexpr bool PCG = EPI == EPI_PCG0 || EPI == EPI_PCG;
-  constexpr int P2 = pow2_at_least(TL::NT);
-  __shared__ double s_x[TE][NN], s_yx[TE][NN], s_gxf[TE][NP][2], s_gyf[TE][NP][2];
-  __shared__ double s_red[PCG ? P2 : 1];
-  const Tile2D tl = a.tiles[blockIdx.x];
-  const Inst2D I = a.inst[tl.inst];
+  auto& s_x = sm.x;
+  auto& s_yx = sm.yx;
+  auto& s_gxf = sm.gxf;
+  auto& s_gyf = sm.gyf;
   const ElemView vr = elem_view<NP>(tl, I, 0), vc = elem_view<NP>(tl, I, 1);
   const BasisDev& B = a.B;
   const double hw = B.hw;
@@ -406,7 +418,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
     }
   }
   __syncthreads();
-  if (!PCG && !vc.valid) return;
+  if (!PCG && !vc.valid) return 0.0;
   double part = 0.0;  // PCG inner-product partial of this thread
 
   // ---- eta-phase: y faces of the column, y-stiffness transpose, mass, epilogue
@@ -476,6 +488,19 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
       }
     }
   }
+  return part;
+}
+
+template <int NP, int EPI>
+__global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply(ApplyArgs2D a) {
+  using TL = Tiling2D<NP>;
+  constexpr bool PCG = EPI == EPI_PCG0 || EPI == EPI_PCG;
+  constexpr int P2 = pow2_at_least(TL::NT);
+  __shared__ ApplySmem<NP> sm;
+  __shared__ double s_red[PCG ? P2 : 1];
+  const Tile2D tl = a.tiles[blockIdx.x];
+  const Inst2D I = a.inst[tl.inst];
+  const double part = apply_tile<NP, EPI>(a, tl, I, sm);
   if (PCG) {
     const double tot = block_sum<P2>(part, s_red);
     inst_sum_last_block(a.isum, tl.inst, I.ntiles, tot, a.partials, blockIdx.x, I.tile0, I.ntiles);

@@ -19,6 +19,7 @@ struct SensHypArgs2D;
 struct PdePrepArgs2D;
 struct PdeBArgs2D;
 struct PdeRkArgs2D;
+struct PcgPersistArgs;
 
 template <int NP> int threads2d();
 template <int NP> void launch_k2_setup(const SetupArgs2D& a, int nblocks, cudaStream_t s);
@@ -33,5 +34,9 @@ template <int NP> void launch_k2_pde_prep(const PdePrepArgs2D& a, int nblocks, c
 template <int NP> void launch_k2_pde_b(const PdeBArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void launch_k2_pde_rk(const PdeRkArgs2D& a, int nblocks, cudaStream_t s);
 template <int NP> void tile_shape2d(int* tx, int* ty);
+// Persistent PCG solve: resident CTAs per SM of k2_pcg_persist, and its
+// cooperative launch on `grid` CTAs (every CTA resident, or the launch fails).
+template <int NP> int pcg_persist_blocks_per_sm();
+template <int NP> cudaError_t launch_k2_pcg_persist(const PcgPersistArgs& a, int grid, cudaStream_t s);
 
 }  // namespace igrgpu

@@ -5,6 +5,7 @@
 #include "igr2d_rev_kernels.cuh"
 #include "igr2d_sens_kernels.cuh"
 #include "igr2d_pde_kernels.cuh"
+#include "igr2d_pcg_persist.cuh"
 
 namespace igrgpu {
 
@@ -54,6 +55,25 @@ template <int NP> void launch_k2_pde_rk(const PdeRkArgs2D& a, int nb, cudaStream
   k2_pde_rk<NP><<<nb, Tiling2D<NP>::NT, 0, s>>>(a);
 }
 
+template <int NP> int pcg_persist_blocks_per_sm() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k2_pcg_persist<NP>, Tiling2D<NP>::NT, 0) != cudaSuccess) return 0;
+  return n;
+}
+template <int NP> cudaError_t launch_k2_pcg_persist(const PcgPersistArgs& a, int grid, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid, 1, 1);
+  cfg.blockDim = dim3(Tiling2D<NP>::NT, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k2_pcg_persist<NP>, a);
+}
+
 #define IGR2D_INSTANTIATE(NP)                                                                        \
   template int threads2d<NP>();                                                                      \
   template void tile_shape2d<NP>(int*, int*);                                                        \
@@ -67,6 +87,8 @@ template <int NP> void launch_k2_pde_rk(const PdeRkArgs2D& a, int nb, cudaStream
   template void launch_k2_sens_hyp_rk<NP>(const SensHypArgs2D&, int, cudaStream_t);                   \
   template void launch_k2_pde_prep<NP>(const PdePrepArgs2D&, int, cudaStream_t);                       \
   template void launch_k2_pde_b<NP>(const PdeBArgs2D&, int, cudaStream_t);                             \
-  template void launch_k2_pde_rk<NP>(const PdeRkArgs2D&, int, cudaStream_t);
+  template void launch_k2_pde_rk<NP>(const PdeRkArgs2D&, int, cudaStream_t);                           \
+  template int pcg_persist_blocks_per_sm<NP>();                                                        \
+  template cudaError_t launch_k2_pcg_persist<NP>(const PcgPersistArgs&, int, cudaStream_t);
 
 }  // namespace igrgpu

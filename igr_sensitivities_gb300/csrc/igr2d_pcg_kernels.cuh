@@ -18,8 +18,11 @@
 //
 // The pointwise kernels (k2_pcg_update, k2_pcg_rev_update) run one block per
 // tile group (TILE_GROUP tiles of one instance): thread t takes node t of
-// every tile of the group, so the block reduction is paid once per group.
-// Group j of an instance writes its partial to partials[tile0 + j].
+// every tile of the group, so the block reduction's synchronisation is paid
+// once per group. The forward update reduces each tile of the group in its
+// own fixed tree and writes partials[tile]; the persistent PCG kernel forms
+// the same tile partials. The reverse update reduces the group as one and
+// group j of an instance writes partials[tile0 + j].
 #pragma once
 #include "igr2d_kernels.cuh"  // Tiling2D
 #include "igr_device.cuh"
@@ -49,7 +52,7 @@ struct PcgUpdateArgs {
   const double *x_in, *p, *ap, *r_in, *cinvM;
   double *x_out, *r_out;
   const double* al;         // per-instance alpha_k
-  double* partials;         // per-group partials of rz_{k+1}
+  double* partials;         // per-tile partials of rz_{k+1}
   InstSum isum;             // rz_{k+1} and beta_k
 };
 
@@ -57,42 +60,91 @@ struct PcgUpdateArgs {
 __host__ __device__ __forceinline__ int inst_groups(const Inst2D& I) { return (I.ntiles + TILE_GROUP - 1) / TILE_GROUP; }
 
 // Writes a group's partial (group j of the instance to partials[tile0 + j])
-// and, when fused, lets the instance's last group complete the sum.
+// and, when fused, lets the instance's last group complete the sum (the
+// reverse update's inner product).
 __device__ __forceinline__ void group_partial(const InstSum& isum, const TileGroup& g, const Inst2D& I, double tot,
                                               double* partials) {
   const int ng = inst_groups(I);
   inst_sum_last_block(isum, g.inst, ng, tot, partials, I.tile0 + (g.first - I.tile0) / TILE_GROUP, I.tile0, ng);
 }
 
+// The partial of one tile's r . M^-1 r: node idx of the tile (its index in
+// tile_node's order) contributes r_idx (r_idx m_idx) in slot idx of a 256-slot
+// fixed tree (slots past the tile's nodes hold 0). Both the update kernel and
+// the persistent PCG kernel form it this way, so their sums agree bitwise.
+template <int P2>
+__device__ __forceinline__ void tile_tree(double* s, int tid, int nthreads) {
+#pragma unroll
+  for (int w = P2 / 2; w > 0; w >>= 1) {
+    for (int v = tid; v < w; v += nthreads) s[v] += s[v + w];
+    __syncthreads();
+  }
+}
+
+// Thread 0 stores the group's tile partials (tile g.first + j to
+// partials[g.first + j]); with isum.cnt set the instance's last group (the
+// counter counts groups) sums the instance's tile partials and completes the
+// InstSum.
+__device__ __forceinline__ void group_tile_partials(const InstSum& a, const TileGroup& g, const Inst2D& I,
+                                                    const double* vals, int stride, double* partials) {
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < g.count; ++j) partials[g.first + j] = vals[j * stride];
+    if (a.cnt) {
+      __threadfence();
+      s_last = atomicAdd(a.cnt + g.inst, 1) == inst_groups(I) - 1;
+    }
+  }
+  if (!a.cnt) return;
+  __syncthreads();
+  if (!s_last || threadIdx.x >= 32) return;
+  __threadfence();
+  const double sum = warp_sum_partials(partials + I.tile0, I.ntiles);
+  if (threadIdx.x == 0) {
+    inst_sum_finish(a, g.inst, sum);
+    a.cnt[g.inst] = 0;
+  }
+}
+
 template <int NP>
 __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
   constexpr int P2 = PCG_THREADS, G = TILE_GROUP;
-  __shared__ double s_red[P2];
+  constexpr int cnt = Tiling2D<NP>::TE * NP * NP;
+  static_assert(cnt <= P2, "one node of each tile per thread");
+  __shared__ double s_red[G][P2];
   const TileGroup g = a.groups[blockIdx.x];
   const Inst2D I = a.inst[g.inst];
   const double al = a.al[g.inst];
-  constexpr int cnt = Tiling2D<NP>::TE * NP * NP;
-  double part = 0.0;
-  for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-    long long n[G];
-    bool ok[G];
+  const int idx = threadIdx.x;
+  long long n[G];
+  bool ok[G];
 #pragma unroll
-    for (int j = 0; j < G; ++j) ok[j] = j < g.count && tile_node<NP>(a.tiles[g.first + j], I, idx, &n[j]);
-    double p[G], ap[G], x[G], r[G], im[G];
+  for (int j = 0; j < G; ++j) ok[j] = idx < cnt && j < g.count && tile_node<NP>(a.tiles[g.first + j], I, idx, &n[j]);
+  double p[G], ap[G], x[G], r[G], im[G];
 #pragma unroll
-    for (int j = 0; j < G; ++j)
-      if (ok[j]) { p[j] = a.p[n[j]]; ap[j] = a.ap[n[j]]; x[j] = a.x_in[n[j]]; r[j] = a.r_in[n[j]]; im[j] = a.cinvM[n[j]]; }
+  for (int j = 0; j < G; ++j)
+    if (ok[j]) { p[j] = a.p[n[j]]; ap[j] = a.ap[n[j]]; x[j] = a.x_in[n[j]]; r[j] = a.r_in[n[j]]; im[j] = a.cinvM[n[j]]; }
 #pragma unroll
-    for (int j = 0; j < G; ++j)
-      if (ok[j]) {
-        a.x_out[n[j]] = fma(al, p[j], x[j]);
-        const double rn = fma(-al, ap[j], r[j]);
-        a.r_out[n[j]] = rn;
-        part = fma(rn, rn * im[j], part);
-      }
+  for (int j = 0; j < G; ++j) {
+    double part = 0.0;
+    if (ok[j]) {
+      a.x_out[n[j]] = fma(al, p[j], x[j]);
+      const double rn = fma(-al, ap[j], r[j]);
+      a.r_out[n[j]] = rn;
+      part = fma(rn, rn * im[j], 0.0);
+    }
+    s_red[j][idx] = part;
   }
-  const double tot = block_sum<P2>(part, s_red);
-  group_partial(a.isum, g, I, tot, a.partials);
+  __syncthreads();
+#pragma unroll
+  for (int w = P2 / 2; w > 0; w >>= 1) {
+    if (idx < w) {
+#pragma unroll
+      for (int j = 0; j < G; ++j) s_red[j][idx] += s_red[j][idx + w];
+    }
+    __syncthreads();
+  }
+  group_tile_partials(a.isum, g, I, &s_red[0][0], P2, a.partials);
 }
 
 // ---------------------------------------------------------------------------
@@ -171,7 +223,7 @@ void launch_k2_pcg_rev_update(const PcgRevArgs& a, int nblocks, cudaStream_t s) 
 // Per-instance sums in a separate launch (InstSum with cnt null): one warp
 // per instance over the instance's tile partials, or its group partials when
 // grouped.
-__global__ void __launch_bounds__(32) k2_inst_sum(const Inst2D* inst, const double* partials, int grouped, InstSum a) {
+static __global__ void __launch_bounds__(32) k2_inst_sum(const Inst2D* inst, const double* partials, int grouped, InstSum a) {
   const int i = blockIdx.x;
   const Inst2D I = inst[i];
   const double s = warp_sum_partials(partials + I.tile0, grouped ? inst_groups(I) : I.ntiles);

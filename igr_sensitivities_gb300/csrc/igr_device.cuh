@@ -72,7 +72,7 @@ enum : int {
 };
 
 // Status word shared by the kernels and the host (device memory).
-enum : int { DEV_OK = 0, DEV_NONFINITE = 1 };
+enum : int { DEV_OK = 0, DEV_NONFINITE = 1, DEV_TIMEOUT = 2 };
 
 __device__ __forceinline__ void flag_nonfinite(int* status) {
   if (status) atomicOr(status, DEV_NONFINITE);

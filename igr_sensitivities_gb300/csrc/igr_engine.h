@@ -96,6 +96,7 @@ struct Ctx {
   int cluster1d = 0;            // 1D: CTAs per instance (0 = chosen per launch)
   int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
   bool use_graphs = true;       // replay repeated forward steps as CUDA graphs
+  bool pcg_persistent = true;   // 2D untaped PCG solves of one wave of tiles in one persistent launch
   Autotune tune;
   Profiler prof;
 };

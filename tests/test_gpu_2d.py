@@ -439,3 +439,39 @@ def test_pcg_forward_and_adjoint_other_degrees(igr, oracle, p, nex, ney):
     assert num <= RTOL_GRAD * den
     assert abs(res[5] - dgr) <= RTOL_GRAD * abs(dgr)
     assert abs(res[6] - dar) <= RTOL_GRAD * abs(dar)
+
+
+@pytest.mark.parametrize("case", ["forward", "forward_batch", "tangent", "solve", "forward_128"])
+def test_persistent_pcg_equals_two_kernel_form(igr, oracle, case):
+    """The persistent PCG solve (one cooperative launch per solve, grid
+    barriers between its phases) gives bitwise the two-kernel result, also
+    when the forward's RK steps replay as CUDA graphs."""
+    from igr_sensitivities_gb300 import Context
+    g = 1.4
+    ne = 128 if case == "forward_128" else 8
+    basis, mesh, _ = setup(igr, oracle, 3, ne, 6 if ne == 8 else ne)
+    alpha = 3.0 * (1 / ne) ** 2
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 7), width=0.12 if ne == 8 else 0.03)
+    dt = W.cfl_dt_2d(mesh, 3, q0, g, 0.1)
+
+    def run(ctx):
+        rng = np.random.default_rng(4)
+        if case in ("forward", "forward_128"):
+            return igr.run_forward(*q0, dt, 3 * dt * 0.999, basis, mesh, g, alpha, n_iter=12, solver="pcg", ctx=ctx)
+        if case == "forward_batch":
+            q = np.stack([np.stack([flat(a) for a in q0])] * 3)
+            return igr.forward_batch(q, [1.3, 1.4, 1.5], [alpha, 0.5 * alpha, 2 * alpha], [dt] * 3, 3, basis, mesh,
+                                     n_iter=10, solver="pcg", ctx=ctx)
+        if case == "tangent":
+            s0 = [rng.standard_normal(mesh.x.shape) * 1e-3 for _ in range(4)]
+            return igr.run_sensitivity(*q0, *s0, dt, 3 * dt * 0.999, basis, mesh, g, alpha, n_iter=9, solver="pcg",
+                                       ctx=ctx)
+        S = np.zeros(mesh.x.shape, order="F")
+        igr.solve_elliptic_(S, *q0, basis, mesh, alpha, n_iter=25, solver="pcg", ctx=ctx)
+        return (S,)
+
+    a_ctx, b_ctx = Context(0), Context(0)
+    b_ctx.set_pcg_persistent(False)
+    A, B = run(a_ctx), run(b_ctx)
+    for x, y in zip(A, B):
+        assert np.array_equal(np.asarray(x), np.asarray(y))

@@ -64,6 +64,7 @@ def test_2d_tuned_pcg_sums_keep_results(igr, oracle, solver, tmp_path):
     run = lambda ctx: igr.run_forward(*q0, dt, 5 * dt * 0.999, basis, mesh, g, alpha, n_iter=7, solver=solver, ctx=ctx)
     plain = run(Context(0))
     ctx = Context(0)
+    ctx.set_pcg_persistent(False)  # the inner-product form is a choice of the two-kernel PCG iteration
     cache = tmp_path / "tune2d.txt"
     ctx.set_autotune(True, str(cache))
     tuned = run(ctx)
