@@ -18,9 +18,10 @@
 // The barrier counts arrivals in groups of 32 CTAs (one counter per group, on
 // its own cache line, then one top counter), so that no single address takes
 // an atomic from every CTA, and releases the grid by advancing a generation
-// word. Waits are bounded: a CTA that waits longer than PCG_BARRIER_NS sets
-// DEV_TIMEOUT in the status word and the kernel returns (the host reports
-// IGR_ETIMEOUT). With a cooperative launch every CTA is resident, so the limit
+// word; its atomics and loads carry GPU-scope release / acquire semantics
+// instead of full fences. Waits are bounded: a CTA that waits longer than
+// PCG_BARRIER_NS sets DEV_TIMEOUT in the status word and the kernel returns
+// (the host reports IGR_ETIMEOUT). With a cooperative launch every CTA is resident, so the limit
 // is a guard, not the path.
 #pragma once
 #include "igr2d_kernels.cuh"
@@ -49,26 +50,39 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+// atomic add with acquire-release semantics at GPU scope; returns the old value
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
 
-// Thread 0: counts this CTA's arrival; true for the CTA that arrives last.
+// Thread 0, after a CTA barrier: counts this CTA's arrival (releasing the
+// CTA's writes and acquiring those of the CTAs that arrived before it in its
+// group); true for the CTA that arrives last overall. Grids of at most
+// BAR_GROUP CTAs count on the top counter alone.
 __device__ __forceinline__ bool bar_arrive(const GridBarrier& g, unsigned nblocks) {
-  const unsigned grp = blockIdx.x / BAR_GROUP, ngrp = (nblocks + BAR_GROUP - 1) / BAR_GROUP;
-  const unsigned members = min((unsigned)BAR_GROUP, nblocks - grp * BAR_GROUP);
-  unsigned* gc = g.words + 64 + 32 * grp;
-  __threadfence();
-  if (atomicAdd(gc, 1u) != members - 1) return false;
-  *gc = 0;  // every member has arrived; none touches it again before the release
-  __threadfence();
-  if (atomicAdd(g.words + 32, 1u) != ngrp - 1) return false;
-  g.words[32] = 0;
+  const unsigned ngrp = (nblocks + BAR_GROUP - 1) / BAR_GROUP;
+  if (ngrp > 1) {
+    const unsigned grp = blockIdx.x / BAR_GROUP;
+    const unsigned members = min((unsigned)BAR_GROUP, nblocks - grp * BAR_GROUP);
+    unsigned* gc = g.words + 64 + 32 * grp;
+    if (atom_add_acq_rel_u32(gc, 1u) != members - 1) return false;
+    st_relaxed_u32(gc, 0u);  // every member has arrived; none touches it again before the release
+  }
+  if (atom_add_acq_rel_u32(g.words + 32, 1u) != (ngrp > 1 ? ngrp : nblocks) - 1) return false;
+  st_relaxed_u32(g.words + 32, 0u);
   return true;
 }
 
 // Grid barrier of the launch's nblocks CTAs; every thread calls it. The CTA
 // that arrives last runs last_work() (every thread of it; the partials every
-// CTA wrote before arriving are visible to it) before releasing the others.
-// Writes before the barrier are visible to every CTA after it. Returns false
-// when a wait timed out (the caller returns).
+// CTA wrote before arriving are visible to it) and then releases the others by
+// advancing the generation. Writes before the barrier are visible to every CTA
+// after it. Returns false when a wait timed out (the caller returns).
 template <class F>
 __device__ __forceinline__ bool grid_barrier(const GridBarrier& g, unsigned nblocks, F&& last_work) {
   __shared__ unsigned s_gen;
@@ -81,13 +95,9 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& g, unsigned nblo
   __syncthreads();
   int ok = 1;
   if (s_last) {
-    __threadfence();
     last_work();
     __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(g.words, 1u);
-    }
+    if (threadIdx.x == 0) atom_add_acq_rel_u32(g.words, 1u);
   } else if (threadIdx.x == 0) {
     const unsigned long long t0 = global_ns();
     while (ld_acquire_u32(g.words) == s_gen) {
@@ -96,11 +106,10 @@ __device__ __forceinline__ bool grid_barrier(const GridBarrier& g, unsigned nblo
         ok = 0;
         break;
       }
-      __nanosleep(64);
+      __nanosleep(32);
     }
   }
   if (threadIdx.x == 0) {
-    __threadfence();
     if (ok && (*(volatile int*)g.status & DEV_TIMEOUT)) ok = 0;
     s_ok = ok;
   }
