@@ -501,8 +501,13 @@ static int pcg_persist_capacity(Ctx& c, int np) {
 // two-kernel form pays two launches and two short kernels' latency per
 // iteration. Larger plans keep the two-kernel form, whose waves of tiles
 // hide those costs.
-static bool pcg_persistent(Ctx& c, const Plan2D& P, bool taped) {
+static bool pcg_persistent(Ctx& c, const Plan2D& P, bool taped, int n_iter) {
   if (taped || !c.pcg_persistent || (int)P.inst.size() > PCG_PERSIST_MAX_INST) return false;
+  if ((2LL * n_iter + 1) * PCG_COUNTED_TILES >= (1LL << 31)) return false;  // arrival counts
+  int max_tiles = 0;
+  NP_DISPATCH(P.np, max_tiles = persist_max_inst_tiles<NPV>());
+  for (const auto& I : P.inst)
+    if (I.ntiles > max_tiles) return false;
   const int cap = pcg_persist_capacity(c, P.np);
   return cap >= 1 && P.ntiles() <= cap;
 }
@@ -515,17 +520,30 @@ static void pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, 
   a.op.tiles = P.d_tiles; a.op.inst = P.d_inst; a.op.B = P.B;
   a.op.cm = st.cm; a.op.ckx = st.ckx; a.op.cky = st.cky; a.op.cpx = st.cpx; a.op.cpy = st.cpy; a.op.b = b;
   a.op.cinvM = st.cinvM;
-  a.op.partials = c.ws.dbl("pcgp:part", nb);
+  // partial slots of the 2n + 1 reductions, the scalar record and (published hand-off) the scalars' copies
+  int max_inst_tiles = 0;
+  for (const auto& I : P.inst) max_inst_tiles = std::max(max_inst_tiles, I.ntiles);
+  a.counted = max_inst_tiles <= PCG_COUNTED_TILES ? 1 : 0;
+  const long long npart = (2LL * n + 1) * nb, nscal = pcg_scal_count(n, ni);
+  const long long stride = ((2LL * n + 1) * ni + 15) / 16 * 16;  // copies on separate 128-byte lines
+  const long long nbc = a.counted ? 0 : PCG_BCAST * stride;
+  double* slots = c.ws.dbl("pcgp:slots", (size_t)(npart + nbc + nscal));
+  a.slots = slots;
+  a.bcast = slots + npart;
+  a.bcast_stride = stride;
+  a.scal = slots + npart + nbc;
+  a.cnt = static_cast<unsigned*>(c.ws.get("pcgp:cnt", sizeof(unsigned) * PCG_CNT_STRIDE * ni));
   a.ntiles = nb; a.ninst = ni; a.n_iter = n;
   a.x0 = x0; a.xout = xout; a.r = xa; a.p[0] = xb; a.p[1] = dbuf; a.ap = c.ws.dbl("pcg:ap", P.NG);
-  a.upart = c.ws.dbl("pcgp:upart", nb);
-  a.scal = c.ws.dbl("pcg:scal", (size_t)pcg_scal_count(n, ni));
-  a.beta_cta = c.ws.dbl("pcgp:beta", (size_t)nb * ni);
   a.eps = 1e-30;
-  const int nw = bar_words(nb);
-  unsigned* bar = static_cast<unsigned*>(c.ws.get("pcgp:bar", nw * sizeof(unsigned)));
-  cuda_check(cudaMemsetAsync(bar, 0, nw * sizeof(unsigned), c.stream), "barrier reset");
-  a.bar.words = bar; a.bar.status = c.d_status;
+  a.status = c.d_status;
+  if (a.counted) {
+    cuda_check(cudaMemsetAsync(a.cnt, 0, sizeof(unsigned) * PCG_CNT_STRIDE * ni, c.stream), "arrival counters");
+  } else {
+    LaunchScope ls(c, KID_OTHER);
+    k2_pcg_persist_fill<<<grid_for(npart + nbc), 256, 0, c.stream>>>(slots, npart + nbc);
+  }
+  cuda_check(cudaGetLastError(), "persistent PCG slot fill");
   cudaError_t e = cudaSuccess;
   {
     LaunchScope ls(c, KID_APPLY);
@@ -536,7 +554,7 @@ static void pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, 
 
 static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b, const double* x0,
                       double* xout, bool taped, double* xa, double* xb, double* dbuf) {
-  if (pcg_persistent(c, P, taped)) {
+  if (pcg_persistent(c, P, taped, o.n_iter)) {
     pcg_solve_persistent(c, P, o, st, b, x0, xout, xa, xb, dbuf);
     return;
   }

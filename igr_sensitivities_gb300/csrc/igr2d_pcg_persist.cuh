@@ -4,141 +4,213 @@
 // The two-kernel form (k2_apply<EPI_PCG> + k2_pcg_update per iteration, each
 // completing its inner product in its last block) spends much of a small
 // instance's iteration on two launches and the latency of two short kernels.
-// Here one grid of co-resident CTAs (a cooperative launch; at most one tile per
-// CTA) runs the whole solve, with a grid barrier after each inner product:
-//   phase A: p_k formed on load, A p_k, per-tile partials of p_k . A p_k
-//            | barrier: the last CTA to arrive forms pAp_k and alpha_k |
-//   phase B: x_{k+1}, r_{k+1} on the CTA's own tiles, per-tile partials of r . M^-1 r
-//            | barrier: the last CTA to arrive forms rz_{k+1} and beta_k |
+// Here one grid of co-resident CTAs (a cooperative launch, one tile per CTA)
+// runs the whole solve. Instances are independent, so there is no grid-wide
+// barrier, only a hand-off of each inner product among the instance's CTAs:
+//   phase A: p_k formed on load, A p_k; the tile's partial of p_k . A p_k
+//            | pAp_k, alpha_k = rz_k / (pAp_k + eps) |
+//   phase B: x_{k+1}, r_{k+1} on the CTA's tile; its partial of r . M^-1 r
+//            | rz_{k+1}, beta_k = rz_{k+1} / (rz_k + eps) |
 // The operator runs the same apply_tile code and block tree as k2_apply, the
 // update forms each tile's partial in the same 256-slot tree as k2_pcg_update,
-// and the scalars come from the same canonical sums of the tile partials, so
-// the result is bitwise the two-kernel result.
+// and the partials are summed in warp_sum_partials' order, so the result is
+// bitwise the two-kernel result.
 //
-// The barrier counts arrivals in groups of 32 CTAs (one counter per group, on
-// its own cache line, then one top counter), so that no single address takes
-// an atomic from every CTA, and releases the grid by advancing a generation
-// word; its atomics and loads carry GPU-scope release / acquire semantics
-// instead of full fences. Waits are bounded: a CTA that waits longer than
-// PCG_BARRIER_NS sets DEV_TIMEOUT in the status word and the kernel returns
-// (the host reports IGR_ETIMEOUT). With a cooperative launch every CTA is resident, so the limit
-// is a guard, not the path.
+// Every reduction e (0: r_0 . p_0; 2k + 1: p_k . A p_k; 2k + 2:
+// r_{k+1} . M^-1 r_{k+1}) has its own partial slot per tile, so no slot is
+// reused within a launch. The hand-off has two forms, by instance size:
+//   counted (instances of at most PCG_COUNTED_TILES tiles): a CTA stores its
+//     partial and adds 1 to its instance's arrival counter with release
+//     semantics; each CTA waits (acquire loads of the one counter word) until
+//     the count reaches (e + 1) x tiles, then reads all of the instance's
+//     partials and forms the sum itself;
+//   published (larger instances, whose partials all CTAs reading at once
+//     would crowd a few L2 lines): the partial slots and the scalars' slots
+//     hold PCG_SENTINEL (a signalling-NaN bit pattern, which no arithmetic
+//     produces) from a fill before the launch; a CTA stores its partial with
+//     release semantics; the instance's first tile (its writer CTA) polls the
+//     instance's slots (relaxed loads, many in flight at once) until none
+//     holds the sentinel, acquires, sums and publishes the scalar with release
+//     semantics to PCG_BCAST copies on separate lines, and every other CTA
+//     polls the copy of its own tile number modulo PCG_BCAST.
+// Waits are bounded: a CTA that waits longer than PCG_WAIT_NS sets DEV_TIMEOUT
+// in the status word and the kernel returns (the host reports IGR_ETIMEOUT).
+// With a cooperative launch every CTA is resident, so the limit is a guard,
+// not the path.
 #pragma once
 #include "igr2d_kernels.cuh"
 #include "igr2d_pcg_kernels.cuh"
 
 namespace igrgpu {
 
-constexpr int PCG_PERSIST_MAX_INST = 32;            // instances of a plan the persistent form takes
-constexpr long long PCG_BARRIER_NS = 1000000000LL;  // grid barrier wait limit (1 s)
-constexpr int BAR_GROUP = 32;                       // CTAs per arrival counter
-// barrier words: generation at [0], top counter at [32], group counter g at [64 + 32 g] (128-byte lines)
-__host__ __device__ constexpr int bar_words(int nblocks) { return 64 + 32 * ((nblocks + BAR_GROUP - 1) / BAR_GROUP); }
+constexpr int PCG_PERSIST_MAX_INST = 32;             // instances of a plan the persistent form takes
+constexpr long long PCG_WAIT_NS = 1000000000LL;      // limit of one wait (1 s)
+constexpr unsigned long long PCG_SENTINEL = 0x7FF4DEAD7FF4DEADull;  // "not yet written" (signalling NaN)
+constexpr int PCG_COUNTED_TILES = 256;               // instances up to this many tiles: counted hand-off
+constexpr int PCG_BCAST = 32;                        // copies of a published scalar
+constexpr int PCG_CNT_STRIDE = 32;                   // words between arrival counters (one 128-byte line each)
 
-struct GridBarrier {
-  unsigned* words;  // zero before the launch
-  int* status;      // DEV_TIMEOUT on a wait past the limit
-};
+// Partial slots each writer thread polls, and so the tiles an instance may
+// have (slots per thread x threads per CTA, about 1280).
+template <int NP>
+__host__ __device__ constexpr int persist_slots_per_thread() {
+  return (1280 + Tiling2D<NP>::NT - 1) / Tiling2D<NP>::NT < 32 ? (1280 + Tiling2D<NP>::NT - 1) / Tiling2D<NP>::NT : 32;
+}
+template <int NP>
+__host__ __device__ constexpr int persist_max_inst_tiles() { return persist_slots_per_thread<NP>() * Tiling2D<NP>::NT; }
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-// atomic add with acquire-release semantics at GPU scope; returns the old value
-__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
-  unsigned old;
-  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_release_f64(double* p, double v) {
+  asm volatile("st.release.gpu.global.b64 [%0], %1;" :: "l"(p), "l"(__double_as_longlong(v)) : "memory");
 }
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
-// Thread 0, after a CTA barrier: counts this CTA's arrival (releasing the
-// CTA's writes and acquiring those of the CTAs that arrived before it in its
-// group); true for the CTA that arrives last overall. Grids of at most
-// BAR_GROUP CTAs count on the top counter alone.
-__device__ __forceinline__ bool bar_arrive(const GridBarrier& g, unsigned nblocks) {
-  const unsigned ngrp = (nblocks + BAR_GROUP - 1) / BAR_GROUP;
-  if (ngrp > 1) {
-    const unsigned grp = blockIdx.x / BAR_GROUP;
-    const unsigned members = min((unsigned)BAR_GROUP, nblocks - grp * BAR_GROUP);
-    unsigned* gc = g.words + 64 + 32 * grp;
-    if (atom_add_acq_rel_u32(gc, 1u) != members - 1) return false;
-    st_relaxed_u32(gc, 0u);  // every member has arrived; none touches it again before the release
+struct PcgPersistArgs {
+  ApplyArgs2D op;                  // tiles, instances, basis, coefficients, b, cinvM
+  int ntiles, ninst, n_iter;
+  int counted;                     // counted hand-off (else published)
+  const double* x0;                // warm start (read only)
+  double *xout, *r, *p[2], *ap;    // solution and the CG vectors
+  double* slots;                   // partials: reduction e, tile t at slots[e * ntiles + t]
+  double* scal;                    // per instance: rz_0..rz_n, pAp_0..pAp_{n-1}, alpha, beta (as pcg_solve)
+  double* bcast;                   // published: copy j of reduction e's scalar of instance i at
+  long long bcast_stride;          //   bcast[j * bcast_stride + e * ninst + i]
+  unsigned* cnt;                   // counted: arrivals of instance i at cnt[i * PCG_CNT_STRIDE]
+  double eps;
+  int* status;
+  // at the launch: counted, cnt zero; published, slots and bcast PCG_SENTINEL
+};
+
+// The canonical sum of stage[0 .. count) (warp_sum_partials' order: lane l
+// adds l, l + 32, ... in turn, then a shuffle tree) by warp 0, to every thread.
+__device__ __forceinline__ double stage_sum(const double* stage, int count, double* s_sum) {
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double acc = 0.0;
+    for (int k = threadIdx.x; k < count; k += 32) acc += stage[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) *s_sum = acc;
   }
-  if (atom_add_acq_rel_u32(g.words + 32, 1u) != (ngrp > 1 ? ngrp : nblocks) - 1) return false;
-  st_relaxed_u32(g.words + 32, 0u);
-  return true;
+  __syncthreads();
+  return *s_sum;
 }
 
-// Grid barrier of the launch's nblocks CTAs; every thread calls it. The CTA
-// that arrives last runs last_work() (every thread of it; the partials every
-// CTA wrote before arriving are visible to it) and then releases the others by
-// advancing the generation. Writes before the barrier are visible to every CTA
-// after it. Returns false when a wait timed out (the caller returns).
-template <class F>
-__device__ __forceinline__ bool grid_barrier(const GridBarrier& g, unsigned nblocks, F&& last_work) {
-  __shared__ unsigned s_gen;
-  __shared__ int s_last, s_ok;
+// Counted hand-off, every thread; thread 0 has stored the CTA's partial.
+// Counts the CTA's arrival, waits for the instance's target count, stages the
+// partials and returns their sum. *s_ok = 0 on timeout.
+__device__ __forceinline__ double counted_sum(unsigned* cnt, unsigned target, const double* part, int count,
+                                              double* stage, int* status, double* s_sum, int* s_ok) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    s_gen = ld_acquire_u32(g.words);
-    s_last = bar_arrive(g, nblocks) ? 1 : 0;
-  }
-  __syncthreads();
-  int ok = 1;
-  if (s_last) {
-    last_work();
-    __syncthreads();
-    if (threadIdx.x == 0) atom_add_acq_rel_u32(g.words, 1u);
-  } else if (threadIdx.x == 0) {
+    red_release_add_u32(cnt, 1u);
+    int ok = 1;
     const unsigned long long t0 = global_ns();
-    while (ld_acquire_u32(g.words) == s_gen) {
-      if (global_ns() - t0 > (unsigned long long)PCG_BARRIER_NS) {
-        atomicOr(g.status, DEV_TIMEOUT);
+    while ((int)(ld_acquire_u32(cnt) - target) < 0) {
+      if (global_ns() - t0 > (unsigned long long)PCG_WAIT_NS) {
+        atomicOr(status, DEV_TIMEOUT);
         ok = 0;
         break;
       }
-      __nanosleep(32);
+      __nanosleep(20);
     }
-  }
-  if (threadIdx.x == 0) {
-    if (ok && (*(volatile int*)g.status & DEV_TIMEOUT)) ok = 0;
-    s_ok = ok;
+    *s_ok = ok;
   }
   __syncthreads();
-  return s_ok != 0;
+#pragma unroll 4
+  for (int j = threadIdx.x; j < count; j += blockDim.x) stage[j] = __ldcg(part + j);
+  return stage_sum(stage, count, s_sum);
 }
 
-struct PcgPersistArgs {
-  ApplyArgs2D op;                  // tiles, instances, basis, coefficients, b, cinvM; op.partials: per tile
-  int ntiles, ninst, n_iter;
-  const double* x0;                // warm start (read only)
-  double *xout, *r, *p[2], *ap;    // solution and the CG vectors
-  double* upart;                   // per-tile partials of r . M^-1 r
-  double* scal;                    // per instance: rz_0..rz_n, pAp_0..pAp_{n-1}, alpha, beta (as pcg_solve)
-  double* beta_cta;                // per CTA and instance: beta_{k-1} for the operator loads
-  double eps;
-  GridBarrier bar;
-};
-
-// Warp 0 (of the last CTA): the canonical sum of each instance's tile
-// partials, handed to f(i, sum) on lane 0.
-template <class F>
-__device__ __forceinline__ void inst_tile_sums(const Inst2D* inst, int ninst, const double* partials, F&& f) {
-  if (threadIdx.x >= 32) return;
-  for (int i = 0; i < ninst; ++i) {
-    const Inst2D I = inst[i];
-    const double s = warp_sum_partials(partials + I.tile0, I.ntiles);
-    if (threadIdx.x == 0) f(i, s);
+// Published hand-off, writer CTA, every thread: waits until none of the
+// instance's partial slots (slots[0 .. count)) holds the sentinel, stages
+// them, acquires and returns their sum. Thread j polls slots j, j + NT, ...
+// with up to 16 of its pending loads in flight at once. *s_ok = 0 on timeout.
+template <int NP>
+__device__ __forceinline__ double gathered_sum(const double* slots, int count, double* stage, int* status,
+                                               double* s_sum, int* s_ok) {
+  constexpr int SPT = persist_slots_per_thread<NP>();
+  constexpr int NT = Tiling2D<NP>::NT;
+  constexpr int CH = 16;  // loads in flight per thread (registers)
+  const int tid = threadIdx.x;
+  __syncthreads();
+  if (tid == 0) *s_ok = 1;
+  __syncthreads();
+  unsigned pend = 0;
+#pragma unroll
+  for (int m = 0; m < SPT; ++m)
+    if (tid + m * NT < count) pend |= 1u << m;
+  const unsigned long long t0 = global_ns();
+  while (pend) {
+#pragma unroll
+    for (int c0 = 0; c0 < SPT; c0 += CH) {
+      unsigned long long v[CH];
+#pragma unroll
+      for (int j = 0; j < CH; ++j) {
+        const int m = c0 + j;
+        v[j] = m < SPT && ((pend >> m) & 1u) ? ld_relaxed_u64(slots + tid + m * NT) : PCG_SENTINEL;
+      }
+#pragma unroll
+      for (int j = 0; j < CH; ++j) {
+        const int m = c0 + j;
+        if (m < SPT && ((pend >> m) & 1u) && v[j] != PCG_SENTINEL) {
+          stage[tid + m * NT] = __longlong_as_double((long long)v[j]);
+          pend &= ~(1u << m);
+        }
+      }
+    }
+    if (!pend) break;
+    if (global_ns() - t0 > (unsigned long long)PCG_WAIT_NS) {
+      atomicOr(status, DEV_TIMEOUT);
+      *s_ok = 0;
+      break;
+    }
+    __nanosleep(20);
   }
+  fence_acq_rel_gpu();
+  return stage_sum(stage, count, s_sum);
+}
+
+// Published hand-off, every thread of a CTA other than the writer: waits
+// until *slot no longer holds the sentinel and returns it (acquired).
+// *s_ok = 0 on timeout.
+__device__ __forceinline__ double wait_published(const double* slot, int* status, double* s_val, int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned long long v;
+    const unsigned long long t0 = global_ns();
+    while ((v = ld_relaxed_u64(slot)) == PCG_SENTINEL) {
+      if (global_ns() - t0 > (unsigned long long)PCG_WAIT_NS) {
+        atomicOr(status, DEV_TIMEOUT);
+        ok = 0;
+        break;
+      }
+      __nanosleep(20);
+    }
+    fence_acq_rel_gpu();
+    *s_val = __longlong_as_double((long long)v);
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_val;
 }
 
 template <int NP>
@@ -148,32 +220,59 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT, 8) k2_pcg_persist(PcgPersist
   constexpr int UV = PCG_THREADS;        // slots of a tile's update tree
   constexpr int cnt = TL::TE * NP * NP;  // nodes of a tile
   static_assert(cnt <= UV, "one tree slot per node");
+  static_assert(TL::NT >= PCG_BCAST, "one thread per published copy");
   __shared__ ApplySmem<NP> sm;
   __shared__ double s_red[UV > P2 ? UV : P2];
-  const unsigned G = gridDim.x;
+  __shared__ double s_val, s_beta[PCG_PERSIST_MAX_INST], s_stage[persist_max_inst_tiles<NP>()];
+  __shared__ int s_ok;
+  const int t = blockIdx.x;  // the CTA's tile (the grid is the plan's tiles)
   const int ni = a.ninst, n = a.n_iter;
+  const Tile2D tl = a.op.tiles[t];
+  const Inst2D I = a.op.inst[tl.inst];
+  const bool writer = t == I.tile0;  // the instance's first tile records (and publishes) its scalars
+  const long long is = tl.inst;
   double* RZ = a.scal;
   double* PAP = a.scal + (long long)(n + 1) * ni;
   double* AL = a.scal + (long long)(2 * n + 1) * ni;
   double* BT = a.scal + (long long)(3 * n + 1) * ni;
-  double* beta = a.beta_cta + (long long)blockIdx.x * ni;
   const double eps = a.eps;
 
-  // ---- r_0 = b - A x_0, p_0 = M^-1 r_0, partials of r_0 . p_0
+  // Reduction e of the instance, after the CTA's partial tot (known to thread
+  // 0) is formed: stores it and sets *scalar = scal_of(sum) in every thread;
+  // CTAs that form the sum also get it in *sum. False on timeout.
+  auto reduce = [&](int e, double tot, auto&& scal_of, double* sum, double* scalar) -> bool {
+    double* part = a.slots + (long long)e * a.ntiles;
+    if (a.counted) {
+      if (threadIdx.x == 0) part[t] = tot;
+      *sum = counted_sum(a.cnt + is * PCG_CNT_STRIDE, (unsigned)(e + 1) * (unsigned)I.ntiles, part + I.tile0, I.ntiles,
+                         s_stage, a.status, &s_val, &s_ok);
+      if (!s_ok) return false;
+      *scalar = scal_of(*sum);
+      return true;
+    }
+    if (threadIdx.x == 0) st_release_f64(part + t, tot);
+    double* pub = a.bcast + (long long)e * ni + is;
+    if (writer) {
+      *sum = gathered_sum<NP>(part + I.tile0, I.ntiles, s_stage, a.status, &s_val, &s_ok);
+      if (!s_ok) return false;
+      *scalar = scal_of(*sum);
+      if (threadIdx.x < PCG_BCAST) st_release_f64(pub + threadIdx.x * a.bcast_stride, *scalar);
+      return true;
+    }
+    *scalar = wait_published(pub + (t % PCG_BCAST) * a.bcast_stride, a.status, &s_val, &s_ok);
+    return s_ok != 0;
+  };
+
+  // ---- r_0 = b - A x_0, p_0 = M^-1 r_0, partial of r_0 . p_0
+  double rz = 0.0, sum = 0.0, scalar = 0.0;  // rz_k: CTAs that form the sums
   {
     ApplyArgs2D op = a.op;
     op.x = a.x0; op.r_out = a.r; op.p_out = a.p[0];
-    for (int t = blockIdx.x; t < a.ntiles; t += G) {
-      const Tile2D tl = op.tiles[t];
-      const Inst2D I = op.inst[tl.inst];
-      const double tot = block_sum<P2>(apply_tile<NP, EPI_PCG0>(op, tl, I, sm), s_red);
-      if (threadIdx.x == 0) op.partials[t] = tot;
-    }
+    const double tot = block_sum<P2>(apply_tile<NP, EPI_PCG0>(op, tl, I, sm), s_red);
+    if (!reduce(0, tot, [](double s) { return s; }, &sum, &scalar)) return;
+    rz = sum;
+    if (writer && threadIdx.x == 0) RZ[is] = rz;
   }
-  if (!grid_barrier(a.bar, G, [&] {
-        inst_tile_sums(a.op.inst, ni, a.op.partials, [&](int i, double s) { RZ[i] = s; });
-      }))
-    return;
 
   for (int k = 0; k < n; ++k) {
     // ---- phase A: A p_k (p_k = M^-1 r_k + beta_{k-1} p_{k-1} formed on load for k > 0)
@@ -182,61 +281,54 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT, 8) k2_pcg_persist(PcgPersist
       if (k == 0) {
         op.x = a.p[0];
       } else {
-        if (threadIdx.x < ni) beta[threadIdx.x] = __ldcg(BT + (long long)(k - 1) * ni + threadIdx.x);
-        __syncthreads();
-        op.pcg_r = a.r; op.pcg_p = a.p[(k - 1) & 1]; op.pcg_beta = beta;
+        op.pcg_r = a.r; op.pcg_p = a.p[(k - 1) & 1]; op.pcg_beta = s_beta;
         op.p_out = a.p[k & 1];
       }
       op.ap_out = a.ap;
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        const Tile2D tl = op.tiles[t];
-        const Inst2D I = op.inst[tl.inst];
-        const double tot = block_sum<P2>(apply_tile<NP, EPI_PCG>(op, tl, I, sm), s_red);
-        if (threadIdx.x == 0) op.partials[t] = tot;
-      }
+      const double tot = block_sum<P2>(apply_tile<NP, EPI_PCG>(op, tl, I, sm), s_red);
+      if (!reduce(2 * k + 1, tot, [&](double pap) { return rz / (pap + eps); }, &sum, &scalar)) return;
     }
-    if (!grid_barrier(a.bar, G, [&] {
-          inst_tile_sums(a.op.inst, ni, a.op.partials, [&](int i, double s) {
-            PAP[(long long)k * ni + i] = s;
-            AL[(long long)k * ni + i] = __ldcg(RZ + (long long)k * ni + i) / (s + eps);  // alpha_k
-          });
-        }))
-      return;
-    // ---- phase B on the CTA's own tiles (whose p_k and A p_k it wrote in phase A):
-    // x_{k+1} = x_k + alpha_k p_k, r_{k+1} = r_k - alpha_k A p_k, tile partials of r . M^-1 r
+    const double al = scalar;  // alpha_k
+    if (writer && threadIdx.x == 0) {
+      PAP[(long long)k * ni + is] = sum;
+      AL[(long long)k * ni + is] = al;
+    }
+    // ---- phase B on the CTA's tile (whose p_k and A p_k it wrote in phase A):
+    // x_{k+1} = x_k + alpha_k p_k, r_{k+1} = r_k - alpha_k A p_k, tile partial of r . M^-1 r
     {
       const double* xin = k == 0 ? a.x0 : a.xout;
       const double* pk = a.p[k & 1];
-      for (int t = blockIdx.x; t < a.ntiles; t += G) {
-        const Tile2D tl = a.op.tiles[t];
-        const Inst2D I = a.op.inst[tl.inst];
-        const double al = __ldcg(AL + (long long)k * ni + tl.inst);
-        for (int v = threadIdx.x; v < UV; v += blockDim.x) {
-          double part = 0.0;
-          long long nd;
-          if (v < cnt && tile_node<NP>(tl, I, v, &nd)) {
-            const double p = pk[nd], apv = a.ap[nd], x = xin[nd], r = a.r[nd], im = a.op.cinvM[nd];
-            a.xout[nd] = fma(al, p, x);
-            const double rn = fma(-al, apv, r);
-            a.r[nd] = rn;
-            part = fma(rn, rn * im, 0.0);
-          }
-          s_red[v] = part;
+      for (int v = threadIdx.x; v < UV; v += blockDim.x) {
+        double part = 0.0;
+        long long nd;
+        if (v < cnt && tile_node<NP>(tl, I, v, &nd)) {
+          const double p = pk[nd], apv = a.ap[nd], x = xin[nd], r = a.r[nd], im = a.op.cinvM[nd];
+          a.xout[nd] = fma(al, p, x);
+          const double rn = fma(-al, apv, r);
+          a.r[nd] = rn;
+          part = fma(rn, rn * im, 0.0);
         }
-        __syncthreads();
-        tile_tree<UV>(s_red, threadIdx.x, blockDim.x);
-        if (threadIdx.x == 0) a.upart[t] = s_red[0];
-        __syncthreads();
+        s_red[v] = part;
       }
+      __syncthreads();
+      tile_tree<UV>(s_red, threadIdx.x, blockDim.x);
+      if (!reduce(2 * k + 2, s_red[0], [&](double rzn) { return rzn / (rz + eps); }, &sum, &scalar)) return;
     }
-    if (!grid_barrier(a.bar, G, [&] {
-          inst_tile_sums(a.op.inst, ni, a.upart, [&](int i, double rzn) {
-            RZ[(long long)(k + 1) * ni + i] = rzn;
-            BT[(long long)k * ni + i] = rzn / (__ldcg(RZ + (long long)k * ni + i) + eps);  // beta_k
-          });
-        }))
-      return;
+    const double bt = scalar;  // beta_k
+    rz = sum;
+    if (writer && threadIdx.x == 0) {
+      RZ[(long long)(k + 1) * ni + is] = sum;
+      BT[(long long)k * ni + is] = bt;
+    }
+    if (threadIdx.x == 0) s_beta[is] = bt;
+    __syncthreads();  // s_beta before the next operator's loads
   }
+}
+
+// Fills [p, p + n) with PCG_SENTINEL.
+static __global__ void k2_pcg_persist_fill(double* p, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = __longlong_as_double((long long)PCG_SENTINEL);
 }
 
 }  // namespace igrgpu
