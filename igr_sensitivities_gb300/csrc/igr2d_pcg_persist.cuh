@@ -13,8 +13,8 @@
 //            | rz_{k+1}, beta_k = rz_{k+1} / (rz_k + eps) |
 // The operator runs the same apply_tile code and block tree as k2_apply, the
 // update forms each tile's partial in the same 256-slot tree as k2_pcg_update,
-// and the partials are summed in warp_sum_partials' order, so the result is
-// bitwise the two-kernel result.
+// and the partials are summed in warp_sum_partials' order (sum_lanes64), so
+// the result is bitwise the two-kernel result.
 //
 // Every reduction e (0: r_0 . p_0; 2k + 1: p_k . A p_k; 2k + 2:
 // r_{k+1} . M^-1 r_{k+1}) has its own partial slot per tile, so no slot is
@@ -98,21 +98,6 @@ struct PcgPersistArgs {
   // at the launch: counted, cnt zero; published, slots and bcast PCG_SENTINEL
 };
 
-// The canonical sum of stage[0 .. count) (warp_sum_partials' order: lane l
-// adds l, l + 32, ... in turn, then a shuffle tree) by warp 0, to every thread.
-__device__ __forceinline__ double stage_sum(const double* stage, int count, double* s_sum) {
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double acc = 0.0;
-    for (int k = threadIdx.x; k < count; k += 32) acc += stage[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (threadIdx.x == 0) *s_sum = acc;
-  }
-  __syncthreads();
-  return *s_sum;
-}
-
 // Counted hand-off, every thread; thread 0 has stored the CTA's partial.
 // Counts the CTA's arrival, waits for the instance's target count, stages the
 // partials and returns their sum. *s_ok = 0 on timeout.
@@ -136,7 +121,7 @@ __device__ __forceinline__ double counted_sum(unsigned* cnt, unsigned target, co
   __syncthreads();
 #pragma unroll 4
   for (int j = threadIdx.x; j < count; j += blockDim.x) stage[j] = __ldcg(part + j);
-  return stage_sum(stage, count, s_sum);
+  return sum_lanes64(stage, count, s_sum);
 }
 
 // Published hand-off, writer CTA, every thread: waits until none of the
@@ -185,7 +170,7 @@ __device__ __forceinline__ double gathered_sum(const double* slots, int count, d
     __nanosleep(20);
   }
   fence_acq_rel_gpu();
-  return stage_sum(stage, count, s_sum);
+  return sum_lanes64(stage, count, s_sum);
 }
 
 // Published hand-off, every thread of a CTA other than the writer: waits

@@ -170,16 +170,46 @@ __device__ __forceinline__ void inst_sum_finish(const InstSum& a, int i, double 
   a.PAPB[i] = -s * rz0 / (den * den);
 }
 
-// The canonical sum of count partials, by one warp: lane l adds partials
-// l, l + 32, ... in order, then a fixed shuffle tree; lane 0 holds the sum.
+// The canonical sum of count partials: 64 strided lane sums (lane v adds
+// partials v, v + 64, ... in order, from 0), then lane l < 32 adds lane
+// l + 32's sum to its own, then a fixed shuffle tree. One warp forms it here
+// (lane l carries lanes l and l + 32); lane 0 holds the sum. A CTA of 64
+// threads forms the same bits with its two warps' lane sums in parallel
+// (sum_lanes64), which halves the dependent FP64 adds on its critical path.
 __device__ __forceinline__ double warp_sum_partials(const double* p, int count) {
   const int l = threadIdx.x & 31;
-  double acc = 0.0;
-#pragma unroll 16
-  for (int k = l; k < count; k += 32) acc += __ldcg(p + k);
+  double a0 = 0.0, a1 = 0.0;
+#pragma unroll 8
+  for (int k = l; k < count; k += 64) {
+    a0 += __ldcg(p + k);
+    if (k + 32 < count) a1 += __ldcg(p + k + 32);
+  }
+  double acc = a0 + a1;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   return acc;
+}
+
+// warp_sum_partials' sum of v[0 .. count) (shared memory) by every thread of
+// the CTA (blockDim >= 32): the 64 lane sums in parallel, then warp 0 adds
+// them up. Every thread gets the sum (*s_sum: shared).
+__device__ __forceinline__ double sum_lanes64(const double* v, int count, double* s_sum) {
+  __shared__ double s_acc[64];
+  __syncthreads();
+  for (int lane = threadIdx.x; lane < 64; lane += blockDim.x) {
+    double a = 0.0;
+    for (int k = lane; k < count; k += 64) a += v[k];
+    s_acc[lane] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double acc = s_acc[threadIdx.x] + s_acc[threadIdx.x + 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) *s_sum = acc;
+  }
+  __syncthreads();
+  return *s_sum;
 }
 
 // Called by every thread (blockDim >= 32) with the block's partial v, known
