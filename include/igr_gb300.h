@@ -98,10 +98,10 @@ int igr_set_cluster_size_1d(igr_ctx* ctx, int cs);
 int igr_set_graphs(igr_ctx* ctx, int on);
 /* 2D untaped PCG solves (forward, tangent, stand-alone and continuous-adjoint
  * solves) whose tiles fit one wave of resident CTAs: one persistent
- * cooperative launch per solve with grid barriers between its phases (1,
- * default) or two kernels per iteration (0). Results are bitwise the same. A
- * barrier that waits past its time limit (1 s) makes the call return
- * IGR_ETIMEOUT. No reference counterpart. */
+ * cooperative launch per solve, whose CTAs hand each inner product on within
+ * each instance (1, default), or two kernels per iteration (0). Results are
+ * bitwise the same. A hand-off that waits past its time limit (1 s) makes the
+ * call return IGR_ETIMEOUT. No reference counterpart. */
 int igr_set_pcg_persistent(igr_ctx* ctx, int on);
 /* Autotuning of launch choices that leave results bitwise unchanged: the 1D
  * CTAs per instance (when not forced by igr_set_cluster_size_1d) and whether
