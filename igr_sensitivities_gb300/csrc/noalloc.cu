@@ -138,10 +138,13 @@ extern "C" int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const 
   }
   const int ntx = (d->n_ex + tx - 1) / tx, nty = (d->n_ey + ty - 1) / ty;
   if ((long long)ntx * nty > NOALLOC_MAX_TILES) return IGR_EINVAL;  // not reachable under the node limit
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the call ends by synchronising its stream and stages the tile list from a reused host array: not capturable
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) return IGR_EINVAL;
   unsigned char* base = nullptr;
   int rc = scratch_on_current_device(&base);
   if (rc != IGR_OK) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   BasisDev B;
   try {
     B = make_basis_dev(d->p, d->xi, d->w, d->D);

@@ -282,8 +282,9 @@ int igr2d_cg_fixed(igr_ctx* ctx, const igr_disc2d* d, double alpha, const double
  * lazy module loading the first call on each device loads the library's
  * kernels there, which reserves the array then: make that first call during
  * set-up. The first call on each device (and the first after the device's
- * context was reset) looks up the array's address; make it before any stream
- * capture. */
+ * context was reset) looks up the array's address. The call synchronises its
+ * stream before it returns, so it cannot be recorded into a CUDA graph: on a
+ * stream that is capturing it returns IGR_EINVAL without touching the stream. */
 int igr2d_apply_sip_noalloc(const igr_disc2d* d, double alpha, const double* x_dev, const double* rho_dev,
                             double* y_dev, void* stream);
 

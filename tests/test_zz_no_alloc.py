@@ -67,3 +67,30 @@ def test_apply_sip_noalloc_rejects_oversize(igr):
     x = np.zeros(mesh.x.shape)
     rc, _ = _call(igr, basis, mesh, 1e-3, x, np.ones(mesh.x.shape))
     assert rc == 1  # IGR_EINVAL
+
+
+def test_apply_sip_noalloc_refuses_stream_capture(igr):
+    # the call synchronises its stream, so on a capturing stream it must return IGR_EINVAL without touching it,
+    # leaving the caller's capture valid
+    import torch
+    lib = igr._lib.lib()
+    basis = igr.DGBasis(3)
+    mesh = igr.CartesianMesh2D(8, 8, 1.0, 1.0, basis)
+    d = igr._disc2d(basis, mesh)
+    dev = torch.device("cuda", 0)
+    xd = torch.ones(mesh.x.size, dtype=torch.float64, device=dev)
+    rd = torch.ones_like(xd)
+    yd = torch.zeros_like(xd)
+    D = C.POINTER(C.c_double)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        rc = lib.igr2d_apply_sip_noalloc(C.byref(d), C.c_double(1e-3), C.cast(C.c_void_p(xd.data_ptr()), D),
+                                         C.cast(C.c_void_p(rd.data_ptr()), D), C.cast(C.c_void_p(yd.data_ptr()), D),
+                                         C.c_void_p(s.cuda_stream))
+        out = xd * 3.0
+    assert rc == 1  # IGR_EINVAL
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.all(out == 3.0) and torch.all(yd == 0.0)
