@@ -82,6 +82,11 @@ class Context:
         solve (default on) or two kernels per iteration; bitwise the same."""
         check(self, lib().igr_set_pcg_persistent(self.handle, C.c_int(1 if on else 0)))
 
+    def test_pcg_drop_tile(self, tile):
+        """Test hook: the next persistent PCG launch runs with one tile's CTA
+        leaving early, so the call returns IGR_ETIMEOUT (6) after 1 s."""
+        check(self, lib().igr_test_pcg_drop_tile(self.handle, C.c_int(int(tile))))
+
     def set_autotune(self, on, cache_path=None):
         """Measure result-invariant launch choices (1D CTAs per instance, 2D fused
         or separate PCG inner products) on the first call of each batch shape and

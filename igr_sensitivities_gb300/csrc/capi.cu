@@ -171,6 +171,12 @@ int igr_set_pcg_persistent(igr_ctx* ctx, int on) {
   return IGR_OK;
 }
 
+int igr_test_pcg_drop_tile(igr_ctx* ctx, int tile) {
+  if (!ctx) return IGR_EINVAL;
+  ctx->c.pcg_drop_tile = tile;
+  return IGR_OK;
+}
+
 int igr_set_autotune(igr_ctx* ctx, int on, const char* cache_path) {
   if (!ctx) return IGR_EINVAL;
   ctx->c.err.clear();

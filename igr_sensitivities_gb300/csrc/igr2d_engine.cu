@@ -537,6 +537,8 @@ static void pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, 
   a.x0 = x0; a.xout = xout; a.r = xa; a.p[0] = xb; a.p[1] = dbuf; a.ap = c.ws.dbl("pcg:ap", P.NG);
   a.eps = 1e-30;
   a.status = c.d_status;
+  a.drop_tile = c.pcg_drop_tile;
+  c.pcg_drop_tile = -1;  // one launch
   if (a.counted) {
     cuda_check(cudaMemsetAsync(a.cnt, 0, sizeof(unsigned) * PCG_CNT_STRIDE * ni, c.stream), "arrival counters");
   } else {
@@ -724,7 +726,7 @@ static void check_status(Ctx& c) {
   int st = 0;
   cuda_check(cudaMemcpyAsync(&st, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream), "status readback");
   cuda_check(cudaStreamSynchronize(c.stream), "stream sync");
-  if (st & DEV_TIMEOUT) throw Error(6, "a grid barrier of the persistent PCG solve gave up waiting");
+  if (st & DEV_TIMEOUT) throw Error(6, "a hand-off wait of the persistent PCG solve gave up (a CTA stopped early)");
   if (st & DEV_NONFINITE) throw Error(3, "non-finite value or non-positive density in the state");
 }
 

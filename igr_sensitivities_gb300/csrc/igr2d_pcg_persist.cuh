@@ -95,6 +95,7 @@ struct PcgPersistArgs {
   unsigned* cnt;                   // counted: arrivals of instance i at cnt[i * PCG_CNT_STRIDE]
   double eps;
   int* status;
+  int drop_tile;                   // test hook: this tile's CTA leaves before its first p.Ap hand-off (-1: none)
   // at the launch: counted, cnt zero; published, slots and bcast PCG_SENTINEL
 };
 
@@ -226,6 +227,7 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT, 8) k2_pcg_persist(PcgPersist
   // 0) is formed: stores it and sets *scalar = scal_of(sum) in every thread;
   // CTAs that form the sum also get it in *sum. False on timeout.
   auto reduce = [&](int e, double tot, auto&& scal_of, double* sum, double* scalar) -> bool {
+    if (e == 1 && t == a.drop_tile) return false;  // a CTA that stops early: the others' waits run out
     double* part = a.slots + (long long)e * a.ntiles;
     if (a.counted) {
       if (threadIdx.x == 0) part[t] = tot;

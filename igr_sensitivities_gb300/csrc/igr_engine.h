@@ -97,6 +97,7 @@ struct Ctx {
   int last_cluster1d = 0;       // 1D: CTAs per instance of the last launch
   bool use_graphs = true;       // replay repeated forward steps as CUDA graphs
   bool pcg_persistent = true;   // 2D untaped PCG solves of one wave of tiles in one persistent launch
+  int pcg_drop_tile = -1;       // test hook for the next persistent PCG launch (igr_test_pcg_drop_tile)
   Autotune tune;
   Profiler prof;
 };

@@ -103,6 +103,12 @@ int igr_set_graphs(igr_ctx* ctx, int on);
  * bitwise the same. A hand-off that waits past its time limit (1 s) makes the
  * call return IGR_ETIMEOUT. No reference counterpart. */
 int igr_set_pcg_persistent(igr_ctx* ctx, int on);
+/* Test hook for the timeout path. The next persistent PCG launch on this
+ * context runs with the CTA of tile `tile` (plan order) leaving before its
+ * first p.Ap hand-off, as a CTA that stopped early would. The instance's other
+ * CTAs give up after 1 s, the call returns IGR_ETIMEOUT and the context stays
+ * usable. Nothing faults or hangs. -1 clears it. No reference counterpart. */
+int igr_test_pcg_drop_tile(igr_ctx* ctx, int tile);
 /* Autotuning of launch choices that leave results bitwise unchanged: the 1D
  * CTAs per instance (when not forced by igr_set_cluster_size_1d) and whether
  * the 2D PCG inner products complete inside their kernels. on = 1 measures

@@ -475,3 +475,31 @@ def test_persistent_pcg_equals_two_kernel_form(igr, oracle, case):
     A, B = run(a_ctx), run(b_ctx)
     for x, y in zip(A, B):
         assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
+@pytest.mark.parametrize("ne,drop", [((8, 6), 0), ((8, 6), 3), ((72, 72), 0), ((72, 72), 201)])
+def test_persistent_pcg_wait_times_out_and_context_recovers(igr, oracle, ne, drop):
+    """A CTA of the persistent PCG solve that leaves early (the test hook drops
+    one tile's CTA before its first p.Ap hand-off) makes the instance's other
+    CTAs give up after their bounded wait: the call returns IGR_ETIMEOUT, and
+    the same context then solves normally, bitwise as a fresh one. 8 x 6 runs
+    the counted hand-off (4 tiles), 72^2 the published one (324 tiles); tile 0
+    is the instance's writer CTA."""
+    from igr_sensitivities_gb300 import Context
+    from igr_sensitivities_gb300._lib import IGRError
+    g = 1.4
+    basis, mesh, _ = setup(igr, oracle, 3, *ne)
+    alpha = 3.0 / (ne[0] * ne[1])
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 11), width=0.1)
+
+    def solve(ctx):
+        S = np.zeros(mesh.x.shape, order="F")
+        igr.solve_elliptic_(S, *q0, basis, mesh, alpha, n_iter=20, solver="pcg", ctx=ctx)
+        return S
+
+    ctx = Context(0)
+    ctx.test_pcg_drop_tile(drop)
+    with pytest.raises(IGRError) as err:
+        solve(ctx)
+    assert err.value.code == 6
+    assert np.array_equal(solve(ctx), solve(Context(0)))
