@@ -503,7 +503,9 @@ static int pcg_persist_capacity(Ctx& c, int np) {
 // hide those costs.
 static bool pcg_persistent(Ctx& c, const Plan2D& P, bool taped, int n_iter) {
   if (taped || !c.pcg_persistent || (int)P.inst.size() > PCG_PERSIST_MAX_INST) return false;
-  if ((2LL * n_iter + 1) * PCG_COUNTED_TILES >= (1LL << 31)) return false;  // arrival counts
+  // one partial slot per tile and reduction: keep that under 64 MB (about 3,000 iterations at 1,216 tiles),
+  // which also keeps the arrival counts ((2 n_iter + 1) x tiles) far below 2^31
+  if ((2LL * n_iter + 1) * P.ntiles() * (long long)sizeof(double) > (64LL << 20)) return false;
   int max_tiles = 0;
   NP_DISPATCH(P.np, max_tiles = persist_max_inst_tiles<NPV>());
   for (const auto& I : P.inst)
