@@ -18,8 +18,10 @@
 //
 // Coefficient adjoints are carried as Z = (1/rho) * d(.)/d(1/rho) so that the
 // stored coefficients (all proportional to 1/rho) are reused directly:
-// Zm collects the mass part, Zs the alpha-proportional stiffness/face part;
-// then d/d rho = -Z/rho and d/d alpha = Zs/alpha.
+// Zm collects the mass part without its coefficient (the sum over the
+// solve's reverse applies of +-u x, which k2_setup_rev multiplies by the mass
+// coefficient once, instead of every apply), Zs the alpha-proportional
+// stiffness/face part; then d/d rho = -Z/rho and d/d alpha = Zs/alpha.
 #pragma once
 #include "igr2d_kernels.cuh"
 
@@ -528,16 +530,16 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
       const double cmn = a.cm[n];
       double w = fma(cmn, uc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
       w = dot_col<NP>(B, l, sy, w);
-      // zscale is -1 (r = b - A x) or +1 (A p): applied through fma signs, not a multiply
-      const double zm = a.zscale > 0 ? (cmn * uc[l]) * vc_[l] : -(cmn * uc[l]) * vc_[l];
+      // zscale is -1 (r = b - A x) or +1 (A p): applied through operand signs, not a multiply
+      const double uz = a.zscale > 0 ? uc[l] : -uc[l];
       const double zs = a.zscale > 0 ? zc[l] + s_zr[e][l * NP + t] : -(zc[l] + s_zr[e][l * NP + t]);
       double xb = a.xb[n] - w;
       if (PCG) xb = fma(ppb, a.apk[n], fma(pal, a.xconst[n], xb));
       a.xb[n] = xb;
       if (a.bb_op == 1) a.bb[n] = uc[l];
       else if (a.bb_op == 2) a.bb[n] += uc[l];
-      if (a.first) { a.Zm[n] = zm; a.Zs[n] = zs; }
-      else { a.Zm[n] += zm; a.Zs[n] += zs; }
+      if (a.first) { a.Zm[n] = uz * vc_[l]; a.Zs[n] = zs; }
+      else { a.Zm[n] = fma(uz, vc_[l], a.Zm[n]); a.Zs[n] += zs; }
       if (PCG && a.has_next) part = fma(xb, a.p_next[n], part);
       if (SREV == SREV_CHEB && a.has_next) {
         const double dbv = a.db[n] + xb;
@@ -704,10 +706,10 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_setup_rev(SetupRevArgs2D 
     // d/d(1/rho) of diag(A): mass + row-phase x stiffness + column-phase y stiffness and faces
     const double m0 = B.w[t] * B.w[l] * I.jx * I.jy;  // mass coefficient without 1/rho
     const double ibt = fma(Mb, m0, s_ib[e][l * NP + t] + ib[l]);
-    const double zm = a.Zm[n], zs = a.Zs[n];
+    const double zs = a.Zs[n], zms = fma(cmn, a.Zm[n], zs);  // Zm + Zs, with Zm's mass coefficient
     a.Qs[0][n] += uxb[l] * ir;
     a.Qs[1][n] += uyb[l] * ir;
-    const double rb = -(fma(uxb[l], cux[l], uyb[l] * cuy[l]) * ir) - ir * fma(ibt, ir, zm + zs);
+    const double rb = -(fma(uxb[l], cux[l], uyb[l] * cuy[l]) * ir) - ir * fma(ibt, ir, zms);
     a.Qs[2][n] += rb;
     // d/dalpha: Zs/alpha + Mb (M - mass)/alpha + bb b/alpha
     a.anode[n] += fma(Mb, a.cM[n] - cmn, fma(a.bb[n], a.b[n], zs)) * I.ialpha;
