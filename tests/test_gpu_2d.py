@@ -441,27 +441,33 @@ def test_pcg_forward_and_adjoint_other_degrees(igr, oracle, p, nex, ney):
     assert abs(res[6] - dar) <= RTOL_GRAD * abs(dar)
 
 
-@pytest.mark.parametrize("case", ["forward", "forward_batch", "tangent", "solve", "forward_128"])
+@pytest.mark.parametrize("case", ["forward", "forward_batch", "tangent", "solve", "forward_128", "forward_p1",
+                                  "forward_p2", "forward_p4", "batch_published"])
 def test_persistent_pcg_equals_two_kernel_form(igr, oracle, case):
-    """The persistent PCG solve (one cooperative launch per solve, grid
-    barriers between its phases) gives bitwise the two-kernel result, also
-    when the forward's RK steps replay as CUDA graphs."""
+    """The persistent PCG solve (one cooperative launch per solve, per-instance
+    hand-offs of the inner products) gives bitwise the two-kernel result, also
+    when the forward's RK steps replay as CUDA graphs. Counted hand-offs (up to
+    256 tiles per instance) and published ones (forward_128: 1024 tiles;
+    batch_published: two 72^2 instances of 324 tiles) at p = 1..4."""
     from igr_sensitivities_gb300 import Context
     g = 1.4
-    ne = 128 if case == "forward_128" else 8
-    basis, mesh, _ = setup(igr, oracle, 3, ne, 6 if ne == 8 else ne)
-    alpha = 3.0 * (1 / ne) ** 2
-    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 7), width=0.12 if ne == 8 else 0.03)
-    dt = W.cfl_dt_2d(mesh, 3, q0, g, 0.1)
+    p = {"forward_p1": 1, "forward_p2": 2, "forward_p4": 4}.get(case, 3)
+    ne = {"forward_128": (128, 128), "forward_p1": (13, 9), "forward_p2": (10, 14), "forward_p4": (22, 22),
+          "batch_published": (72, 72)}.get(case, (8, 6))
+    basis, mesh, _ = setup(igr, oracle, p, *ne)
+    alpha = 3.0 / (ne[0] * ne[1])
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 7), width=0.12 if ne[0] < 32 else 0.03)
+    dt = W.cfl_dt_2d(mesh, p, q0, g, 0.1)
 
     def run(ctx):
         rng = np.random.default_rng(4)
-        if case in ("forward", "forward_128"):
+        if case.startswith("forward") and case != "forward_batch":
             return igr.run_forward(*q0, dt, 3 * dt * 0.999, basis, mesh, g, alpha, n_iter=12, solver="pcg", ctx=ctx)
-        if case == "forward_batch":
-            q = np.stack([np.stack([flat(a) for a in q0])] * 3)
-            return igr.forward_batch(q, [1.3, 1.4, 1.5], [alpha, 0.5 * alpha, 2 * alpha], [dt] * 3, 3, basis, mesh,
-                                     n_iter=10, solver="pcg", ctx=ctx)
+        if case in ("forward_batch", "batch_published"):
+            nb = 3 if case == "forward_batch" else 2
+            q = np.stack([np.stack([flat(a) for a in q0])] * nb)
+            return igr.forward_batch(q, [1.3, 1.4, 1.5][:nb], [alpha, 0.5 * alpha, 2 * alpha][:nb], [dt] * nb, 3,
+                                     basis, mesh, n_iter=10, solver="pcg", ctx=ctx)
         if case == "tangent":
             s0 = [rng.standard_normal(mesh.x.shape) * 1e-3 for _ in range(4)]
             return igr.run_sensitivity(*q0, *s0, dt, 3 * dt * 0.999, basis, mesh, g, alpha, n_iter=9, solver="pcg",
