@@ -514,7 +514,11 @@ static bool pcg_persistent(Ctx& c, const Plan2D& P, bool taped, int n_iter) {
   return cap >= 1 && P.ntiles() <= cap;
 }
 
-static void pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b,
+// Returns false, having launched nothing that matters (the slot fill only),
+// when the device refuses the cooperative launch (too many CTAs to be
+// resident at once, e.g. beside another process's work); the caller then
+// runs the two-kernel form.
+static bool pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b,
                                  const double* x0, double* xout, double* xa, double* xb, double* dbuf) {
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   PcgPersistArgs a;
@@ -553,15 +557,18 @@ static void pcg_solve_persistent(Ctx& c, const Plan2D& P, const Solve2DOpts& o, 
     LaunchScope ls(c, KID_APPLY);
     NP_DISPATCH(P.np, e = launch_k2_pcg_persist<NPV>(a, nb, c.stream));
   }
+  if (e == cudaErrorCooperativeLaunchTooLarge) {
+    (void)cudaGetLastError();  // clear it: nothing was launched
+    --c.launches;
+    return false;
+  }
   cuda_check(e, "persistent PCG launch");
+  return true;
 }
 
 static void pcg_solve(Ctx& c, const Plan2D& P, const Solve2DOpts& o, StageBuf& st, const double* b, const double* x0,
                       double* xout, bool taped, double* xa, double* xb, double* dbuf) {
-  if (pcg_persistent(c, P, taped, o.n_iter)) {
-    pcg_solve_persistent(c, P, o, st, b, x0, xout, xa, xb, dbuf);
-    return;
-  }
+  if (pcg_persistent(c, P, taped, o.n_iter) && pcg_solve_persistent(c, P, o, st, b, x0, xout, xa, xb, dbuf)) return;
   const int nb = P.ntiles(), n = o.n_iter, ni = (int)P.inst.size();
   const long long NG = P.NG;
   double* part = c.ws.dbl("red:part", nb);
