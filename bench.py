@@ -38,18 +38,18 @@ METRIC = "2D P3 128Â² adjoint gradients/s: batched vs plain, same GPU, rel err â
 # FP64 flops per node executed by each kernel family, P3, Chebyshev epilogues:
 # (2 DFMA + DADD + DMUL) of one ncu capture divided by the launch's nodes
 # (profiles/adjoint2d_kernels_128.md). Used for the live roofline.
-FLOPS_PER_NODE = {0: 86.0, 1: 47.8, 2: 167.0, 3: 235.5, 4: 78.2, 5: 136.0}
+FLOPS_PER_NODE = {0: 86.0, 1: 47.8, 2: 167.0, 3: 235.5, 4: 78.45, 5: 137.0}
 # Algorithmic FP64 bytes per node per launch: one read of every live field and
 # one write of every output field (halo re-reads excluded), for the HBM fraction.
 BYTES_PER_NODE = {0: 8 * 11, 1: 8 * 13, 2: 8 * 17, 3: 8 * 35, 4: 8 * 23, 5: 8 * 19}
 # DRAM bytes per node of one launch of each family, measured with ncu on an
 # 8-instance case whose fields exceed L2 (profiles/adjoint2d_kernels_128.md);
 # scaled by the launch's node count for `roofline.traffic`.
-TRAFFIC_PER_NODE = {0: 61.9, 1: 91.8, 2: 123.7, 3: 208.1, 4: 143.8, 5: 141.0}
+TRAFFIC_PER_NODE = {0: 61.9, 1: 91.8, 2: 123.7, 3: 208.1, 4: 151.6, 5: 140.8}
 # FP64 instructions per node (DFMA + DADD + DMUL thread instructions of the same
 # captures): the issue-rate view of the FP64 roof, whose peak is half the DFMA
 # probe's flop rate (one DFMA = 2 flops).
-INST_PER_NODE = {0: 59.0, 1: 30.0, 2: 107.0, 3: 155.1, 4: 52.5, 5: 90.3}
+INST_PER_NODE = {0: 59.0, 1: 30.0, 2: 107.0, 3: 155.1, 4: 52.1, 5: 90.3}
 FAMILY = {0: "k2_setup", 1: "k2_apply", 2: "k2_hyp_rk", 3: "k2_hyp_rev", 4: "k2_apply_rev", 5: "k2_setup_rev"}
 # Algorithmic FP64 operations per node: the reference's arithmetic as restated in the oracle, counted with an
 # operation-counting scalar (+ - * / sqrt |x| max = 1 each, a multiply-add = 2), and its reverse by the
