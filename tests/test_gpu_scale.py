@@ -10,7 +10,8 @@ step count the oracle finishes in seconds (OpenMP over instances):
       groups of 5 (5120 tiles per group), 3 of 200 steps
   2D 128^2 P3 gradients with PCG 10 in one group of 5 (5120 tiles: the
       separate-launch inner products), 2 steps
-  2D 128^2 P3 forward, PCG 60, 3 of 500 steps
+  2D 128^2 P3 forward, PCG 60, 3 of 500 steps (persistent solves, published hand-offs)
+  2D 64^2 P3 and 22^2 P4 forwards, PCG 60, 3 steps (persistent solves, counted hand-offs)
   1D N_e = 256 P3 forward, Jacobi 50, the whole T = 0.1
 Tolerances (relative L2): forward state and Sigma 1e-11 (Sigma of the PCG-60
 forward: 3x the oracle's own change under a one-ulp input perturbation,
@@ -160,6 +161,29 @@ def test_forward_128_pcg60_matches_oracle(igr, oracle):
     _, Sp = oracle.run_forward_2d(G, g, alpha, dt, T, 60, "pcg", fp)
     spread = rel(Sp, Sr)
     assert rel(flat(out[4]), Sr) <= max(RTOL_FWD, 3.0 * spread), spread
+
+
+@pytest.mark.parametrize("p,ne,nst", [(3, 64, 3), (4, 22, 3)])
+def test_forward_pcg60_counted_handoff_matches_oracle(igr, oracle, p, ne, nst):
+    # single instances whose PCG-60 solves run as persistent launches with counted hand-offs (256 P3 tiles at
+    # 64^2; 66 P4 tiles at 22^2, the finest OtD resolution below 30), against the oracle
+    g = 1.4
+    basis = igr.DGBasis(p)
+    mesh = igr.CartesianMesh2D(ne, ne, 1.0, 1.0, basis)
+    q0 = W.seeded_pulses_2d(mesh, g, W.seed_for(2, 1), n_pulses=3, width=0.05)
+    dt = W.cfl_dt_2d(mesh, p, q0, g, 0.1)
+    alpha, T = 3.0 / ne ** 2, nst * dt * 0.999
+    out = igr.run_forward(*q0, dt, T, basis, mesh, g, alpha, n_iter=60, solver="pcg")
+    G = oracle.Grid2D(p, ne, ne)
+    f0 = [flat(a) for a in q0]
+    qr, Sr = oracle.run_forward_2d(G, g, alpha, dt, T, 60, "pcg", f0)
+    for a, b in zip(out[:4], qr):
+        assert rel(flat(a), b) <= RTOL_FWD
+    # Sigma on the scale of the oracle's own change under a one-ulp input perturbation (as for 128^2)
+    rng = np.random.default_rng(1)
+    fp = [np.nextafter(a, a + rng.choice([-1.0, 1.0], size=a.size)) if v >= 2 else a for v, a in enumerate(f0)]
+    _, Sp = oracle.run_forward_2d(G, g, alpha, dt, T, 60, "pcg", fp)
+    assert rel(flat(out[4]), Sr) <= max(RTOL_FWD, 3.0 * rel(Sp, Sr))
 
 
 def test_forward_1d_256_jacobi50_full_matches_oracle(igr, oracle):
