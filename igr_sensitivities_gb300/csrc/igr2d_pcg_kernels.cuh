@@ -74,11 +74,17 @@ __device__ __forceinline__ void group_partial(const InstSum& isum, const TileGro
 // the persistent PCG kernel form it this way, so their sums agree bitwise.
 template <int P2>
 __device__ __forceinline__ void tile_tree(double* s, int tid, int nthreads) {
+  static_assert(P2 >= 64, "shared-memory levels down to 32 slots");
 #pragma unroll
-  for (int w = P2 / 2; w > 0; w >>= 1) {
+  for (int w = P2 / 2; w >= 32; w >>= 1) {
     for (int v = tid; v < w; v += nthreads) s[v] += s[v + w];
     __syncthreads();
   }
+  if (tid < 32) {
+    const double x = warp_tree_tail<32>(s[tid]);
+    if (tid == 0) s[0] = x;
+  }
+  __syncthreads();
 }
 
 // Thread 0 stores the group's tile partials (tile g.first + j to
@@ -137,13 +143,21 @@ __global__ void __launch_bounds__(PCG_THREADS) k2_pcg_update(PcgUpdateArgs a) {
   }
   __syncthreads();
 #pragma unroll
-  for (int w = P2 / 2; w > 0; w >>= 1) {
+  for (int w = P2 / 2; w >= 32; w >>= 1) {
     if (idx < w) {
 #pragma unroll
       for (int j = 0; j < G; ++j) s_red[j][idx] += s_red[j][idx + w];
     }
     __syncthreads();
   }
+  // the last five levels of tile j's tree in warp j (the same pairs as tile_tree)
+  static_assert(G * 32 <= P2, "a warp per tile of the group");
+  if ((idx >> 5) < G) {
+    const int j = idx >> 5;
+    const double x = warp_tree_tail<32>(s_red[j][idx & 31]);
+    if ((idx & 31) == 0) s_red[j][0] = x;
+  }
+  __syncthreads();
   group_tile_partials(a.isum, g, I, &s_red[0][0], P2, a.partials);
 }
 

@@ -97,20 +97,41 @@ __device__ __forceinline__ bool not_positive_finite(double x) {
   return __double_as_longlong(x) <= 0 || nonfinite_bits(x);
 }
 
-// Deterministic sum over the threads of a block (fixed tree order). P2 is a
-// power of two >= blockDim.x; every thread must call it; s_red holds P2
-// doubles. Returns the sum to every thread.
+// The last levels of a pairwise tree whose 32 (or fewer) remaining values sit
+// in the lanes of one warp: lane v adds lane v + w for w = W/2 .. 1, the pairs
+// (and so the bits) of the shared-memory tree; lane 0 ends with the sum.
+template <int W>
+__device__ __forceinline__ double warp_tree_tail(double x) {
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1) {
+    const double u = __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) < o) x += u;
+  }
+  return x;
+}
+
+// Deterministic sum over the threads of a block (fixed pairwise tree: slot v
+// adds slot v + w for w = P2/2 .. 1). P2 is a power of two >= blockDim.x;
+// every thread must call it; s_red holds P2 doubles. The levels down to 32
+// slots run in shared memory, the last five in warp 0 by shuffles (the same
+// pairs). Returns the sum to every thread.
 template <int P2>
 __device__ __forceinline__ double block_sum(double v, double* s_red) {
+  constexpr int W = P2 < 32 ? P2 : 32;
   const int tid = threadIdx.x;
   s_red[tid] = v;
   for (int k = tid + blockDim.x; k < P2; k += blockDim.x) s_red[k] = 0.0;
   __syncthreads();
 #pragma unroll
-  for (int w = P2 / 2; w > 0; w >>= 1) {
+  for (int w = P2 / 2; w >= 32; w >>= 1) {
     if (tid < w) s_red[tid] += s_red[tid + w];
     __syncthreads();
   }
+  if (tid < 32) {
+    const double x = warp_tree_tail<W>(tid < W ? s_red[tid] : 0.0);
+    if (tid == 0) s_red[0] = x;
+  }
+  __syncthreads();
   const double r = s_red[0];
   __syncthreads();
   return r;
