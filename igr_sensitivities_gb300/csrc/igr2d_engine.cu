@@ -478,7 +478,7 @@ static InstSum inst_sum0(int* cnt, double* out, const double* qnum = nullptr, co
 static void inst_sum_after(Ctx& c, const Plan2D& P, const double* partials, bool grouped, const InstSum& s) {
   if (s.cnt) return;
   LaunchScope ls(c, KID_OTHER);
-  k2_inst_sum<<<(int)P.inst.size(), 32, 0, c.stream>>>(P.d_inst, partials, grouped ? 1 : 0, s);
+  k2_inst_sum<<<(int)P.inst.size(), 64, 0, c.stream>>>(P.d_inst, partials, grouped ? 1 : 0, s);
 }
 
 // Fixed-count Jacobi-preconditioned CG (pcg_fixed!, elliptic.jl:329-347) on

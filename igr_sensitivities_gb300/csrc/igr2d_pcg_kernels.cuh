@@ -234,14 +234,27 @@ void launch_k2_pcg_rev_update(const PcgRevArgs& a, int nblocks, cudaStream_t s) 
   k2_pcg_rev_update<NP><<<nblocks, PCG_THREADS, 0, s>>>(a);
 }
 
-// Per-instance sums in a separate launch (InstSum with cnt null): one warp
-// per instance over the instance's tile partials, or its group partials when
-// grouped.
-static __global__ void __launch_bounds__(32) k2_inst_sum(const Inst2D* inst, const double* partials, int grouped, InstSum a) {
+// Per-instance sums in a separate launch (InstSum with cnt null): one
+// 64-thread block per instance over the instance's tile partials, or its
+// group partials when grouped, in warp_sum_partials' order with the 64 lane
+// sums on both warps (half the dependent FP64 adds of one warp).
+static __global__ void __launch_bounds__(64) k2_inst_sum(const Inst2D* inst, const double* partials, int grouped, InstSum a) {
+  __shared__ double s_acc[64];
   const int i = blockIdx.x;
   const Inst2D I = inst[i];
-  const double s = warp_sum_partials(partials + I.tile0, grouped ? inst_groups(I) : I.ntiles);
-  if (threadIdx.x == 0) inst_sum_finish(a, i, s);
+  const double* p = partials + I.tile0;
+  const int count = grouped ? inst_groups(I) : I.ntiles;
+  double acc = 0.0;
+#pragma unroll 8
+  for (int k = threadIdx.x; k < count; k += 64) acc += __ldcg(p + k);
+  s_acc[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = s_acc[threadIdx.x] + s_acc[threadIdx.x + 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (threadIdx.x == 0) inst_sum_finish(a, i, x);
+  }
 }
 
 // Reverse of the PCG start (p_0 = z_0, rz_0 = r_0 . z_0, z_0 = M^-1 r_0):
