@@ -460,7 +460,9 @@ __device__ __forceinline__ double apply_tile(const ApplyArgs2D& a, const Tile2D 
 #pragma unroll
     for (int l = 0; l < NP; ++l) {
       const long long n = vc.base + l * NP + t;
-      double y = fma(a.cm[n], xc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
+      // y-face flux at the column's end nodes (l is a compile-time index: interior nodes add nothing)
+      const double syx = s_yx[e][l * NP + t];
+      double y = fma(a.cm[n], xc[l], (l == 0) ? syx - Fb : ((l == L) ? syx + Ft : syx));
       y = dot_col<NP>(B, l, sy, y);
       if (EPI == EPI_RESID) { a.y_out[n] = y; continue; }
       if (EPI == EPI_PCG) {

@@ -528,7 +528,8 @@ __global__ void __launch_bounds__(Tiling2D<NP>::NT) k2_apply_rev(ApplyRevArgs2D 
     for (int l = 0; l < NP; ++l) {
       const long long n = vc.base + l * NP + t;
       const double cmn = a.cm[n];
-      double w = fma(cmn, uc[l], s_yx[e][l * NP + t] + ((l == 0) ? -Fb : ((l == L) ? Ft : 0.0)));
+      const double syx = s_yx[e][l * NP + t];  // y-face flux at the end nodes only (l is compile-time)
+      double w = fma(cmn, uc[l], (l == 0) ? syx - Fb : ((l == L) ? syx + Ft : syx));
       w = dot_col<NP>(B, l, sy, w);
       // zscale is -1 (r = b - A x) or +1 (A p): applied through operand signs, not a multiply
       const double uz = a.zscale > 0 ? uc[l] : -uc[l];
